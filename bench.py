@@ -1,0 +1,389 @@
+"""Benchmark of the QuIDS rule step on GB300: child objects/s per simulate() step.
+
+Workload (default "circuit24"): the plain quantum_computer rule at scale --
+24 qubits at one byte each, all |0>, 6 seeded layers (Hadamard rule on a
+random half of the qubits, then 24 random CNOT/Z modifiers), max_num_object
+2^22, simple truncation, tolerance 1e-18, align 8.  One bench step is the
+whole circuit from |0...0> (72 rule applications, 144 modifiers); the metric
+is the sum of symbolic children over the step's rule applications divided by
+the step time.
+
+"qcgd12": one step of the QCGD rule sequence (step, coin, split_merge,
+erase_create) on a 12-node cycle graph, starting from the state after the
+first step (the reference needs ~60 s on 8 cores for it).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--config NAME]
+
+--impl reference times the CPU restatement of the reference algorithm
+(oracle/quids_port.cpp, OpenMP + libstdc++ parallel mode) on all host cores.
+Under torchrun each rank runs an independent replica (the step does not
+shard across GPUs); rank 0 prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "child objects/s per simulate() step"
+UNIT = "children/s"
+MAX24 = 1 << 22
+L2_BYTES = 129 * 1024 * 1024
+
+
+# ------------------------------------------------------------------ workloads
+def workload(name):
+    from quids_gb300 import workloads as W
+    if name == "circuit24":
+        gates = [g for layer in W.circuit_layers(0) for g in layer]
+        return {"name": name, "init": W.qc_zero_state(24), "gates": gates, "max": MAX24, "tolerance": 1e-18,
+                "align": 8, "config": {"workload": "quantum_computer circuit, 24 qubits x 1 byte, 6 layers "
+                                       "(H on a seeded random half + 24 CNOT/Z), max_num_object 2^22",
+                                       "qubits": 24, "layers": 6, "max_num_object": MAX24, "seed": 0,
+                                       "tolerance": 1e-18, "align_byte_length": 8}}
+    if name == "qcgd12":
+        return {"name": name, "init": None, "gates": W.qcgd_step_rules(), "max": 1 << 24, "tolerance": 1e-18,
+                "align": 8, "config": {"workload": "QCGD step (step, coin, split_merge, erase_create) on the "
+                                       "state after step 0 of a 12-node cycle graph, max_num_object 2^24",
+                                       "nodes": 12, "seed": 1, "max_num_object": 1 << 24}}
+    raise SystemExit(f"unknown config {name}")
+
+
+def qcgd12_initial(port=None):
+    """State after the first QCGD step of the 12-node graph (computed with the
+    GPU path when no oracle is given)."""
+    from quids_gb300 import workloads as W
+    return W.qcgd_single_state(12, seed=1)
+
+
+# ------------------------------------------------------------------ helpers
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.p:
+            time.sleep(0.25)
+            self.p.terminate()
+            try:
+                self.out, _ = self.p.communicate(timeout=5)
+            except Exception:
+                self.p.kill()
+
+    def summary(self):
+        rows = [r.split(",") for r in (self.out or "").strip().splitlines() if r.count(",") >= 8]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if "Active" in r[5 + i] and "Not" not in r[5 + i]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def run_step_gpu(ctx, quids, wl, init_state, stats_acc=None):
+    """One bench step on device-resident input: returns (children, final it_t)."""
+    it = init_state
+    children = 0
+    spare = []
+    for g in wl["gates"]:
+        r = quids.rule_from(g.kind == "rule", g.code, g.params)
+        if g.kind == "mod":
+            quids.simulate(it, r)
+            continue
+        nxt = spare.pop() if spare else quids.it_t(ctx)
+        in_bytes = it.num_bytes
+        st = quids.simulate(it, r, nxt, None, wl["max"])
+        st["_in_bytes"] = in_bytes
+        children += st["num_object"]
+        if stats_acc is not None:
+            stats_acc.append(st)
+        if it is not init_state:
+            spare.append(it)
+        it = nxt
+    return children, it
+
+
+# per-stage algorithmic bytes (compulsory HBM traffic of each stage's kernels)
+def stage_bytes(st):
+    NP, NC, NU, NS = st["num_parents_kept"], st["num_object"], st["num_object_after_interferences"], st["num_object_out"]
+    sp = st.get("_in_bytes", 0)
+    sbar_p = sp / NP if NP else 0
+    sbar_c = st["out_bytes"] / NS if NS else 0
+    M = st["table_capacity"]
+    return {
+        0: 12.0 * st["num_parents"] + 8.0 * NP + sp,                   # num_child: sizes/begins/bytes, offsets
+        1: sp + 36.0 * NP + 28.0 * NC,                                  # symbolic: parents in, 28 B/child out
+        2: 28.0 * NC + 48.0 * NU + 48.0 * M,                            # insert: records in, slots, table init
+        3: 12.0 * NC + 80.0 * NU,                                       # compaction: slot/rep per child, groups out
+        4: 16.0 * NU * 2 + 24.0 * NS,                                   # select passes (first pass) + survivors
+        5: 28.0 * NS,                                                   # layout scan
+        6: NS * (sbar_p + sbar_c + 40.0),                               # populate
+        7: 48.0 * NS,                                                   # normalize
+    }
+
+
+def ours(args, rank, world):
+    import torch
+    import quids_gb300 as quids
+    from quids_gb300 import capi
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    wl = workload(args.config)
+    quids.tolerance, quids.align_byte_length = wl["tolerance"], wl["align"]
+    ctx = quids.Context(dev)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=f"cuda:{dev}")
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.int32, device=f"cuda:{dev}")
+
+    init_packed = wl["init"]
+    if init_packed is None:  # qcgd12: state after step 0, computed on the GPU
+        from quids_gb300 import workloads as W
+        it = quids.it_t(ctx, W.qcgd_single_state(12, seed=1))
+        _, it = run_step_gpu(ctx, quids, wl, it)
+        init_packed = it.download()
+    init = quids.it_t(ctx, init_packed)
+
+    # warm-up
+    for _ in range(args.warmup):
+        run_step_gpu(ctx, quids, wl, quids.it_t(ctx, init_packed))
+    ctx.synchronize()
+
+    # timed: device-resident input, L2 flushed before each step (outside the events)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ctx.synchronize()
+    launches0 = ctx.lib.quids_gpu_ctx_launch_count(ctx.h)
+    ms = []
+    children = 0
+    stats = []
+    t_wall0 = time.perf_counter()
+    with Clocks(dev) as clk:
+        for _ in range(args.steps):
+            src = quids.it_t(ctx, init_packed)
+            with torch.cuda.stream(stream):
+                flush.fill_(1)
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+            c, _ = run_step_gpu(ctx, quids, wl, src, stats)
+            with torch.cuda.stream(stream):
+                e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+            children += c
+    ctx.synchronize()
+    t_wall = time.perf_counter() - t_wall0
+    launches = ctx.lib.quids_gpu_ctx_launch_count(ctx.h) - launches0
+    total_ms = sum(ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device=f"cuda:{dev}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * children / (total_ms / 1e3)
+
+    # dominant stage and its roofline (stage times are CUDA events on the library's stream)
+    stage_t = [0.0] * 8
+    stage_b = [0.0] * 8
+    for st in stats:
+        sb = stage_bytes(st)
+        for k in range(8):
+            stage_t[k] += st["stage_ms"][k]
+            stage_b[k] += sb[k]
+    dom = max(range(8), key=lambda k: stage_t[k])
+    names = ["num_child+offsets", "symbolic", "table_insert", "group_compaction", "truncation_select",
+             "output_layout", "finalize_populate", "normalize"]
+    peak, peak_kind = peaks()
+    achieved = stage_b[dom] / (stage_t[dom] / 1e3) / 1e9 if stage_t[dom] > 0 else 0.0
+    step_bytes = sum(st["algorithmic_bytes"] for st in stats)
+
+    # e2e through the public API with host buffers (pinned), copies inside the timed region
+    e2e = None
+    if rank == 0 or world > 1:
+        objects, begin, size, mag = init_packed
+        pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()  # noqa: E731
+        h_in = tuple(pin(a) for a in (objects, begin, size, mag))
+        h2d = sum(a.nbytes for a in h_in)
+        final_n = stats[-1]["num_object_out"]
+        final_b = stats[-1]["out_bytes"]
+        h_out = (torch.empty(max(final_b, 1), dtype=torch.uint8).pin_memory(),
+                 torch.empty(final_n + 1, dtype=torch.int64).pin_memory(),
+                 torch.empty(max(final_n, 1), dtype=torch.int32).pin_memory(),
+                 torch.empty(max(final_n, 1), dtype=torch.complex128).pin_memory())
+        d2h = final_b + 8 * (final_n + 1) + 4 * final_n + 16 * final_n
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        e2e_children = 0
+        for _ in range(args.steps):
+            src = quids.it_t(ctx, h_in)
+            c, out = run_step_gpu(ctx, quids, wl, src)
+            e2e_children += c
+            capi.check(ctx.lib.quids_gpu_state_download(out.h, h_out[0].data_ptr(), h_out[1].data_ptr(),
+                                                        h_out[2].data_ptr(), h_out[3].data_ptr()), "download")
+        ctx.synchronize()
+        t_e2e = time.perf_counter() - t0
+        e2e = {"value": e2e_children / t_e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h), "ms_per_step": 1e3 * t_e2e / args.steps}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(wl, init_packed, samples=1)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded generators; the reference publishes no dataset)",
+            "config": dict(wl["config"], parallelism=f"replicas x{world}",
+                           l2="flushed before every step (256 MiB write)",
+                           children_per_step=children // args.steps),
+            "e2e": e2e,
+            "gpu_launches": int(launches),
+            "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                         "traffic": None,
+                         "stage_ms_per_step": [t / args.steps for t in stage_t],
+                         "step_algorithmic_GBps": step_bytes / (total_ms / 1e3) / 1e9},
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "wall_s_timed": t_wall,
+        }
+        print(json.dumps(line), flush=True)
+
+
+def cpu_baseline(wl, init_packed, samples=1):
+    """The oracle port (the reference algorithm restated, OpenMP) on all host cores."""
+    from oracle.oracle import Oracle
+    o = Oracle("port")
+    cores = os.cpu_count() or 1
+    o.set_threads(cores)
+    o.set_globals(wl["tolerance"], True, wl["align"])
+
+    def one():
+        s = o.new_state(init_packed)
+        ch = 0
+        for g in wl["gates"]:
+            if g.kind == "mod":
+                o.modifier(s, g.code, g.params)
+            else:
+                t = o.new_state()
+                ch += o.simulate(s, g.code, g.params, t, wl["max"])[0]
+                s = t
+        return ch
+
+    one()  # warm-up
+    t0 = time.perf_counter()
+    ch = sum(one() for _ in range(samples))
+    dt = time.perf_counter() - t0
+    return {"value": ch / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{samples} full step(s) of the {wl['name']} workload ({ch} children, {dt:.2f} s)"}
+
+
+def reference(args, rank, world):
+    if rank != 0:
+        return
+    wl = workload(args.config)
+    init_packed = wl["init"]
+    if init_packed is None:
+        print(json.dumps({"impl": "reference", "unavailable": "qcgd12 reference arm not wired"}))
+        return
+    from oracle.oracle import Oracle
+    o = Oracle("port")
+    cores = os.cpu_count() or 1
+    o.set_threads(cores)
+    o.set_globals(wl["tolerance"], True, wl["align"])
+
+    def one():
+        s = o.new_state(init_packed)
+        ch = 0
+        for g in wl["gates"]:
+            if g.kind == "mod":
+                o.modifier(s, g.code, g.params)
+            else:
+                t = o.new_state()
+                ch += o.simulate(s, g.code, g.params, t, wl["max"])[0]
+                s = t
+        return ch
+
+    for _ in range(args.warmup):
+        one()
+    t0 = time.perf_counter()
+    ch = sum(one() for _ in range(args.steps))
+    dt = time.perf_counter() - t0
+    v = ch / dt
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": dict(wl["config"], parallelism="host cores"),
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} full step(s) of {wl['name']}"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="circuit24", choices=["circuit24", "qcgd12"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1 and args.impl == "ours":
+        import torch
+        torch.distributed.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    try:
+        if args.impl == "reference":
+            reference(args, rank, world)
+        else:
+            ours(args, rank, world)
+    finally:
+        if world > 1 and args.impl == "ours":
+            import torch
+            torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,179 @@
+/*
+ * quids_gpu.h -- C ABI of the GB300-native QuIDS rule step.
+ *
+ * This library replaces, on one GPU, the two entry points of the reference
+ * header-only library (jolatechno/QuIDS):
+ *
+ *   void quids::simulate(it_t &iteration, rule_t const *rule, it_t &next_iteration,
+ *                        sy_it_t &symbolic_iteration, size_t max_num_object, debug_t)
+ *                                                           src/quids.hpp:448-543
+ *   void quids::simulate(it_t &iteration, modifier_t const rule)
+ *                                                           src/quids.hpp:436-438
+ *
+ * The state (`it_t`, src/quids.hpp:149-335) lives in device memory as the same
+ * packed structure of arrays: object bytes with every object padded to
+ * align_byte_length (get_alignment_offset, src/quids.hpp:93-102), u64 begin
+ * offsets (n+1), u32 sizes and complex<double> magnitudes (interleaved re, im).
+ *
+ * All calls return QUIDS_OK (0) or a negative status; no call throws, traps
+ * the GPU or exits the process.  A context owns one CUDA stream and its
+ * scratch memory; contexts are independent, a context is not thread-safe.
+ */
+#ifndef QUIDS_GPU_H
+#define QUIDS_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+#define QUIDS_OK 0
+#define QUIDS_ERR_BAD_ARG (-1)              /* null/aliased handles, unknown kind */
+#define QUIDS_ERR_OOM (-2)                  /* device allocation failed */
+#define QUIDS_ERR_TABLE_FULL (-3)           /* collision table probe limit reached */
+#define QUIDS_ERR_CHILD_COUNT_OVERFLOW (-4) /* a parent's child count does not fit u32 */
+#define QUIDS_ERR_SIZE_BOUND (-5)           /* a child larger than the rule's max_child_size */
+#define QUIDS_ERR_TIMEOUT (-6)              /* a bounded device wait gave up */
+#define QUIDS_ERR_CUDA (-7)                 /* a CUDA runtime call failed */
+#define QUIDS_ERR_NO_DEVICE (-8)            /* no CUDA device */
+#define QUIDS_ERR_UNSUPPORTED (-9)          /* valid request this build does not implement */
+
+/* ------------------------------------------------------- rules/modifiers */
+/* rules (classes derived from quids::rule, src/quids.hpp:105-146) */
+#define QUIDS_RULE_HADAMARD 1            /* quantum_computer::hadamard  src/rules/quantum_computer.hpp:31-50 */
+#define QUIDS_RULE_QCGD_ERASE_CREATE 2   /* qcgd::erase_create          src/rules/qcgd.hpp:459-532 */
+#define QUIDS_RULE_QCGD_COIN 3           /* qcgd::coin                  src/rules/qcgd.hpp:534-605 */
+#define QUIDS_RULE_QCGD_SPLIT_MERGE 4    /* qcgd::split_merge           src/rules/qcgd.hpp:607-1036 */
+
+/* modifiers (modifier_t, src/quids.hpp:86) */
+#define QUIDS_MOD_CNOT 1                 /* quantum_computer::cnot   src/rules/quantum_computer.hpp:25-29 */
+#define QUIDS_MOD_X 2                    /* quantum_computer::Xgate  :52-56 */
+#define QUIDS_MOD_Y 3                    /* quantum_computer::Ygate  :58-66 */
+#define QUIDS_MOD_Z 4                    /* quantum_computer::Zgate  :68-75 (negates AND flips) */
+#define QUIDS_MOD_QCGD_STEP 5            /* qcgd::step               src/rules/qcgd.hpp:443-449 */
+#define QUIDS_MOD_QCGD_REVERSED_STEP 6   /* qcgd::reversed_step      src/rules/qcgd.hpp:451-457 */
+
+/* Parameters of a rule or modifier.  Unused fields are ignored.
+ *   HADAMARD: bit            X/Y/Z: bit            CNOT: control, bit
+ *   QCGD rules: theta, phi, xi (constructor arguments of the reference rules;
+ *   do = polar(sin theta, phi), do_not = polar(cos theta, xi) are formed on
+ *   the host exactly as src/rules/qcgd.hpp:466-471 does). */
+typedef struct quids_gpu_rule_params {
+    uint64_t bit;
+    uint64_t control;
+    double theta;
+    double phi;
+    double xi;
+} quids_gpu_rule_params;
+
+/* Knobs of one rule step: the reference's globals (src/quids.hpp:59-75) and
+ * the max_num_object argument of simulate(). */
+typedef struct quids_gpu_params {
+    double tolerance;            /* quids::tolerance: keep children with norm > tolerance */
+    uint64_t max_num_object;     /* UINT64_MAX = no cap ("-1"); 0 = auto (not supported) */
+    int32_t simple_truncation;   /* must be 1 (probabilistic truncation unsupported) */
+    uint32_t align_byte_length;  /* quids::align_byte_length for the output state */
+    double table_load_factor;    /* collision table max load; 0 -> default 0.5 */
+    uint32_t block_size;         /* threads per block for per-item kernels; 0 -> default */
+    uint32_t reserved;
+} quids_gpu_params;
+
+/* Counters of one rule step (the reference's public counters plus timing). */
+typedef struct quids_gpu_step_stats {
+    uint64_t num_parents;                    /* iteration.num_object */
+    uint64_t num_parents_kept;               /* after parent pre-truncation */
+    uint64_t num_object;                     /* symbolic_iteration.num_object (children) */
+    uint64_t num_object_after_interferences; /* symbolic_iteration.num_object_after_interferences */
+    uint64_t num_object_out;                 /* next_iteration.num_object */
+    uint64_t max_child_size;                 /* max over parents of get_num_child's bound */
+    uint64_t table_capacity;                 /* collision table slots */
+    uint64_t out_bytes;                      /* object bytes of next_iteration */
+    double total_proba;                      /* next_iteration.total_proba (before normalisation) */
+    double algorithmic_bytes;                /* compulsory HBM traffic of this step */
+    float ms_total;                          /* device time of the step (CUDA events) */
+    /* device time per stage (CUDA events bracketing each stage's launches):
+     * 0 num_child + parent truncation + child offsets, 1 symbolic iteration,
+     * 2 collision table insert, 3 group compaction (zero elimination),
+     * 4 truncation select, 5 output layout, 6 finalize populate, 7 normalize */
+    float stage_ms[8];
+    uint64_t kernel_launches;                /* kernels this step launched */
+} quids_gpu_step_stats;
+
+typedef struct quids_gpu_ctx quids_gpu_ctx;
+typedef struct quids_gpu_state quids_gpu_state;
+
+/* ---------------------------------------------------------------- context */
+int quids_gpu_ctx_create(int device, quids_gpu_ctx **out);
+int quids_gpu_ctx_destroy(quids_gpu_ctx *ctx);
+/* the cudaStream_t every call of this context is ordered on */
+void *quids_gpu_ctx_stream(quids_gpu_ctx *ctx);
+int quids_gpu_ctx_synchronize(quids_gpu_ctx *ctx);
+/* bytes of device scratch memory currently held by the context */
+uint64_t quids_gpu_ctx_scratch_bytes(quids_gpu_ctx *ctx);
+/* release the context's scratch memory */
+int quids_gpu_ctx_trim(quids_gpu_ctx *ctx);
+const char *quids_gpu_status_string(int status);
+/* number of kernels launched by this context since its creation */
+uint64_t quids_gpu_ctx_launch_count(quids_gpu_ctx *ctx);
+
+/* ----------------------------------------------------------------- states
+ * A state is the device-resident `it_t`.  Handles are not copyable;
+ * `next_iteration` must be a different handle from `iteration`
+ * (src/quids.hpp:443, it_t has no copy semantics). */
+int quids_gpu_state_create(quids_gpu_ctx *ctx, quids_gpu_state **out);
+int quids_gpu_state_destroy(quids_gpu_state *st);
+/* Host -> device.  object i = objects[begin[i] .. begin[i] + size[i]);
+ * magnitude = 2 n doubles; num_bytes = bytes of `objects` to copy (begin[n]).
+ * The layout is kept as given (offsets need not follow the alignment). */
+int quids_gpu_state_upload(quids_gpu_state *st, uint64_t num_object, const uint8_t *objects,
+                           const uint64_t *begin, const uint32_t *size, const double *magnitude,
+                           uint64_t num_bytes);
+int quids_gpu_state_num_object(const quids_gpu_state *st, uint64_t *num_object);
+int quids_gpu_state_num_bytes(const quids_gpu_state *st, uint64_t *num_bytes);
+int quids_gpu_state_total_proba(const quids_gpu_state *st, double *total_proba);
+/* Device -> host into caller buffers sized from num_object / num_bytes
+ * (begin has num_object + 1 entries).  Any pointer may be NULL to skip it. */
+int quids_gpu_state_download(quids_gpu_state *st, uint8_t *objects, uint64_t *begin,
+                             uint32_t *size, double *magnitude);
+/* Device pointers of the state's arrays (valid until the next call that
+ * writes the state). */
+int quids_gpu_state_device_arrays(quids_gpu_state *st, void **objects, void **begin, void **size,
+                                  void **magnitude);
+
+/* ------------------------------------------------------------- the step */
+/* quids::simulate(iteration, rule, next_iteration, symbolic_iteration,
+ * max_num_object)  src/quids.hpp:448-543.  `stats` may be NULL. */
+int quids_gpu_simulate(quids_gpu_ctx *ctx, quids_gpu_state *iteration, int rule_kind,
+                       const quids_gpu_rule_params *rule, quids_gpu_state *next_iteration,
+                       const quids_gpu_params *params, quids_gpu_step_stats *stats);
+
+/* quids::simulate(iteration, modifier)  src/quids.hpp:436-438 -> apply_modifier
+ * src/quids.hpp:973-980: in place, sizes unchanged, no normalisation. */
+int quids_gpu_apply_modifier(quids_gpu_ctx *ctx, quids_gpu_state *iteration, int modifier_kind,
+                             const quids_gpu_rule_params *modifier);
+
+/* ------------------------------------------------------ rule-level access
+ * Materialises every child of every parent of `iteration` (the symbolic
+ * iteration of src/quids.hpp:647-721 with the child bytes kept): children
+ * are numbered parent by parent, child_id ascending.  Call once with
+ * child_bytes = NULL to get *num_children and *bytes_needed (children are
+ * packed at stride max_child_size rounded up to 8); then with buffers of
+ * those sizes.  hash / size / magnitude get one entry per child. */
+int quids_gpu_rule_children(quids_gpu_ctx *ctx, quids_gpu_state *iteration, int rule_kind,
+                            const quids_gpu_rule_params *rule, uint64_t *num_children,
+                            uint64_t *stride, uint8_t *child_bytes, uint64_t *hash,
+                            uint32_t *size, double *magnitude);
+
+/* MurmurHash64A of libstdc++'s std::hash<std::string_view> (seed 0xc70f6907),
+ * the reference's default hasher (src/quids.hpp:143-145), computed on the GPU
+ * for `n` byte strings of one state.  out = n u64. */
+int quids_gpu_state_hash(quids_gpu_ctx *ctx, quids_gpu_state *st, int rule_kind,
+                         const quids_gpu_rule_params *rule, uint64_t *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QUIDS_GPU_H */

@@ -1,0 +1,323 @@
+"""quids_gb300 -- the QuIDS rule step on one GB300 GPU.
+
+A host-side mirror of the reference's public interface (src/quids.hpp):
+
+    import quids_gb300 as quids
+    from quids_gb300 import rules
+    quids.tolerance = 1e-18                      # quids::tolerance (src/quids.hpp:62)
+    ctx = quids.Context()                        # one GPU, one CUDA stream
+    it, nxt, sy = quids.it_t(ctx), quids.it_t(ctx), quids.sy_it_t()
+    it.append(bytes(12), 1 + 0j)                 # iteration::append (:174-188)
+    quids.simulate(it, rules.hadamard(3), nxt, sy, max_num_object)   # (:448-543)
+    quids.simulate(nxt, rules.Zgate(3))          # modifier (:436-438)
+    nxt.num_object, nxt.total_proba, sy.num_object, sy.num_object_after_interferences
+
+Every call goes through the C ABI of include/quids_gpu.h into the in-tree
+CUDA library; there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import capi
+from .capi import QuidsError, U64_MAX
+
+# reference globals (src/quids.hpp:59-75); read at every simulate() call
+tolerance: float = 1e-30          # TOLERANCE default (src/quids.hpp:30-32)
+align_byte_length: int = 8        # ALIGNMENT_BYTE_LENGTH (src/quids.hpp:27-29)
+simple_truncation: bool = True    # only simple truncation is implemented
+table_load_factor: float = 0.5    # collision table maximum load
+
+
+class rules:
+    """Rule and modifier constructors (src/rules/quantum_computer.hpp, src/rules/qcgd.hpp)."""
+
+    @dataclass(frozen=True)
+    class _R:
+        kind: int
+        is_rule: bool
+        bit: int = 0
+        control: int = 0
+        theta: float = 0.0
+        phi: float = 0.0
+        xi: float = 0.0
+
+        def params(self) -> capi.RuleParams:
+            return capi.RuleParams(self.bit, self.control, self.theta, self.phi, self.xi)
+
+    @staticmethod
+    def hadamard(bit):
+        return rules._R(1, True, bit=int(bit))
+
+    @staticmethod
+    def erase_create(theta, phi=0.0, xi=0.0):
+        return rules._R(2, True, theta=float(theta), phi=float(phi), xi=float(xi))
+
+    @staticmethod
+    def coin(theta, phi=0.0, xi=0.0):
+        return rules._R(3, True, theta=float(theta), phi=float(phi), xi=float(xi))
+
+    @staticmethod
+    def split_merge(theta, phi=0.0, xi=0.0):
+        return rules._R(4, True, theta=float(theta), phi=float(phi), xi=float(xi))
+
+    @staticmethod
+    def cnot(control_bit, bit):
+        return rules._R(1, False, bit=int(bit), control=int(control_bit))
+
+    @staticmethod
+    def Xgate(bit):
+        return rules._R(2, False, bit=int(bit))
+
+    @staticmethod
+    def Ygate(bit):
+        return rules._R(3, False, bit=int(bit))
+
+    @staticmethod
+    def Zgate(bit):
+        return rules._R(4, False, bit=int(bit))
+
+    step = None            # set below (QCGD modifiers take no parameters)
+    reversed_step = None
+
+
+rules.step = rules._R(5, False)
+rules.reversed_step = rules._R(6, False)
+
+
+def rule_from(kind_is_rule: bool, code: int, params=()):
+    """Build a rule/modifier from the numeric codes used by quids_gb300.workloads."""
+    p = list(params)
+    if kind_is_rule:
+        if code == 1:
+            return rules.hadamard(p[0])
+        return rules._R(code, True, theta=float(p[0]), phi=float(p[1]) if len(p) > 1 else 0.0,
+                        xi=float(p[2]) if len(p) > 2 else 0.0)
+    if code == 1:
+        return rules.cnot(p[0], p[1])
+    if code in (2, 3, 4):
+        return rules._R(code, False, bit=int(p[0]))
+    return rules._R(code, False)
+
+
+class Context:
+    """A device context: one GPU, one CUDA stream, the step's scratch memory."""
+
+    def __init__(self, device: int = 0):
+        self.lib = capi.load()
+        h = C.c_void_p()
+        capi.check(self.lib.quids_gpu_ctx_create(int(device), C.byref(h)), "quids_gpu_ctx_create")
+        self.h = h
+        self.device = device
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.quids_gpu_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self) -> int:
+        return int(self.lib.quids_gpu_ctx_stream(self.h) or 0)
+
+    def synchronize(self):
+        capi.check(self.lib.quids_gpu_ctx_synchronize(self.h), "synchronize")
+
+    @property
+    def scratch_bytes(self) -> int:
+        return int(self.lib.quids_gpu_ctx_scratch_bytes(self.h))
+
+    def trim(self):
+        capi.check(self.lib.quids_gpu_ctx_trim(self.h), "trim")
+
+
+_default_ctx = None
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+class sy_it_t:
+    """symbolic_iteration (src/quids.hpp:338-429): the step's public counters."""
+
+    def __init__(self):
+        self.num_object = 0
+        self.num_object_after_interferences = 0
+        self.stats = {}
+
+
+class it_t:
+    """iteration (src/quids.hpp:149-335) held in device memory."""
+
+    def __init__(self, ctx: Context | None = None, packed=None):
+        self.ctx = ctx or default_context()
+        self.lib = self.ctx.lib
+        h = C.c_void_p()
+        capi.check(self.lib.quids_gpu_state_create(self.ctx.h, C.byref(h)), "state_create")
+        self.h = h
+        self._pending = []
+        if packed is not None:
+            self.upload(packed)
+
+    def __del__(self):
+        try:
+            if self.h:
+                self.lib.quids_gpu_state_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+    # ---- host <-> device
+    def upload(self, packed):
+        """packed = (objects u8, begin u64[n+1], size u32[n], mag complex128[n])"""
+        objects, begin, size, mag = packed
+        objects = np.ascontiguousarray(objects, dtype=np.uint8)
+        begin = np.ascontiguousarray(begin, dtype=np.uint64)
+        size = np.ascontiguousarray(size, dtype=np.uint32)
+        mag = np.ascontiguousarray(mag, dtype=np.complex128)
+        n = int(size.shape[0])
+        nbytes = int(objects.shape[0])
+        capi.check(self.lib.quids_gpu_state_upload(
+            self.h, n, objects.ctypes.data if nbytes else None, begin.ctypes.data, size.ctypes.data,
+            mag.ctypes.data, nbytes), "state_upload")
+        self._pending = []
+
+    def download(self):
+        self._flush()
+        n, nb = self.num_object, self.num_bytes
+        objects = np.zeros(max(nb, 1), dtype=np.uint8)
+        begin = np.zeros(n + 1, dtype=np.uint64)
+        size = np.zeros(max(n, 1), dtype=np.uint32)
+        mag = np.zeros(max(n, 1), dtype=np.complex128)
+        capi.check(self.lib.quids_gpu_state_download(self.h, objects.ctypes.data, begin.ctypes.data,
+                                                     size.ctypes.data, mag.ctypes.data), "state_download")
+        return objects[:nb], begin, size[:n], mag[:n]
+
+    def _flush(self):
+        if not self._pending:
+            return
+        pend, self._pending = self._pending, []
+        from .workloads import pack, unpack
+        objs, mags = unpack(self.download()) if self._n_device() else ([], np.zeros(0, np.complex128))
+        objs = list(objs) + [o for o, _ in pend]
+        mags = list(mags) + [m for _, m in pend]
+        self.upload(pack(objs, mags, align_byte_length))
+
+    def _n_device(self) -> int:
+        v = C.c_uint64()
+        capi.check(self.lib.quids_gpu_state_num_object(self.h, C.byref(v)))
+        return int(v.value)
+
+    # ---- reference interface
+    def append(self, obj: bytes, mag: complex = 1.0):
+        """iteration::append (src/quids.hpp:174-188)"""
+        self._pending.append((bytes(obj), complex(mag)))
+
+    @property
+    def num_object(self) -> int:
+        return self._n_device() + len(self._pending)
+
+    @property
+    def num_bytes(self) -> int:
+        v = C.c_uint64()
+        capi.check(self.lib.quids_gpu_state_num_bytes(self.h, C.byref(v)))
+        return int(v.value)
+
+    @property
+    def total_proba(self) -> float:
+        v = C.c_double()
+        capi.check(self.lib.quids_gpu_state_total_proba(self.h, C.byref(v)))
+        return float(v.value)
+
+    def get_object(self, oid: int):
+        """iteration::get_object (src/quids.hpp:254-258): (bytes, magnitude)"""
+        objects, begin, size, mag = self.download()
+        b = int(begin[oid])
+        return objects[b: b + int(size[oid])].tobytes(), complex(mag[oid])
+
+    def average_value(self, observable) -> float:
+        """iteration::average_value (src/quids.hpp:208-234), evaluated on the host."""
+        objects, begin, size, mag = self.download()
+        tot = 0.0
+        for i in range(len(size)):
+            b = int(begin[i])
+            tot += observable(objects[b: b + int(size[i])].tobytes()) * abs(mag[i]) ** 2
+        return tot
+
+
+def _params(max_num_object, flags=0):
+    return capi.Params(float(tolerance), int(max_num_object) & U64_MAX, int(bool(simple_truncation)),
+                       int(align_byte_length), float(table_load_factor), 0, int(flags))
+
+
+def simulate(iteration: it_t, rule, next_iteration: it_t | None = None, symbolic_iteration: sy_it_t | None = None,
+             max_num_object: int = U64_MAX, flags: int = 0):
+    """quids::simulate.  With a rule: (iteration, rule, next_iteration, sy_it, max_num_object)
+    (src/quids.hpp:448-543); with a modifier: (iteration, modifier) (:436-438).
+    max_num_object = U64_MAX means no truncation (the reference's -1)."""
+    iteration._flush()
+    lib = iteration.lib
+    p = rule.params()
+    if not rule.is_rule:
+        capi.check(lib.quids_gpu_apply_modifier(iteration.ctx.h, iteration.h, rule.kind, C.byref(p)),
+                   "apply_modifier")
+        return None
+    if next_iteration is None or next_iteration is iteration:
+        raise QuidsError(-1, "simulate: next_iteration must be a distinct it_t")
+    next_iteration._pending = []
+    stats = capi.StepStats()
+    prm = _params(max_num_object, flags)
+    capi.check(lib.quids_gpu_simulate(iteration.ctx.h, iteration.h, rule.kind, C.byref(p), next_iteration.h,
+                                      C.byref(prm), C.byref(stats)), "simulate")
+    d = stats.as_dict()
+    if symbolic_iteration is not None:
+        symbolic_iteration.num_object = d["num_object"]
+        symbolic_iteration.num_object_after_interferences = d["num_object_after_interferences"]
+        symbolic_iteration.stats = d
+    return d
+
+
+def rule_children(iteration: it_t, rule):
+    """Every child of every parent with its bytes, hash, size and magnitude
+    (the symbolic iteration with the child bytes kept)."""
+    iteration._flush()
+    lib = iteration.lib
+    p = rule.params()
+    nc = C.c_uint64()
+    stride = C.c_uint64()
+    capi.check(lib.quids_gpu_rule_children(iteration.ctx.h, iteration.h, rule.kind, C.byref(p), C.byref(nc),
+                                           C.byref(stride), None, None, None, None), "rule_children")
+    n, s = int(nc.value), int(stride.value)
+    bytes_ = np.zeros(max(n * s, 1), dtype=np.uint8)
+    hashes = np.zeros(max(n, 1), dtype=np.uint64)
+    sizes = np.zeros(max(n, 1), dtype=np.uint32)
+    mags = np.zeros(max(n, 1), dtype=np.complex128)
+    if n:
+        capi.check(lib.quids_gpu_rule_children(iteration.ctx.h, iteration.h, rule.kind, C.byref(p), C.byref(nc),
+                                               C.byref(stride), bytes_.ctypes.data, hashes.ctypes.data,
+                                               sizes.ctypes.data, mags.ctypes.data), "rule_children")
+    children = [bytes_[i * s: i * s + int(sizes[i])].tobytes() for i in range(n)]
+    return children, hashes[:n], mags[:n]
+
+
+def state_hash(iteration: it_t, rule):
+    """The rule's hasher over every object of a state, computed on the GPU."""
+    iteration._flush()
+    n = iteration.num_object
+    out = np.zeros(max(n, 1), dtype=np.uint64)
+    p = rule.params()
+    capi.check(iteration.lib.quids_gpu_state_hash(iteration.ctx.h, iteration.h, rule.kind, C.byref(p),
+                                                  out.ctypes.data), "state_hash")
+    return out[:n]

@@ -1,0 +1,115 @@
+"""ctypes binding of the C ABI in ``include/quids_gpu.h``.
+
+Loads the in-tree ``quids_gb300/_lib/libquids_gb300.so``; there is no CPU
+fallback: if the library is missing, ``load()`` raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import build as _build
+
+U64_MAX = (1 << 64) - 1
+
+QUIDS_OK = 0
+STATUS = {
+    0: "ok", -1: "bad argument", -2: "device out of memory", -3: "collision table full",
+    -4: "child count overflow", -5: "child larger than max_child_size bound",
+    -6: "bounded device wait expired", -7: "CUDA runtime error", -8: "no CUDA device",
+    -9: "unsupported request",
+}
+FLAG_NO_FAST_HASH = 1
+
+
+class QuidsError(RuntimeError):
+    def __init__(self, code: int, what: str = ""):
+        self.code = code
+        super().__init__(f"{what}: {STATUS.get(code, 'unknown status')} ({code})")
+
+
+class RuleParams(C.Structure):
+    _fields_ = [("bit", C.c_uint64), ("control", C.c_uint64), ("theta", C.c_double),
+                ("phi", C.c_double), ("xi", C.c_double)]
+
+
+class Params(C.Structure):
+    _fields_ = [("tolerance", C.c_double), ("max_num_object", C.c_uint64), ("simple_truncation", C.c_int32),
+                ("align_byte_length", C.c_uint32), ("table_load_factor", C.c_double),
+                ("block_size", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+class StepStats(C.Structure):
+    _fields_ = [("num_parents", C.c_uint64), ("num_parents_kept", C.c_uint64), ("num_object", C.c_uint64),
+                ("num_object_after_interferences", C.c_uint64), ("num_object_out", C.c_uint64),
+                ("max_child_size", C.c_uint64), ("table_capacity", C.c_uint64), ("out_bytes", C.c_uint64),
+                ("total_proba", C.c_double), ("algorithmic_bytes", C.c_double), ("ms_total", C.c_float),
+                ("stage_ms", C.c_float * 8), ("kernel_launches", C.c_uint64)]
+
+    def as_dict(self):
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k != "stage_ms"}
+        d["stage_ms"] = list(self.stage_ms)
+        return d
+
+
+EXPORTS = [
+    "quids_gpu_ctx_create", "quids_gpu_ctx_destroy", "quids_gpu_ctx_stream", "quids_gpu_ctx_synchronize",
+    "quids_gpu_ctx_scratch_bytes", "quids_gpu_ctx_trim", "quids_gpu_status_string", "quids_gpu_ctx_launch_count",
+    "quids_gpu_state_create", "quids_gpu_state_destroy", "quids_gpu_state_upload", "quids_gpu_state_num_object",
+    "quids_gpu_state_num_bytes", "quids_gpu_state_total_proba", "quids_gpu_state_download",
+    "quids_gpu_state_device_arrays", "quids_gpu_simulate", "quids_gpu_apply_modifier",
+    "quids_gpu_rule_children", "quids_gpu_state_hash",
+]
+
+_lib = None
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load the CUDA library (building it first if absent and nvcc exists)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = lib_path()
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise OSError(f"CUDA library not built: {path}")
+        _build.build()
+    L = C.CDLL(path)
+    vp = C.c_void_p
+    u64p = C.POINTER(C.c_uint64)
+    L.quids_gpu_ctx_create.argtypes = [C.c_int, C.POINTER(vp)]
+    L.quids_gpu_ctx_destroy.argtypes = [vp]
+    L.quids_gpu_ctx_stream.argtypes = [vp]
+    L.quids_gpu_ctx_stream.restype = vp
+    L.quids_gpu_ctx_synchronize.argtypes = [vp]
+    L.quids_gpu_ctx_scratch_bytes.argtypes = [vp]
+    L.quids_gpu_ctx_scratch_bytes.restype = C.c_uint64
+    L.quids_gpu_ctx_trim.argtypes = [vp]
+    L.quids_gpu_status_string.argtypes = [C.c_int]
+    L.quids_gpu_status_string.restype = C.c_char_p
+    L.quids_gpu_ctx_launch_count.argtypes = [vp]
+    L.quids_gpu_ctx_launch_count.restype = C.c_uint64
+    L.quids_gpu_state_create.argtypes = [vp, C.POINTER(vp)]
+    L.quids_gpu_state_destroy.argtypes = [vp]
+    L.quids_gpu_state_upload.argtypes = [vp, C.c_uint64, vp, vp, vp, vp, C.c_uint64]
+    L.quids_gpu_state_num_object.argtypes = [vp, u64p]
+    L.quids_gpu_state_num_bytes.argtypes = [vp, u64p]
+    L.quids_gpu_state_total_proba.argtypes = [vp, C.POINTER(C.c_double)]
+    L.quids_gpu_state_download.argtypes = [vp, vp, vp, vp, vp]
+    L.quids_gpu_state_device_arrays.argtypes = [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)]
+    L.quids_gpu_simulate.argtypes = [vp, vp, C.c_int, C.POINTER(RuleParams), vp, C.POINTER(Params),
+                                     C.POINTER(StepStats)]
+    L.quids_gpu_apply_modifier.argtypes = [vp, vp, C.c_int, C.POINTER(RuleParams)]
+    L.quids_gpu_rule_children.argtypes = [vp, vp, C.c_int, C.POINTER(RuleParams), u64p, u64p, vp, vp, vp, vp]
+    L.quids_gpu_state_hash.argtypes = [vp, vp, C.c_int, C.POINTER(RuleParams), vp]
+    _lib = L
+    return L
+
+
+def check(rc: int, what: str = "quids_gpu"):
+    if rc != QUIDS_OK:
+        raise QuidsError(rc, what)

@@ -1,0 +1,303 @@
+// capi.cu -- the extern "C" entry points of include/quids_gpu.h.
+//
+// Built-in rules are instantiated here; the rule and modifier objects are
+// formed on the host from quids_gpu_rule_params exactly as the reference's
+// constructors form them (src/rules/quantum_computer.hpp, src/rules/qcgd.hpp).
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <new>
+
+#include "engine.cuh"
+#include "rules_qc.cuh"
+#include "rules_qcgd.cuh"
+
+using namespace qd;
+using namespace qd::engine;
+
+namespace {
+
+qcgd::factors make_factors(const quids_gpu_rule_params *p) {
+    // src/rules/qcgd.hpp:466-471
+    std::complex<double> d = std::polar(std::sin(p->theta), p->phi);
+    std::complex<double> dn = std::polar(std::cos(p->theta), p->xi);
+    std::complex<double> dc = std::conj(d), dnc = std::conj(dn);
+    std::complex<double> ndnc = -dnc;
+    qcgd::factors f;
+    f.d = {d.real(), d.imag()};
+    f.dc = {dc.real(), dc.imag()};
+    f.dn = {dn.real(), dn.imag()};
+    f.ndnc = {ndnc.real(), ndnc.imag()};
+    return f;
+}
+
+rules::hadamard make_hadamard(const quids_gpu_rule_params *p) {
+    rules::hadamard h;
+    h.bit = p->bit;
+    h.inv_sqrt2 = 1 / std::sqrt(2);  // quantum_computer.hpp:41
+    return h;
+}
+
+template <class F>
+int dispatch_rule(int kind, const quids_gpu_rule_params *p, F &&f) {
+    if (!p) return QUIDS_ERR_BAD_ARG;
+    switch (kind) {
+    case QUIDS_RULE_HADAMARD: return f(make_hadamard(p));
+    case QUIDS_RULE_QCGD_ERASE_CREATE: return f(qcgd::erase_create{make_factors(p)});
+    case QUIDS_RULE_QCGD_COIN: return f(qcgd::coin{make_factors(p)});
+    case QUIDS_RULE_QCGD_SPLIT_MERGE: return f(qcgd::split_merge{make_factors(p)});
+    }
+    return QUIDS_ERR_BAD_ARG;
+}
+
+__global__ void k_set_words_zero(uint64_t *w, int n) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) w[i] = 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *quids_gpu_status_string(int s) {
+    switch (s) {
+    case QUIDS_OK: return "ok";
+    case QUIDS_ERR_BAD_ARG: return "bad argument";
+    case QUIDS_ERR_OOM: return "device out of memory";
+    case QUIDS_ERR_TABLE_FULL: return "collision table full";
+    case QUIDS_ERR_CHILD_COUNT_OVERFLOW: return "child count overflow";
+    case QUIDS_ERR_SIZE_BOUND: return "child larger than max_child_size bound";
+    case QUIDS_ERR_TIMEOUT: return "bounded device wait expired";
+    case QUIDS_ERR_CUDA: return "CUDA runtime error";
+    case QUIDS_ERR_NO_DEVICE: return "no CUDA device";
+    case QUIDS_ERR_UNSUPPORTED: return "unsupported request";
+    }
+    return "unknown status";
+}
+
+int quids_gpu_ctx_create(int device, quids_gpu_ctx **out) {
+    if (!out) return QUIDS_ERR_BAD_ARG;
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        return QUIDS_ERR_NO_DEVICE;
+    }
+    if (device < 0 || device >= count) return QUIDS_ERR_BAD_ARG;
+    QD_CUDA(cudaSetDevice(device));
+    auto *ctx = new (std::nothrow) quids_gpu_ctx();
+    if (!ctx) return QUIDS_ERR_OOM;
+    ctx->device = device;
+    int rc = QUIDS_OK;
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) rc = QUIDS_ERR_CUDA;
+    if (!rc) ctx->num_sms = prop.multiProcessorCount;
+    if (!rc) rc = cuda_status(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+    if (!rc) rc = cuda_status(cudaMalloc(&ctx->d_words, W_COUNT_WORDS * sizeof(uint64_t)));
+    if (!rc) rc = cuda_status(cudaMallocHost(&ctx->h_words, W_COUNT_WORDS * sizeof(uint64_t)));
+    if (!rc) rc = cuda_status(cudaMalloc(&ctx->d_sel, 2 * sizeof(qd::prim::select_state)));
+    if (!rc) rc = cuda_status(cudaMalloc(&ctx->d_hist, 256 * sizeof(unsigned long long)));
+    if (!rc) rc = cuda_status(cudaEventCreate(&ctx->ev0));
+    if (!rc) rc = cuda_status(cudaEventCreate(&ctx->ev1));
+    for (int k = 0; k < 16 && !rc; ++k) rc = cuda_status(cudaEventCreate(&ctx->ev_stage[k]));
+    if (!rc) {
+        k_set_words_zero<<<1, 32, 0, ctx->stream>>>(ctx->d_words, W_COUNT_WORDS);
+        rc = cuda_status(cudaStreamSynchronize(ctx->stream));
+    }
+    if (rc) {
+        quids_gpu_ctx_destroy(ctx);
+        return rc;
+    }
+    *out = ctx;
+    return QUIDS_OK;
+}
+
+int quids_gpu_ctx_destroy(quids_gpu_ctx *ctx) {
+    if (!ctx) return QUIDS_ERR_BAD_ARG;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (auto &b : ctx->buf) release(b);
+    if (ctx->d_words) cudaFree(ctx->d_words);
+    if (ctx->h_words) cudaFreeHost(ctx->h_words);
+    if (ctx->d_sel) cudaFree(ctx->d_sel);
+    if (ctx->d_hist) cudaFree(ctx->d_hist);
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    for (auto &e : ctx->ev_stage)
+        if (e) cudaEventDestroy(e);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return QUIDS_OK;
+}
+
+void *quids_gpu_ctx_stream(quids_gpu_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
+
+uint64_t quids_gpu_ctx_launch_count(quids_gpu_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+int quids_gpu_ctx_synchronize(quids_gpu_ctx *ctx) {
+    if (!ctx) return QUIDS_ERR_BAD_ARG;
+    QD_CUDA(cudaSetDevice(ctx->device));
+    QD_CUDA(cudaStreamSynchronize(ctx->stream));
+    return QUIDS_OK;
+}
+
+uint64_t quids_gpu_ctx_scratch_bytes(quids_gpu_ctx *ctx) {
+    if (!ctx) return 0;
+    uint64_t t = 0;
+    for (auto &b : ctx->buf) t += b.cap;
+    return t;
+}
+
+int quids_gpu_ctx_trim(quids_gpu_ctx *ctx) {
+    if (!ctx) return QUIDS_ERR_BAD_ARG;
+    QD_CUDA(cudaSetDevice(ctx->device));
+    QD_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (auto &b : ctx->buf) release(b);
+    return QUIDS_OK;
+}
+
+int quids_gpu_state_create(quids_gpu_ctx *ctx, quids_gpu_state **out) {
+    if (!ctx || !out) return QUIDS_ERR_BAD_ARG;
+    auto *st = new (std::nothrow) quids_gpu_state();
+    if (!st) return QUIDS_ERR_OOM;
+    st->ctx = ctx;
+    *out = st;
+    return QUIDS_OK;
+}
+
+int quids_gpu_state_destroy(quids_gpu_state *st) {
+    if (!st) return QUIDS_ERR_BAD_ARG;
+    cudaSetDevice(st->ctx->device);
+    cudaStreamSynchronize(st->ctx->stream);
+    release(st->objects);
+    release(st->begin);
+    release(st->size);
+    release(st->mag);
+    delete st;
+    return QUIDS_OK;
+}
+
+int quids_gpu_state_upload(quids_gpu_state *st, uint64_t n, const uint8_t *objects, const uint64_t *begin,
+                           const uint32_t *size, const double *magnitude, uint64_t num_bytes) {
+    if (!st) return QUIDS_ERR_BAD_ARG;
+    if (n && (!begin || !size || !magnitude)) return QUIDS_ERR_BAD_ARG;
+    if (num_bytes && !objects) return QUIDS_ERR_BAD_ARG;
+    for (uint64_t i = 0; i < n; ++i)
+        if (begin[i] + size[i] > num_bytes) return QUIDS_ERR_BAD_ARG;
+    quids_gpu_ctx *ctx = st->ctx;
+    QD_CUDA(cudaSetDevice(ctx->device));
+    QD_TRY(ensure_state(st, n, num_bytes));
+    cudaStream_t s = ctx->stream;
+    if (num_bytes) QD_CUDA(cudaMemcpyAsync(st->objects.p, objects, num_bytes, cudaMemcpyHostToDevice, s));
+    if (n) {
+        QD_CUDA(cudaMemcpyAsync(st->begin.p, begin, (n + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, s));
+        QD_CUDA(cudaMemcpyAsync(st->size.p, size, n * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+        QD_CUDA(cudaMemcpyAsync(st->mag.p, magnitude, n * 2 * sizeof(double), cudaMemcpyHostToDevice, s));
+    } else {
+        QD_CUDA(cudaMemsetAsync(st->begin.p, 0, sizeof(uint64_t), s));
+    }
+    QD_CUDA(cudaStreamSynchronize(s));
+    st->n = n;
+    st->nbytes = num_bytes;
+    st->total_proba = 1;
+    return QUIDS_OK;
+}
+
+int quids_gpu_state_num_object(const quids_gpu_state *st, uint64_t *n) {
+    if (!st || !n) return QUIDS_ERR_BAD_ARG;
+    *n = st->n;
+    return QUIDS_OK;
+}
+
+int quids_gpu_state_num_bytes(const quids_gpu_state *st, uint64_t *nb) {
+    if (!st || !nb) return QUIDS_ERR_BAD_ARG;
+    *nb = st->nbytes;
+    return QUIDS_OK;
+}
+
+int quids_gpu_state_total_proba(const quids_gpu_state *st, double *p) {
+    if (!st || !p) return QUIDS_ERR_BAD_ARG;
+    *p = st->total_proba;
+    return QUIDS_OK;
+}
+
+int quids_gpu_state_download(quids_gpu_state *st, uint8_t *objects, uint64_t *begin, uint32_t *size,
+                             double *magnitude) {
+    if (!st) return QUIDS_ERR_BAD_ARG;
+    quids_gpu_ctx *ctx = st->ctx;
+    QD_CUDA(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    if (objects && st->nbytes)
+        QD_CUDA(cudaMemcpyAsync(objects, st->objects.p, st->nbytes, cudaMemcpyDeviceToHost, s));
+    if (begin) {
+        if (st->n)
+            QD_CUDA(cudaMemcpyAsync(begin, st->begin.p, (st->n + 1) * sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
+        else
+            begin[0] = 0;
+    }
+    if (size && st->n) QD_CUDA(cudaMemcpyAsync(size, st->size.p, st->n * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+    if (magnitude && st->n)
+        QD_CUDA(cudaMemcpyAsync(magnitude, st->mag.p, st->n * 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    QD_CUDA(cudaStreamSynchronize(s));
+    return QUIDS_OK;
+}
+
+int quids_gpu_state_device_arrays(quids_gpu_state *st, void **objects, void **begin, void **size, void **magnitude) {
+    if (!st) return QUIDS_ERR_BAD_ARG;
+    if (objects) *objects = st->objects.p;
+    if (begin) *begin = st->begin.p;
+    if (size) *size = st->size.p;
+    if (magnitude) *magnitude = st->mag.p;
+    return QUIDS_OK;
+}
+
+int quids_gpu_simulate(quids_gpu_ctx *ctx, quids_gpu_state *iteration, int rule_kind,
+                       const quids_gpu_rule_params *rule, quids_gpu_state *next_iteration,
+                       const quids_gpu_params *params, quids_gpu_step_stats *stats) {
+    if (!params) return QUIDS_ERR_BAD_ARG;
+    quids_gpu_params prm = *params;
+    return dispatch_rule(rule_kind, rule, [&](auto r) {
+        return simulate_rule(ctx, iteration, r, next_iteration, prm, stats);
+    });
+}
+
+int quids_gpu_apply_modifier(quids_gpu_ctx *ctx, quids_gpu_state *st, int kind, const quids_gpu_rule_params *p) {
+    if (!p) return QUIDS_ERR_BAD_ARG;
+    switch (kind) {
+    case QUIDS_MOD_CNOT: return apply_modifier(ctx, st, rules::cnot{p->control, p->bit});
+    case QUIDS_MOD_X: return apply_modifier(ctx, st, rules::xgate{p->bit});
+    case QUIDS_MOD_Y: return apply_modifier(ctx, st, rules::ygate{p->bit});
+    case QUIDS_MOD_Z: return apply_modifier(ctx, st, rules::zgate{p->bit});
+    case QUIDS_MOD_QCGD_STEP: return apply_modifier(ctx, st, qcgd::step{});
+    case QUIDS_MOD_QCGD_REVERSED_STEP: return apply_modifier(ctx, st, qcgd::reversed_step{});
+    }
+    return QUIDS_ERR_BAD_ARG;
+}
+
+int quids_gpu_rule_children(quids_gpu_ctx *ctx, quids_gpu_state *iteration, int rule_kind,
+                            const quids_gpu_rule_params *rule, uint64_t *num_children, uint64_t *stride,
+                            uint8_t *child_bytes, uint64_t *hash, uint32_t *size, double *magnitude) {
+    return dispatch_rule(rule_kind, rule, [&](auto r) {
+        return rule_children(ctx, iteration, r, num_children, stride, child_bytes, hash, size, magnitude);
+    });
+}
+
+int quids_gpu_state_hash(quids_gpu_ctx *ctx, quids_gpu_state *st, int rule_kind, const quids_gpu_rule_params *rule,
+                         uint64_t *out) {
+    if (!ctx || !st || !out || st->ctx != ctx) return QUIDS_ERR_BAD_ARG;
+    if (st->n == 0) return QUIDS_OK;
+    QD_CUDA(cudaSetDevice(ctx->device));
+    qd_dbuf d;
+    QD_TRY(ensure(d, st->n * sizeof(uint64_t)));
+    int rc = dispatch_rule(rule_kind, rule, [&](auto r) {
+        k_state_hash<<<grid_for(ctx, st->n), prim::kThreads, 0, ctx->stream>>>(
+            r, (const char *)st->objects.p, (const uint64_t *)st->begin.p, (const uint32_t *)st->size.p, st->n,
+            (uint64_t *)d.p);
+        return launched(ctx);
+    });
+    if (!rc) rc = cuda_status(cudaMemcpyAsync(out, d.p, st->n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    if (!rc) rc = cuda_status(cudaStreamSynchronize(ctx->stream));
+    release(d);
+    return rc;
+}
+
+}  // extern "C"

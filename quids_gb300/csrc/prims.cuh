@@ -1,0 +1,392 @@
+// prims.cuh -- rule-independent device primitives of the rule step:
+//   * single-pass scan and stream compaction with decoupled look-back
+//     (tiles taken in order from an atomic counter, bounded waits),
+//   * top-k radix select on 64-bit keys,
+//   * the collision table (open addressing, 64-bit keys, exact fixed-point
+//     magnitude sums),
+//   * deterministic normalisation.
+// Every wait on another block is bounded: on expiry it records
+// QUIDS_ERR_TIMEOUT in the status word and the kernel returns.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/quids_gpu.h"
+#include "qd_common.cuh"
+
+namespace qd::prim {
+
+constexpr int kThreads = 256;
+constexpr int kItems = 8;
+constexpr int kTile = kThreads * kItems;
+constexpr uint64_t kFlagAgg = 1ull << 62;
+constexpr uint64_t kFlagInc = 2ull << 62;
+constexpr uint64_t kValMask = (1ull << 62) - 1;
+constexpr uint32_t kSpinLimit = 1u << 22;  // x ~64 ns sleep: well under a second
+constexpr uint64_t kEmptyKey = ~0ull;
+
+__device__ __forceinline__ void set_error(int *err, int code) { atomicCAS(err, 0, code); }
+
+__device__ __forceinline__ uint64_t warp_sum(uint64_t v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ uint64_t ld_volatile_u64(const uint64_t *p) {
+    return *(const volatile uint64_t *)p;
+}
+__device__ __forceinline__ void st_volatile_u64(uint64_t *p, uint64_t v) { *(volatile uint64_t *)p = v; }
+
+// Block-wide exclusive scan of one u64 per thread; returns the exclusive
+// value, writes the block total to *total.  Uses `sm` (kThreads/32 + 1 u64).
+__device__ __forceinline__ uint64_t block_excl_scan(uint64_t v, uint64_t *sm, uint64_t &total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint64_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint64_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) sm[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint64_t w = lane < kThreads / 32 ? sm[lane] : 0;
+        uint64_t s = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint64_t y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        if (lane < kThreads / 32) sm[lane] = s - w;
+        if (lane == kThreads / 32 - 1) sm[kThreads / 32] = s;
+    }
+    __syncthreads();
+    uint64_t r = sm[warp] + x - v;
+    total = sm[kThreads / 32];
+    __syncthreads();
+    return r;
+}
+
+struct lookback {
+    uint64_t *status;   // one word per tile, zeroed before the launch
+    uint32_t *counter;  // tile ticket, zeroed before the launch
+    int *err;
+};
+
+// Exclusive prefix of tile `tile` given its aggregate; all threads call it.
+__device__ uint64_t tile_prefix(const lookback &lb, uint32_t tile, uint64_t aggregate, uint64_t *bcast) {
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        uint64_t prefix = 0;
+        if (tile == 0) {
+            if (lane == 0) st_volatile_u64(&lb.status[0], kFlagInc | (aggregate & kValMask));
+        } else {
+            if (lane == 0) st_volatile_u64(&lb.status[tile], kFlagAgg | (aggregate & kValMask));
+            int64_t base = (int64_t)tile - 1;
+            bool failed = false;
+            while (true) {
+                int64_t j = base - lane;
+                uint64_t s = kFlagInc;  // tiles before 0 contribute an inclusive 0
+                if (j >= 0) {
+                    uint32_t it = 0;
+                    s = ld_volatile_u64(&lb.status[j]);
+                    while ((s >> 62) == 0 && ++it < kSpinLimit) {
+                        __nanosleep(64);
+                        s = ld_volatile_u64(&lb.status[j]);
+                    }
+                    if ((s >> 62) == 0) {
+                        failed = true;
+                        s = kFlagInc;
+                    }
+                }
+                unsigned inc = __ballot_sync(0xffffffffu, (s >> 62) == 2);
+                uint64_t v = s & kValMask;
+                if (inc) {
+                    int first = __ffs(inc) - 1;
+                    if (lane > first) v = 0;
+                    prefix += warp_sum(v);
+                    break;
+                }
+                prefix += warp_sum(v);
+                base -= 32;
+            }
+            if (__any_sync(0xffffffffu, failed) && lane == 0) set_error(lb.err, QUIDS_ERR_TIMEOUT);
+            if (lane == 0) st_volatile_u64(&lb.status[tile], kFlagInc | ((prefix + aggregate) & kValMask));
+        }
+        if (lane == 0) *bcast = prefix;
+    }
+    __syncthreads();
+    uint64_t p = *bcast;
+    __syncthreads();
+    return p;
+}
+
+__device__ __forceinline__ uint32_t next_tile(const lookback &lb, uint32_t *sm_tile) {
+    if (threadIdx.x == 0) *sm_tile = atomicAdd(lb.counter, 1u);
+    __syncthreads();
+    uint32_t t = *sm_tile;
+    __syncthreads();
+    return t;
+}
+
+// --------------------------------------------------------------- scan
+// out[i] = sum_{j<i} f(j) for i in [0, n], *total = sum; f(i) is called
+// exactly once per item (it may have side effects, e.g. gathers).
+template <class F>
+__global__ void __launch_bounds__(kThreads) k_scan_excl(F f, const uint64_t *d_n, uint64_t *out,
+                                                         uint64_t *d_total, lookback lb) {
+    __shared__ uint64_t sm[kThreads / 32 + 1];
+    __shared__ uint64_t bcast;
+    __shared__ uint32_t sm_tile;
+    const uint64_t n = *d_n;
+    const uint64_t ntiles = (n + kTile - 1) / kTile;
+    if (n == 0) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            out[0] = 0;
+            if (d_total) *d_total = 0;
+        }
+        return;
+    }
+    while (true) {
+        uint32_t tile = next_tile(lb, &sm_tile);
+        if (tile >= ntiles) break;
+        const uint64_t base = (uint64_t)tile * kTile + (uint64_t)threadIdx.x * kItems;
+        uint64_t v[kItems];
+        uint64_t tsum = 0;
+#pragma unroll
+        for (int k = 0; k < kItems; ++k) {
+            uint64_t i = base + k;
+            v[k] = i < n ? f(i) : 0;
+            tsum += v[k];
+        }
+        uint64_t agg;
+        uint64_t texcl = block_excl_scan(tsum, sm, agg);
+        uint64_t prefix = tile_prefix(lb, tile, agg, &bcast);
+        uint64_t run = prefix + texcl;
+#pragma unroll
+        for (int k = 0; k < kItems; ++k) {
+            uint64_t i = base + k;
+            if (i < n) out[i] = run;
+            run += v[k];
+        }
+        if (tile == ntiles - 1 && threadIdx.x == kThreads - 1) {
+            out[n] = prefix + agg;
+            if (d_total) *d_total = prefix + agg;
+        }
+    }
+}
+
+// ------------------------------------------------------------- compact
+// Stream compaction preserving order: P::select(i) -> bool, P::emit(i, j)
+// writes item i to output slot j.  *d_count = number selected.
+template <class P>
+__global__ void __launch_bounds__(kThreads) k_compact(P p, const uint64_t *d_n, uint64_t *d_count,
+                                                       lookback lb) {
+    __shared__ uint64_t sm[kThreads / 32 + 1];
+    __shared__ uint64_t bcast;
+    __shared__ uint32_t sm_tile;
+    const uint64_t n = *d_n;
+    const uint64_t ntiles = (n + kTile - 1) / kTile;
+    if (n == 0) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) *d_count = 0;
+        return;
+    }
+    while (true) {
+        uint32_t tile = next_tile(lb, &sm_tile);
+        if (tile >= ntiles) break;
+        const uint64_t base = (uint64_t)tile * kTile + (uint64_t)threadIdx.x * kItems;
+        uint32_t flags = 0;
+        uint64_t cnt = 0;
+#pragma unroll
+        for (int k = 0; k < kItems; ++k) {
+            uint64_t i = base + k;
+            if (i < n && p.select(i)) {
+                flags |= 1u << k;
+                ++cnt;
+            }
+        }
+        uint64_t agg;
+        uint64_t texcl = block_excl_scan(cnt, sm, agg);
+        uint64_t prefix = tile_prefix(lb, tile, agg, &bcast);
+        uint64_t j = prefix + texcl;
+#pragma unroll
+        for (int k = 0; k < kItems; ++k)
+            if (flags & (1u << k)) p.emit(base + k, j++);
+        if (tile == ntiles - 1 && threadIdx.x == kThreads - 1) *d_count = prefix + agg;
+    }
+}
+
+// --------------------------------------------------------- radix select
+// Top-k selection on 64-bit keys, 8 bits per pass from the top.  State is
+// device resident so the passes need no host round trip.
+struct select_state {
+    uint64_t prefix;     // key bits fixed so far
+    uint64_t mask;       // which bits of prefix are fixed
+    uint64_t k_rem;      // how many items still to take among those matching prefix
+    uint64_t n_better;   // items strictly better than the threshold
+    uint64_t n_equal;    // items equal to the threshold (after the last pass)
+    uint32_t active;     // 0: nothing to select (k >= n), pass kernels return
+    uint32_t pad;
+};
+
+// descending = true: keep the k largest keys; false: the k smallest.
+// K::key(i) -> u64, K::eligible(i) -> bool (restricts the population)
+template <class K>
+__global__ void __launch_bounds__(kThreads) k_radix_hist(K kf, const uint64_t *d_n, const select_state *st,
+                                                          int shift, unsigned long long *hist) {
+    __shared__ unsigned int sh[256];
+    if (!st->active) return;
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) sh[i] = 0;
+    __syncthreads();
+    const uint64_t n = *d_n, prefix = st->prefix, mask = st->mask;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        if (!kf.eligible(i)) continue;
+        uint64_t k = kf.key(i);
+        if ((k & mask) == prefix) atomicAdd(&sh[(k >> shift) & 255], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 256; i += blockDim.x)
+        if (sh[i]) atomicAdd(&hist[i], (unsigned long long)sh[i]);
+}
+
+__global__ void k_radix_pick(select_state *st, unsigned long long *hist, int shift, bool descending) {
+    // one warp: cumulative counts in preference order
+    if (threadIdx.x != 0) return;
+    if (!st->active) return;
+    uint64_t above = 0;
+    int d = 0;
+    for (int s = 0; s < 256; ++s) {
+        d = descending ? 255 - s : s;
+        uint64_t c = hist[d];
+        if (above + c >= st->k_rem) break;
+        above += c;
+    }
+    st->prefix |= (uint64_t)d << shift;
+    st->mask |= 255ull << shift;
+    st->n_better += above;
+    st->k_rem -= above;
+    st->n_equal = hist[d];
+    for (int s = 0; s < 256; ++s) hist[s] = 0;
+}
+
+// ---------------------------------------------------- collision table
+// keys[M] (kEmptyKey = free), rep[M+1] (min child index, ~0 = none),
+// acc[M+1][4] (re lo, re hi, im lo, im hi).  Slot M holds the children whose
+// hash equals kEmptyKey.
+struct table {
+    uint64_t *keys;
+    uint64_t *rep;
+    unsigned long long *acc;
+    uint64_t mask;      // M - 1
+    int log2m;
+    uint32_t max_probes;
+};
+
+__device__ __forceinline__ uint64_t table_home(uint64_t h, int log2m) {
+    return (h * 0x9E3779B97F4A7C15ull) >> (64 - log2m);
+}
+
+__device__ __forceinline__ void fix_atomic_add(unsigned long long *w, fix128 v) {
+    unsigned long long old = atomicAdd(&w[0], (unsigned long long)v.lo);
+    unsigned long long carry = (old + v.lo) < old ? 1ull : 0ull;
+    unsigned long long hi = v.hi + carry;
+    if (hi) atomicAdd(&w[1], hi);
+}
+
+// Inserts every child: slot_of[c] = its group's slot; rep = min child index;
+// acc += magnitude (exact fixed point with scale 2^-F, F from the largest
+// component and the child count).
+__global__ void __launch_bounds__(kThreads) k_table_insert(table t, const uint64_t *hash, const double2 *mag,
+                                                            const uint64_t *d_n, const unsigned long long *d_maxabs,
+                                                            uint32_t *slot_of, int *err) {
+    const uint64_t n = *d_n;
+    double maxabs = __longlong_as_double((long long)*d_maxabs);
+    const int F = fix_scale(maxabs, n);
+    const uint64_t M = t.mask + 1;
+    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t h = hash[c];
+        uint64_t s;
+        if (h == kEmptyKey) {
+            s = M;
+        } else {
+            s = table_home(h, t.log2m);
+            uint32_t probe = 0;
+            while (true) {
+                uint64_t k = ld_volatile_u64(&t.keys[s]);
+                if (k == h) break;
+                if (k == kEmptyKey) {
+                    uint64_t old = atomicCAS((unsigned long long *)&t.keys[s], kEmptyKey, h);
+                    if (old == kEmptyKey || old == h) break;
+                }
+                s = (s + 1) & t.mask;
+                if (++probe >= t.max_probes) {
+                    set_error(err, QUIDS_ERR_TABLE_FULL);
+                    s = ~0ull;
+                    break;
+                }
+            }
+            if (s == ~0ull) {
+                slot_of[c] = 0xffffffffu;
+                continue;
+            }
+        }
+        atomicMin((unsigned long long *)&t.rep[s], (unsigned long long)c);
+        double2 m = mag[c];
+        fix_atomic_add(&t.acc[4 * s + 0], to_fix(m.x, F));
+        fix_atomic_add(&t.acc[4 * s + 2], to_fix(m.y, F));
+        slot_of[c] = (uint32_t)s;
+    }
+}
+
+// --------------------------------------------------------- normalisation
+constexpr int kNormBlocks = 512;
+
+// partial[b] = sum of norms over the fixed chunk of block b (fixed order)
+__global__ void __launch_bounds__(kThreads) k_norm_partial(const double2 *mag, const uint64_t *d_n, double *partial) {
+    __shared__ double sm[kThreads];
+    const uint64_t n = *d_n;
+    const uint64_t chunk = (n + gridDim.x - 1) / gridDim.x;
+    const uint64_t b = (uint64_t)blockIdx.x * chunk;
+    const uint64_t e = min(n, b + chunk);
+    double s = 0;
+    for (uint64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
+        double2 m = mag[i];
+        s = dadd(s, cnorm(mag_t{m.x, m.y}));
+    }
+    sm[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = kThreads / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sm[threadIdx.x] = dadd(sm[threadIdx.x], sm[threadIdx.x + o]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = sm[0];
+}
+
+// total = sum of partials (fixed order); factor = sqrt(total)
+__global__ void k_norm_final(const double *partial, int np, double *d_total, double *d_factor) {
+    __shared__ double sm[kNormBlocks];
+    for (int i = threadIdx.x; i < kNormBlocks; i += blockDim.x) sm[i] = i < np ? partial[i] : 0.0;
+    __syncthreads();
+    for (int o = kNormBlocks / 2; o > 0; o >>= 1) {
+        for (int i = threadIdx.x; i < o; i += blockDim.x) sm[i] = dadd(sm[i], sm[i + o]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        *d_total = sm[0];
+        *d_factor = __dsqrt_rn(sm[0]);
+    }
+}
+
+// mag /= factor when factor != 1 (src/quids.hpp:1008-1013)
+__global__ void __launch_bounds__(kThreads) k_norm_scale(double2 *mag, const uint64_t *d_n, const double *d_factor) {
+    const double f = *d_factor;
+    if (f == 1.0) return;
+    const uint64_t n = *d_n;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        double2 m = mag[i];
+        mag[i] = make_double2(__ddiv_rn(m.x, f), __ddiv_rn(m.y, f));
+    }
+}
+
+}  // namespace qd::prim

@@ -1,0 +1,486 @@
+// rules_qcgd.cuh -- QCGD (quantum causal graph dynamics) rules as device rules.
+//
+// Reference: src/rules/qcgd.hpp.  Object layout (:63-112):
+//   [u16 n][u8 left[n]][u8 right[n]][u16 name_begin[n+1]][name sub-nodes]
+// A name sub-node (:35-61) is 16 bytes {i16 hmlz_and_element,
+// i16 right_or_type, 4 padding bytes, u64 hash}; the sub-node array starts at
+// byte 4+4n, so its u64 fields are misaligned for even n.  Every access here
+// goes through qd_common's alignment-safe helpers.
+//
+// The graph hash (hash_graph, :122-146) and the name algebra
+// (operations::left/right/merge, :181-209) are restated bit for bit; the
+// rules add a hash_child fast path that yields the child's hash, size and
+// magnitude without writing its bytes (the child's hash depends only on the
+// root sub-node hash of each node and the left/right bits).
+#pragma once
+#include "qd_common.cuh"
+
+namespace qd::qcgd {
+
+enum : int16_t { dot_l_t = -3, dot_r_t = -2, element_t = -1 };
+
+// utils::hash_combine, src/rules/qcgd.hpp:11-25
+QD_HD void hash_combine(uint64_t &seed, uint64_t v) {
+    constexpr uint64_t m = 0xc6a4a7935bd1e995ull;
+    seed *= m;
+    seed ^= v >> 47;
+    seed *= m;
+    seed ^= v;
+    seed *= m;
+    seed += 0xe6546b64ull;
+}
+
+// ---- accessors (n passed explicitly: the count is read once per object)
+QD_HD int num_nodes(const char *o) { return ld_u16(o); }
+QD_HD bool L(const char *o, int i) { return o[2 + i] != 0; }
+QD_HD bool R(const char *o, int n, int i) { return o[2 + n + i] != 0; }
+QD_HD int name_begin(const char *o, int n, int i) { return ld_u16(o + 2 + 2 * n + 2 * i); }
+QD_HD const char *names(const char *o, int n) { return o + 4 + 4 * n; }
+QD_HD char *names(char *o, int n) { return o + 4 + 4 * n; }
+
+struct sub_node {
+    int16_t hmlz, rot;
+    uint32_t pad;
+    uint64_t hash;
+};
+QD_HD sub_node get_node(const char *base, int k) {
+    const char *p = base + 16 * k;
+    uint32_t w = ld_u32(p);
+    sub_node s;
+    s.hmlz = (int16_t)(w & 0xffff);
+    s.rot = (int16_t)(w >> 16);
+    s.pad = ld_u32(p + 4);
+    s.hash = ld_u64(p + 8);
+    return s;
+}
+QD_HD int16_t node_rot(const char *base, int k) { return (int16_t)ld_u16(base + 16 * k + 2); }
+QD_HD int16_t node_hmlz(const char *base, int k) { return (int16_t)ld_u16(base + 16 * k); }
+QD_HD uint64_t node_hash(const char *base, int k) { return ld_u64(base + 16 * k + 8); }
+QD_HD void put_node(char *base, int k, sub_node s) {
+    char *p = base + 16 * k;
+    st_u16(p, (uint16_t)s.hmlz);
+    st_u16(p + 2, (uint16_t)s.rot);
+    st_u16(p + 4, 0);
+    st_u16(p + 6, 0);
+    st_u64(p + 8, s.hash);
+}
+
+// sub_node constructors, :43-60
+QD_HD sub_node make_dot(sub_node x, int16_t type) {
+    sub_node s;
+    s.rot = type;
+    s.hmlz = (type == dot_l_t && x.hmlz < 0) ? -1 : 1;
+    s.pad = 0;
+    s.hash = x.hash;
+    hash_combine(s.hash, (uint64_t)(int64_t)type);
+    return s;
+}
+QD_HD sub_node make_pair(sub_node l, sub_node r, int16_t right_offset) {
+    sub_node s;
+    s.rot = right_offset;
+    s.hmlz = (l.hmlz < 0 || r.hmlz < 0) ? -1 : 1;
+    s.pad = 0;
+    s.hash = l.hash;
+    hash_combine(s.hash, r.hash);
+    return s;
+}
+
+// graphs::hash_graph, :122-146
+QD_HD uint64_t hash_graph(const char *o) {
+    int n = num_nodes(o);
+    const char *nm = names(o, n);
+    uint64_t lh = 0, rh = 0, nh = 0;
+    for (int i = 0; i < n; ++i) {
+        if (L(o, i)) hash_combine(lh, (uint64_t)i);
+        if (R(o, n, i)) hash_combine(rh, (uint64_t)i);
+        hash_combine(nh, node_hash(nm, name_begin(o, n, i)));
+    }
+    hash_combine(nh, lh);
+    hash_combine(nh, rh);
+    return nh;
+}
+
+// operations::get_operations, :174-179
+QD_HD void get_operations(const char *p, int n, int i, bool &split, bool &merge) {
+    merge = false;
+    split = L(p, i) && R(p, n, i);
+    if (!split && i + 1 < n) merge = L(p, i) && R(p, n, i + 1) && !L(p, i + 1);
+}
+
+// ---------------------------------------------------------------- name ops
+// A child node's name is one operation on parent name ranges [b, e)
+// (sub-node indices into the parent's name array).
+enum name_op { OP_COPY = 0, OP_LEFT = 1, OP_RIGHT = 2, OP_MERGE = 3 };
+
+// writes the name into dst[d..) and returns the end index
+QD_HD int write_name(const char *src, char *dst, int d, int op, int b1, int e1, int b2, int e2) {
+    switch (op) {
+    case OP_COPY:
+        copy_bytes(dst + 16 * d, src + 16 * b1, 16u * (uint32_t)(e1 - b1));
+        return d + (e1 - b1);
+    case OP_LEFT: {  // operations::left, :194-200
+        int16_t rot = node_rot(src, b1);
+        if (rot >= 0) {
+            copy_bytes(dst + 16 * d, src + 16 * (b1 + 1), 16u * (uint32_t)(rot - 1));
+            return d + rot - 1;
+        }
+        put_node(dst, d, make_dot(get_node(src, b1), dot_l_t));
+        copy_bytes(dst + 16 * (d + 1), src + 16 * b1, 16u * (uint32_t)(e1 - b1));
+        return d + 1 + (e1 - b1);
+    }
+    case OP_RIGHT: {  // operations::right, :202-208
+        int16_t rot = node_rot(src, b1);
+        if (rot >= 0) {
+            copy_bytes(dst + 16 * d, src + 16 * (b1 + rot), 16u * (uint32_t)(e1 - b1 - rot));
+            return d + (e1 - b1 - rot);
+        }
+        put_node(dst, d, make_dot(get_node(src, b1), dot_r_t));
+        copy_bytes(dst + 16 * (d + 1), src + 16 * b1, 16u * (uint32_t)(e1 - b1));
+        return d + 1 + (e1 - b1);
+    }
+    default: {  // operations::merge, :181-192
+        if (node_rot(src, b1) == dot_l_t && node_rot(src, b2) == dot_r_t &&
+            node_hash(src, b1 + 1) == node_hash(src, b2 + 1)) {
+            copy_bytes(dst + 16 * d, src + 16 * (b1 + 1), 16u * (uint32_t)(e1 - b1 - 1));
+            return d + (e1 - b1 - 1);
+        }
+        put_node(dst, d, make_pair(get_node(src, b1), get_node(src, b2), (int16_t)(e1 - b1 + 1)));
+        copy_bytes(dst + 16 * (d + 1), src + 16 * b1, 16u * (uint32_t)(e1 - b1));
+        copy_bytes(dst + 16 * (d + 1 + e1 - b1), src + 16 * b2, 16u * (uint32_t)(e2 - b2));
+        return d + 1 + (e1 - b1) + (e2 - b2);
+    }
+    }
+}
+
+// root hash and sub-node count of the name an operation would write
+QD_HD uint64_t name_root_hash(const char *src, int op, int b1, int e1, int b2, int e2, int &len) {
+    switch (op) {
+    case OP_COPY:
+        len = e1 - b1;
+        return node_hash(src, b1);
+    case OP_LEFT: {
+        int16_t rot = node_rot(src, b1);
+        if (rot >= 0) {
+            len = rot - 1;
+            return node_hash(src, b1 + 1);
+        }
+        len = 1 + (e1 - b1);
+        uint64_t h = node_hash(src, b1);
+        hash_combine(h, (uint64_t)(int64_t)dot_l_t);
+        return h;
+    }
+    case OP_RIGHT: {
+        int16_t rot = node_rot(src, b1);
+        if (rot >= 0) {
+            len = e1 - b1 - rot;
+            return node_hash(src, b1 + rot);
+        }
+        len = 1 + (e1 - b1);
+        uint64_t h = node_hash(src, b1);
+        hash_combine(h, (uint64_t)(int64_t)dot_r_t);
+        return h;
+    }
+    default: {
+        // a dot node is always followed by its operand, so b1+1 / b2+1 are
+        // only read when both roots are dot nodes
+        if (node_rot(src, b1) == dot_l_t && node_rot(src, b2) == dot_r_t) {
+            uint64_t hl1 = node_hash(src, b1 + 1);
+            if (hl1 == node_hash(src, b2 + 1)) {
+                len = e1 - b1 - 1;
+                return hl1;
+            }
+        }
+        len = 1 + (e1 - b1) + (e2 - b2);
+        uint64_t h = node_hash(src, b1);
+        hash_combine(h, node_hash(src, b2));
+        return h;
+    }
+    }
+}
+
+// ------------------------------------------------------------ the factors
+// do = polar(sin theta, phi), do_not = polar(cos theta, xi), formed on the
+// host (:466-471); the rules use do, conj(do), do_not and -conj(do_not).
+struct factors {
+    mag_t d, dc, dn, ndnc;
+};
+
+// ---------------------------------------------------- erase_create / coin
+// erase_create (:459-532): a site is a node with left == right;
+// coin (:534-605): a site is a node with left != right.  Children = 2^sites
+// (u32, wraps to 0 at 32 sites like the reference's uint).  Per site, in node
+// order, using child_id bits LSB first: bit 1 flips both bits and multiplies
+// by conj? conj(do) : do; bit 0 multiplies by conj? -conj(do_not) : do_not,
+// with conj = both set (erase_create) or left set (coin).
+template <bool ON_XOR>
+struct flip_rule {
+    factors f;
+
+    QD_HD static bool site(bool l, bool r) { return ON_XOR ? (l != r) : (l == r); }
+    QD_HD static bool conj_of(bool l, bool r) { return ON_XOR ? l : (l && r); }
+
+    QD_HD void get_num_child(const char *pb, const char *pe, uint32_t &num_child,
+                             uint32_t &max_child_size) const {
+        max_child_size = (uint32_t)(pe - pb);
+        int n = num_nodes(pb);
+        uint32_t nc = 1;
+        for (int i = 0; i < n; ++i)
+            if (site(L(pb, i), R(pb, n, i))) nc *= 2;
+        num_child = nc;
+    }
+    QD_HD void apply(const char *pb, int n, uint32_t cid, mag_t *mag, char *cb, uint64_t *lh,
+                     uint64_t *rh) const {
+        for (int i = 0; i < n; ++i) {
+            bool l = L(pb, i), r = R(pb, n, i);
+            if (site(l, r)) {
+                bool c = conj_of(l, r);
+                if (cid & 1) {
+                    if (mag) *mag = cmul(*mag, c ? f.dc : f.d);
+                    l = !l;
+                    r = !r;
+                    if (cb) {
+                        cb[2 + i] = l;
+                        cb[2 + n + i] = r;
+                    }
+                } else if (mag) {
+                    *mag = cmul(*mag, c ? f.ndnc : f.dn);
+                }
+                cid >>= 1;
+            }
+            if (lh) {
+                if (l) hash_combine(*lh, (uint64_t)i);
+                if (r) hash_combine(*rh, (uint64_t)i);
+            }
+        }
+    }
+    QD_HD void populate_child(const char *pb, const char *pe, char *cb, uint32_t child_id,
+                              uint32_t &size, mag_t &mag) const {
+        size = (uint32_t)(pe - pb);
+        copy_bytes(cb, pb, size);
+        apply(pb, num_nodes(pb), child_id, &mag, cb, nullptr, nullptr);
+    }
+    QD_HD void populate_child_simple(const char *pb, const char *pe, char *cb,
+                                     uint32_t child_id) const {
+        copy_bytes(cb, pb, (uint32_t)(pe - pb));
+        apply(pb, num_nodes(pb), child_id, nullptr, cb, nullptr, nullptr);
+    }
+    QD_HD uint64_t hasher(const char *b, const char *) const { return hash_graph(b); }
+    QD_HD uint64_t hash_child(const char *pb, const char *pe, uint32_t child_id, uint32_t &size,
+                              mag_t &mag) const {
+        size = (uint32_t)(pe - pb);
+        int n = num_nodes(pb);
+        uint64_t lh = 0, rh = 0, nh = 0;
+        apply(pb, n, child_id, &mag, nullptr, &lh, &rh);
+        const char *nm = names(pb, n);
+        for (int i = 0; i < n; ++i) hash_combine(nh, node_hash(nm, name_begin(pb, n, i)));
+        hash_combine(nh, lh);
+        hash_combine(nh, rh);
+        return nh;
+    }
+};
+using erase_create = flip_rule<false>;
+using coin = flip_rule<true>;
+
+// ------------------------------------------------------------ split_merge
+// split_merge, :607-1036.  Sites: a split at node i (left && right) or a
+// merge of nodes i, i+1 (left_i && right_{i+1} && !left_{i+1}); the wrap
+// sites are a split of node 0 and a merge of nodes n-1 and 0.  The child's
+// nodes are produced in increasing index order by `walk`, which hands each
+// (index, left, right, name operation) to a sink: a byte writer for
+// populate_child, a hash accumulator for hash_child.
+struct split_merge {
+    factors f;
+
+    QD_HD static void wrap_sites(const char *p, int n, bool &first_split, bool &last_merge) {
+        last_merge = false;
+        first_split = L(p, 0) && R(p, n, 0);
+        if (!first_split && n > 1) last_merge = R(p, n, 0) && L(p, n - 1) && !R(p, n, n - 1);
+    }
+
+    QD_HD void get_num_child(const char *pb, const char *pe, uint32_t &num_child,
+                             uint32_t &max_child_size) const {
+        max_child_size = 4 * (uint32_t)(pe - pb);
+        int n = num_nodes(pb);
+        bool fs, lm;
+        wrap_sites(pb, n, fs, lm);
+        uint32_t nc = (fs || lm) ? 2 : 1;
+        for (int i = fs; i < n - lm; ++i) {
+            bool s, m;
+            get_operations(pb, n, i, s, m);
+            if (s || m) nc *= 2;
+        }
+        num_child = nc;
+    }
+
+    // first pass (:647-700): wrap decisions, child node count, magnitude
+    struct plan {
+        bool fs, lm;
+        int n, cn;
+        uint32_t cid;  // child id with the wrap bits consumed
+    };
+    QD_HD plan make_plan(const char *p, uint32_t cid, mag_t *mag) const {
+        plan pl;
+        int n = pl.n = num_nodes(p);
+        bool fs, lm;
+        wrap_sites(p, n, fs, lm);
+        fs = fs && (cid & 1);
+        if (fs) {
+            if (mag) *mag = cmul(*mag, f.d);
+            cid >>= 1;
+        }
+        if (lm) {
+            if (cid & 1) {
+                if (mag) *mag = cmul(*mag, f.dc);
+            } else {
+                lm = false;
+                if (mag) *mag = cmul(*mag, f.ndnc);
+            }
+            cid >>= 1;
+        }
+        int cn = n + fs - lm;
+        uint32_t bits = cid;
+        for (int i = fs + lm; i < n - lm; ++i) {
+            bool s, m;
+            get_operations(p, n, i, s, m);
+            if (!(s || m)) continue;
+            if (bits & 1) {
+                cn += (int)s - (int)m;
+                if (mag) *mag = cmul(*mag, s ? f.d : f.dc);
+            } else if (mag) {
+                *mag = cmul(*mag, s ? f.dn : f.ndnc);
+            }
+            bits >>= 1;
+        }
+        pl.fs = fs;
+        pl.lm = lm;
+        pl.cn = cn;
+        pl.cid = cid;
+        return pl;
+    }
+
+    // second pass (:702-845)
+    template <class Sink>
+    QD_HD static void walk(const char *p, const plan &pl, Sink &sink) {
+        const int n = pl.n, cn = pl.cn;
+        const bool fs = pl.fs, lm = pl.lm;
+        uint32_t cid = pl.cid;
+        const char *pn = names(p, n);
+        bool overflow = false;
+        if (fs) {
+            bool most_left_zero = true;
+            if (node_rot(pn, 0) >= 0 && node_hmlz(pn, 1) > 0) most_left_zero = false;
+            int e0 = name_begin(p, n, 1);
+            if (most_left_zero) {
+                sink.emit(0, true, false, OP_LEFT, 0, e0, 0, 0);
+                sink.emit(1, false, true, OP_RIGHT, 0, e0, 0, 0);
+            } else {
+                overflow = true;
+                sink.emit(0, false, true, OP_RIGHT, 0, e0, 0, 0);
+            }
+        }
+        if (lm)
+            sink.emit(0, true, true, OP_MERGE, name_begin(p, n, n - 1), name_begin(p, n, n), 0,
+                      name_begin(p, n, 1));
+        int off = (int)fs - (int)overflow;
+        for (int i = fs + lm; i < n - lm; ++i) {
+            bool s, m;
+            get_operations(p, n, i, s, m);
+            bool taken = false;
+            if (s || m) {
+                taken = cid & 1;
+                if (taken) {
+                    int b = name_begin(p, n, i), e = name_begin(p, n, i + 1);
+                    if (s) {
+                        sink.emit(i + off, true, false, OP_LEFT, b, e, 0, 0);
+                        sink.emit(i + off + 1, false, true, OP_RIGHT, b, e, 0, 0);
+                    } else {
+                        sink.emit(i + off, true, true, OP_MERGE, b, e, e, name_begin(p, n, i + 2));
+                    }
+                    off += (int)s - (int)m;
+                    i += m;
+                }
+                cid >>= 1;
+            }
+            if (!taken)
+                sink.emit(i + off, L(p, i), R(p, n, i), OP_COPY, name_begin(p, n, i),
+                          name_begin(p, n, i + 1), 0, 0);
+        }
+        if (overflow) sink.emit(cn - 1, true, false, OP_LEFT, 0, name_begin(p, n, 1), 0, 0);
+    }
+
+    struct byte_sink {
+        const char *pn;
+        char *c;
+        int cn;
+        char *cnm;
+        QD_HD void emit(int k, bool l, bool r, int op, int b1, int e1, int b2, int e2) {
+            c[2 + k] = l;
+            c[2 + cn + k] = r;
+            int d = ld_u16(c + 2 + 2 * cn + 2 * k);
+            int e = write_name(pn, cnm, d, op, b1, e1, b2, e2);
+            st_u16(c + 2 + 2 * cn + 2 * (k + 1), (uint16_t)e);
+        }
+    };
+    struct hash_sink {
+        const char *pn;
+        uint64_t lh, rh, nh;
+        int len;
+        QD_HD void emit(int k, bool l, bool r, int op, int b1, int e1, int b2, int e2) {
+            if (l) hash_combine(lh, (uint64_t)k);
+            if (r) hash_combine(rh, (uint64_t)k);
+            int ln;
+            hash_combine(nh, name_root_hash(pn, op, b1, e1, b2, e2, ln));
+            len += ln;
+        }
+    };
+
+    QD_HD void build(const char *p, char *c, uint32_t child_id, mag_t *mag, uint32_t *size) const {
+        plan pl = make_plan(p, child_id, mag);
+        st_u16(c, (uint16_t)pl.cn);
+        st_u16(c + 2 + 2 * pl.cn, 0);
+        byte_sink s{names(p, pl.n), c, pl.cn, names(c, pl.cn)};
+        walk(p, pl, s);
+        if (size) *size = 4 + 4 * (uint32_t)pl.cn + 16 * (uint32_t)ld_u16(c + 2 + 2 * pl.cn + 2 * pl.cn);
+    }
+    QD_HD void populate_child(const char *pb, const char *, char *cb, uint32_t child_id,
+                              uint32_t &size, mag_t &mag) const {
+        build(pb, cb, child_id, &mag, &size);
+    }
+    QD_HD void populate_child_simple(const char *pb, const char *, char *cb, uint32_t child_id) const {
+        build(pb, cb, child_id, nullptr, nullptr);
+    }
+    QD_HD uint64_t hasher(const char *b, const char *) const { return hash_graph(b); }
+    QD_HD uint64_t hash_child(const char *pb, const char *, uint32_t child_id, uint32_t &size,
+                              mag_t &mag) const {
+        plan pl = make_plan(pb, child_id, &mag);
+        hash_sink s{names(pb, pl.n), 0, 0, 0, 0};
+        walk(pb, pl, s);
+        hash_combine(s.nh, s.lh);
+        hash_combine(s.nh, s.rh);
+        size = 4 + 4 * (uint32_t)pl.cn + 16 * (uint32_t)s.len;
+        return s.nh;
+    }
+};
+
+// step / reversed_step modifiers, :443-457: rotate `left` one place towards
+// index 0 and `right` one place away from it (step), or the reverse.
+template <bool REVERSED>
+struct step_mod {
+    QD_HD void operator()(char *b, char *, mag_t &) const {
+        int n = num_nodes(b);
+        if (n <= 0) return;
+        char *l = b + 2, *r = b + 2 + n;
+        char *a = REVERSED ? r : l;  // rotated towards 0
+        char *z = REVERSED ? l : r;  // rotated away from 0
+        char a0 = a[0];
+        for (int i = 0; i + 1 < n; ++i) a[i] = a[i + 1];
+        a[n - 1] = a0;
+        char zl = z[n - 1];
+        for (int i = n - 1; i > 0; --i) z[i] = z[i - 1];
+        z[0] = zl;
+    }
+};
+using step = step_mod<false>;
+using reversed_step = step_mod<true>;
+
+}  // namespace qd::qcgd

@@ -1,0 +1,75 @@
+// Host build of the device rule headers (quids_gb300/csrc/rules_*.cuh) for
+// CPU tests: the same source the GPU kernels instantiate, compiled by g++,
+// exposed through a small C interface so tests can compare every rule
+// callback with the oracle on the CPU.
+#include <cstdint>
+#include "../../quids_gb300/csrc/rules_qc.cuh"
+#include "../../quids_gb300/csrc/rules_qcgd.cuh"
+#include <cmath>
+#include <complex>
+
+using namespace qd;
+
+namespace {
+qcgd::factors factors(const double *p) {
+    std::complex<double> d = std::polar(std::sin(p[0]), p[1]);
+    std::complex<double> dn = std::polar(std::cos(p[0]), p[2]);
+    std::complex<double> ndnc = -std::conj(dn);
+    return {{d.real(), d.imag()}, {d.real(), -d.imag()}, {dn.real(), dn.imag()}, {ndnc.real(), ndnc.imag()}};
+}
+template <class F> int with_rule(int kind, const double *p, F f) {
+    switch (kind) {
+    case 1: { rules::hadamard h{(uint64_t)p[0], 1 / std::sqrt(2)}; return f(h); }
+    case 2: return f(qcgd::erase_create{factors(p)});
+    case 3: return f(qcgd::coin{factors(p)});
+    case 4: return f(qcgd::split_merge{factors(p)});
+    }
+    return -1;
+}
+}
+
+extern "C" {
+int shim_num_child(int kind, const double *p, const uint8_t *o, uint32_t sz, uint32_t *nc, uint32_t *mcs) {
+    return with_rule(kind, p, [&](auto r) { r.get_num_child((const char *)o, (const char *)o + sz, *nc, *mcs); return 0; });
+}
+int shim_populate_child(int kind, const double *p, const uint8_t *o, uint32_t sz, uint32_t cid, uint8_t *c,
+                        uint32_t *csz, double *mag) {
+    return with_rule(kind, p, [&](auto r) {
+        mag_t m{mag[0], mag[1]};
+        r.populate_child((const char *)o, (const char *)o + sz, (char *)c, cid, *csz, m);
+        mag[0] = m.re; mag[1] = m.im;
+        return 0;
+    });
+}
+int shim_populate_child_simple(int kind, const double *p, const uint8_t *o, uint32_t sz, uint32_t cid, uint8_t *c) {
+    return with_rule(kind, p, [&](auto r) { r.populate_child_simple((const char *)o, (const char *)o + sz, (char *)c, cid); return 0; });
+}
+uint64_t shim_hash_child(int kind, const double *p, const uint8_t *o, uint32_t sz, uint32_t cid, uint32_t *csz,
+                         double *mag) {
+    uint64_t h = 0;
+    with_rule(kind, p, [&](auto r) {
+        mag_t m{mag[0], mag[1]};
+        h = r.hash_child((const char *)o, (const char *)o + sz, cid, *csz, m);
+        mag[0] = m.re; mag[1] = m.im;
+        return 0;
+    });
+    return h;
+}
+uint64_t shim_murmur(const uint8_t *b, uint64_t len) { return murmur64a((const char *)b, len); }
+uint64_t shim_hash_graph(const uint8_t *b) { return qcgd::hash_graph((const char *)b); }
+int shim_modifier(int kind, const double *p, uint8_t *o, uint32_t sz, double *mag) {
+    mag_t m{mag[0], mag[1]};
+    char *b = (char *)o, *e = b + sz;
+    switch (kind) {
+    case 1: rules::cnot{(uint64_t)p[0], (uint64_t)p[1]}(b, e, m); break;
+    case 2: rules::xgate{(uint64_t)p[0]}(b, e, m); break;
+    case 3: rules::ygate{(uint64_t)p[0]}(b, e, m); break;
+    case 4: rules::zgate{(uint64_t)p[0]}(b, e, m); break;
+    case 5: qcgd::step{}(b, e, m); break;
+    case 6: qcgd::reversed_step{}(b, e, m); break;
+    default: return -1;
+    }
+    mag[0] = m.re; mag[1] = m.im;
+    return 0;
+}
+}

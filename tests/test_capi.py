@@ -1,0 +1,61 @@
+"""The C ABI library: it builds for sm_103a, loads, and exports every
+function include/quids_gpu.h declares.  No compute call is made here."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import pytest
+
+from quids_gb300 import build as qbuild
+from quids_gb300 import capi
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "quids_gpu.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(quids_gpu_\w+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def lib_path():
+    return qbuild.build()
+
+
+def test_header_declares_the_abi():
+    names = declared_functions()
+    assert "quids_gpu_simulate" in names and "quids_gpu_apply_modifier" in names
+    assert set(names) == set(capi.EXPORTS)
+
+
+def test_library_exports_every_declared_symbol(lib_path):
+    out = subprocess.run(["nm", "-D", "--defined-only", lib_path], capture_output=True, text=True, check=True).stdout
+    exported = set(re.findall(r"\bT (quids_gpu_\w+)", out))
+    missing = set(declared_functions()) - exported
+    assert not missing, f"not exported: {sorted(missing)}"
+
+
+def test_library_loads_with_ctypes(lib_path):
+    L = capi.load()
+    for name in declared_functions():
+        assert getattr(L, name) is not None
+    assert L.quids_gpu_status_string(-3) == b"collision table full"
+
+
+def test_sm103a_cubin_embedded(lib_path):
+    r = subprocess.run(["cuobjdump", "--list-elf", lib_path], capture_output=True, text=True)
+    if r.returncode != 0:
+        pytest.skip("cuobjdump unavailable")
+    assert "sm_103a" in r.stdout
+
+
+def test_no_device_is_an_error_not_a_crash(lib_path):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    L = capi.load()
+    h = C.c_void_p()
+    assert L.quids_gpu_ctx_create(0, C.byref(h)) == -8

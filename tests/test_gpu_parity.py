@@ -1,0 +1,226 @@
+"""GPU parity: the CUDA rule step through the C ABI against the oracle and the
+golden fixtures of the reference.  Every comparison is per step from an
+identical input state (set parity keyed on bytes, magnitudes within 1e-12
+relative floored at 1e-9, a tie band at truncation cutoffs)."""
+import math
+
+import numpy as np
+import pytest
+
+import quids_gb300 as quids
+from quids_gb300 import capi, workloads as W
+from quids_gb300 import rules
+from tests.parity import assert_state_parity, canon, is_qcgd_kind, load_golden, packed
+
+pytestmark = pytest.mark.gpu
+U64_MAX = capi.U64_MAX
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = quids.Context(0)
+    yield c
+    c.close()
+
+
+@pytest.fixture(autouse=True)
+def knobs():
+    quids.tolerance, quids.align_byte_length = 1e-18, 8
+    yield
+    quids.tolerance, quids.align_byte_length = 1e-18, 8
+
+
+def gpu_step(ctx, p, kind, params, maxn=U64_MAX, flags=0):
+    a, b = quids.it_t(ctx, p), quids.it_t(ctx)
+    sy = quids.sy_it_t()
+    quids.simulate(a, quids.rule_from(True, kind, params), b, sy, maxn, flags=flags)
+    return b, sy
+
+
+def test_golden_steps(ctx):
+    z, man = load_golden()
+    for k, case in enumerate(man["steps"]):
+        quids.tolerance, quids.align_byte_length = case["tolerance"], case["align"]
+        maxn = int(case["max"])
+        for flags in (0, capi.FLAG_NO_FAST_HASH):
+            b, sy = gpu_step(ctx, packed(z, f"step{k}_in"), case["kind"], case["params"], maxn, flags)
+            what = f"{case['name']} flags={flags}"
+            assert sy.num_object == case["num_object"], what
+            assert sy.num_object_after_interferences == case["num_object_after_interferences"], what
+            got = b.download()
+            assert_state_parity(got, packed(z, f"step{k}_out"), is_qcgd_kind(case["kind"]),
+                                truncated=maxn < case["num_object_after_interferences"], what=what)
+            assert b.total_proba == pytest.approx(case["total_proba"], rel=1e-12, abs=1e-300), what
+            # layout: offsets follow the requested alignment
+            objects, begin, size, _ = got
+            al = case["align"]
+            if al > 1 and len(size):
+                assert all(int(x) % al == 0 for x in begin), what
+
+
+def test_golden_children_and_hashes(ctx, port):
+    """Every child the GPU rule produces (bytes, magnitude, hash) against the
+    reference's populate_child on the same parents."""
+    z, man = load_golden()
+    for ri, c in enumerate(man["children"]):
+        pp = packed(z, f"children{ri}_parents")
+        it = quids.it_t(ctx, pp)
+        children, hashes, mags = quids.rule_children(it, quids.rule_from(True, c["kind"], c["params"]))
+        parents, _ = W.unpack(pp)
+        start = {}
+        idx = 0
+        for pi, g in enumerate(parents):
+            start[pi] = idx
+            idx += port.num_child(c["kind"], c["params"], g)[0]
+        assert idx == len(children)
+        outs, omags = W.unpack(packed(z, f"children{ri}_out"))
+        for o, m, pi, cid in zip(outs, omags, z[f"children{ri}_pid"], z[f"children{ri}_cid"]):
+            k = start[int(pi)] + int(cid)
+            got = children[k]
+            mk = W.graph_padding_mask(o) if c["kind"] != 1 else np.ones(len(o), bool)
+            assert len(got) == len(o)
+            assert (np.frombuffer(got, np.uint8)[mk] == np.frombuffer(o, np.uint8)[mk]).all()
+            assert complex(mags[k]) == m  # same rounding as the reference: bit-exact
+            href = port.hash_bytes(o) if c["kind"] == 1 else port.qcgd_hash_graph(o)
+            assert int(hashes[k]) == href
+
+
+def test_default_hasher_on_gpu_is_std_hash(ctx):
+    z, _ = load_golden()
+    data, lens, vals = z["hash_bytes_data"], z["hash_bytes_len"], z["hash_bytes_value"]
+    objs, off = [], 0
+    for L in lens:
+        objs.append(data[off: off + int(L)].tobytes())
+        off += int(L)
+    for al in (8, 1):
+        it = quids.it_t(ctx, W.pack(objs, [1.0] * len(objs), al))
+        h = quids.state_hash(it, rules.hadamard(0))
+        assert [int(x) for x in h] == [int(v) for v in vals]
+
+
+def test_graph_hash_on_gpu(ctx):
+    z, _ = load_golden()
+    for al in (8, 0):
+        objs, _ = W.unpack(packed(z, "graphs"))
+        it = quids.it_t(ctx, W.pack(objs, [1.0] * len(objs), al))
+        h = quids.state_hash(it, rules.coin(0.5))
+        assert [int(x) for x in h] == [int(v) for v in z["graphs_hash"]]
+
+
+def test_modifiers(ctx, port):
+    rng = W.Rng(9)
+    objs = list(dict.fromkeys(bytes(rng.below(2) for _ in range(11)) for _ in range(500)))
+    mags = np.array([complex(rng.uniform(-1, 1), rng.uniform(-1, 1)) for _ in objs])
+    p = W.pack(objs, mags, 8)
+    for kind, params in [(1, (2, 5)), (2, (3,)), (3, (4,)), (4, (0,)), (4, (10,))]:
+        st = port.new_state(p)
+        port.modifier(st, kind, params)
+        it = quids.it_t(ctx, p)
+        quids.simulate(it, quids.rule_from(False, kind, params))
+        g, e = it.download(), st.store()
+        assert np.array_equal(g[0], e[0]) and np.array_equal(g[1], e[1])
+        assert np.array_equal(g[3], e[3])
+    graphs = [W.random_graph(n, rng) for n in range(1, 20)]
+    gp = W.pack(graphs, [1.0] * len(graphs), 8)
+    for kind in (5, 6):
+        st = port.new_state(gp)
+        port.modifier(st, kind, ())
+        it = quids.it_t(ctx, gp)
+        quids.simulate(it, quids.rule_from(False, kind, ()))
+        assert np.array_equal(it.download()[0], st.store()[0])
+
+
+def _trajectory(ctx, port, p, gates, maxn, qcgd, check_every=True):
+    a_gpu = quids.it_t(ctx, p)
+    a_cpu = port.new_state(p)
+    for gi, g in enumerate(gates):
+        if g.kind == "mod":
+            quids.simulate(a_gpu, quids.rule_from(False, g.code, g.params))
+            port.modifier(a_cpu, g.code, g.params)
+            continue
+        # parity per step from an identical input: feed the GPU's input to the oracle
+        inp = a_gpu.download()
+        ref_in = port.new_state(inp)
+        ref_out = port.new_state()
+        nc, nu = port.simulate(ref_in, g.code, g.params, ref_out, maxn)
+        b_gpu = quids.it_t(ctx)
+        sy = quids.sy_it_t()
+        quids.simulate(a_gpu, quids.rule_from(True, g.code, g.params), b_gpu, sy, maxn)
+        assert (sy.num_object, sy.num_object_after_interferences) == (nc, nu), f"gate {gi}"
+        if check_every or gi == len(gates) - 1:
+            assert_state_parity(b_gpu.download(), ref_out.store(), qcgd, truncated=maxn < nu, what=f"gate {gi}")
+        assert b_gpu.total_proba == pytest.approx(ref_out.total_proba, rel=1e-12)
+        a_gpu = b_gpu
+    return a_gpu
+
+
+def test_circuit_small_full_trajectory(ctx, port):
+    """12 qubits, Hadamard on each then 40 seeded gates, no truncation:
+    set-exact after every gate against the oracle, and against the golden
+    reference trajectory."""
+    port.set_globals(1e-18, True, 8)
+    _trajectory(ctx, port, W.qc_zero_state(12), W.circuit_small(0), U64_MAX, False)
+
+
+def test_circuit_layers_truncated(ctx, port):
+    """24 qubits, seeded layers, max_num_object 2^12 (truncation exercised)."""
+    port.set_globals(1e-18, True, 8)
+    gates = [g for layer in W.circuit_layers(0)[:4] for g in layer]
+    _trajectory(ctx, port, W.qc_zero_state(24), gates, 1 << 12, False, check_every=False)
+
+
+def test_qcgd_steps(ctx, port):
+    """QCGD step/coin/split_merge/erase_create on an 8-node graph, 2 steps."""
+    port.set_globals(1e-18, True, 8)
+    _trajectory(ctx, port, W.qcgd_single_state(8, seed=1), W.qcgd_step_rules() * 2, U64_MAX, True)
+
+
+def test_qcgd_truncated(ctx, port):
+    port.set_globals(1e-18, True, 8)
+    _trajectory(ctx, port, W.qcgd_single_state(9, seed=4), W.qcgd_step_rules() * 2, 2000, True)
+
+
+def test_deterministic(ctx):
+    p = W.qcgd_single_state(9, seed=2)
+    outs = []
+    for _ in range(2):
+        it = quids.it_t(ctx, p)
+        for g in W.qcgd_step_rules() * 2:
+            if g.kind == "mod":
+                quids.simulate(it, quids.rule_from(False, g.code, g.params))
+            else:
+                nxt = quids.it_t(ctx)
+                quids.simulate(it, quids.rule_from(True, g.code, g.params), nxt, quids.sy_it_t(), 5000)
+                it = nxt
+        outs.append(it.download())
+    for a, b in zip(*outs):
+        assert np.array_equal(a, b)
+
+
+def test_empty_and_zero_children(ctx):
+    a, b = quids.it_t(ctx), quids.it_t(ctx)
+    sy = quids.sy_it_t()
+    quids.simulate(a, rules.hadamard(0), b, sy)
+    assert b.num_object == 0 and sy.num_object == 0 and b.total_proba == 0
+    # every child cancels: the state empties
+    p = W.pack([bytes([0]), bytes([1])], [1 / math.sqrt(2), -1 / math.sqrt(2)], 8)
+    # H|0> - H|1> = sqrt2 |1>: one survivor
+    b2, sy2 = gpu_step(ctx, p, 1, (0,))
+    assert sy2.num_object == 4 and sy2.num_object_after_interferences == 1 and b2.num_object == 1
+
+
+def test_bad_arguments_are_errors(ctx):
+    a = quids.it_t(ctx, W.qc_zero_state(4))
+    with pytest.raises(capi.QuidsError):
+        quids.simulate(a, rules.hadamard(0), a, quids.sy_it_t())
+    b = quids.it_t(ctx)
+    quids.simple_truncation = False
+    try:
+        with pytest.raises(capi.QuidsError) as e:
+            quids.simulate(a, rules.hadamard(0), b, quids.sy_it_t())
+        assert e.value.code == -9
+    finally:
+        quids.simple_truncation = True
+    # the context stays usable after an error
+    quids.simulate(a, rules.hadamard(0), b, quids.sy_it_t())
+    assert b.num_object == 2
