@@ -114,6 +114,8 @@ class Context:
         self.device = device
 
     def close(self):
+        """Destroys the context; its states are released with it (their
+        handles stay safe to drop afterwards)."""
         if getattr(self, "h", None):
             self.lib.quids_gpu_ctx_destroy(self.h)
             self.h = None

@@ -115,6 +115,15 @@ int quids_gpu_ctx_destroy(quids_gpu_ctx *ctx) {
     if (!ctx) return QUIDS_ERR_BAD_ARG;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (quids_gpu_state *st : ctx->states) {
+        release(st->objects);
+        release(st->begin);
+        release(st->size);
+        release(st->mag);
+        st->n = st->nbytes = 0;
+        st->ctx = nullptr;
+    }
+    ctx->states.clear();
     for (auto &b : ctx->buf) release(b);
     if (ctx->d_words) cudaFree(ctx->d_words);
     if (ctx->h_words) cudaFreeHost(ctx->h_words);
@@ -160,14 +169,20 @@ int quids_gpu_state_create(quids_gpu_ctx *ctx, quids_gpu_state **out) {
     auto *st = new (std::nothrow) quids_gpu_state();
     if (!st) return QUIDS_ERR_OOM;
     st->ctx = ctx;
+    ctx->states.insert(st);
     *out = st;
     return QUIDS_OK;
 }
 
 int quids_gpu_state_destroy(quids_gpu_state *st) {
     if (!st) return QUIDS_ERR_BAD_ARG;
+    if (!st->ctx) {  // its context is gone and has already released the memory
+        delete st;
+        return QUIDS_OK;
+    }
     cudaSetDevice(st->ctx->device);
     cudaStreamSynchronize(st->ctx->stream);
+    st->ctx->states.erase(st);
     release(st->objects);
     release(st->begin);
     release(st->size);
@@ -178,7 +193,7 @@ int quids_gpu_state_destroy(quids_gpu_state *st) {
 
 int quids_gpu_state_upload(quids_gpu_state *st, uint64_t n, const uint8_t *objects, const uint64_t *begin,
                            const uint32_t *size, const double *magnitude, uint64_t num_bytes) {
-    if (!st) return QUIDS_ERR_BAD_ARG;
+    if (!st || !st->ctx) return QUIDS_ERR_BAD_ARG;
     if (n && (!begin || !size || !magnitude)) return QUIDS_ERR_BAD_ARG;
     if (num_bytes && !objects) return QUIDS_ERR_BAD_ARG;
     for (uint64_t i = 0; i < n; ++i)
@@ -222,7 +237,7 @@ int quids_gpu_state_total_proba(const quids_gpu_state *st, double *p) {
 
 int quids_gpu_state_download(quids_gpu_state *st, uint8_t *objects, uint64_t *begin, uint32_t *size,
                              double *magnitude) {
-    if (!st) return QUIDS_ERR_BAD_ARG;
+    if (!st || !st->ctx) return QUIDS_ERR_BAD_ARG;
     quids_gpu_ctx *ctx = st->ctx;
     QD_CUDA(cudaSetDevice(ctx->device));
     cudaStream_t s = ctx->stream;

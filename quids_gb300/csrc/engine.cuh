@@ -10,6 +10,7 @@
 #include <cstdint>
 #include <cstring>
 #include <type_traits>
+#include <unordered_set>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -79,10 +80,13 @@ struct quids_gpu_ctx {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaEvent_t ev_stage[16] = {};  // start/end of the 8 stages of a step
     uint64_t launches = 0;          // kernels launched by this context
+    // live states: destroying the context releases their device memory and
+    // orphans them, so states may be destroyed after their context
+    std::unordered_set<struct quids_gpu_state *> states;
 };
 
 struct quids_gpu_state {
-    quids_gpu_ctx *ctx = nullptr;
+    quids_gpu_ctx *ctx = nullptr;  // null once the context is destroyed
     uint64_t n = 0;
     uint64_t nbytes = 0;
     double total_proba = 1;
