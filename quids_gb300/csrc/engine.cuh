@@ -180,10 +180,10 @@ inline int launched(quids_gpu_ctx *ctx, uint64_t n = 1) {
     return cuda_status(cudaGetLastError());
 }
 
-__global__ void k_set_word(uint64_t *w, uint64_t v) { *w = v; }
+static __global__ void k_set_word(uint64_t *w, uint64_t v) { *w = v; }
 
 // moves a sticky modifier error into the step's status word
-__global__ void k_take_status(int *src, uint64_t *status_word) {
+static __global__ void k_take_status(int *src, uint64_t *status_word) {
     int e = *src;
     if (e) {
         *(int *)status_word = e;
@@ -492,7 +492,7 @@ struct key_parent_index_ties {
     }
 };
 
-__global__ void k_select_init(prim::select_state *st, const uint64_t *d_n, uint64_t k) {
+static __global__ void k_select_init(prim::select_state *st, const uint64_t *d_n, uint64_t k) {
     prim::select_state s{};
     s.k_rem = k;
     s.active = k < *d_n ? 1u : 0u;
@@ -500,7 +500,7 @@ __global__ void k_select_init(prim::select_state *st, const uint64_t *d_n, uint6
     st[1] = prim::select_state{};
 }
 // second selection among threshold ties, only when not all ties are kept
-__global__ void k_select_ties_init(prim::select_state *st) {
+static __global__ void k_select_ties_init(prim::select_state *st) {
     prim::select_state s{};
     s.k_rem = st[0].k_rem;
     s.active = (st[0].active && st[0].k_rem < st[0].n_equal) ? 1u : 0u;

@@ -250,7 +250,7 @@ __global__ void __launch_bounds__(kThreads) k_radix_hist(K kf, const uint64_t *d
         if (sh[i]) atomicAdd(&hist[i], (unsigned long long)sh[i]);
 }
 
-__global__ void k_radix_pick(select_state *st, unsigned long long *hist, int shift, bool descending) {
+static __global__ void k_radix_pick(select_state *st, unsigned long long *hist, int shift, bool descending) {
     // one warp: cumulative counts in preference order
     if (threadIdx.x != 0) return;
     if (!st->active) return;
@@ -297,7 +297,7 @@ __device__ __forceinline__ void fix_atomic_add(unsigned long long *w, fix128 v) 
 // Inserts every child: slot_of[c] = its group's slot; rep = min child index;
 // acc += magnitude (exact fixed point with scale 2^-F, F from the largest
 // component and the child count).
-__global__ void __launch_bounds__(kThreads) k_table_insert(table t, const uint64_t *hash, const double2 *mag,
+static __global__ void __launch_bounds__(kThreads) k_table_insert(table t, const uint64_t *hash, const double2 *mag,
                                                             const uint64_t *d_n, const unsigned long long *d_maxabs,
                                                             uint32_t *slot_of, int *err) {
     const uint64_t n = *d_n;
@@ -343,7 +343,7 @@ __global__ void __launch_bounds__(kThreads) k_table_insert(table t, const uint64
 constexpr int kNormBlocks = 512;
 
 // partial[b] = sum of norms over the fixed chunk of block b (fixed order)
-__global__ void __launch_bounds__(kThreads) k_norm_partial(const double2 *mag, const uint64_t *d_n, double *partial) {
+static __global__ void __launch_bounds__(kThreads) k_norm_partial(const double2 *mag, const uint64_t *d_n, double *partial) {
     __shared__ double sm[kThreads];
     const uint64_t n = *d_n;
     const uint64_t chunk = (n + gridDim.x - 1) / gridDim.x;
@@ -364,7 +364,7 @@ __global__ void __launch_bounds__(kThreads) k_norm_partial(const double2 *mag, c
 }
 
 // total = sum of partials (fixed order); factor = sqrt(total)
-__global__ void k_norm_final(const double *partial, int np, double *d_total, double *d_factor) {
+static __global__ void k_norm_final(const double *partial, int np, double *d_total, double *d_factor) {
     __shared__ double sm[kNormBlocks];
     for (int i = threadIdx.x; i < kNormBlocks; i += blockDim.x) sm[i] = i < np ? partial[i] : 0.0;
     __syncthreads();
@@ -379,7 +379,7 @@ __global__ void k_norm_final(const double *partial, int np, double *d_total, dou
 }
 
 // mag /= factor when factor != 1 (src/quids.hpp:1008-1013)
-__global__ void __launch_bounds__(kThreads) k_norm_scale(double2 *mag, const uint64_t *d_n, const double *d_factor) {
+static __global__ void __launch_bounds__(kThreads) k_norm_scale(double2 *mag, const uint64_t *d_n, const double *d_factor) {
     const double f = *d_factor;
     if (f == 1.0) return;
     const uint64_t n = *d_n;
