@@ -40,6 +40,7 @@ extern "C" {
 #define QUIDS_ERR_CUDA (-7)                 /* a CUDA runtime call failed */
 #define QUIDS_ERR_NO_DEVICE (-8)            /* no CUDA device */
 #define QUIDS_ERR_UNSUPPORTED (-9)          /* valid request this build does not implement */
+#define QUIDS_ERR_NOALLOC_LIMIT (-10)       /* beyond the static scratch of quids_gpu_rule_children_noalloc */
 
 /* ------------------------------------------------------- rules/modifiers */
 /* rules (classes derived from quids::rule, src/quids.hpp:105-146) */
@@ -166,6 +167,32 @@ int quids_gpu_rule_children(quids_gpu_ctx *ctx, quids_gpu_state *iteration, int 
                             const quids_gpu_rule_params *rule, uint64_t *num_children,
                             uint64_t *stride, uint8_t *child_bytes, uint64_t *hash,
                             uint32_t *size, double *magnitude);
+
+/* No counterpart in the reference.  The children enumeration of
+ * quids_gpu_rule_children for callers that must not allocate device memory:
+ * code whose device memory is all owned by another allocator (a pool or a
+ * fixed per-process budget that a stray cudaMalloc would break) and code that
+ * cannot pay the implicit device synchronisation of cudaMalloc/cudaFree.  It
+ * needs no context and allocates nothing; the caller passes device pointers
+ * to the input state (as quids_gpu_state_device_arrays gives them) and to the
+ * outputs, and a stream.  Its scratch is a static device array of
+ * QUIDS_NOALLOC_SCRATCH_BYTES (about 3 MiB) that every GPU loading this
+ * library holds until the process exits; a state of more than
+ * QUIDS_NOALLOC_MAX_PARENTS objects is rejected with QUIDS_ERR_NOALLOC_LIMIT.
+ * The first call on a device looks up the array's device address (with that
+ * device current): make that first call before any stream capture.  Calls
+ * share the array, so calls whose GPU work overlaps race on it.
+ * Call with d_child_bytes = NULL to get *num_children and *stride; then with
+ * capacity >= *num_children and buffers of capacity * stride bytes, capacity
+ * u64 hashes, capacity u32 sizes and 2 * capacity doubles.  Synchronises the
+ * stream before returning. */
+#define QUIDS_NOALLOC_MAX_PARENTS (1u << 18)
+#define QUIDS_NOALLOC_SCRATCH_BYTES 3147520u
+int quids_gpu_rule_children_noalloc(void *stream, uint64_t num_object, const uint8_t *d_objects,
+                                    const uint64_t *d_begin, const uint32_t *d_size, const double *d_magnitude,
+                                    int rule_kind, const quids_gpu_rule_params *rule, uint64_t capacity,
+                                    uint64_t *num_children, uint64_t *stride, uint8_t *d_child_bytes,
+                                    uint64_t *d_hash, uint32_t *d_child_size, double *d_child_magnitude);
 
 /* MurmurHash64A of libstdc++'s std::hash<std::string_view> (seed 0xc70f6907),
  * the reference's default hasher (src/quids.hpp:143-145), computed on the GPU

@@ -17,7 +17,7 @@ STATUS = {
     0: "ok", -1: "bad argument", -2: "device out of memory", -3: "collision table full",
     -4: "child count overflow", -5: "child larger than max_child_size bound",
     -6: "bounded device wait expired", -7: "CUDA runtime error", -8: "no CUDA device",
-    -9: "unsupported request",
+    -9: "unsupported request", -10: "beyond the static scratch of the no-allocation entry point",
 }
 FLAG_NO_FAST_HASH = 1
 
@@ -58,7 +58,7 @@ EXPORTS = [
     "quids_gpu_state_create", "quids_gpu_state_destroy", "quids_gpu_state_upload", "quids_gpu_state_num_object",
     "quids_gpu_state_num_bytes", "quids_gpu_state_total_proba", "quids_gpu_state_download",
     "quids_gpu_state_device_arrays", "quids_gpu_simulate", "quids_gpu_apply_modifier",
-    "quids_gpu_rule_children", "quids_gpu_state_hash",
+    "quids_gpu_rule_children", "quids_gpu_state_hash", "quids_gpu_rule_children_noalloc",
 ]
 
 _lib = None
@@ -106,6 +106,8 @@ def load(build_if_missing: bool = True):
     L.quids_gpu_apply_modifier.argtypes = [vp, vp, C.c_int, C.POINTER(RuleParams)]
     L.quids_gpu_rule_children.argtypes = [vp, vp, C.c_int, C.POINTER(RuleParams), u64p, u64p, vp, vp, vp, vp]
     L.quids_gpu_state_hash.argtypes = [vp, vp, C.c_int, C.POINTER(RuleParams), vp]
+    L.quids_gpu_rule_children_noalloc.argtypes = [vp, C.c_uint64, vp, vp, vp, vp, C.c_int, C.POINTER(RuleParams),
+                                                  C.c_uint64, u64p, u64p, vp, vp, vp, vp]
     _lib = L
     return L
 

@@ -70,6 +70,7 @@ const char *quids_gpu_status_string(int s) {
     case QUIDS_ERR_CUDA: return "CUDA runtime error";
     case QUIDS_ERR_NO_DEVICE: return "no CUDA device";
     case QUIDS_ERR_UNSUPPORTED: return "unsupported request";
+    case QUIDS_ERR_NOALLOC_LIMIT: return "beyond the static scratch of the no-allocation entry point";
     }
     return "unknown status";
 }

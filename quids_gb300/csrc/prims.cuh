@@ -75,7 +75,7 @@ struct lookback {
 };
 
 // Exclusive prefix of tile `tile` given its aggregate; all threads call it.
-__device__ uint64_t tile_prefix(const lookback &lb, uint32_t tile, uint64_t aggregate, uint64_t *bcast) {
+static __device__ uint64_t tile_prefix(const lookback &lb, uint32_t tile, uint64_t aggregate, uint64_t *bcast) {
     if (threadIdx.x < 32) {
         const int lane = threadIdx.x;
         uint64_t prefix = 0;
