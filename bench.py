@@ -117,7 +117,7 @@ class Clocks:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def run_step_gpu(ctx, quids, wl, init_state, stats_acc=None):
+def run_step_gpu(ctx, quids, wl, init_state, stats_acc=None, flags=0):
     """One bench step on device-resident input: returns (children, final it_t)."""
     it = init_state
     children = 0
@@ -129,7 +129,7 @@ def run_step_gpu(ctx, quids, wl, init_state, stats_acc=None):
             continue
         nxt = spare.pop() if spare else quids.it_t(ctx)
         in_bytes = it.num_bytes
-        st = quids.simulate(it, r, nxt, None, wl["max"])
+        st = quids.simulate(it, r, nxt, None, wl["max"], flags=flags)
         st["_in_bytes"] = in_bytes
         children += st["num_object"]
         if stats_acc is not None:
@@ -150,12 +150,12 @@ def stage_bytes(st):
     return {
         0: 12.0 * st["num_parents"] + 8.0 * NP + sp,                   # num_child: sizes/begins/bytes, offsets
         1: sp + 36.0 * NP + 28.0 * NC,                                  # symbolic: parents in, 28 B/child out
-        2: 28.0 * NC + 48.0 * NU + 48.0 * M,                            # insert: records in, slots, table init
-        3: 12.0 * NC + 80.0 * NU,                                       # compaction: slot/rep per child, groups out
-        4: 16.0 * NU * 2 + 24.0 * NS,                                   # select passes (first pass) + survivors
-        5: 28.0 * NS,                                                   # layout scan
-        6: NS * (sbar_p + sbar_c + 40.0),                               # populate
-        7: 48.0 * NS,                                                   # normalize
+        2: 8.0 * M + 36.0 * NC + 36.0 * NU,                             # keys clear; hash+slot, slot+mag; groups
+        3: 8.0 * NC + 36.0 * NU + (44.0 * NS if NU == NS else 40.0 * NU),  # slot/rep per child; groups out
+        4: 8.0 * NU + 44.0 * NS,                                        # select (first pass) + layout of survivors
+        5: 8.0 * (NC / 2048.0),                                         # per-tile norm sums
+        6: NS * (sbar_p + sbar_c + 48.0),                               # populate + normalise magnitudes
+        7: 0.0,
     }
 
 
@@ -203,7 +203,7 @@ def ours(args, rank, world):
                 e0 = torch.cuda.Event(enable_timing=True)
                 e1 = torch.cuda.Event(enable_timing=True)
                 e0.record(stream)
-            c, _ = run_step_gpu(ctx, quids, wl, src, stats)
+            c, _ = run_step_gpu(ctx, quids, wl, src)
             with torch.cuda.stream(stream):
                 e1.record(stream)
             e1.synchronize()
@@ -212,6 +212,15 @@ def ours(args, rank, world):
     ctx.synchronize()
     t_wall = time.perf_counter() - t_wall0
     launches = ctx.lib.quids_gpu_ctx_launch_count(ctx.h) - launches0
+
+    # stage timing: the same steps again with CUDA events around every stage
+    # of every rule application (live, on the library's stream)
+    for _ in range(args.steps):
+        src = quids.it_t(ctx, init_packed)
+        with torch.cuda.stream(stream):
+            flush.fill_(1)
+        run_step_gpu(ctx, quids, wl, src, stats, flags=capi.FLAG_STAGE_TIMING)
+    ctx.synchronize()
     total_ms = sum(ms)
     if world > 1:
         t = torch.tensor([total_ms], device=f"cuda:{dev}")
@@ -228,8 +237,8 @@ def ours(args, rank, world):
             stage_t[k] += st["stage_ms"][k]
             stage_b[k] += sb[k]
     dom = max(range(8), key=lambda k: stage_t[k])
-    names = ["num_child+offsets", "symbolic", "table_insert", "group_compaction", "truncation_select",
-             "output_layout", "finalize_populate", "normalize"]
+    names = ["num_child+offsets", "symbolic", "collision_table", "group_compaction+layout",
+             "truncation+layout", "total_proba", "finalize_populate+normalize", "unused"]
     peak, peak_kind = peaks()
     achieved = stage_b[dom] / (stage_t[dom] / 1e3) / 1e9 if stage_t[dom] > 0 else 0.0
     step_bytes = sum(st["algorithmic_bytes"] for st in stats)

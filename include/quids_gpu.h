@@ -78,9 +78,14 @@ typedef struct quids_gpu_params {
     int32_t simple_truncation;   /* must be 1 (probabilistic truncation unsupported) */
     uint32_t align_byte_length;  /* quids::align_byte_length for the output state */
     double table_load_factor;    /* collision table max load; 0 -> default 0.5 */
-    uint32_t block_size;         /* threads per block for per-item kernels; 0 -> default */
-    uint32_t reserved;
+    uint32_t block_size;         /* reserved, 0 */
+    uint32_t flags;              /* QUIDS_FLAG_* */
 } quids_gpu_params;
+
+/* quids_gpu_params.flags */
+#define QUIDS_FLAG_NO_FAST_HASH 1u   /* hash children through populate_child + hasher, not hash_child */
+#define QUIDS_FLAG_STAGE_TIMING 2u   /* record per-stage CUDA events and synchronise at the end of the
+                                        step, so stats carries timings and total_proba */
 
 /* Counters of one rule step (the reference's public counters plus timing). */
 typedef struct quids_gpu_step_stats {
@@ -92,13 +97,16 @@ typedef struct quids_gpu_step_stats {
     uint64_t max_child_size;                 /* max over parents of get_num_child's bound */
     uint64_t table_capacity;                 /* collision table slots */
     uint64_t out_bytes;                      /* object bytes of next_iteration */
-    double total_proba;                      /* next_iteration.total_proba (before normalisation) */
+    double total_proba;                      /* next_iteration.total_proba (before normalisation);
+                                                NaN unless QUIDS_FLAG_STAGE_TIMING (read it from the state) */
     double algorithmic_bytes;                /* compulsory HBM traffic of this step */
-    float ms_total;                          /* device time of the step (CUDA events) */
-    /* device time per stage (CUDA events bracketing each stage's launches):
-     * 0 num_child + parent truncation + child offsets, 1 symbolic iteration,
-     * 2 collision table insert, 3 group compaction (zero elimination),
-     * 4 truncation select, 5 output layout, 6 finalize populate, 7 normalize */
+    float ms_total;                          /* device time of the step (QUIDS_FLAG_STAGE_TIMING) */
+    /* device time per stage (CUDA events bracketing each stage's launches,
+     * QUIDS_FLAG_STAGE_TIMING only): 0 num_child + parent truncation + child
+     * offsets, 1 symbolic iteration, 2 collision table (claim + accumulate),
+     * 3 group compaction (+ output layout when no truncation is possible),
+     * 4 truncation (select + compaction with output layout), 5 total
+     * probability, 6 finalize populate with normalisation, 7 unused */
     float stage_ms[8];
     uint64_t kernel_launches;                /* kernels this step launched */
 } quids_gpu_step_stats;

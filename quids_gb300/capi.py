@@ -20,6 +20,7 @@ STATUS = {
     -9: "unsupported request", -10: "beyond the static scratch of the no-allocation entry point",
 }
 FLAG_NO_FAST_HASH = 1
+FLAG_STAGE_TIMING = 2
 
 
 class QuidsError(RuntimeError):
@@ -36,7 +37,7 @@ class RuleParams(C.Structure):
 class Params(C.Structure):
     _fields_ = [("tolerance", C.c_double), ("max_num_object", C.c_uint64), ("simple_truncation", C.c_int32),
                 ("align_byte_length", C.c_uint32), ("table_load_factor", C.c_double),
-                ("block_size", C.c_uint32), ("reserved", C.c_uint32)]
+                ("block_size", C.c_uint32), ("flags", C.c_uint32)]
 
 
 class StepStats(C.Structure):

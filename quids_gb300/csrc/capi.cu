@@ -121,7 +121,9 @@ int quids_gpu_ctx_destroy(quids_gpu_ctx *ctx) {
         release(st->begin);
         release(st->size);
         release(st->mag);
+        release(st->d_total);
         st->n = st->nbytes = 0;
+        st->total_pending = false;
         st->ctx = nullptr;
     }
     ctx->states.clear();
@@ -188,6 +190,7 @@ int quids_gpu_state_destroy(quids_gpu_state *st) {
     release(st->begin);
     release(st->size);
     release(st->mag);
+    release(st->d_total);
     delete st;
     return QUIDS_OK;
 }
@@ -215,6 +218,7 @@ int quids_gpu_state_upload(quids_gpu_state *st, uint64_t n, const uint8_t *objec
     st->n = n;
     st->nbytes = num_bytes;
     st->total_proba = 1;
+    st->total_pending = false;
     return QUIDS_OK;
 }
 
@@ -232,6 +236,14 @@ int quids_gpu_state_num_bytes(const quids_gpu_state *st, uint64_t *nb) {
 
 int quids_gpu_state_total_proba(const quids_gpu_state *st, double *p) {
     if (!st || !p) return QUIDS_ERR_BAD_ARG;
+    if (st->total_pending && st->ctx) {  // written on the device by the last step
+        QD_CUDA(cudaSetDevice(st->ctx->device));
+        double v = 0;
+        QD_CUDA(cudaMemcpyAsync(&v, st->d_total.p, sizeof(double), cudaMemcpyDeviceToHost, st->ctx->stream));
+        QD_CUDA(cudaStreamSynchronize(st->ctx->stream));
+        st->total_proba = v;
+        st->total_pending = false;
+    }
     *p = st->total_proba;
     return QUIDS_OK;
 }

@@ -9,6 +9,7 @@
 #pragma once
 #include <cstdint>
 #include <cstring>
+#include <limits>
 #include <type_traits>
 #include <unordered_set>
 #include <vector>
@@ -19,8 +20,6 @@
 #include "prims.cuh"
 #include "qd_common.cuh"
 
-#define QUIDS_FLAG_NO_FAST_HASH 1u
-
 // --------------------------------------------------------------- buffers
 struct qd_dbuf {
     void *p = nullptr;
@@ -28,26 +27,24 @@ struct qd_dbuf {
 };
 
 enum qd_buf_id {
-    B_NCHILD,      // u32 [N]
-    B_CBEGIN,      // u64 [NP+1]
-    B_PIDX,        // u64 [NP] kept parents (pre-truncation)
-    B_PKEY,        // unused
-    B_HASH,        // u64 [NC]
-    B_CMAG,        // double2 [NC]
-    B_CSIZE,       // u32 [NC]
-    B_SLOT,        // u32 [NC]
-    B_KEYS,        // u64 [M]
-    B_REP,         // u64 [M+1]
-    B_ACC,         // u64 [4(M+1)]
-    B_UCHILD,      // u64 [NU]
+    B_NCHILD,      // u32 [N] children per parent
+    B_CBEGIN,      // u64 [NP+1] child offsets over the kept parents
+    B_PIDX,        // u64 [NP] kept parents (parent pre-truncation)
+    B_HASH,        // u64 [NC] child hashes
+    B_CMAG,        // double2 [NC] child magnitudes
+    B_CSIZE,       // u32 [NC] child sizes
+    B_SLOT,        // u32 [NC] collision-table slot of each child
+    B_KEYS,        // u64 [M] table keys
+    B_REP,         // u32 [M+1] group representative (minimum child index)
+    B_ACC,         // u64 [4(M+1)] group magnitude sums, 128-bit fixed point
+    B_UCHILD,      // u64 [NU] groups kept after zero elimination (truncation path)
     B_UMAG,        // double2 [NU]
-    B_UNORM,       // u64 [NU]
+    B_UNORM,       // u64 [NU] IEEE bits of the group norm
     B_UHASH,       // u64 [NU]
-    B_SCHILD,      // u64 [NS]
-    B_SMAG,        // double2 [NS]
-    B_LOOKBACK,    // u64 [tiles + 1]
-    B_NORM,        // double [kNormBlocks]
-    B_MODSTATUS,   // int: sticky error of modifier launches (checked at the next step)
+    B_SCHILD,      // u64 [NS] representative child of each survivor
+    B_LOOKBACK,    // u64 [3 (tiles + 2)] look-back chains
+    B_TILENORM,    // double [tiles] per-tile norm sums of the survivors
+    B_MODSTATUS,   // int: sticky error of modifier launches (reported by the next step)
     B_COUNT
 };
 
@@ -89,8 +86,11 @@ struct quids_gpu_state {
     quids_gpu_ctx *ctx = nullptr;  // null once the context is destroyed
     uint64_t n = 0;
     uint64_t nbytes = 0;
-    double total_proba = 1;
-    qd_dbuf objects, begin, size, mag;
+    // total probability: known on the host, or still in d_total on the device
+    // (written by the last step without a host synchronisation)
+    mutable double total_proba = 1;
+    mutable bool total_pending = false;
+    qd_dbuf objects, begin, size, mag, d_total;
 };
 
 namespace qd::engine {
@@ -151,21 +151,6 @@ inline unsigned grid_for(quids_gpu_ctx *ctx, uint64_t n, int per_sm = 8) {
     return (unsigned)g;
 }
 
-// zeroed look-back workspace for a single-pass scan/compaction over n items
-inline int lookback_ws(quids_gpu_ctx *ctx, uint64_t n, prim::lookback &lb, unsigned &grid) {
-    uint64_t tiles = (n + prim::kTile - 1) / prim::kTile;
-    QD_TRY(ensure(ctx->buf[B_LOOKBACK], (tiles + 2) * sizeof(uint64_t)));
-    uint64_t *ws = bufp<uint64_t>(ctx, B_LOOKBACK);
-    QD_CUDA(cudaMemsetAsync(ws, 0, (tiles + 2) * sizeof(uint64_t), ctx->stream));
-    lb.status = ws + 1;
-    lb.counter = (uint32_t *)ws;
-    lb.err = (int *)(ctx->d_words + W_STATUS);
-    uint64_t g = tiles < 1 ? 1 : tiles;
-    uint64_t cap = (uint64_t)ctx->num_sms * 4;
-    grid = (unsigned)(g < cap ? g : cap);
-    return QUIDS_OK;
-}
-
 inline int read_words(quids_gpu_ctx *ctx) {
     QD_CUDA(cudaMemcpyAsync(ctx->h_words, ctx->d_words, W_COUNT_WORDS * sizeof(uint64_t),
                             cudaMemcpyDeviceToHost, ctx->stream));
@@ -197,8 +182,6 @@ inline int set_word(quids_gpu_ctx *ctx, qd_word w, uint64_t v) {
     return launched(ctx);
 }
 
-inline void stage_begin(quids_gpu_ctx *ctx, int k) { cudaEventRecord(ctx->ev_stage[2 * k], ctx->stream); }
-inline void stage_end(quids_gpu_ctx *ctx, int k) { cudaEventRecord(ctx->ev_stage[2 * k + 1], ctx->stream); }
 
 // ---------------------------------------------------------- rule traits
 template <class R, class = void>
@@ -298,6 +281,44 @@ struct parents_view {
     uint64_t np;
 };
 
+// The children of one tile come from a contiguous run of parents; their
+// offsets are staged in shared memory so each child finds its parent with a
+// short search there instead of a search over the whole offset array.
+constexpr int kSymItems = 4;
+constexpr int kTileChildren = prim::kThreads * kSymItems;
+constexpr int kStagedParents = kTileChildren;
+
+struct parent_tile {
+    uint64_t plo;
+    int count;  // staged parents, or -1: too many, search globally
+};
+
+__device__ __forceinline__ void stage_parents(const parents_view &pv, uint64_t c_first, uint64_t c_last,
+                                              uint64_t *s_cb, parent_tile *s_pt) {
+    if (threadIdx.x == 0) {
+        uint64_t plo = parent_of(pv.cbeg, pv.np, c_first);
+        uint64_t phi = parent_of(pv.cbeg, pv.np, c_last);
+        s_pt->plo = plo;
+        s_pt->count = (phi - plo + 1 <= (uint64_t)kStagedParents) ? (int)(phi - plo + 1) : -1;
+    }
+    __syncthreads();
+    const int cnt = s_pt->count;
+    const uint64_t plo = s_pt->plo;
+    for (int k = threadIdx.x; k <= cnt; k += blockDim.x) s_cb[k] = pv.cbeg[plo + k];
+    __syncthreads();
+}
+
+__device__ __forceinline__ uint64_t find_parent(const parents_view &pv, const uint64_t *s_cb, const parent_tile &pt,
+                                                uint64_t c) {
+    if (pt.count < 0) return parent_of(pv.cbeg, pv.np, c);
+    int lo = 0, hi = pt.count;  // s_cb[lo] <= c < s_cb[hi]
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (s_cb[mid] <= c) lo = mid; else hi = mid;
+    }
+    return pt.plo + (uint64_t)lo;
+}
+
 // Symbolic iteration (src/quids.hpp:705-719): per child, its magnitude,
 // size and hash.  FAST: the rule's hash_child; otherwise populate_child into
 // a per-thread buffer of MAXC bytes followed by the rule's hasher.
@@ -305,34 +326,47 @@ template <class Rule, int MAXC, bool FAST>
 __global__ void __launch_bounds__(prim::kThreads)
     k_symbolic(Rule rule, parents_view pv, const uint64_t *d_nc, uint64_t *hash, double2 *cmag, uint32_t *csize,
                unsigned long long *d_maxabs, int *err) {
+    __shared__ uint64_t s_cb[kStagedParents + 1];
+    __shared__ parent_tile s_pt;
     const uint64_t nc = *d_nc;
+    const uint64_t ntiles = (nc + kTileChildren - 1) / kTileChildren;
     double mx = 0;
-    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += (uint64_t)gridDim.x * blockDim.x) {
-        uint64_t p = parent_of(pv.cbeg, pv.np, c);
-        uint64_t oid = pv.pidx ? pv.pidx[p] : p;
-        uint32_t cid = (uint32_t)(c - pv.cbeg[p]);
-        const char *pb = pv.objects + pv.begin[oid];
-        const char *pe = pb + pv.size[oid];
-        double2 pm = pv.mag[oid];
-        mag_t m{pm.x, pm.y};
-        uint32_t sz = 0;
-        uint64_t h;
-        if constexpr (FAST) {
-            h = rule.hash_child(pb, pe, cid, sz, m);
-        } else {
-            uint64_t buf[MAXC / 8];
-            rule.populate_child(pb, pe, (char *)buf, cid, sz, m);
-            if (sz > MAXC) {
-                prim::set_error(err, QUIDS_ERR_SIZE_BOUND);
-                sz = MAXC;
+    for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const uint64_t c0 = t * kTileChildren;
+        const uint64_t c1 = c0 + kTileChildren < nc ? c0 + kTileChildren : nc;
+        stage_parents(pv, c0, c1 - 1, s_cb, &s_pt);
+        const parent_tile pt = s_pt;
+#pragma unroll
+        for (int k = 0; k < kSymItems; ++k) {
+            const uint64_t c = c0 + threadIdx.x + (uint64_t)k * prim::kThreads;
+            if (c >= c1) break;
+            uint64_t p = find_parent(pv, s_cb, pt, c);
+            uint64_t oid = pv.pidx ? pv.pidx[p] : p;
+            uint32_t cid = (uint32_t)(c - pv.cbeg[p]);
+            const char *pb = pv.objects + pv.begin[oid];
+            const char *pe = pb + pv.size[oid];
+            double2 pm = pv.mag[oid];
+            mag_t m{pm.x, pm.y};
+            uint32_t sz = 0;
+            uint64_t h;
+            if constexpr (FAST) {
+                h = rule.hash_child(pb, pe, cid, sz, m);
+            } else {
+                uint64_t buf[MAXC / 8];
+                rule.populate_child(pb, pe, (char *)buf, cid, sz, m);
+                if (sz > MAXC) {
+                    prim::set_error(err, QUIDS_ERR_SIZE_BOUND);
+                    sz = MAXC;
+                }
+                h = rule_hash(rule, (const char *)buf, (const char *)buf + sz);
             }
-            h = rule_hash(rule, (const char *)buf, (const char *)buf + sz);
+            hash[c] = h;
+            cmag[c] = make_double2(m.re, m.im);
+            csize[c] = sz;
+            double a = fabs(m.re) > fabs(m.im) ? fabs(m.re) : fabs(m.im);
+            mx = mx > a ? mx : a;
         }
-        hash[c] = h;
-        cmag[c] = make_double2(m.re, m.im);
-        csize[c] = sz;
-        double a = fabs(m.re) > fabs(m.im) ? fabs(m.re) : fabs(m.im);
-        mx = mx > a ? mx : a;
+        __syncthreads();  // the next tile restages s_cb
     }
     unsigned long long bits = (unsigned long long)__double_as_longlong(mx);
     for (int o = 16; o > 0; o >>= 1) {
@@ -342,30 +376,50 @@ __global__ void __launch_bounds__(prim::kThreads)
     if ((threadIdx.x & 31) == 0 && bits) atomicMax(d_maxabs, bits);
 }
 
-// Finalize (src/quids.hpp:958-967): populate_child_simple of each survivor
-// into the packed output, padding zeroed.
+// Finalize (src/quids.hpp:958-967) fused with normalisation (:1008-1013):
+// populate_child_simple of each survivor into the packed output (padding
+// zeroed) and mag /= sqrt(total) when that factor is not 1.
 template <class Rule, int MAXC>
 __global__ void __launch_bounds__(prim::kThreads)
     k_populate(Rule rule, parents_view pv, const uint64_t *schild, const uint64_t *d_ns, const uint64_t *obegin,
-               const uint32_t *osize, char *objects, int *err) {
+               const uint32_t *osize, char *objects, double2 *omag, const double *d_factor, int *err) {
+    __shared__ uint64_t s_cb[kStagedParents + 1];
+    __shared__ parent_tile s_pt;
     const uint64_t ns = *d_ns;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ns; i += (uint64_t)gridDim.x * blockDim.x) {
-        uint64_t c = schild[i];
-        uint64_t p = parent_of(pv.cbeg, pv.np, c);
-        uint64_t oid = pv.pidx ? pv.pidx[p] : p;
-        uint32_t cid = (uint32_t)(c - pv.cbeg[p]);
-        const char *pb = pv.objects + pv.begin[oid];
-        const char *pe = pb + pv.size[oid];
-        uint64_t buf[MAXC / 8];
-        rule_populate_simple(rule, pb, pe, (char *)buf, cid);
-        uint32_t sz = osize[i];
-        if (sz > MAXC) {
-            prim::set_error(err, QUIDS_ERR_SIZE_BOUND);
-            sz = MAXC;
+    const double f = *d_factor;
+    const uint64_t ntiles = (ns + kTileChildren - 1) / kTileChildren;
+    for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const uint64_t i0 = t * kTileChildren;
+        const uint64_t i1 = i0 + kTileChildren < ns ? i0 + kTileChildren : ns;
+        stage_parents(pv, schild[i0], schild[i1 - 1], s_cb, &s_pt);
+        const parent_tile pt = s_pt;
+#pragma unroll
+        for (int k = 0; k < kSymItems; ++k) {
+            const uint64_t i = i0 + threadIdx.x + (uint64_t)k * prim::kThreads;
+            if (i >= i1) break;
+            const uint64_t c = schild[i];
+            uint64_t p = find_parent(pv, s_cb, pt, c);
+            uint64_t oid = pv.pidx ? pv.pidx[p] : p;
+            uint32_t cid = (uint32_t)(c - pv.cbeg[p]);
+            const char *pb = pv.objects + pv.begin[oid];
+            const char *pe = pb + pv.size[oid];
+            uint64_t buf[MAXC / 8];
+            rule_populate_simple(rule, pb, pe, (char *)buf, cid);
+            uint32_t sz = osize[i];
+            if (sz > MAXC) {
+                prim::set_error(err, QUIDS_ERR_SIZE_BOUND);
+                sz = MAXC;
+            }
+            const uint64_t ob = obegin[i], oe = obegin[i + 1];
+            char *dst = objects + ob;
+            copy_bytes(dst, (const char *)buf, sz);
+            for (uint64_t q = ob + sz; q < oe; ++q) objects[q] = 0;
+            if (f != 1.0) {
+                double2 m = omag[i];
+                omag[i] = make_double2(__ddiv_rn(m.x, f), __ddiv_rn(m.y, f));
+            }
         }
-        char *dst = objects + obegin[i];
-        copy_bytes(dst, (const char *)buf, sz);
-        for (uint64_t k = obegin[i] + sz; k < obegin[i + 1]; ++k) objects[k] = 0;
+        __syncthreads();
     }
 }
 
@@ -425,38 +479,76 @@ struct scan_nchild {
     __device__ uint64_t operator()(uint64_t i) const { return nchild[pidx ? pidx[i] : i]; }
 };
 
-// a child is kept after collisions if it is its group's representative and
-// the group's summed norm is above tolerance (src/quids.hpp:785-823)
-struct compact_groups {
+__device__ __forceinline__ uint32_t padded_size(uint32_t sz, uint32_t align) {
+    if (align <= 1) return sz;
+    uint32_t pad = align - sz % align;
+    return pad == align ? sz : sz + pad;
+}
+
+// A child represents its group when it is the group's lowest symbolic index
+// (src/quids.hpp:785-809 keeps one member per hash); the group survives zero
+// elimination when its summed norm is above tolerance (src/quids.hpp:819-823).
+struct group_view {
     const uint32_t *slot_of;
-    const uint64_t *rep;
+    const uint32_t *rep;
     const unsigned long long *acc;
-    const uint64_t *hash;
     const uint64_t *d_nc;
     const unsigned long long *d_maxabs;
     double tolerance;
+    __device__ __forceinline__ mag_t sum(uint32_t s) const {
+        const int F = fix_scale(__longlong_as_double((long long)*d_maxabs), *d_nc);
+        const ulonglong4_32a a = *(const ulonglong4_32a *)&acc[4ull * s];
+        return mag_t{from_fix(fix128{a.x, a.y}, F), from_fix(fix128{a.z, a.w}, F)};
+    }
+    __device__ __forceinline__ bool kept(uint64_t c, mag_t &m) const {
+        const uint32_t s = slot_of[c];
+        if (s == 0xffffffffu || rep[s] != (uint32_t)c) return false;
+        m = sum(s);
+        return cnorm(m) > tolerance;
+    }
+};
+
+// no truncation possible: survivors straight into the output layout
+struct groups_layout {
+    group_view g;
+    const uint32_t *csize;
+    uint32_t align;
+    double2 *omag;
+    uint32_t *osize;
+    uint64_t *obegin;
+    uint64_t *schild;
+    __device__ bool select(uint64_t c) const {
+        mag_t m;
+        return g.kept(c, m);
+    }
+    __device__ uint64_t bytes(uint64_t c) const { return padded_size(csize[c], align); }
+    __device__ double norm(uint64_t c) const { return cnorm(g.sum(g.slot_of[c])); }
+    __device__ void emit(uint64_t c, uint64_t j, uint64_t off) const {
+        const mag_t m = g.sum(g.slot_of[c]);
+        omag[j] = make_double2(m.re, m.im);
+        osize[j] = csize[c];
+        obegin[j] = off;
+        schild[j] = c;
+    }
+};
+
+// truncation possible: keep the groups with their norms for the selection
+struct groups_collect {
+    group_view g;
+    const uint64_t *hash;
     uint64_t *uchild;
     double2 *umag;
     uint64_t *unorm;
     uint64_t *uhash;
     __device__ bool select(uint64_t c) const {
-        uint32_t s = slot_of[c];
-        if (s == 0xffffffffu) return false;
-        if (rep[s] != c) return false;
-        int F = fix_scale(__longlong_as_double((long long)*d_maxabs), *d_nc);
-        double re = from_fix(fix128{acc[4ull * s], acc[4ull * s + 1]}, F);
-        double im = from_fix(fix128{acc[4ull * s + 2], acc[4ull * s + 3]}, F);
-        return cnorm(mag_t{re, im}) > tolerance;
+        mag_t m;
+        return g.kept(c, m);
     }
     __device__ void emit(uint64_t c, uint64_t j) const {
-        uint32_t s = slot_of[c];
-        int F = fix_scale(__longlong_as_double((long long)*d_maxabs), *d_nc);
-        double re = from_fix(fix128{acc[4ull * s], acc[4ull * s + 1]}, F);
-        double im = from_fix(fix128{acc[4ull * s + 2], acc[4ull * s + 3]}, F);
+        const mag_t m = g.sum(g.slot_of[c]);
         uchild[j] = c;
-        umag[j] = make_double2(re, im);
-        double nrm = cnorm(mag_t{re, im});
-        unorm[j] = (uint64_t)__double_as_longlong(nrm);
+        umag[j] = make_double2(m.re, m.im);
+        unorm[j] = (uint64_t)__double_as_longlong(cnorm(m));
         uhash[j] = hash[c];
     }
 };
@@ -507,14 +599,20 @@ static __global__ void k_select_ties_init(prim::select_state *st) {
     st[1] = s;
 }
 
-struct keep_truncated {
+// the truncation's survivors (norm above the cutoff, ties by lower hash) into
+// the output layout (src/quids.hpp:866-948)
+struct keep_layout {
     const uint64_t *unorm;
     const uint64_t *uhash;
     const uint64_t *uchild;
     const double2 *umag;
     const prim::select_state *st;
+    const uint32_t *csize;
+    uint32_t align;
+    double2 *omag;
+    uint32_t *osize;
+    uint64_t *obegin;
     uint64_t *schild;
-    double2 *smag;
     __device__ bool select(uint64_t i) const {
         if (!st[0].active) return true;
         uint64_t k = unorm[i];
@@ -522,9 +620,14 @@ struct keep_truncated {
         if (k < st[0].prefix) return false;
         return !st[1].active || uhash[i] <= st[1].prefix;
     }
-    __device__ void emit(uint64_t i, uint64_t j) const {
-        schild[j] = uchild[i];
-        smag[j] = umag[i];
+    __device__ uint64_t bytes(uint64_t i) const { return padded_size(csize[uchild[i]], align); }
+    __device__ double norm(uint64_t i) const { return __longlong_as_double((long long)unorm[i]); }
+    __device__ void emit(uint64_t i, uint64_t j, uint64_t off) const {
+        const uint64_t c = uchild[i];
+        omag[j] = umag[i];
+        osize[j] = csize[c];
+        obegin[j] = off;
+        schild[j] = c;
     }
 };
 
@@ -541,27 +644,6 @@ struct keep_parents {
         return !st[1].active || i <= st[1].prefix;
     }
     __device__ void emit(uint64_t i, uint64_t j) const { pidx[j] = i; }
-};
-
-// output layout: size, magnitude and padded size of survivor i
-struct scan_out_sizes {
-    const uint64_t *schild;
-    const double2 *smag;
-    const uint32_t *csize;
-    uint32_t *osize;
-    double2 *omag;
-    uint32_t align;
-    __device__ uint64_t operator()(uint64_t i) const {
-        uint32_t sz = csize[schild[i]];
-        osize[i] = sz;
-        omag[i] = smag[i];
-        uint32_t pad = 0;
-        if (align > 1) {
-            pad = align - sz % align;
-            if (pad == align) pad = 0;
-        }
-        return (uint64_t)sz + pad;
-    }
 };
 
 // ------------------------------------------------------------ radix select
@@ -589,16 +671,12 @@ inline uint64_t next_pow2(uint64_t v) {
     while (p < v) p <<= 1;
     return p;
 }
-inline int ilog2(uint64_t v) {
-    int l = 0;
-    while ((1ull << l) < v) ++l;
-    return l;
-}
 
 // ------------------------------------------------------------- the step
 template <class Rule, int MAXC>
 inline int launch_symbolic(quids_gpu_ctx *ctx, const Rule &rule, const parents_view &pv, uint64_t nc, bool fast) {
-    unsigned grid = grid_for(ctx, nc);
+    uint64_t tiles = (nc + kTileChildren - 1) / kTileChildren;
+    unsigned grid = (unsigned)(tiles < (uint64_t)ctx->num_sms * 8 ? tiles : (uint64_t)ctx->num_sms * 8);
     uint64_t *d_nc = ctx->d_words + W_NC;
     unsigned long long *d_maxabs = (unsigned long long *)(ctx->d_words + W_MAXABS);
     int *err = (int *)(ctx->d_words + W_STATUS);
@@ -617,25 +695,16 @@ inline int launch_symbolic(quids_gpu_ctx *ctx, const Rule &rule, const parents_v
 }
 
 template <class Rule, int MAXC>
-inline int launch_populate(quids_gpu_ctx *ctx, const Rule &rule, const parents_view &pv, const uint64_t *schild,
-                           uint64_t ns, quids_gpu_state *out) {
-    unsigned grid = grid_for(ctx, ns);
+inline int launch_populate(quids_gpu_ctx *ctx, const Rule &rule, const parents_view &pv, uint64_t ns,
+                           quids_gpu_state *out) {
+    uint64_t tiles = (ns + kTileChildren - 1) / kTileChildren;
+    unsigned grid = (unsigned)(tiles < (uint64_t)ctx->num_sms * 8 ? tiles : (uint64_t)ctx->num_sms * 8);
+    if (grid < 1) grid = 1;
     k_populate<Rule, MAXC><<<grid, prim::kThreads, 0, ctx->stream>>>(
-        rule, pv, schild, ctx->d_words + W_NS, (const uint64_t *)out->begin.p, (const uint32_t *)out->size.p,
-        (char *)out->objects.p, (int *)(ctx->d_words + W_STATUS));
+        rule, pv, bufp<uint64_t>(ctx, B_SCHILD), ctx->d_words + W_NS, (const uint64_t *)out->begin.p,
+        (const uint32_t *)out->size.p, (char *)out->objects.p, (double2 *)out->mag.p,
+        (const double *)(ctx->d_words + W_FACTOR), (int *)(ctx->d_words + W_STATUS));
     return launched(ctx);
-}
-
-inline int normalize(quids_gpu_ctx *ctx, quids_gpu_state *st) {
-    QD_TRY(ensure(ctx->buf[B_NORM], prim::kNormBlocks * sizeof(double)));
-    double *partial = bufp<double>(ctx, B_NORM);
-    prim::k_norm_partial<<<prim::kNormBlocks, prim::kThreads, 0, ctx->stream>>>((const double2 *)st->mag.p,
-                                                                              ctx->d_words + W_NS, partial);
-    prim::k_norm_final<<<1, 512, 0, ctx->stream>>>(partial, prim::kNormBlocks, (double *)(ctx->d_words + W_TOTAL),
-                                                  (double *)(ctx->d_words + W_FACTOR));
-    prim::k_norm_scale<<<grid_for(ctx, st->n ? st->n : 1), prim::kThreads, 0, ctx->stream>>>(
-        (double2 *)st->mag.p, ctx->d_words + W_NS, (const double *)(ctx->d_words + W_FACTOR));
-    return launched(ctx, 3);
 }
 
 inline int ensure_state(quids_gpu_state *st, uint64_t n, uint64_t nbytes) {
@@ -643,7 +712,24 @@ inline int ensure_state(quids_gpu_state *st, uint64_t n, uint64_t nbytes) {
     QD_TRY(ensure(st->begin, (n + 1) * sizeof(uint64_t)));
     QD_TRY(ensure(st->size, n * sizeof(uint32_t)));
     QD_TRY(ensure(st->mag, n * sizeof(double2)));
+    QD_TRY(ensure(st->d_total, sizeof(double)));
     return QUIDS_OK;
+}
+
+// zeroed look-back chain `slot` (0..2) of the step for a pass over n items
+inline int lookback_chain(quids_gpu_ctx *ctx, uint64_t n_cap, int slot, prim::lookback &lb) {
+    const uint64_t words = (n_cap + prim::kTile - 1) / prim::kTile + 2;
+    uint64_t *ws = bufp<uint64_t>(ctx, B_LOOKBACK) + (uint64_t)slot * words;
+    QD_CUDA(cudaMemsetAsync(ws, 0, words * sizeof(uint64_t), ctx->stream));
+    lb.status = ws + 1;
+    lb.counter = (uint32_t *)ws;
+    lb.err = (int *)(ctx->d_words + W_STATUS);
+    return QUIDS_OK;
+}
+inline unsigned lookback_grid(quids_gpu_ctx *ctx, uint64_t n) {
+    uint64_t tiles = (n + prim::kTile - 1) / prim::kTile;
+    uint64_t cap = (uint64_t)ctx->num_sms * 4;
+    return (unsigned)(tiles < 1 ? 1 : (tiles < cap ? tiles : cap));
 }
 
 template <class Rule>
@@ -656,38 +742,66 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, qui
     const uint64_t N = in->n;
     const uint64_t maxn = prm.max_num_object;
     const double load = prm.table_load_factor > 0 && prm.table_load_factor < 0.95 ? prm.table_load_factor : 0.5;
+    const bool timing = (prm.flags & QUIDS_FLAG_STAGE_TIMING) != 0;
+    const bool fast = (prm.flags & QUIDS_FLAG_NO_FAST_HASH) == 0;
     const uint64_t launches0 = ctx->launches;
     quids_gpu_step_stats s{};
     s.num_parents = N;
-    bool stage_used[8] = {};
-    auto finish_empty = [&]() -> int {
-        out->n = 0;
-        out->nbytes = 0;
-        out->total_proba = 0;  // normalize() of an empty state (src/quids.hpp:986-992)
-        QD_TRY(ensure_state(out, 0, 8));
-        QD_CUDA(cudaMemsetAsync(out->begin.p, 0, sizeof(uint64_t), ctx->stream));
-        QD_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
-        QD_CUDA(cudaStreamSynchronize(ctx->stream));
-        cudaEventElapsedTime(&s.ms_total, ctx->ev0, ctx->ev1);
+    s.total_proba = std::numeric_limits<double>::quiet_NaN();  // until known on the host
+    bool used[8] = {};
+    auto begin_stage = [&](int k) {
+        if (timing) {
+            cudaEventRecord(ctx->ev_stage[2 * k], ctx->stream);
+            used[k] = true;
+        }
+    };
+    auto end_stage = [&](int k) {
+        if (timing) cudaEventRecord(ctx->ev_stage[2 * k + 1], ctx->stream);
+    };
+    auto finish = [&](bool empty) -> int {
+        if (empty) {
+            out->n = 0;
+            out->nbytes = 0;
+            out->total_proba = 0;  // normalize() of an empty state (src/quids.hpp:986-992)
+            out->total_pending = false;
+            QD_TRY(ensure_state(out, 0, 8));
+            QD_CUDA(cudaMemsetAsync(out->begin.p, 0, sizeof(uint64_t), ctx->stream));
+        }
+        if (timing) {
+            QD_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
+            QD_CUDA(cudaStreamSynchronize(ctx->stream));
+            cudaEventElapsedTime(&s.ms_total, ctx->ev0, ctx->ev1);
+            for (int k = 0; k < 8; ++k)
+                if (used[k]) cudaEventElapsedTime(&s.stage_ms[k], ctx->ev_stage[2 * k], ctx->ev_stage[2 * k + 1]);
+            double tp;
+            if (out->total_pending) {
+                QD_CUDA(cudaMemcpy(&tp, out->d_total.p, sizeof(double), cudaMemcpyDeviceToHost));
+                out->total_proba = tp;
+                out->total_pending = false;
+            }
+            s.total_proba = out->total_proba;
+        } else if (empty) {
+            s.total_proba = 0;
+        }
         s.kernel_launches = ctx->launches - launches0;
         if (stats) *stats = s;
         return QUIDS_OK;
     };
-    QD_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
+    if (timing) QD_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
     QD_CUDA(cudaMemsetAsync(ctx->d_words, 0, W_COUNT_WORDS * sizeof(uint64_t), ctx->stream));
     if (ctx->buf[B_MODSTATUS].p) {  // an earlier modifier met an unfit object
         k_take_status<<<1, 1, 0, ctx->stream>>>(bufp<int>(ctx, B_MODSTATUS), ctx->d_words + W_STATUS);
         QD_TRY(launched(ctx));
     }
-    if (N == 0) return finish_empty();
+    if (N == 0) return finish(true);
     int *err = (int *)(ctx->d_words + W_STATUS);
 
     // ---- stage 0: num_child (src/quids.hpp:548-569), parent pre-truncation
     // (src/quids.hpp:613-642, ties by lower index), child offsets (:666-673)
-    stage_begin(ctx, 0);
-    stage_used[0] = true;
+    begin_stage(0);
     QD_TRY(set_word(ctx, W_N, N));
     QD_TRY(ensure(ctx->buf[B_NCHILD], N * sizeof(uint32_t)));
+    QD_TRY(ensure(ctx->buf[B_LOOKBACK], 3 * ((N + prim::kTile - 1) / prim::kTile + 2) * sizeof(uint64_t)));
     k_num_child<Rule><<<grid_for(ctx, N), prim::kThreads, 0, ctx->stream>>>(
         rule, (const char *)in->objects.p, (const uint64_t *)in->begin.p, (const uint32_t *)in->size.p, N,
         bufp<uint32_t>(ctx, B_NCHILD), (unsigned long long *)(ctx->d_words + W_MAXSIZE), err);
@@ -700,10 +814,10 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, qui
         key_parent_index_ties k2{(const double2 *)in->mag.p, ctx->d_sel};
         QD_TRY(radix_select(ctx, ctx->d_words + W_N, N, maxn, k1, k2, false));
         prim::lookback lb;
-        unsigned g;
-        QD_TRY(lookback_ws(ctx, N, lb, g));
+        QD_TRY(lookback_chain(ctx, N, 0, lb));
         keep_parents kp{(const double2 *)in->mag.p, ctx->d_sel, bufp<uint64_t>(ctx, B_PIDX)};
-        prim::k_compact<<<g, prim::kThreads, 0, ctx->stream>>>(kp, ctx->d_words + W_N, ctx->d_words + W_NP, lb);
+        prim::k_compact<<<lookback_grid(ctx, N), prim::kThreads, 0, ctx->stream>>>(kp, ctx->d_words + W_N,
+                                                                                  ctx->d_words + W_NP, lb);
         QD_TRY(launched(ctx));
         NP = maxn;
         pidx = bufp<uint64_t>(ctx, B_PIDX);
@@ -714,15 +828,14 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, qui
     QD_TRY(ensure(ctx->buf[B_CBEGIN], (NP + 1) * sizeof(uint64_t)));
     {
         prim::lookback lb;
-        unsigned g;
-        QD_TRY(lookback_ws(ctx, NP, lb, g));
+        QD_TRY(lookback_chain(ctx, N, 1, lb));
         scan_nchild f{bufp<uint32_t>(ctx, B_NCHILD), pidx};
-        prim::k_scan_excl<<<g, prim::kThreads, 0, ctx->stream>>>(f, ctx->d_words + W_NP, bufp<uint64_t>(ctx, B_CBEGIN),
-                                                               ctx->d_words + W_NC, lb);
+        prim::k_scan_excl<<<lookback_grid(ctx, NP), prim::kThreads, 0, ctx->stream>>>(
+            f, ctx->d_words + W_NP, bufp<uint64_t>(ctx, B_CBEGIN), ctx->d_words + W_NC, lb);
         QD_TRY(launched(ctx));
     }
-    stage_end(ctx, 0);
-    int st = read_words(ctx);
+    end_stage(0);
+    int st = read_words(ctx);  // host synchronisation 1: child count and size bound
     if (st) return st;
     const uint64_t NC = ctx->h_words[W_NC];
     const uint64_t maxsize = ctx->h_words[W_MAXSIZE];
@@ -730,154 +843,143 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, qui
     s.max_child_size = maxsize;
     parents_view pv{(const char *)in->objects.p, (const uint64_t *)in->begin.p, (const uint32_t *)in->size.p,
                     (const double2 *)in->mag.p, bufp<uint64_t>(ctx, B_CBEGIN), pidx, NP};
-    if (NC == 0) return finish_empty();
-    const bool fast = !(prm.reserved & QUIDS_FLAG_NO_FAST_HASH);
-    if (maxsize > 4096) return QUIDS_ERR_SIZE_BOUND;  // per-thread child buffer bound
+    if (NC == 0) return finish(true);
+    if (NC >= 0xffffffffull) return QUIDS_ERR_UNSUPPORTED;  // child indices are u32 in the table
+    if (maxsize > 4096) return QUIDS_ERR_SIZE_BOUND;        // per-thread child buffer bound
+    const bool may_truncate = maxn < NC;
+    const uint64_t NSB = may_truncate ? maxn : NC;  // bound on the survivors
 
-    // ---- stage 1: symbolic iteration (src/quids.hpp:647-721)
+    uint64_t M = (uint64_t)((double)NC / load) + 1;
+    if (M < 1024) M = 1024;
+    if (M >= 0xffffffffull) return QUIDS_ERR_OOM;  // slot indices (and the extra slot M) are u32
+    s.table_capacity = M;
+    const uint64_t tiles_nc = (NC + prim::kTile - 1) / prim::kTile;
     QD_TRY(ensure(ctx->buf[B_HASH], NC * sizeof(uint64_t)));
     QD_TRY(ensure(ctx->buf[B_CMAG], NC * sizeof(double2)));
     QD_TRY(ensure(ctx->buf[B_CSIZE], NC * sizeof(uint32_t)));
     QD_TRY(ensure(ctx->buf[B_SLOT], NC * sizeof(uint32_t)));
-    uint64_t M = next_pow2((uint64_t)((double)NC / load) + 1);
-    if (M < 1024) M = 1024;
-    if (M > (1ull << 31)) return QUIDS_ERR_OOM;  // slot indices (and the extra slot M) are u32
-    s.table_capacity = M;
     QD_TRY(ensure(ctx->buf[B_KEYS], M * sizeof(uint64_t)));
-    QD_TRY(ensure(ctx->buf[B_REP], (M + 1) * sizeof(uint64_t)));
+    QD_TRY(ensure(ctx->buf[B_REP], (M + 1) * sizeof(uint32_t)));
     QD_TRY(ensure(ctx->buf[B_ACC], 4 * (M + 1) * sizeof(uint64_t)));
-    QD_TRY(ensure(ctx->buf[B_UCHILD], NC * sizeof(uint64_t)));
-    QD_TRY(ensure(ctx->buf[B_UMAG], NC * sizeof(double2)));
-    QD_TRY(ensure(ctx->buf[B_UNORM], NC * sizeof(uint64_t)));
-    QD_TRY(ensure(ctx->buf[B_UHASH], NC * sizeof(uint64_t)));
-    stage_begin(ctx, 1);
-    stage_used[1] = true;
+    QD_TRY(ensure(ctx->buf[B_SCHILD], NSB * sizeof(uint64_t)));
+    QD_TRY(ensure(ctx->buf[B_TILENORM], tiles_nc * sizeof(double)));
+    QD_TRY(ensure(ctx->buf[B_LOOKBACK], 3 * (tiles_nc + 2) * sizeof(uint64_t)));
+    QD_TRY(ensure(out->begin, (NSB + 1) * sizeof(uint64_t)));
+    QD_TRY(ensure(out->size, NSB * sizeof(uint32_t)));
+    QD_TRY(ensure(out->mag, NSB * sizeof(double2)));
+    QD_TRY(ensure(out->d_total, sizeof(double)));
+    if (may_truncate) {
+        QD_TRY(ensure(ctx->buf[B_UCHILD], NC * sizeof(uint64_t)));
+        QD_TRY(ensure(ctx->buf[B_UMAG], NC * sizeof(double2)));
+        QD_TRY(ensure(ctx->buf[B_UNORM], NC * sizeof(uint64_t)));
+        QD_TRY(ensure(ctx->buf[B_UHASH], NC * sizeof(uint64_t)));
+    }
+
+    // ---- stage 1: symbolic iteration (src/quids.hpp:647-721)
+    begin_stage(1);
     if (maxsize <= 256) {
         QD_TRY((launch_symbolic<Rule, 256>(ctx, rule, pv, NC, fast)));
     } else {
         QD_TRY((launch_symbolic<Rule, 4096>(ctx, rule, pv, NC, fast)));
     }
-    stage_end(ctx, 1);
+    end_stage(1);
 
     // ---- stage 2: collision table (src/quids.hpp:726-809)
-    stage_begin(ctx, 2);
-    stage_used[2] = true;
-    QD_CUDA(cudaMemsetAsync(ctx->buf[B_KEYS].p, 0xff, M * sizeof(uint64_t), ctx->stream));
-    QD_CUDA(cudaMemsetAsync(ctx->buf[B_REP].p, 0xff, (M + 1) * sizeof(uint64_t), ctx->stream));
-    QD_CUDA(cudaMemsetAsync(ctx->buf[B_ACC].p, 0, 4 * (M + 1) * sizeof(uint64_t), ctx->stream));
-    prim::table tb{bufp<uint64_t>(ctx, B_KEYS), bufp<uint64_t>(ctx, B_REP), bufp<unsigned long long>(ctx, B_ACC), M - 1,
-                   ilog2(M), (uint32_t)(M < 65536 ? M : 65536)};
-    prim::k_table_insert<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
-        tb, bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG), ctx->d_words + W_NC,
-        (const unsigned long long *)(ctx->d_words + W_MAXABS), bufp<uint32_t>(ctx, B_SLOT), err);
-    QD_TRY(launched(ctx));
-    stage_end(ctx, 2);
+    begin_stage(2);
+    prim::table tb{bufp<uint64_t>(ctx, B_KEYS), bufp<uint32_t>(ctx, B_REP), bufp<unsigned long long>(ctx, B_ACC), M,
+                   65536u};
+    QD_CUDA(cudaMemsetAsync(tb.keys, 0xff, M * sizeof(uint64_t), ctx->stream));
+    QD_CUDA(cudaMemsetAsync(tb.rep + M, 0xff, sizeof(uint32_t), ctx->stream));          // the extra slot
+    QD_CUDA(cudaMemsetAsync(tb.acc + 4 * M, 0, 4 * sizeof(uint64_t), ctx->stream));
+    prim::k_table_claim<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
+        tb, bufp<uint64_t>(ctx, B_HASH), ctx->d_words + W_NC, bufp<uint32_t>(ctx, B_SLOT), err);
+    prim::k_table_accumulate<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
+        tb, bufp<uint32_t>(ctx, B_SLOT), bufp<double2>(ctx, B_CMAG), ctx->d_words + W_NC,
+        (const unsigned long long *)(ctx->d_words + W_MAXABS));
+    QD_TRY(launched(ctx, 2));
+    end_stage(2);
 
-    // ---- stage 3: representatives with norm > tolerance, in symbolic order (src/quids.hpp:819-823)
-    stage_begin(ctx, 3);
-    stage_used[3] = true;
-    {
-        prim::lookback lb;
-        unsigned g;
-        QD_TRY(lookback_ws(ctx, NC, lb, g));
-        compact_groups cg{bufp<uint32_t>(ctx, B_SLOT), bufp<uint64_t>(ctx, B_REP), bufp<unsigned long long>(ctx, B_ACC),
-                          bufp<uint64_t>(ctx, B_HASH), ctx->d_words + W_NC,
-                          (const unsigned long long *)(ctx->d_words + W_MAXABS), prm.tolerance,
-                          bufp<uint64_t>(ctx, B_UCHILD), bufp<double2>(ctx, B_UMAG), bufp<uint64_t>(ctx, B_UNORM),
-                          bufp<uint64_t>(ctx, B_UHASH)};
-        prim::k_compact<<<g, prim::kThreads, 0, ctx->stream>>>(cg, ctx->d_words + W_NC, ctx->d_words + W_NU, lb);
+    // ---- stage 3 (+4): representatives above tolerance (src/quids.hpp:819-823),
+    // truncation (src/quids.hpp:866-900, ties by lower hash) and the output
+    // layout (src/quids.hpp:927-948), with per-tile norm sums for normalize
+    group_view gv{bufp<uint32_t>(ctx, B_SLOT), bufp<uint32_t>(ctx, B_REP), bufp<unsigned long long>(ctx, B_ACC),
+                  ctx->d_words + W_NC, (const unsigned long long *)(ctx->d_words + W_MAXABS), prm.tolerance};
+    const uint32_t align = prm.align_byte_length;
+    double *tile_norm = bufp<double>(ctx, B_TILENORM);
+    begin_stage(3);
+    if (!may_truncate) {
+        prim::lookback lbc, lbb;
+        QD_TRY(lookback_chain(ctx, NC, 0, lbc));
+        QD_TRY(lookback_chain(ctx, NC, 1, lbb));
+        groups_layout f{gv, bufp<uint32_t>(ctx, B_CSIZE), align, (double2 *)out->mag.p, (uint32_t *)out->size.p,
+                        (uint64_t *)out->begin.p, bufp<uint64_t>(ctx, B_SCHILD)};
+        prim::k_compact_layout<<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
+            f, ctx->d_words + W_NC, ctx->d_words + W_NS, ctx->d_words + W_OUTBYTES, (uint64_t *)out->begin.p,
+            tile_norm, lbc, lbb);
         QD_TRY(launched(ctx));
-    }
-    stage_end(ctx, 3);
-    st = read_words(ctx);
-    if (st) return st;
-    const uint64_t NU = ctx->h_words[W_NU];
-    s.num_object_after_interferences = NU;
-    if (NU == 0) return finish_empty();
-
-    // ---- stage 4: truncation (src/quids.hpp:866-900), ties by lower hash
-    const uint64_t *schild = bufp<uint64_t>(ctx, B_UCHILD);
-    const double2 *smag = bufp<double2>(ctx, B_UMAG);
-    uint64_t NS = NU;
-    if (maxn < NU) {
-        QD_TRY(ensure(ctx->buf[B_SCHILD], maxn * sizeof(uint64_t)));
-        QD_TRY(ensure(ctx->buf[B_SMAG], maxn * sizeof(double2)));
-        stage_begin(ctx, 4);
-        stage_used[4] = true;
+        end_stage(3);
+    } else {
+        prim::lookback lb;
+        QD_TRY(lookback_chain(ctx, NC, 0, lb));
+        groups_collect f{gv, bufp<uint64_t>(ctx, B_HASH), bufp<uint64_t>(ctx, B_UCHILD), bufp<double2>(ctx, B_UMAG),
+                         bufp<uint64_t>(ctx, B_UNORM), bufp<uint64_t>(ctx, B_UHASH)};
+        prim::k_compact<<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(f, ctx->d_words + W_NC,
+                                                                                   ctx->d_words + W_NU, lb);
+        QD_TRY(launched(ctx));
+        end_stage(3);
+        begin_stage(4);
         key_unorm k1{bufp<uint64_t>(ctx, B_UNORM)};
         key_uhash_ties k2{bufp<uint64_t>(ctx, B_UNORM), bufp<uint64_t>(ctx, B_UHASH), ctx->d_sel};
-        QD_TRY(radix_select(ctx, ctx->d_words + W_NU, NU, maxn, k1, k2, false));
-        prim::lookback lb;
-        unsigned g;
-        QD_TRY(lookback_ws(ctx, NU, lb, g));
-        keep_truncated kt{bufp<uint64_t>(ctx, B_UNORM), bufp<uint64_t>(ctx, B_UHASH), bufp<uint64_t>(ctx, B_UCHILD),
-                          bufp<double2>(ctx, B_UMAG), ctx->d_sel, bufp<uint64_t>(ctx, B_SCHILD),
-                          bufp<double2>(ctx, B_SMAG)};
-        prim::k_compact<<<g, prim::kThreads, 0, ctx->stream>>>(kt, ctx->d_words + W_NU, ctx->d_words + W_NS, lb);
+        QD_TRY(radix_select(ctx, ctx->d_words + W_NU, NC, maxn, k1, k2, false));
+        prim::lookback lbc, lbb;
+        QD_TRY(lookback_chain(ctx, NC, 1, lbc));
+        QD_TRY(lookback_chain(ctx, NC, 2, lbb));
+        keep_layout kl{bufp<uint64_t>(ctx, B_UNORM), bufp<uint64_t>(ctx, B_UHASH), bufp<uint64_t>(ctx, B_UCHILD),
+                       bufp<double2>(ctx, B_UMAG), ctx->d_sel, bufp<uint32_t>(ctx, B_CSIZE), align,
+                       (double2 *)out->mag.p, (uint32_t *)out->size.p, (uint64_t *)out->begin.p,
+                       bufp<uint64_t>(ctx, B_SCHILD)};
+        prim::k_compact_layout<<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
+            kl, ctx->d_words + W_NU, ctx->d_words + W_NS, ctx->d_words + W_OUTBYTES, (uint64_t *)out->begin.p,
+            tile_norm, lbc, lbb);
         QD_TRY(launched(ctx));
-        stage_end(ctx, 4);
-        schild = bufp<uint64_t>(ctx, B_SCHILD);
-        smag = bufp<double2>(ctx, B_SMAG);
-        NS = maxn;
-    } else {
-        QD_TRY(set_word(ctx, W_NS, NU));
+        end_stage(4);
     }
-
-    // ---- stage 5: output layout (src/quids.hpp:927-948)
-    QD_TRY(ensure(out->begin, (NS + 1) * sizeof(uint64_t)));
-    QD_TRY(ensure(out->size, NS * sizeof(uint32_t)));
-    QD_TRY(ensure(out->mag, NS * sizeof(double2)));
-    stage_begin(ctx, 5);
-    stage_used[5] = true;
-    {
-        prim::lookback lb;
-        unsigned g;
-        QD_TRY(lookback_ws(ctx, NS, lb, g));
-        scan_out_sizes f{schild, smag, bufp<uint32_t>(ctx, B_CSIZE), (uint32_t *)out->size.p, (double2 *)out->mag.p,
-                         prm.align_byte_length};
-        prim::k_scan_excl<<<g, prim::kThreads, 0, ctx->stream>>>(f, ctx->d_words + W_NS, (uint64_t *)out->begin.p,
-                                                               ctx->d_words + W_OUTBYTES, lb);
-        QD_TRY(launched(ctx));
-    }
-    stage_end(ctx, 5);
-    st = read_words(ctx);
+    st = read_words(ctx);  // host synchronisation 2: survivors and their bytes
     if (st) return st;
+    const uint64_t NS = ctx->h_words[W_NS];
+    const uint64_t NU = may_truncate ? ctx->h_words[W_NU] : NS;
     const uint64_t outbytes = ctx->h_words[W_OUTBYTES];
+    s.num_object_after_interferences = NU;
+    if (NS == 0) return finish(true);
     QD_TRY(ensure(out->objects, outbytes));
 
-    // ---- stage 6: finalize populate (src/quids.hpp:958-967)
-    stage_begin(ctx, 6);
-    stage_used[6] = true;
+    // ---- stage 5: total probability (src/quids.hpp:1002-1008), in a fixed order
+    begin_stage(5);
+    prim::k_norm_from_tiles<<<1, 1024, 0, ctx->stream>>>(tile_norm, ctx->d_words + (may_truncate ? W_NU : W_NC),
+                                                        (double *)(ctx->d_words + W_TOTAL),
+                                                        (double *)(ctx->d_words + W_FACTOR));
+    QD_TRY(launched(ctx));
+    QD_CUDA(cudaMemcpyAsync(out->d_total.p, ctx->d_words + W_TOTAL, sizeof(double), cudaMemcpyDeviceToDevice,
+                            ctx->stream));
+    end_stage(5);
+
+    // ---- stage 6: finalize populate (src/quids.hpp:958-967) + normalisation
+    begin_stage(6);
     if (maxsize <= 256) {
-        QD_TRY((launch_populate<Rule, 256>(ctx, rule, pv, schild, NS, out)));
+        QD_TRY((launch_populate<Rule, 256>(ctx, rule, pv, NS, out)));
     } else {
-        QD_TRY((launch_populate<Rule, 4096>(ctx, rule, pv, schild, NS, out)));
+        QD_TRY((launch_populate<Rule, 4096>(ctx, rule, pv, NS, out)));
     }
-    stage_end(ctx, 6);
+    end_stage(6);
     out->n = NS;
     out->nbytes = outbytes;
-
-    // ---- stage 7: normalize (src/quids.hpp:985-1017)
-    stage_begin(ctx, 7);
-    stage_used[7] = true;
-    QD_TRY(normalize(ctx, out));
-    stage_end(ctx, 7);
-    QD_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
-    st = read_words(ctx);
-    if (st) return st;
-    std::memcpy(&out->total_proba, &ctx->h_words[W_TOTAL], sizeof(double));
-    cudaEventElapsedTime(&s.ms_total, ctx->ev0, ctx->ev1);
-    for (int k = 0; k < 8; ++k)
-        if (stage_used[k]) cudaEventElapsedTime(&s.stage_ms[k], ctx->ev_stage[2 * k], ctx->ev_stage[2 * k + 1]);
+    out->total_pending = true;
 
     s.num_object_out = NS;
     s.out_bytes = outbytes;
-    s.total_proba = out->total_proba;
-    s.kernel_launches = ctx->launches - launches0;
     double sp = (double)in->nbytes, sbar_p = N ? sp / (double)N : 0, sbar_c = NS ? (double)outbytes / NS : 0;
     s.algorithmic_bytes = sp + 24.0 * N + 72.0 * NC + 24.0 * NU + (double)NS * (sbar_p + sbar_c + 24.0);
-    if (stats) *stats = s;
-    return QUIDS_OK;
+    return finish(false);
 }
 
 template <class Mod>
@@ -910,18 +1012,20 @@ int rule_children(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, uin
     }
     QD_TRY(set_word(ctx, W_NP, N));
     QD_TRY(ensure(ctx->buf[B_NCHILD], N * sizeof(uint32_t)));
+    QD_TRY(ensure(ctx->buf[B_LOOKBACK], 3 * ((N + prim::kTile - 1) / prim::kTile + 2) * sizeof(uint64_t)));
     k_num_child<Rule><<<grid_for(ctx, N), prim::kThreads, 0, ctx->stream>>>(
         rule, (const char *)in->objects.p, (const uint64_t *)in->begin.p, (const uint32_t *)in->size.p, N,
         bufp<uint32_t>(ctx, B_NCHILD), (unsigned long long *)(ctx->d_words + W_MAXSIZE),
         (int *)(ctx->d_words + W_STATUS));
+    QD_TRY(launched(ctx));
     QD_TRY(ensure(ctx->buf[B_CBEGIN], (N + 1) * sizeof(uint64_t)));
     {
         prim::lookback lb;
-        unsigned g;
-        QD_TRY(lookback_ws(ctx, N, lb, g));
+        QD_TRY(lookback_chain(ctx, N, 0, lb));
         scan_nchild f{bufp<uint32_t>(ctx, B_NCHILD), nullptr};
-        prim::k_scan_excl<<<g, prim::kThreads, 0, ctx->stream>>>(f, ctx->d_words + W_NP, bufp<uint64_t>(ctx, B_CBEGIN),
-                                                               ctx->d_words + W_NC, lb);
+        prim::k_scan_excl<<<lookback_grid(ctx, N), prim::kThreads, 0, ctx->stream>>>(
+            f, ctx->d_words + W_NP, bufp<uint64_t>(ctx, B_CBEGIN), ctx->d_words + W_NC, lb);
+        QD_TRY(launched(ctx));
     }
     int st = read_words(ctx);
     if (st) return st;
@@ -942,7 +1046,7 @@ int rule_children(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, uin
     QD_CUDA(cudaMemsetAsync(dbytes.p, 0, NC * stride, ctx->stream));
     k_children<Rule><<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
         rule, pv, NC, stride, (char *)dbytes.p, (uint64_t *)dhash.p, (uint32_t *)dsize.p, (double2 *)dmag.p);
-    rc = cuda_status(cudaGetLastError());
+    rc = launched(ctx);
     if (!rc) rc = cuda_status(cudaMemcpyAsync(bytes, dbytes.p, NC * stride, cudaMemcpyDeviceToHost, ctx->stream));
     if (!rc && hash) rc = cuda_status(cudaMemcpyAsync(hash, dhash.p, NC * 8, cudaMemcpyDeviceToHost, ctx->stream));
     if (!rc && size) rc = cuda_status(cudaMemcpyAsync(size, dsize.p, NC * 4, cudaMemcpyDeviceToHost, ctx->stream));

@@ -271,121 +271,185 @@ static __global__ void k_radix_pick(select_state *st, unsigned long long *hist, 
 }
 
 // ---------------------------------------------------- collision table
-// keys[M] (kEmptyKey = free), rep[M+1] (min child index, ~0 = none),
-// acc[M+1][4] (re lo, re hi, im lo, im hi).  Slot M holds the children whose
-// hash equals kEmptyKey.
+// keys[M] (kEmptyKey = free; set by a memset before each step), rep[M+1]
+// (u32 minimum child index) and acc[M+1][4] (re lo, re hi, im lo, im hi: one
+// 32-byte sector per slot).  A slot's rep and acc are initialised by the
+// thread whose CAS claims the slot, so only the keys are cleared per step.
+// Slot M holds the children whose hash equals kEmptyKey (initialised by the
+// host).  M need not be a power of two: the home slot is the high half of
+// (mixed hash) * M.
 struct table {
     uint64_t *keys;
-    uint64_t *rep;
+    uint32_t *rep;
     unsigned long long *acc;
-    uint64_t mask;      // M - 1
-    int log2m;
+    uint64_t m;         // slots
     uint32_t max_probes;
 };
 
-__device__ __forceinline__ uint64_t table_home(uint64_t h, int log2m) {
-    return (h * 0x9E3779B97F4A7C15ull) >> (64 - log2m);
+__device__ __forceinline__ uint64_t table_home(uint64_t h, uint64_t m) {
+    return __umul64hi(h * 0x9E3779B97F4A7C15ull, m);
 }
 
 __device__ __forceinline__ void fix_atomic_add(unsigned long long *w, fix128 v) {
+    if ((v.lo | v.hi) == 0) return;
     unsigned long long old = atomicAdd(&w[0], (unsigned long long)v.lo);
     unsigned long long carry = (old + v.lo) < old ? 1ull : 0ull;
     unsigned long long hi = v.hi + carry;
     if (hi) atomicAdd(&w[1], hi);
 }
 
-// Inserts every child: slot_of[c] = its group's slot; rep = min child index;
-// acc += magnitude (exact fixed point with scale 2^-F, F from the largest
-// component and the child count).
-static __global__ void __launch_bounds__(kThreads) k_table_insert(table t, const uint64_t *hash, const double2 *mag,
-                                                            const uint64_t *d_n, const unsigned long long *d_maxabs,
-                                                            uint32_t *slot_of, int *err) {
+// Pass 1: every child finds or claims the slot of its hash; slot_of[c] = slot
+// (0xffffffff when the probe limit is reached: QUIDS_ERR_TABLE_FULL).
+static __global__ void __launch_bounds__(kThreads) k_table_claim(table t, const uint64_t *hash, const uint64_t *d_n,
+                                                           uint32_t *slot_of, int *err) {
     const uint64_t n = *d_n;
-    double maxabs = __longlong_as_double((long long)*d_maxabs);
-    const int F = fix_scale(maxabs, n);
-    const uint64_t M = t.mask + 1;
     for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (uint64_t)gridDim.x * blockDim.x) {
-        uint64_t h = hash[c];
+        const uint64_t h = hash[c];
         uint64_t s;
         if (h == kEmptyKey) {
-            s = M;
+            s = t.m;
         } else {
-            s = table_home(h, t.log2m);
+            s = table_home(h, t.m);
             uint32_t probe = 0;
             while (true) {
                 uint64_t k = ld_volatile_u64(&t.keys[s]);
                 if (k == h) break;
                 if (k == kEmptyKey) {
                     uint64_t old = atomicCAS((unsigned long long *)&t.keys[s], kEmptyKey, h);
-                    if (old == kEmptyKey || old == h) break;
+                    if (old == kEmptyKey) {  // claimed: initialise the slot's group
+                        ulonglong4_32a zero;
+                        zero.x = zero.y = zero.z = zero.w = 0;
+                        t.rep[s] = 0xffffffffu;
+                        *(ulonglong4_32a *)&t.acc[4 * s] = zero;
+                        break;
+                    }
+                    if (old == h) break;
                 }
-                s = (s + 1) & t.mask;
+                if (++s == t.m) s = 0;
                 if (++probe >= t.max_probes) {
                     set_error(err, QUIDS_ERR_TABLE_FULL);
                     s = ~0ull;
                     break;
                 }
             }
-            if (s == ~0ull) {
-                slot_of[c] = 0xffffffffu;
-                continue;
-            }
         }
-        atomicMin((unsigned long long *)&t.rep[s], (unsigned long long)c);
-        double2 m = mag[c];
-        fix_atomic_add(&t.acc[4 * s + 0], to_fix(m.x, F));
-        fix_atomic_add(&t.acc[4 * s + 2], to_fix(m.y, F));
         slot_of[c] = (uint32_t)s;
     }
 }
 
-// --------------------------------------------------------- normalisation
-constexpr int kNormBlocks = 512;
-
-// partial[b] = sum of norms over the fixed chunk of block b (fixed order)
-static __global__ void __launch_bounds__(kThreads) k_norm_partial(const double2 *mag, const uint64_t *d_n, double *partial) {
-    __shared__ double sm[kThreads];
+// Pass 2: rep = minimum child index of the group; acc += magnitude as an
+// exact 128-bit fixed-point sum per component (scale 2^-F, F from the largest
+// component and the child count), so the sum is independent of the order of
+// the atomics.
+static __global__ void __launch_bounds__(kThreads) k_table_accumulate(table t, const uint32_t *slot_of,
+                                                                const double2 *mag, const uint64_t *d_n,
+                                                                const unsigned long long *d_maxabs) {
     const uint64_t n = *d_n;
-    const uint64_t chunk = (n + gridDim.x - 1) / gridDim.x;
-    const uint64_t b = (uint64_t)blockIdx.x * chunk;
-    const uint64_t e = min(n, b + chunk);
+    const int F = fix_scale(__longlong_as_double((long long)*d_maxabs), n);
+    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t s = slot_of[c];
+        if (s == 0xffffffffu) continue;
+        atomicMin(&t.rep[s], (uint32_t)c);
+        const double2 m = mag[c];
+        fix_atomic_add(&t.acc[4ull * s + 0], to_fix(m.x, F));
+        fix_atomic_add(&t.acc[4ull * s + 2], to_fix(m.y, F));
+    }
+}
+
+// --------------------------------------------- compaction + byte offsets
+// Order-preserving compaction that also lays out the selected items'
+// variable-size payloads: P::select(i) -> bool, P::bytes(i) -> padded size,
+// P::norm(i) -> double, P::emit(i, j, byte_offset).  Two look-back chains
+// (count, bytes) in one pass; per tile, the sum of the selected norms in item
+// order goes to tile_norm[tile] (a fixed decomposition: deterministic).
+// At the end: *d_count, *d_bytes and begin_out[count] = total bytes.
+template <class P>
+__global__ void __launch_bounds__(kThreads) k_compact_layout(P p, const uint64_t *d_n, uint64_t *d_count,
+                                                              uint64_t *d_bytes, uint64_t *begin_out,
+                                                              double *tile_norm, lookback lb_count,
+                                                              lookback lb_bytes) {
+    __shared__ uint64_t sm[kThreads / 32 + 1];
+    __shared__ double smd[kThreads];
+    __shared__ uint64_t bcast;
+    __shared__ uint32_t sm_tile;
+    const uint64_t n = *d_n;
+    const uint64_t ntiles = (n + kTile - 1) / kTile;
+    if (n == 0) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            *d_count = 0;
+            *d_bytes = 0;
+            begin_out[0] = 0;
+        }
+        return;
+    }
+    while (true) {
+        uint32_t tile = next_tile(lb_count, &sm_tile);
+        if (tile >= ntiles) break;
+        const uint64_t base = (uint64_t)tile * kTile + (uint64_t)threadIdx.x * kItems;
+        uint32_t flags = 0;
+        uint64_t cnt = 0, bytes = 0;
+        double nrm = 0;
+#pragma unroll
+        for (int k = 0; k < kItems; ++k) {
+            uint64_t i = base + k;
+            if (i < n && p.select(i)) {
+                flags |= 1u << k;
+                ++cnt;
+                bytes += p.bytes(i);
+                nrm = dadd(nrm, p.norm(i));
+            }
+        }
+        // deterministic per-tile norm sum: fixed tree over threads
+        smd[threadIdx.x] = nrm;
+        __syncthreads();
+        for (int o = kThreads / 2; o > 0; o >>= 1) {
+            if (threadIdx.x < o) smd[threadIdx.x] = dadd(smd[threadIdx.x], smd[threadIdx.x + o]);
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) tile_norm[tile] = smd[0];
+        uint64_t agg_c, agg_b;
+        uint64_t excl_c = block_excl_scan(cnt, sm, agg_c);
+        uint64_t excl_b = block_excl_scan(bytes, sm, agg_b);
+        uint64_t pre_c = tile_prefix(lb_count, tile, agg_c, &bcast);
+        uint64_t pre_b = tile_prefix(lb_bytes, tile, agg_b, &bcast);
+        uint64_t j = pre_c + excl_c, off = pre_b + excl_b;
+#pragma unroll
+        for (int k = 0; k < kItems; ++k)
+            if (flags & (1u << k)) {
+                uint64_t i = base + k;
+                p.emit(i, j++, off);
+                off += p.bytes(i);
+            }
+        if (tile == ntiles - 1 && threadIdx.x == kThreads - 1) {
+            *d_count = pre_c + agg_c;
+            *d_bytes = pre_b + agg_b;
+            begin_out[pre_c + agg_c] = pre_b + agg_b;
+        }
+    }
+}
+
+// --------------------------------------------------------- normalisation
+// total = sum of the per-tile norm sums in tile order (one block, fixed
+// tree); factor = sqrt(total) (src/quids.hpp:1004-1008).
+static __global__ void __launch_bounds__(1024) k_norm_from_tiles(const double *tile_norm, const uint64_t *d_items,
+                                                                  double *d_total, double *d_factor) {
+    __shared__ double sm[1024];
+    const uint64_t nt = (*d_items + kTile - 1) / kTile;
+    const uint64_t per = (nt + 1023) / 1024;
     double s = 0;
-    for (uint64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
-        double2 m = mag[i];
-        s = dadd(s, cnorm(mag_t{m.x, m.y}));
+    for (uint64_t k = 0; k < per; ++k) {
+        uint64_t t = (uint64_t)threadIdx.x * per + k;
+        if (t < nt) s = dadd(s, tile_norm[t]);
     }
     sm[threadIdx.x] = s;
     __syncthreads();
-    for (int o = kThreads / 2; o > 0; o >>= 1) {
+    for (int o = 512; o > 0; o >>= 1) {
         if (threadIdx.x < o) sm[threadIdx.x] = dadd(sm[threadIdx.x], sm[threadIdx.x + o]);
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) partial[blockIdx.x] = sm[0];
-}
-
-// total = sum of partials (fixed order); factor = sqrt(total)
-static __global__ void k_norm_final(const double *partial, int np, double *d_total, double *d_factor) {
-    __shared__ double sm[kNormBlocks];
-    for (int i = threadIdx.x; i < kNormBlocks; i += blockDim.x) sm[i] = i < np ? partial[i] : 0.0;
-    __syncthreads();
-    for (int o = kNormBlocks / 2; o > 0; o >>= 1) {
-        for (int i = threadIdx.x; i < o; i += blockDim.x) sm[i] = dadd(sm[i], sm[i + o]);
         __syncthreads();
     }
     if (threadIdx.x == 0) {
         *d_total = sm[0];
         *d_factor = __dsqrt_rn(sm[0]);
-    }
-}
-
-// mag /= factor when factor != 1 (src/quids.hpp:1008-1013)
-static __global__ void __launch_bounds__(kThreads) k_norm_scale(double2 *mag, const uint64_t *d_n, const double *d_factor) {
-    const double f = *d_factor;
-    if (f == 1.0) return;
-    const uint64_t n = *d_n;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        double2 m = mag[i];
-        mag[i] = make_double2(__ddiv_rn(m.x, f), __ddiv_rn(m.y, f));
     }
 }
 
