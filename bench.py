@@ -118,26 +118,24 @@ class Clocks:
 
 
 def run_step_gpu(ctx, quids, wl, init_state, stats_acc=None, flags=0):
-    """One bench step on device-resident input: returns (children, final it_t)."""
-    it = init_state
+    """One bench step on device-resident input, through quids_gpu_run (the
+    gate list in one library call): returns (children, final it_t)."""
+    if "_ops" not in wl:
+        wl["_ops"] = [quids.rule_from(g.kind == "rule", g.code, g.params) for g in wl["gates"]]
+    if "_spare" not in wl:
+        wl["_spare"] = quids.it_t(ctx)
+    in_bytes = init_state.num_bytes
+    final, stats = quids.run(init_state, wl["_spare"], wl["_ops"], wl["max"], flags)
+    if final is wl["_spare"]:  # keep a free handle for the next step
+        wl["_spare"] = init_state
     children = 0
-    spare = []
-    for g in wl["gates"]:
-        r = quids.rule_from(g.kind == "rule", g.code, g.params)
-        if g.kind == "mod":
-            quids.simulate(it, r)
-            continue
-        nxt = spare.pop() if spare else quids.it_t(ctx)
-        in_bytes = it.num_bytes
-        st = quids.simulate(it, r, nxt, None, wl["max"], flags=flags)
+    for st in stats:
         st["_in_bytes"] = in_bytes
+        in_bytes = st["out_bytes"]
         children += st["num_object"]
-        if stats_acc is not None:
-            stats_acc.append(st)
-        if it is not init_state:
-            spare.append(it)
-        it = nxt
-    return children, it
+    if stats_acc is not None:
+        stats_acc.extend(stats)
+    return children, final
 
 
 # per-stage algorithmic bytes (compulsory HBM traffic of each stage's kernels)

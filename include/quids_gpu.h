@@ -164,6 +164,21 @@ int quids_gpu_simulate(quids_gpu_ctx *ctx, quids_gpu_state *iteration, int rule_
 int quids_gpu_apply_modifier(quids_gpu_ctx *ctx, quids_gpu_state *iteration, int modifier_kind,
                              const quids_gpu_rule_params *modifier);
 
+/* A loop of quids::simulate calls in one call: ops are applied in order,
+ * modifiers in place (src/quids.hpp:436) and rules from the current state
+ * into the other of the two handles (src/quids.hpp:448), the ping-pong of the
+ * reference's examples (examples/quantum_computer_test.cpp:26-49).  The
+ * final state is *a (*final_index = 0) or *b (1).  rule_stats, if not NULL,
+ * receives one entry per rule op, in order. */
+typedef struct quids_gpu_op {
+    int32_t is_rule;              /* 1: rule (QUIDS_RULE_*), 0: modifier (QUIDS_MOD_*) */
+    int32_t kind;
+    quids_gpu_rule_params params;
+} quids_gpu_op;
+int quids_gpu_run(quids_gpu_ctx *ctx, quids_gpu_state *a, quids_gpu_state *b, const quids_gpu_op *ops,
+                  uint64_t n_ops, const quids_gpu_params *params, quids_gpu_step_stats *rule_stats,
+                  int *final_index);
+
 /* ------------------------------------------------------ rule-level access
  * Materialises every child of every parent of `iteration` (the symbolic
  * iteration of src/quids.hpp:647-721 with the child bytes kept): children

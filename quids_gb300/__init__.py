@@ -291,6 +291,28 @@ def simulate(iteration: it_t, rule, next_iteration: it_t | None = None, symbolic
     return d
 
 
+def run(a: it_t, b: it_t, ops, max_num_object: int = U64_MAX, flags: int = 0):
+    """Applies a list of rules and modifiers in one library call (the loop of
+    simulate() calls of the reference's examples, ping-ponging between two
+    iterations).  ops: rules/modifiers from ``rules``.  Returns
+    (final it_t, list of per-rule stats)."""
+    a._flush()
+    arr = (capi.Op * max(len(ops), 1))()
+    n_rules = 0
+    for i, r in enumerate(ops):
+        arr[i].is_rule = int(r.is_rule)
+        arr[i].kind = r.kind
+        arr[i].params = r.params()
+        n_rules += int(r.is_rule)
+    stats = (capi.StepStats * max(n_rules, 1))()
+    fin = C.c_int(0)
+    prm = _params(max_num_object, flags)
+    b._pending = []
+    rc = a.lib.quids_gpu_run(a.ctx.h, a.h, b.h, arr, len(ops), C.byref(prm), stats, C.byref(fin))
+    capi.check(rc, "run")
+    return (a if fin.value == 0 else b), [stats[i].as_dict() for i in range(n_rules)]
+
+
 def rule_children(iteration: it_t, rule):
     """Every child of every parent with its bytes, hash, size and magnitude
     (the symbolic iteration with the child bytes kept)."""

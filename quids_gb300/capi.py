@@ -40,6 +40,10 @@ class Params(C.Structure):
                 ("block_size", C.c_uint32), ("flags", C.c_uint32)]
 
 
+class Op(C.Structure):
+    _fields_ = [("is_rule", C.c_int32), ("kind", C.c_int32), ("params", RuleParams)]
+
+
 class StepStats(C.Structure):
     _fields_ = [("num_parents", C.c_uint64), ("num_parents_kept", C.c_uint64), ("num_object", C.c_uint64),
                 ("num_object_after_interferences", C.c_uint64), ("num_object_out", C.c_uint64),
@@ -59,7 +63,7 @@ EXPORTS = [
     "quids_gpu_state_create", "quids_gpu_state_destroy", "quids_gpu_state_upload", "quids_gpu_state_num_object",
     "quids_gpu_state_num_bytes", "quids_gpu_state_total_proba", "quids_gpu_state_download",
     "quids_gpu_state_device_arrays", "quids_gpu_simulate", "quids_gpu_apply_modifier",
-    "quids_gpu_rule_children", "quids_gpu_state_hash", "quids_gpu_rule_children_noalloc",
+    "quids_gpu_rule_children", "quids_gpu_state_hash", "quids_gpu_rule_children_noalloc", "quids_gpu_run",
 ]
 
 _lib = None
@@ -105,6 +109,8 @@ def load(build_if_missing: bool = True):
     L.quids_gpu_simulate.argtypes = [vp, vp, C.c_int, C.POINTER(RuleParams), vp, C.POINTER(Params),
                                      C.POINTER(StepStats)]
     L.quids_gpu_apply_modifier.argtypes = [vp, vp, C.c_int, C.POINTER(RuleParams)]
+    L.quids_gpu_run.argtypes = [vp, vp, vp, C.POINTER(Op), C.c_uint64, C.POINTER(Params), C.POINTER(StepStats),
+                                C.POINTER(C.c_int)]
     L.quids_gpu_rule_children.argtypes = [vp, vp, C.c_int, C.POINTER(RuleParams), u64p, u64p, vp, vp, vp, vp]
     L.quids_gpu_state_hash.argtypes = [vp, vp, C.c_int, C.POINTER(RuleParams), vp]
     L.quids_gpu_rule_children_noalloc.argtypes = [vp, C.c_uint64, vp, vp, vp, vp, C.c_int, C.POINTER(RuleParams),

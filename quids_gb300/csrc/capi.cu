@@ -7,6 +7,7 @@
 #include <complex>
 #include <cstring>
 #include <new>
+#include <utility>
 
 #include "engine.cuh"
 #include "rules_qc.cuh"
@@ -299,6 +300,31 @@ int quids_gpu_apply_modifier(quids_gpu_ctx *ctx, quids_gpu_state *st, int kind, 
     case QUIDS_MOD_QCGD_REVERSED_STEP: return apply_modifier(ctx, st, qcgd::reversed_step{});
     }
     return QUIDS_ERR_BAD_ARG;
+}
+
+int quids_gpu_run(quids_gpu_ctx *ctx, quids_gpu_state *a, quids_gpu_state *b, const quids_gpu_op *ops,
+                  uint64_t n_ops, const quids_gpu_params *params, quids_gpu_step_stats *rule_stats,
+                  int *final_index) {
+    if (!ctx || !a || !b || a == b || (!ops && n_ops) || !params || !final_index) return QUIDS_ERR_BAD_ARG;
+    quids_gpu_state *cur = a, *other = b;
+    uint64_t r = 0;
+    for (uint64_t i = 0; i < n_ops; ++i) {
+        const quids_gpu_op &op = ops[i];
+        int rc;
+        if (op.is_rule) {
+            rc = quids_gpu_simulate(ctx, cur, op.kind, &op.params, other, params, rule_stats ? rule_stats + r : nullptr);
+            ++r;
+            if (!rc) std::swap(cur, other);
+        } else {
+            rc = quids_gpu_apply_modifier(ctx, cur, op.kind, &op.params);
+        }
+        if (rc) {
+            *final_index = cur == a ? 0 : 1;
+            return rc;
+        }
+    }
+    *final_index = cur == a ? 0 : 1;
+    return QUIDS_OK;
 }
 
 int quids_gpu_rule_children(quids_gpu_ctx *ctx, quids_gpu_state *iteration, int rule_kind,

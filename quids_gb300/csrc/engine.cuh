@@ -286,7 +286,7 @@ struct parents_view {
 // short search there instead of a search over the whole offset array.
 constexpr int kSymItems = 4;
 constexpr int kTileChildren = prim::kThreads * kSymItems;
-constexpr int kStagedParents = kTileChildren;
+constexpr int kStagedParents = 4 * kTileChildren;
 
 struct parent_tile {
     uint64_t plo;

@@ -240,10 +240,20 @@ __global__ void __launch_bounds__(kThreads) k_radix_hist(K kf, const uint64_t *d
     for (int i = threadIdx.x; i < 256; i += blockDim.x) sh[i] = 0;
     __syncthreads();
     const uint64_t n = *d_n, prefix = st->prefix, mask = st->mask;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        if (!kf.eligible(i)) continue;
-        uint64_t k = kf.key(i);
-        if ((k & mask) == prefix) atomicAdd(&sh[(k >> shift) & 255], 1u);
+    const int lane = threadIdx.x & 31;
+    const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+    const uint64_t warp = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    // warp-uniform loop; lanes holding the same digit aggregate their count
+    // (the keys' leading bits are often identical: one bin takes most items)
+    for (uint64_t base = warp * 32; base < n; base += warps * 32) {
+        const uint64_t i = base + lane;
+        unsigned d = 256;
+        if (i < n && kf.eligible(i)) {
+            uint64_t k = kf.key(i);
+            if ((k & mask) == prefix) d = (unsigned)((k >> shift) & 255);
+        }
+        const unsigned same = __match_any_sync(0xffffffffu, d);
+        if (d < 256 && lane == __ffs(same) - 1) atomicAdd(&sh[d], (unsigned)__popc(same));
     }
     __syncthreads();
     for (int i = threadIdx.x; i < 256; i += blockDim.x)

@@ -224,3 +224,26 @@ def test_bad_arguments_are_errors(ctx):
     # the context stays usable after an error
     quids.simulate(a, rules.hadamard(0), b, quids.sy_it_t())
     assert b.num_object == 2
+
+
+def test_run_gate_list_equals_per_call(ctx):
+    """quids_gpu_run (one call for a gate list) gives the same final state and
+    counters as the same gates applied call by call."""
+    gates = W.circuit_small(0)
+    ops = [quids.rule_from(g.kind == "rule", g.code, g.params) for g in gates]
+    a = quids.it_t(ctx, W.qc_zero_state(12))
+    counts = []
+    for r in ops:
+        if not r.is_rule:
+            quids.simulate(a, r)
+            continue
+        b, sy = quids.it_t(ctx), quids.sy_it_t()
+        quids.simulate(a, r, b, sy)
+        counts.append((sy.num_object, sy.num_object_after_interferences))
+        a = b
+    x, y = quids.it_t(ctx, W.qc_zero_state(12)), quids.it_t(ctx)
+    final, stats = quids.run(x, y, ops)
+    assert [(s["num_object"], s["num_object_after_interferences"]) for s in stats] == counts
+    for u, v in zip(final.download(), a.download()):
+        assert np.array_equal(u, v)
+    assert final.total_proba == a.total_proba
