@@ -145,12 +145,21 @@ def stage_bytes(st):
     sbar_p = sp / NP if NP else 0
     sbar_c = st["out_bytes"] / NS if NS else 0
     M = st["table_capacity"]
+    regions = int(44.0 * M / (32 * 1024 * 1024)) + 1 >= 4   # the library's region rule
+    if regions:   # scatter (24 in, 28 out), insert (28 in, 4 out); mark (8 in, 17 out per rep); flags + gathers
+        s2 = 8.0 * M + 84.0 * NC
+        s3 = 9.0 * NC + 17.0 * NU
+    else:         # insert (24 in, 4 out); per child slot + rep, per rep its sum
+        s2 = 8.0 * M + 28.0 * NC
+        s3 = 8.0 * NC + 32.0 * NU
+    out_layout = 56.0 * NS  # gathered magnitude and size, written magnitude, size, offset, child index
+    trunc = NU > NS
     return {
         0: 12.0 * st["num_parents"] + 8.0 * NP + sp,                   # num_child: sizes/begins/bytes, offsets
         1: sp + 36.0 * NP + 28.0 * NC,                                  # symbolic: parents in, 28 B/child out
-        2: 8.0 * M + 36.0 * NC + 36.0 * NU,                             # keys clear; hash+slot, slot+mag; groups
-        3: 8.0 * NC + 36.0 * NU + (44.0 * NS if NU == NS else 40.0 * NU),  # slot/rep per child; groups out
-        4: 8.0 * NU + 44.0 * NS,                                        # select (first pass) + layout of survivors
+        2: s2,
+        3: s3 + (40.0 * NU if trunc else out_layout),
+        4: (8.0 * NU + 40.0 * NU + out_layout) if trunc else 0.0,       # select (first pass), keep + layout
         5: 8.0 * (NC / 2048.0),                                         # per-tile norm sums
         6: NS * (sbar_p + sbar_c + 48.0),                               # populate + normalise magnitudes
         7: 0.0,

@@ -44,6 +44,15 @@ enum qd_buf_id {
     B_SCHILD,      // u64 [NS] representative child of each survivor
     B_LOOKBACK,    // u64 [3 (tiles + 2)] look-back chains
     B_TILENORM,    // double [tiles] per-tile norm sums of the survivors
+    B_RHASH,       // u64 [NC] child hashes in table-region order
+    B_RIDX,        // u32 [NC] child indices in table-region order
+    B_RMAG,        // double2 [NC] child magnitudes in table-region order
+    B_RSLOT,       // u32 [NC] table slot of each region-ordered child
+    B_FLAG,        // u8 [NC] child represents a kept group (region path)
+    B_GMAG,        // double2 [NC] summed magnitude of a kept group, at its representative (region path)
+    B_RHIST,       // u32 [R] children per table region
+    B_ROFF,        // u64 [R+1] region offsets
+    B_RCUR,        // u64 [R] region write cursors
     B_MODSTATUS,   // int: sticky error of modifier launches (reported by the next step)
     B_COUNT
 };
@@ -322,12 +331,20 @@ __device__ __forceinline__ uint64_t find_parent(const parents_view &pv, const ui
 // Symbolic iteration (src/quids.hpp:705-719): per child, its magnitude,
 // size and hash.  FAST: the rule's hash_child; otherwise populate_child into
 // a per-thread buffer of MAXC bytes followed by the rule's hasher.
+struct region_count {
+    uint64_t m;           // table slots
+    uint32_t r;           // regions (0: no region histogram)
+    unsigned int *hist;   // [r]
+};
+
 template <class Rule, int MAXC, bool FAST>
 __global__ void __launch_bounds__(prim::kThreads)
     k_symbolic(Rule rule, parents_view pv, const uint64_t *d_nc, uint64_t *hash, double2 *cmag, uint32_t *csize,
-               unsigned long long *d_maxabs, int *err) {
+               unsigned long long *d_maxabs, int *err, region_count rc) {
     __shared__ uint64_t s_cb[kStagedParents + 1];
     __shared__ parent_tile s_pt;
+    extern __shared__ unsigned int s_rhist[];  // [rc.r]
+    for (uint32_t i = threadIdx.x; i < rc.r; i += blockDim.x) s_rhist[i] = 0;
     const uint64_t nc = *d_nc;
     const uint64_t ntiles = (nc + kTileChildren - 1) / kTileChildren;
     double mx = 0;
@@ -363,11 +380,15 @@ __global__ void __launch_bounds__(prim::kThreads)
             hash[c] = h;
             cmag[c] = make_double2(m.re, m.im);
             csize[c] = sz;
+            if (rc.r) atomicAdd(&s_rhist[prim::table_region(h, rc.m, rc.r)], 1u);
             double a = fabs(m.re) > fabs(m.im) ? fabs(m.re) : fabs(m.im);
             mx = mx > a ? mx : a;
         }
         __syncthreads();  // the next tile restages s_cb
     }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < rc.r; i += blockDim.x)
+        if (s_rhist[i]) atomicAdd(&rc.hist[i], s_rhist[i]);
     unsigned long long bits = (unsigned long long)__double_as_longlong(mx);
     for (int o = 16; o > 0; o >>= 1) {
         unsigned long long y = __shfl_xor_sync(0xffffffffu, bits, o);
@@ -505,6 +526,88 @@ struct group_view {
         if (s == 0xffffffffu || rep[s] != (uint32_t)c) return false;
         m = sum(s);
         return cnorm(m) > tolerance;
+    }
+};
+
+// items of the collision-table insert: children in index order ...
+struct direct_src {
+    const uint64_t *hash;
+    const double2 *mag;
+    __device__ __forceinline__ void get(uint64_t k, uint64_t &h, uint64_t &c, double2 &m) const {
+        h = hash[k];
+        c = k;
+        m = mag[k];
+    }
+};
+// ... or in table-region order
+struct region_src {
+    const uint64_t *rhash;
+    const uint32_t *ridx;
+    const double2 *rmag;
+    __device__ __forceinline__ void get(uint64_t k, uint64_t &h, uint64_t &c, double2 &m) const {
+        h = rhash[k];
+        c = ridx[k];
+        m = rmag[k];
+    }
+};
+
+// Region path: in region order (the table region in L2), each representative
+// of a group above tolerance marks itself and stores the group's magnitude at
+// its child index, for an index-ordered compaction afterwards.
+static __global__ void __launch_bounds__(prim::kThreads)
+    k_region_groups(group_view g, const uint32_t *rslot, const uint32_t *ridx, uint8_t *flag, double2 *gmag) {
+    const uint64_t n = *g.d_nc;
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t s = rslot[k];
+        if (s == 0xffffffffu) continue;
+        const uint32_t c = ridx[k];
+        if (g.rep[s] != c) continue;
+        const mag_t m = g.sum(s);
+        if (cnorm(m) > g.tolerance) {
+            flag[c] = 1;
+            gmag[c] = make_double2(m.re, m.im);
+        }
+    }
+}
+
+struct flags_layout {
+    const uint8_t *flag;
+    const double2 *gmag;
+    const uint32_t *csize;
+    uint32_t align;
+    double2 *omag;
+    uint32_t *osize;
+    uint64_t *obegin;
+    uint64_t *schild;
+    __device__ bool select(uint64_t c) const { return flag[c] != 0; }
+    __device__ uint64_t bytes(uint64_t c) const { return padded_size(csize[c], align); }
+    __device__ double norm(uint64_t c) const {
+        const double2 m = gmag[c];
+        return cnorm(mag_t{m.x, m.y});
+    }
+    __device__ void emit(uint64_t c, uint64_t j, uint64_t off) const {
+        omag[j] = gmag[c];
+        osize[j] = csize[c];
+        obegin[j] = off;
+        schild[j] = c;
+    }
+};
+
+struct flags_collect {
+    const uint8_t *flag;
+    const double2 *gmag;
+    const uint64_t *hash;
+    uint64_t *uchild;
+    double2 *umag;
+    uint64_t *unorm;
+    uint64_t *uhash;
+    __device__ bool select(uint64_t c) const { return flag[c] != 0; }
+    __device__ void emit(uint64_t c, uint64_t j) const {
+        const double2 m = gmag[c];
+        uchild[j] = c;
+        umag[j] = m;
+        unorm[j] = (uint64_t)__double_as_longlong(cnorm(mag_t{m.x, m.y}));
+        uhash[j] = hash[c];
     }
 };
 
@@ -674,23 +777,25 @@ inline uint64_t next_pow2(uint64_t v) {
 
 // ------------------------------------------------------------- the step
 template <class Rule, int MAXC>
-inline int launch_symbolic(quids_gpu_ctx *ctx, const Rule &rule, const parents_view &pv, uint64_t nc, bool fast) {
+inline int launch_symbolic(quids_gpu_ctx *ctx, const Rule &rule, const parents_view &pv, uint64_t nc, bool fast,
+                           region_count rc) {
     uint64_t tiles = (nc + kTileChildren - 1) / kTileChildren;
     unsigned grid = (unsigned)(tiles < (uint64_t)ctx->num_sms * 8 ? tiles : (uint64_t)ctx->num_sms * 8);
     uint64_t *d_nc = ctx->d_words + W_NC;
     unsigned long long *d_maxabs = (unsigned long long *)(ctx->d_words + W_MAXABS);
     int *err = (int *)(ctx->d_words + W_STATUS);
+    const size_t smem = rc.r * sizeof(unsigned int);
     if constexpr (has_hash_child<Rule>::value) {
         if (fast) {
-            k_symbolic<Rule, 8, true><<<grid, prim::kThreads, 0, ctx->stream>>>(
+            k_symbolic<Rule, 8, true><<<grid, prim::kThreads, smem, ctx->stream>>>(
                 rule, pv, d_nc, bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG), bufp<uint32_t>(ctx, B_CSIZE),
-                d_maxabs, err);
+                d_maxabs, err, rc);
             return launched(ctx);
         }
     }
-    k_symbolic<Rule, MAXC, false><<<grid, prim::kThreads, 0, ctx->stream>>>(
+    k_symbolic<Rule, MAXC, false><<<grid, prim::kThreads, smem, ctx->stream>>>(
         rule, pv, d_nc, bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG), bufp<uint32_t>(ctx, B_CSIZE), d_maxabs,
-        err);
+        err, rc);
     return launched(ctx);
 }
 
@@ -851,16 +956,22 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, qui
 
     uint64_t M = (uint64_t)((double)NC / load) + 1;
     if (M < 1024) M = 1024;
-    if (M >= 0xffffffffull) return QUIDS_ERR_OOM;  // slot indices (and the extra slot M) are u32
+    if (M >= 0xfffffff0ull) return QUIDS_ERR_OOM;  // slot indices (and the extra slots) are u32
     s.table_capacity = M;
+    // tables larger than a share of L2 are filled region by region
+    const double table_bytes = 44.0 * (double)M;
+    uint32_t R = (uint32_t)(table_bytes / (32.0 * 1024 * 1024)) + 1;
+    if (R < 4) R = 1;
+    if (R > prim::kMaxRegions) R = prim::kMaxRegions;
+    const bool regions = R > 1;
     const uint64_t tiles_nc = (NC + prim::kTile - 1) / prim::kTile;
     QD_TRY(ensure(ctx->buf[B_HASH], NC * sizeof(uint64_t)));
     QD_TRY(ensure(ctx->buf[B_CMAG], NC * sizeof(double2)));
     QD_TRY(ensure(ctx->buf[B_CSIZE], NC * sizeof(uint32_t)));
     QD_TRY(ensure(ctx->buf[B_SLOT], NC * sizeof(uint32_t)));
     QD_TRY(ensure(ctx->buf[B_KEYS], M * sizeof(uint64_t)));
-    QD_TRY(ensure(ctx->buf[B_REP], (M + 1) * sizeof(uint32_t)));
-    QD_TRY(ensure(ctx->buf[B_ACC], 4 * (M + 1) * sizeof(uint64_t)));
+    QD_TRY(ensure(ctx->buf[B_REP], (M + 2) * sizeof(uint32_t)));
+    QD_TRY(ensure(ctx->buf[B_ACC], 4 * (M + 2) * sizeof(uint64_t)));
     QD_TRY(ensure(ctx->buf[B_SCHILD], NSB * sizeof(uint64_t)));
     QD_TRY(ensure(ctx->buf[B_TILENORM], tiles_nc * sizeof(double)));
     QD_TRY(ensure(ctx->buf[B_LOOKBACK], 3 * (tiles_nc + 2) * sizeof(uint64_t)));
@@ -874,13 +985,26 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, qui
         QD_TRY(ensure(ctx->buf[B_UNORM], NC * sizeof(uint64_t)));
         QD_TRY(ensure(ctx->buf[B_UHASH], NC * sizeof(uint64_t)));
     }
+    if (regions) {
+        QD_TRY(ensure(ctx->buf[B_RHASH], NC * sizeof(uint64_t)));
+        QD_TRY(ensure(ctx->buf[B_RIDX], NC * sizeof(uint32_t)));
+        QD_TRY(ensure(ctx->buf[B_RMAG], NC * sizeof(double2)));
+        QD_TRY(ensure(ctx->buf[B_RSLOT], NC * sizeof(uint32_t)));
+        QD_TRY(ensure(ctx->buf[B_FLAG], NC));
+        QD_TRY(ensure(ctx->buf[B_GMAG], NC * sizeof(double2)));
+        QD_TRY(ensure(ctx->buf[B_RHIST], R * sizeof(unsigned int)));
+        QD_TRY(ensure(ctx->buf[B_ROFF], (R + 1) * sizeof(uint64_t)));
+        QD_TRY(ensure(ctx->buf[B_RCUR], R * sizeof(uint64_t)));
+        QD_CUDA(cudaMemsetAsync(ctx->buf[B_RHIST].p, 0, R * sizeof(unsigned int), ctx->stream));
+    }
 
     // ---- stage 1: symbolic iteration (src/quids.hpp:647-721)
     begin_stage(1);
+    region_count rc{M, regions ? R : 0u, regions ? bufp<unsigned int>(ctx, B_RHIST) : nullptr};
     if (maxsize <= 256) {
-        QD_TRY((launch_symbolic<Rule, 256>(ctx, rule, pv, NC, fast)));
+        QD_TRY((launch_symbolic<Rule, 256>(ctx, rule, pv, NC, fast, rc)));
     } else {
-        QD_TRY((launch_symbolic<Rule, 4096>(ctx, rule, pv, NC, fast)));
+        QD_TRY((launch_symbolic<Rule, 4096>(ctx, rule, pv, NC, fast, rc)));
     }
     end_stage(1);
 
@@ -889,42 +1013,81 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, qui
     prim::table tb{bufp<uint64_t>(ctx, B_KEYS), bufp<uint32_t>(ctx, B_REP), bufp<unsigned long long>(ctx, B_ACC), M,
                    65536u};
     QD_CUDA(cudaMemsetAsync(tb.keys, 0xff, M * sizeof(uint64_t), ctx->stream));
-    QD_CUDA(cudaMemsetAsync(tb.rep + M, 0xff, sizeof(uint32_t), ctx->stream));          // the extra slot
-    QD_CUDA(cudaMemsetAsync(tb.acc + 4 * M, 0, 4 * sizeof(uint64_t), ctx->stream));
-    prim::k_table_claim<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
-        tb, bufp<uint64_t>(ctx, B_HASH), ctx->d_words + W_NC, bufp<uint32_t>(ctx, B_SLOT), err);
-    prim::k_table_accumulate<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
-        tb, bufp<uint32_t>(ctx, B_SLOT), bufp<double2>(ctx, B_CMAG), ctx->d_words + W_NC,
-        (const unsigned long long *)(ctx->d_words + W_MAXABS));
-    QD_TRY(launched(ctx, 2));
+    QD_CUDA(cudaMemsetAsync(tb.rep + M, 0xff, 2 * sizeof(uint32_t), ctx->stream));  // the two extra slots
+    QD_CUDA(cudaMemsetAsync(tb.acc + 4 * M, 0, 8 * sizeof(uint64_t), ctx->stream));
+    const unsigned long long *d_maxabs = (const unsigned long long *)(ctx->d_words + W_MAXABS);
+    if (!regions) {
+        direct_src src{bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG)};
+        prim::k_table_insert<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
+            tb, src, ctx->d_words + W_NC, d_maxabs, bufp<uint32_t>(ctx, B_SLOT), err);
+        QD_TRY(launched(ctx));
+    } else {
+        prim::k_region_offsets<<<1, 1024, 0, ctx->stream>>>(bufp<unsigned int>(ctx, B_RHIST), R,
+                                                           bufp<uint64_t>(ctx, B_ROFF),
+                                                           bufp<unsigned long long>(ctx, B_RCUR));
+        const uint64_t tiles = tiles_nc;
+        unsigned g = (unsigned)(tiles < (uint64_t)ctx->num_sms * 8 ? tiles : (uint64_t)ctx->num_sms * 8);
+        prim::k_region_scatter<<<g, prim::kThreads, prim::region_scatter_smem(R), ctx->stream>>>(
+            bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG), ctx->d_words + W_NC, M, R,
+            bufp<uint64_t>(ctx, B_ROFF), bufp<unsigned long long>(ctx, B_RCUR), bufp<uint64_t>(ctx, B_RHASH),
+            bufp<uint32_t>(ctx, B_RIDX), bufp<double2>(ctx, B_RMAG), err);
+        region_src src{bufp<uint64_t>(ctx, B_RHASH), bufp<uint32_t>(ctx, B_RIDX), bufp<double2>(ctx, B_RMAG)};
+        prim::k_table_insert<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
+            tb, src, ctx->d_words + W_NC, d_maxabs, bufp<uint32_t>(ctx, B_RSLOT), err);
+        QD_TRY(launched(ctx, 3));
+    }
     end_stage(2);
 
     // ---- stage 3 (+4): representatives above tolerance (src/quids.hpp:819-823),
     // truncation (src/quids.hpp:866-900, ties by lower hash) and the output
     // layout (src/quids.hpp:927-948), with per-tile norm sums for normalize
     group_view gv{bufp<uint32_t>(ctx, B_SLOT), bufp<uint32_t>(ctx, B_REP), bufp<unsigned long long>(ctx, B_ACC),
-                  ctx->d_words + W_NC, (const unsigned long long *)(ctx->d_words + W_MAXABS), prm.tolerance};
+                  ctx->d_words + W_NC, d_maxabs, prm.tolerance};
     const uint32_t align = prm.align_byte_length;
     double *tile_norm = bufp<double>(ctx, B_TILENORM);
     begin_stage(3);
+    if (regions) {  // mark representatives in region order, compact in index order
+        QD_CUDA(cudaMemsetAsync(ctx->buf[B_FLAG].p, 0, NC, ctx->stream));
+        k_region_groups<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
+            gv, bufp<uint32_t>(ctx, B_RSLOT), bufp<uint32_t>(ctx, B_RIDX), bufp<uint8_t>(ctx, B_FLAG),
+            bufp<double2>(ctx, B_GMAG));
+        QD_TRY(launched(ctx));
+    }
     if (!may_truncate) {
         prim::lookback lbc, lbb;
         QD_TRY(lookback_chain(ctx, NC, 0, lbc));
         QD_TRY(lookback_chain(ctx, NC, 1, lbb));
-        groups_layout f{gv, bufp<uint32_t>(ctx, B_CSIZE), align, (double2 *)out->mag.p, (uint32_t *)out->size.p,
-                        (uint64_t *)out->begin.p, bufp<uint64_t>(ctx, B_SCHILD)};
-        prim::k_compact_layout<<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
-            f, ctx->d_words + W_NC, ctx->d_words + W_NS, ctx->d_words + W_OUTBYTES, (uint64_t *)out->begin.p,
-            tile_norm, lbc, lbb);
+        if (regions) {
+            flags_layout f{bufp<uint8_t>(ctx, B_FLAG), bufp<double2>(ctx, B_GMAG), bufp<uint32_t>(ctx, B_CSIZE), align,
+                           (double2 *)out->mag.p, (uint32_t *)out->size.p, (uint64_t *)out->begin.p,
+                           bufp<uint64_t>(ctx, B_SCHILD)};
+            prim::k_compact_layout<<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
+                f, ctx->d_words + W_NC, ctx->d_words + W_NS, ctx->d_words + W_OUTBYTES, (uint64_t *)out->begin.p,
+                tile_norm, lbc, lbb);
+        } else {
+            groups_layout f{gv, bufp<uint32_t>(ctx, B_CSIZE), align, (double2 *)out->mag.p, (uint32_t *)out->size.p,
+                            (uint64_t *)out->begin.p, bufp<uint64_t>(ctx, B_SCHILD)};
+            prim::k_compact_layout<<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
+                f, ctx->d_words + W_NC, ctx->d_words + W_NS, ctx->d_words + W_OUTBYTES, (uint64_t *)out->begin.p,
+                tile_norm, lbc, lbb);
+        }
         QD_TRY(launched(ctx));
         end_stage(3);
     } else {
         prim::lookback lb;
         QD_TRY(lookback_chain(ctx, NC, 0, lb));
-        groups_collect f{gv, bufp<uint64_t>(ctx, B_HASH), bufp<uint64_t>(ctx, B_UCHILD), bufp<double2>(ctx, B_UMAG),
-                         bufp<uint64_t>(ctx, B_UNORM), bufp<uint64_t>(ctx, B_UHASH)};
-        prim::k_compact<<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(f, ctx->d_words + W_NC,
-                                                                                   ctx->d_words + W_NU, lb);
+        if (regions) {
+            flags_collect f{bufp<uint8_t>(ctx, B_FLAG), bufp<double2>(ctx, B_GMAG), bufp<uint64_t>(ctx, B_HASH),
+                            bufp<uint64_t>(ctx, B_UCHILD), bufp<double2>(ctx, B_UMAG), bufp<uint64_t>(ctx, B_UNORM),
+                            bufp<uint64_t>(ctx, B_UHASH)};
+            prim::k_compact<<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(f, ctx->d_words + W_NC,
+                                                                                       ctx->d_words + W_NU, lb);
+        } else {
+            groups_collect f{gv, bufp<uint64_t>(ctx, B_HASH), bufp<uint64_t>(ctx, B_UCHILD),
+                             bufp<double2>(ctx, B_UMAG), bufp<uint64_t>(ctx, B_UNORM), bufp<uint64_t>(ctx, B_UHASH)};
+            prim::k_compact<<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(f, ctx->d_words + W_NC,
+                                                                                       ctx->d_words + W_NU, lb);
+        }
         QD_TRY(launched(ctx));
         end_stage(3);
         begin_stage(4);

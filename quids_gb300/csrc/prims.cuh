@@ -281,13 +281,17 @@ static __global__ void k_radix_pick(select_state *st, unsigned long long *hist, 
 }
 
 // ---------------------------------------------------- collision table
-// keys[M] (kEmptyKey = free; set by a memset before each step), rep[M+1]
-// (u32 minimum child index) and acc[M+1][4] (re lo, re hi, im lo, im hi: one
-// 32-byte sector per slot).  A slot's rep and acc are initialised by the
-// thread whose CAS claims the slot, so only the keys are cleared per step.
-// Slot M holds the children whose hash equals kEmptyKey (initialised by the
-// host).  M need not be a power of two: the home slot is the high half of
-// (mixed hash) * M.
+// keys[M] (kEmptyKey = free; cleared before each step), rep[M+2] (u32
+// minimum child index) and acc[M+2][4] (re lo, re hi, im lo, im hi: one
+// 32-byte sector per slot).  A slot is claimed by a CAS from kEmptyKey to
+// kBusyKey; the claimer initialises rep and acc, fences, then publishes the
+// hash, so the other members of the group only touch an initialised slot and
+// nothing but the keys needs clearing.  Children whose hash is kEmptyKey or
+// kBusyKey use the extra slots M and M+1 (initialised by the host).  M need
+// not be a power of two: the home slot is the high half of (mixed hash) * M.
+constexpr uint64_t kBusyKey = ~0ull - 1;
+constexpr uint32_t kClaimSpinLimit = 1u << 20;
+
 struct table {
     uint64_t *keys;
     uint32_t *rep;
@@ -308,61 +312,161 @@ __device__ __forceinline__ void fix_atomic_add(unsigned long long *w, fix128 v) 
     if (hi) atomicAdd(&w[1], hi);
 }
 
-// Pass 1: every child finds or claims the slot of its hash; slot_of[c] = slot
-// (0xffffffff when the probe limit is reached: QUIDS_ERR_TABLE_FULL).
-static __global__ void __launch_bounds__(kThreads) k_table_claim(table t, const uint64_t *hash, const uint64_t *d_n,
-                                                           uint32_t *slot_of, int *err) {
-    const uint64_t n = *d_n;
-    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t h = hash[c];
-        uint64_t s;
-        if (h == kEmptyKey) {
-            s = t.m;
-        } else {
-            s = table_home(h, t.m);
-            uint32_t probe = 0;
-            while (true) {
-                uint64_t k = ld_volatile_u64(&t.keys[s]);
-                if (k == h) break;
-                if (k == kEmptyKey) {
-                    uint64_t old = atomicCAS((unsigned long long *)&t.keys[s], kEmptyKey, h);
-                    if (old == kEmptyKey) {  // claimed: initialise the slot's group
-                        ulonglong4_32a zero;
-                        zero.x = zero.y = zero.z = zero.w = 0;
-                        t.rep[s] = 0xffffffffu;
-                        *(ulonglong4_32a *)&t.acc[4 * s] = zero;
-                        break;
-                    }
-                    if (old == h) break;
-                }
-                if (++s == t.m) s = 0;
-                if (++probe >= t.max_probes) {
-                    set_error(err, QUIDS_ERR_TABLE_FULL);
-                    s = ~0ull;
-                    break;
-                }
+// slot of hash h (claiming a free one), or ~0 on a full table / expired wait
+__device__ __forceinline__ uint64_t table_slot(const table &t, uint64_t h, int *err) {
+    if (h == kEmptyKey) return t.m;
+    if (h == kBusyKey) return t.m + 1;
+    uint64_t s = table_home(h, t.m);
+    for (uint32_t probe = 0; probe < t.max_probes; ++probe) {
+        uint64_t k = ld_volatile_u64(&t.keys[s]);
+        if (k == kEmptyKey) {
+            k = atomicCAS((unsigned long long *)&t.keys[s], kEmptyKey, kBusyKey);
+            if (k == kEmptyKey) {  // claimed: initialise the group, then publish the key
+                ulonglong4_32a zero;
+                zero.x = zero.y = zero.z = zero.w = 0;
+                t.rep[s] = 0xffffffffu;
+                *(ulonglong4_32a *)&t.acc[4 * s] = zero;
+                __threadfence();
+                atomicExch((unsigned long long *)&t.keys[s], h);
+                return s;
             }
         }
-        slot_of[c] = (uint32_t)s;
+        if (k == kBusyKey) {  // another thread is initialising this slot
+            uint32_t it = 0;
+            do {
+                __nanosleep(32);
+                k = ld_volatile_u64(&t.keys[s]);
+            } while (k == kBusyKey && ++it < kClaimSpinLimit);
+            if (k == kBusyKey) {
+                set_error(err, QUIDS_ERR_TIMEOUT);
+                return ~0ull;
+            }
+        }
+        if (k == h) {
+            __threadfence();  // the claimer's initialisation is visible
+            return s;
+        }
+        if (++s == t.m) s = 0;
+    }
+    set_error(err, QUIDS_ERR_TABLE_FULL);
+    return ~0ull;
+}
+
+// Every child item (src(k) -> hash, child index, magnitude) joins its group:
+// slot_out[k] = slot; rep = minimum child index; acc += magnitude as an exact
+// 128-bit fixed-point sum per component (scale 2^-F, F from the largest
+// component and the child count), independent of the order of the atomics.
+template <class Src>
+__global__ void __launch_bounds__(kThreads) k_table_insert(table t, Src src, const uint64_t *d_n,
+                                                            const unsigned long long *d_maxabs, uint32_t *slot_out,
+                                                            int *err) {
+    const uint64_t n = *d_n;
+    const int F = fix_scale(__longlong_as_double((long long)*d_maxabs), n);
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t h, c;
+        double2 m;
+        src.get(k, h, c, m);
+        const uint64_t s = table_slot(t, h, err);
+        slot_out[k] = (uint32_t)s;
+        if (s == ~0ull) continue;
+        atomicMin(&t.rep[s], (uint32_t)c);
+        fix_atomic_add(&t.acc[4ull * s + 0], to_fix(m.x, F));
+        fix_atomic_add(&t.acc[4ull * s + 2], to_fix(m.y, F));
     }
 }
 
-// Pass 2: rep = minimum child index of the group; acc += magnitude as an
-// exact 128-bit fixed-point sum per component (scale 2^-F, F from the largest
-// component and the child count), so the sum is independent of the order of
-// the atomics.
-static __global__ void __launch_bounds__(kThreads) k_table_accumulate(table t, const uint32_t *slot_of,
-                                                                const double2 *mag, const uint64_t *d_n,
-                                                                const unsigned long long *d_maxabs) {
+// ------------------------------------------------------ table regions
+// For tables larger than L2 the children are first grouped by table region
+// (a contiguous range of home slots), so the insert pass works on one region
+// of the table at a time.  region(h) = home(h) * R / M.
+__device__ __forceinline__ uint32_t table_region(uint64_t h, uint64_t m, uint32_t r) {
+    if (h >= kBusyKey) return 0;
+    return (uint32_t)((table_home(h, m) * (uint64_t)r) / m);
+}
+
+constexpr uint32_t kMaxRegions = 2048;
+__host__ __device__ constexpr size_t region_scatter_smem(uint32_t r) { return 4 * ((r + 1) & ~1u) + 8 * (size_t)r; }
+
+// roff[r] = exclusive prefix of hist (one block), cursor zeroed
+static __global__ void __launch_bounds__(1024) k_region_offsets(const unsigned int *hist, uint32_t r,
+                                                                 uint64_t *roff, unsigned long long *cursor) {
+    __shared__ uint64_t sm[1024];
+    const uint32_t per = (r + 1023) / 1024;
+    uint64_t sum = 0;
+    for (uint32_t k = 0; k < per; ++k) {
+        uint32_t i = threadIdx.x * per + k;
+        if (i < r) sum += hist[i];
+    }
+    sm[threadIdx.x] = sum;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {  // inclusive scan (Hillis-Steele)
+        uint64_t v = threadIdx.x >= (unsigned)o ? sm[threadIdx.x - o] : 0;
+        __syncthreads();
+        sm[threadIdx.x] += v;
+        __syncthreads();
+    }
+    uint64_t run = threadIdx.x ? sm[threadIdx.x - 1] : 0;
+    for (uint32_t k = 0; k < per; ++k) {
+        uint32_t i = threadIdx.x * per + k;
+        if (i < r) {
+            roff[i] = run;
+            cursor[i] = 0;
+            run += hist[i];
+        }
+    }
+    if (threadIdx.x == 1023) roff[r] = sm[1023];
+}
+
+// Scatters the child records into region order: a block reserves, per
+// region, one range for all its items, then each item takes its rank
+// (warp-aggregated shared atomics).  The order inside a region is
+// unspecified; the insert pass does not depend on it.
+static __global__ void __launch_bounds__(kThreads)
+    k_region_scatter(const uint64_t *hash, const double2 *mag, const uint64_t *d_n, uint64_t m, uint32_t r,
+                     const uint64_t *roff, unsigned long long *cursor, uint64_t *rhash, uint32_t *ridx,
+                     double2 *rmag, int *err) {
+    extern __shared__ unsigned int s_region[];  // counts [r], then 8-byte aligned reserved bases [r]
+    unsigned int *s_cnt = s_region;
+    unsigned long long *s_base = (unsigned long long *)(s_region + ((r + 1) & ~1u));
     const uint64_t n = *d_n;
-    const int F = fix_scale(__longlong_as_double((long long)*d_maxabs), n);
-    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t s = slot_of[c];
-        if (s == 0xffffffffu) continue;
-        atomicMin(&t.rep[s], (uint32_t)c);
-        const double2 m = mag[c];
-        fix_atomic_add(&t.acc[4ull * s + 0], to_fix(m.x, F));
-        fix_atomic_add(&t.acc[4ull * s + 2], to_fix(m.y, F));
+    const int lane = threadIdx.x & 31;
+    const uint64_t ntiles = (n + kTile - 1) / kTile;
+    for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        for (uint32_t i = threadIdx.x; i < r; i += blockDim.x) s_cnt[i] = 0;
+        __syncthreads();
+        const uint64_t base = tile * kTile;
+        uint32_t reg[kItems], rank[kItems];
+#pragma unroll
+        for (int k = 0; k < kItems; ++k) {
+            const uint64_t i = base + threadIdx.x + (uint64_t)k * kThreads;
+            unsigned g = 0xffffffffu;
+            if (i < n) g = table_region(hash[i], m, r);
+            const unsigned same = __match_any_sync(0xffffffffu, g);
+            const int leader = __ffs(same) - 1;
+            unsigned first = 0;
+            if (g != 0xffffffffu && lane == leader) first = atomicAdd(&s_cnt[g], (unsigned)__popc(same));
+            first = __shfl_sync(0xffffffffu, first, leader);
+            reg[k] = g;
+            rank[k] = first + (unsigned)__popc(same & ((1u << lane) - 1));
+        }
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < r; i += blockDim.x)
+            if (s_cnt[i]) s_base[i] = roff[i] + atomicAdd(&cursor[i], (unsigned long long)s_cnt[i]);
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < kItems; ++k) {
+            const uint64_t i = base + threadIdx.x + (uint64_t)k * kThreads;
+            if (i >= n) break;
+            const uint64_t pos = s_base[reg[k]] + rank[k];
+            if (pos >= roff[reg[k] + 1]) {  // counts disagree with the histogram
+                set_error(err, QUIDS_ERR_CUDA);
+                continue;
+            }
+            rhash[pos] = hash[i];
+            ridx[pos] = (uint32_t)i;
+            rmag[pos] = mag[i];
+        }
+        __syncthreads();
     }
 }
 

@@ -73,3 +73,43 @@ def assert_state_parity(got, exp, qcgd: bool, truncated: bool = False, what: str
         keys = eo
     bad = [k for k in keys if not mag_close(g[k], e[k])]
     assert not bad, f"{what}: {len(bad)} magnitudes differ, e.g. {g[bad[0]]} vs {e[bad[0]]}"
+
+
+def _rows(p):
+    """fixed-size objects as a (n, size) uint8 matrix, plus magnitudes"""
+    objects, begin, size, mag = p
+    n = len(size)
+    if n == 0:
+        return np.zeros((0, 0), np.uint8), np.zeros(0, np.complex128)
+    sz = int(size[0])
+    assert (np.asarray(size) == sz).all(), "fixed-size comparison on variable-size objects"
+    idx = np.asarray(begin[:n], dtype=np.int64)[:, None] + np.arange(sz, dtype=np.int64)[None, :]
+    return np.asarray(objects)[idx], np.asarray(mag, dtype=np.complex128)
+
+
+def assert_fixed_state_parity(got, exp, truncated=False, what=""):
+    """Vectorised assert_state_parity for states of equal-size objects (large states)."""
+    g_rows, g_mag = _rows(got)
+    e_rows, e_mag = _rows(exp)
+    assert g_rows.shape == e_rows.shape, f"{what}: shapes {g_rows.shape} vs {e_rows.shape}"
+    if len(g_mag) == 0:
+        return
+    gk = np.ascontiguousarray(g_rows).view(np.dtype((np.void, g_rows.shape[1]))).ravel()
+    ek = np.ascontiguousarray(e_rows).view(np.dtype((np.void, e_rows.shape[1]))).ravel()
+    go, eo = np.argsort(gk), np.argsort(ek)
+    gk, ek, g_mag, e_mag = gk[go], ek[eo], g_mag[go], e_mag[eo]
+    if not truncated:
+        assert (gk == ek).all(), f"{what}: object sets differ"
+        keep_g = keep_e = np.ones(len(gk), bool)
+    else:
+        en = np.abs(e_mag) ** 2
+        tau = en.min()
+        band_e = np.abs(en - tau) <= REL * tau * 4
+        band_g = np.abs(np.abs(g_mag) ** 2 - tau) <= REL * tau * 4
+        assert (gk[~band_g] == ek[~band_e]).all() if (~band_g).sum() == (~band_e).sum() else False, \
+            f"{what}: objects outside the tie band differ"
+        keep_g, keep_e = ~band_g, ~band_e
+    a, b = g_mag[keep_g], e_mag[keep_e]
+    tol = REL * np.maximum(np.maximum(np.abs(a), np.abs(b)), FLOOR)
+    bad = np.abs(a - b) > tol
+    assert not bad.any(), f"{what}: {int(bad.sum())} magnitudes differ"

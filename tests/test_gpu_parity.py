@@ -247,3 +247,35 @@ def test_run_gate_list_equals_per_call(ctx):
     for u, v in zip(final.download(), a.download()):
         assert np.array_equal(u, v)
     assert final.total_proba == a.total_proba
+
+
+def test_large_steps_region_path(ctx, port):
+    """The 8.4M-child Hadamard applications of the 24-qubit circuit (the table
+    is filled region by region there) against the oracle from identical
+    inputs, with truncation to 2^22."""
+    from tests.parity import assert_fixed_state_parity
+    port.set_globals(1e-18, True, 8)
+    gates = [g for layer in W.circuit_layers(0) for g in layer]
+    it = quids.it_t(ctx, W.qc_zero_state(24))
+    checked = 0
+    for g in gates:
+        r = quids.rule_from(g.kind == "rule", g.code, g.params)
+        if g.kind == "mod":
+            quids.simulate(it, r)
+            continue
+        nxt, sy = quids.it_t(ctx), quids.sy_it_t()
+        big = it.num_object >= (1 << 21)
+        if big:
+            inp = it.download()
+        quids.simulate(it, r, nxt, sy, 1 << 22)
+        if big:
+            a, b = port.new_state(inp), port.new_state()
+            nc, nu = port.simulate(a, g.code, g.params, b, 1 << 22)
+            assert (sy.num_object, sy.num_object_after_interferences) == (nc, nu)
+            assert_fixed_state_parity(nxt.download(), b.store(), truncated=nu > (1 << 22), what=f"H{g.params}")
+            assert nxt.total_proba == pytest.approx(b.total_proba, rel=1e-12)
+            checked += 1
+            if checked == 3:
+                break
+        it = nxt
+    assert checked == 3
