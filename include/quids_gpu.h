@@ -86,6 +86,8 @@ typedef struct quids_gpu_params {
 #define QUIDS_FLAG_NO_FAST_HASH 1u   /* hash children through populate_child + hasher, not hash_child */
 #define QUIDS_FLAG_STAGE_TIMING 2u   /* record per-stage CUDA events and synchronise at the end of the
                                         step, so stats carries timings and total_proba */
+#define QUIDS_FLAG_NO_REGIONS 4u     /* fill the collision table in child order even when it exceeds L2 */
+#define QUIDS_FLAG_REGIONS 8u        /* fill the collision table region by region even when it is small */
 
 /* Counters of one rule step (the reference's public counters plus timing). */
 typedef struct quids_gpu_step_stats {

@@ -21,6 +21,8 @@ STATUS = {
 }
 FLAG_NO_FAST_HASH = 1
 FLAG_STAGE_TIMING = 2
+FLAG_NO_REGIONS = 4
+FLAG_REGIONS = 8
 
 
 class QuidsError(RuntimeError):

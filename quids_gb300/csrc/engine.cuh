@@ -531,24 +531,20 @@ struct group_view {
 
 // items of the collision-table insert: children in index order ...
 struct direct_src {
-    const uint64_t *hash;
-    const double2 *mag;
-    __device__ __forceinline__ void get(uint64_t k, uint64_t &h, uint64_t &c, double2 &m) const {
-        h = hash[k];
-        c = k;
-        m = mag[k];
-    }
+    const uint64_t *hash_;
+    const double2 *mag_;
+    __device__ __forceinline__ uint64_t hash(uint64_t k) const { return hash_[k]; }
+    __device__ __forceinline__ uint64_t child(uint64_t k) const { return k; }
+    __device__ __forceinline__ double2 mag(uint64_t k) const { return mag_[k]; }
 };
 // ... or in table-region order
 struct region_src {
     const uint64_t *rhash;
     const uint32_t *ridx;
     const double2 *rmag;
-    __device__ __forceinline__ void get(uint64_t k, uint64_t &h, uint64_t &c, double2 &m) const {
-        h = rhash[k];
-        c = ridx[k];
-        m = rmag[k];
-    }
+    __device__ __forceinline__ uint64_t hash(uint64_t k) const { return rhash[k]; }
+    __device__ __forceinline__ uint64_t child(uint64_t k) const { return ridx[k]; }
+    __device__ __forceinline__ double2 mag(uint64_t k) const { return rmag[k]; }
 };
 
 // Region path: in region order (the table region in L2), each representative
@@ -963,6 +959,8 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, qui
     uint32_t R = (uint32_t)(table_bytes / (32.0 * 1024 * 1024)) + 1;
     if (R < 4) R = 1;
     if (R > prim::kMaxRegions) R = prim::kMaxRegions;
+    if (prm.flags & QUIDS_FLAG_NO_REGIONS) R = 1;
+    if ((prm.flags & QUIDS_FLAG_REGIONS) && R < 4) R = 4;
     const bool regions = R > 1;
     const uint64_t tiles_nc = (NC + prim::kTile - 1) / prim::kTile;
     QD_TRY(ensure(ctx->buf[B_HASH], NC * sizeof(uint64_t)));
@@ -970,8 +968,8 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, qui
     QD_TRY(ensure(ctx->buf[B_CSIZE], NC * sizeof(uint32_t)));
     QD_TRY(ensure(ctx->buf[B_SLOT], NC * sizeof(uint32_t)));
     QD_TRY(ensure(ctx->buf[B_KEYS], M * sizeof(uint64_t)));
-    QD_TRY(ensure(ctx->buf[B_REP], (M + 2) * sizeof(uint32_t)));
-    QD_TRY(ensure(ctx->buf[B_ACC], 4 * (M + 2) * sizeof(uint64_t)));
+    QD_TRY(ensure(ctx->buf[B_REP], (M + 1) * sizeof(uint32_t)));
+    QD_TRY(ensure(ctx->buf[B_ACC], 4 * (M + 1) * sizeof(uint64_t)));
     QD_TRY(ensure(ctx->buf[B_SCHILD], NSB * sizeof(uint64_t)));
     QD_TRY(ensure(ctx->buf[B_TILENORM], tiles_nc * sizeof(double)));
     QD_TRY(ensure(ctx->buf[B_LOOKBACK], 3 * (tiles_nc + 2) * sizeof(uint64_t)));
@@ -1013,14 +1011,16 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, qui
     prim::table tb{bufp<uint64_t>(ctx, B_KEYS), bufp<uint32_t>(ctx, B_REP), bufp<unsigned long long>(ctx, B_ACC), M,
                    65536u};
     QD_CUDA(cudaMemsetAsync(tb.keys, 0xff, M * sizeof(uint64_t), ctx->stream));
-    QD_CUDA(cudaMemsetAsync(tb.rep + M, 0xff, 2 * sizeof(uint32_t), ctx->stream));  // the two extra slots
-    QD_CUDA(cudaMemsetAsync(tb.acc + 4 * M, 0, 8 * sizeof(uint64_t), ctx->stream));
+    QD_CUDA(cudaMemsetAsync(tb.rep + M, 0xff, sizeof(uint32_t), ctx->stream));  // the extra slot
+    QD_CUDA(cudaMemsetAsync(tb.acc + 4 * M, 0, 4 * sizeof(uint64_t), ctx->stream));
     const unsigned long long *d_maxabs = (const unsigned long long *)(ctx->d_words + W_MAXABS);
     if (!regions) {
         direct_src src{bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG)};
-        prim::k_table_insert<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
-            tb, src, ctx->d_words + W_NC, d_maxabs, bufp<uint32_t>(ctx, B_SLOT), err);
-        QD_TRY(launched(ctx));
+        prim::k_table_claim<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
+            tb, src, ctx->d_words + W_NC, bufp<uint32_t>(ctx, B_SLOT), err);
+        prim::k_table_accumulate<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
+            tb, src, bufp<uint32_t>(ctx, B_SLOT), ctx->d_words + W_NC, d_maxabs);
+        QD_TRY(launched(ctx, 2));
     } else {
         prim::k_region_offsets<<<1, 1024, 0, ctx->stream>>>(bufp<unsigned int>(ctx, B_RHIST), R,
                                                            bufp<uint64_t>(ctx, B_ROFF),
@@ -1032,9 +1032,11 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, qui
             bufp<uint64_t>(ctx, B_ROFF), bufp<unsigned long long>(ctx, B_RCUR), bufp<uint64_t>(ctx, B_RHASH),
             bufp<uint32_t>(ctx, B_RIDX), bufp<double2>(ctx, B_RMAG), err);
         region_src src{bufp<uint64_t>(ctx, B_RHASH), bufp<uint32_t>(ctx, B_RIDX), bufp<double2>(ctx, B_RMAG)};
-        prim::k_table_insert<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
-            tb, src, ctx->d_words + W_NC, d_maxabs, bufp<uint32_t>(ctx, B_RSLOT), err);
-        QD_TRY(launched(ctx, 3));
+        prim::k_table_claim<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
+            tb, src, ctx->d_words + W_NC, bufp<uint32_t>(ctx, B_RSLOT), err);
+        prim::k_table_accumulate<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
+            tb, src, bufp<uint32_t>(ctx, B_RSLOT), ctx->d_words + W_NC, d_maxabs);
+        QD_TRY(launched(ctx, 4));
     }
     end_stage(2);
 

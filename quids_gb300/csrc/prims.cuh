@@ -281,17 +281,14 @@ static __global__ void k_radix_pick(select_state *st, unsigned long long *hist, 
 }
 
 // ---------------------------------------------------- collision table
-// keys[M] (kEmptyKey = free; cleared before each step), rep[M+2] (u32
-// minimum child index) and acc[M+2][4] (re lo, re hi, im lo, im hi: one
-// 32-byte sector per slot).  A slot is claimed by a CAS from kEmptyKey to
-// kBusyKey; the claimer initialises rep and acc, fences, then publishes the
-// hash, so the other members of the group only touch an initialised slot and
-// nothing but the keys needs clearing.  Children whose hash is kEmptyKey or
-// kBusyKey use the extra slots M and M+1 (initialised by the host).  M need
-// not be a power of two: the home slot is the high half of (mixed hash) * M.
-constexpr uint64_t kBusyKey = ~0ull - 1;
-constexpr uint32_t kClaimSpinLimit = 1u << 20;
-
+// keys[M] (kEmptyKey = free; cleared before each step), rep[M+1] (u32
+// minimum child index) and acc[M+1][4] (re lo, re hi, im lo, im hi: one
+// 32-byte sector per slot).  Pass 1 claims slots (CAS from kEmptyKey) and the
+// claiming thread initialises the slot's rep and acc; pass 2, a separate
+// launch, accumulates, so only the keys need clearing and no fence is needed.
+// Children whose hash is kEmptyKey use the extra slot M (initialised by the
+// host).  M need not be a power of two: the home slot is the high half of
+// (mixed hash) * M.
 struct table {
     uint64_t *keys;
     uint32_t *rep;
@@ -312,64 +309,61 @@ __device__ __forceinline__ void fix_atomic_add(unsigned long long *w, fix128 v) 
     if (hi) atomicAdd(&w[1], hi);
 }
 
-// slot of hash h (claiming a free one), or ~0 on a full table / expired wait
-__device__ __forceinline__ uint64_t table_slot(const table &t, uint64_t h, int *err) {
-    if (h == kEmptyKey) return t.m;
-    if (h == kBusyKey) return t.m + 1;
-    uint64_t s = table_home(h, t.m);
-    for (uint32_t probe = 0; probe < t.max_probes; ++probe) {
-        uint64_t k = ld_volatile_u64(&t.keys[s]);
-        if (k == kEmptyKey) {
-            k = atomicCAS((unsigned long long *)&t.keys[s], kEmptyKey, kBusyKey);
-            if (k == kEmptyKey) {  // claimed: initialise the group, then publish the key
-                ulonglong4_32a zero;
-                zero.x = zero.y = zero.z = zero.w = 0;
-                t.rep[s] = 0xffffffffu;
-                *(ulonglong4_32a *)&t.acc[4 * s] = zero;
-                __threadfence();
-                atomicExch((unsigned long long *)&t.keys[s], h);
-                return s;
+// Pass 1: every child item (src.hash(k)) finds or claims the slot of its
+// hash; slot_out[k] = slot, or 0xffffffff at the probe limit
+// (QUIDS_ERR_TABLE_FULL).
+template <class Src>
+__global__ void __launch_bounds__(kThreads) k_table_claim(table t, Src src, const uint64_t *d_n, uint32_t *slot_out,
+                                                           int *err) {
+    const uint64_t n = *d_n;
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t h = src.hash(k);
+        uint64_t s;
+        if (h == kEmptyKey) {
+            s = t.m;
+        } else {
+            s = table_home(h, t.m);
+            uint32_t probe = 0;
+            while (true) {
+                uint64_t key = ld_volatile_u64(&t.keys[s]);
+                if (key == h) break;
+                if (key == kEmptyKey) {
+                    key = atomicCAS((unsigned long long *)&t.keys[s], kEmptyKey, h);
+                    if (key == kEmptyKey) {  // claimed: initialise the slot's group
+                        ulonglong4_32a zero;
+                        zero.x = zero.y = zero.z = zero.w = 0;
+                        t.rep[s] = 0xffffffffu;
+                        *(ulonglong4_32a *)&t.acc[4 * s] = zero;
+                        break;
+                    }
+                    if (key == h) break;
+                }
+                if (++s == t.m) s = 0;
+                if (++probe >= t.max_probes) {
+                    set_error(err, QUIDS_ERR_TABLE_FULL);
+                    s = ~0ull;
+                    break;
+                }
             }
         }
-        if (k == kBusyKey) {  // another thread is initialising this slot
-            uint32_t it = 0;
-            do {
-                __nanosleep(32);
-                k = ld_volatile_u64(&t.keys[s]);
-            } while (k == kBusyKey && ++it < kClaimSpinLimit);
-            if (k == kBusyKey) {
-                set_error(err, QUIDS_ERR_TIMEOUT);
-                return ~0ull;
-            }
-        }
-        if (k == h) {
-            __threadfence();  // the claimer's initialisation is visible
-            return s;
-        }
-        if (++s == t.m) s = 0;
+        slot_out[k] = (uint32_t)s;
     }
-    set_error(err, QUIDS_ERR_TABLE_FULL);
-    return ~0ull;
 }
 
-// Every child item (src(k) -> hash, child index, magnitude) joins its group:
-// slot_out[k] = slot; rep = minimum child index; acc += magnitude as an exact
-// 128-bit fixed-point sum per component (scale 2^-F, F from the largest
+// Pass 2: rep = minimum child index of the group; acc += magnitude as an
+// exact 128-bit fixed-point sum per component (scale 2^-F, F from the largest
 // component and the child count), independent of the order of the atomics.
 template <class Src>
-__global__ void __launch_bounds__(kThreads) k_table_insert(table t, Src src, const uint64_t *d_n,
-                                                            const unsigned long long *d_maxabs, uint32_t *slot_out,
-                                                            int *err) {
+__global__ void __launch_bounds__(kThreads) k_table_accumulate(table t, Src src, const uint32_t *slot_of,
+                                                                const uint64_t *d_n,
+                                                                const unsigned long long *d_maxabs) {
     const uint64_t n = *d_n;
     const int F = fix_scale(__longlong_as_double((long long)*d_maxabs), n);
     for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
-        uint64_t h, c;
-        double2 m;
-        src.get(k, h, c, m);
-        const uint64_t s = table_slot(t, h, err);
-        slot_out[k] = (uint32_t)s;
-        if (s == ~0ull) continue;
-        atomicMin(&t.rep[s], (uint32_t)c);
+        const uint32_t s = slot_of[k];
+        if (s == 0xffffffffu) continue;
+        atomicMin(&t.rep[s], (uint32_t)src.child(k));
+        const double2 m = src.mag(k);
         fix_atomic_add(&t.acc[4ull * s + 0], to_fix(m.x, F));
         fix_atomic_add(&t.acc[4ull * s + 2], to_fix(m.y, F));
     }
@@ -380,7 +374,7 @@ __global__ void __launch_bounds__(kThreads) k_table_insert(table t, Src src, con
 // (a contiguous range of home slots), so the insert pass works on one region
 // of the table at a time.  region(h) = home(h) * R / M.
 __device__ __forceinline__ uint32_t table_region(uint64_t h, uint64_t m, uint32_t r) {
-    if (h >= kBusyKey) return 0;
+    if (h == kEmptyKey) return 0;
     return (uint32_t)((table_home(h, m) * (uint64_t)r) / m);
 }
 
