@@ -53,6 +53,8 @@ enum qd_buf_id {
     B_RHIST,       // u32 [R] children per table region
     B_ROFF,        // u64 [R+1] region offsets
     B_RCUR,        // u64 [R] region write cursors
+    B_TILEPAR,     // u64 [tiles+1] first parent of each tile of children
+    B_CPAR,        // u32 [NC] kept-parent index of each child
     B_MODSTATUS,   // int: sticky error of modifier launches (reported by the next step)
     B_COUNT
 };
@@ -290,59 +292,41 @@ struct parents_view {
     uint64_t np;
 };
 
-// The children of one tile come from a contiguous run of parents; their
-// offsets are staged in shared memory so each child finds its parent with a
-// short search there instead of a search over the whole offset array.
-constexpr int kSymItems = 4;
-constexpr int kTileChildren = prim::kThreads * kSymItems;
-constexpr int kStagedParents = 4 * kTileChildren;
-
-struct parent_tile {
-    uint64_t plo;
-    int count;  // staged parents, or -1: too many, search globally
-};
-
-__device__ __forceinline__ void stage_parents(const parents_view &pv, uint64_t c_first, uint64_t c_last,
-                                              uint64_t *s_cb, parent_tile *s_pt) {
-    if (threadIdx.x == 0) {
-        uint64_t plo = parent_of(pv.cbeg, pv.np, c_first);
-        uint64_t phi = parent_of(pv.cbeg, pv.np, c_last);
-        s_pt->plo = plo;
-        s_pt->count = (phi - plo + 1 <= (uint64_t)kStagedParents) ? (int)(phi - plo + 1) : -1;
-    }
-    __syncthreads();
-    const int cnt = s_pt->count;
-    const uint64_t plo = s_pt->plo;
-    for (int k = threadIdx.x; k <= cnt; k += blockDim.x) s_cb[k] = pv.cbeg[plo + k];
-    __syncthreads();
-}
-
-__device__ __forceinline__ uint64_t find_parent(const parents_view &pv, const uint64_t *s_cb, const parent_tile &pt,
-                                                uint64_t c) {
-    if (pt.count < 0) return parent_of(pv.cbeg, pv.np, c);
-    int lo = 0, hi = pt.count;  // s_cb[lo] <= c < s_cb[hi]
-    while (hi - lo > 1) {
-        int mid = (lo + hi) >> 1;
-        if (s_cb[mid] <= c) lo = mid; else hi = mid;
-    }
-    return pt.plo + (uint64_t)lo;
-}
-
-// Symbolic iteration (src/quids.hpp:705-719): per child, its magnitude,
-// size and hash.  FAST: the rule's hash_child; otherwise populate_child into
-// a per-thread buffer of MAXC bytes followed by the rule's hasher.
 struct region_count {
     uint64_t m;           // table slots
     uint32_t r;           // regions (0: no region histogram)
     unsigned int *hist;   // [r]
 };
 
+// The children of one tile of kTileChildren come from a contiguous run of
+// parents, [tile_first[t], tile_first[t+1]]; their offsets are staged in
+// shared memory so each child finds its parent with a short search there.
+constexpr int kSymItems = 4;
+constexpr int kTileChildren = prim::kThreads * kSymItems;
+constexpr int kStagedParents = 4 * kTileChildren;
+
+// tile_first[t] = the parent holding child t * kTileChildren; tile_first[tiles] = np - 1
+static __global__ void __launch_bounds__(prim::kThreads)
+    k_tile_parents(const uint64_t *cbeg, uint64_t np, uint64_t tiles, uint64_t *tile_first) {
+    for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < np; p += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t lo = cbeg[p], hi = cbeg[p + 1];
+        if (hi > lo) {
+            for (uint64_t t = (lo + kTileChildren - 1) / kTileChildren; t * kTileChildren < hi; ++t) tile_first[t] = p;
+        }
+        if (p == np - 1) tile_first[tiles] = np - 1;
+    }
+}
+
+// Symbolic iteration (src/quids.hpp:705-719): per child, its magnitude,
+// size, hash and parent.  FAST: the rule's hash_child; otherwise
+// populate_child into a per-thread buffer of MAXC bytes followed by the
+// rule's hasher.
 template <class Rule, int MAXC, bool FAST>
 __global__ void __launch_bounds__(prim::kThreads)
-    k_symbolic(Rule rule, parents_view pv, const uint64_t *d_nc, uint64_t *hash, double2 *cmag, uint32_t *csize,
-               unsigned long long *d_maxabs, int *err, region_count rc) {
+    k_symbolic(Rule rule, parents_view pv, const uint64_t *tile_first, const uint64_t *d_nc, uint64_t *hash,
+               double2 *cmag, uint32_t *csize, uint32_t *cpar, unsigned long long *d_maxabs, int *err,
+               region_count rc) {
     __shared__ uint64_t s_cb[kStagedParents + 1];
-    __shared__ parent_tile s_pt;
     extern __shared__ unsigned int s_rhist[];  // [rc.r]
     for (uint32_t i = threadIdx.x; i < rc.r; i += blockDim.x) s_rhist[i] = 0;
     const uint64_t nc = *d_nc;
@@ -351,13 +335,26 @@ __global__ void __launch_bounds__(prim::kThreads)
     for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const uint64_t c0 = t * kTileChildren;
         const uint64_t c1 = c0 + kTileChildren < nc ? c0 + kTileChildren : nc;
-        stage_parents(pv, c0, c1 - 1, s_cb, &s_pt);
-        const parent_tile pt = s_pt;
+        const uint64_t plo = tile_first[t], phi = tile_first[t + 1];
+        const int count = phi - plo + 1 <= (uint64_t)kStagedParents ? (int)(phi - plo + 1) : -1;
+        __syncthreads();  // the previous tile is done with s_cb
+        for (int k = threadIdx.x; k <= count; k += blockDim.x) s_cb[k] = pv.cbeg[plo + k];
+        __syncthreads();
 #pragma unroll
         for (int k = 0; k < kSymItems; ++k) {
             const uint64_t c = c0 + threadIdx.x + (uint64_t)k * prim::kThreads;
             if (c >= c1) break;
-            uint64_t p = find_parent(pv, s_cb, pt, c);
+            uint64_t p;
+            if (count > 0) {
+                int lo = 0, hi = count;  // s_cb[lo] <= c < s_cb[hi]
+                while (hi - lo > 1) {
+                    int mid = (lo + hi) >> 1;
+                    if (s_cb[mid] <= c) lo = mid; else hi = mid;
+                }
+                p = plo + (uint64_t)lo;
+            } else {
+                p = parent_of(pv.cbeg, pv.np, c);
+            }
             uint64_t oid = pv.pidx ? pv.pidx[p] : p;
             uint32_t cid = (uint32_t)(c - pv.cbeg[p]);
             const char *pb = pv.objects + pv.begin[oid];
@@ -380,11 +377,11 @@ __global__ void __launch_bounds__(prim::kThreads)
             hash[c] = h;
             cmag[c] = make_double2(m.re, m.im);
             csize[c] = sz;
+            cpar[c] = (uint32_t)p;
             if (rc.r) atomicAdd(&s_rhist[prim::table_region(h, rc.m, rc.r)], 1u);
             double a = fabs(m.re) > fabs(m.im) ? fabs(m.re) : fabs(m.im);
             mx = mx > a ? mx : a;
         }
-        __syncthreads();  // the next tile restages s_cb
     }
     __syncthreads();
     for (uint32_t i = threadIdx.x; i < rc.r; i += blockDim.x)
@@ -402,45 +399,33 @@ __global__ void __launch_bounds__(prim::kThreads)
 // zeroed) and mag /= sqrt(total) when that factor is not 1.
 template <class Rule, int MAXC>
 __global__ void __launch_bounds__(prim::kThreads)
-    k_populate(Rule rule, parents_view pv, const uint64_t *schild, const uint64_t *d_ns, const uint64_t *obegin,
-               const uint32_t *osize, char *objects, double2 *omag, const double *d_factor, int *err) {
-    __shared__ uint64_t s_cb[kStagedParents + 1];
-    __shared__ parent_tile s_pt;
+    k_populate(Rule rule, parents_view pv, const uint64_t *schild, const uint32_t *cpar, const uint64_t *d_ns,
+               const uint64_t *obegin, const uint32_t *osize, char *objects, double2 *omag, const double *d_factor,
+               int *err) {
     const uint64_t ns = *d_ns;
     const double f = *d_factor;
-    const uint64_t ntiles = (ns + kTileChildren - 1) / kTileChildren;
-    for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        const uint64_t i0 = t * kTileChildren;
-        const uint64_t i1 = i0 + kTileChildren < ns ? i0 + kTileChildren : ns;
-        stage_parents(pv, schild[i0], schild[i1 - 1], s_cb, &s_pt);
-        const parent_tile pt = s_pt;
-#pragma unroll
-        for (int k = 0; k < kSymItems; ++k) {
-            const uint64_t i = i0 + threadIdx.x + (uint64_t)k * prim::kThreads;
-            if (i >= i1) break;
-            const uint64_t c = schild[i];
-            uint64_t p = find_parent(pv, s_cb, pt, c);
-            uint64_t oid = pv.pidx ? pv.pidx[p] : p;
-            uint32_t cid = (uint32_t)(c - pv.cbeg[p]);
-            const char *pb = pv.objects + pv.begin[oid];
-            const char *pe = pb + pv.size[oid];
-            uint64_t buf[MAXC / 8];
-            rule_populate_simple(rule, pb, pe, (char *)buf, cid);
-            uint32_t sz = osize[i];
-            if (sz > MAXC) {
-                prim::set_error(err, QUIDS_ERR_SIZE_BOUND);
-                sz = MAXC;
-            }
-            const uint64_t ob = obegin[i], oe = obegin[i + 1];
-            char *dst = objects + ob;
-            copy_bytes(dst, (const char *)buf, sz);
-            for (uint64_t q = ob + sz; q < oe; ++q) objects[q] = 0;
-            if (f != 1.0) {
-                double2 m = omag[i];
-                omag[i] = make_double2(__ddiv_rn(m.x, f), __ddiv_rn(m.y, f));
-            }
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ns; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t c = schild[i];
+        const uint64_t p = cpar[c];
+        const uint64_t oid = pv.pidx ? pv.pidx[p] : p;
+        const uint32_t cid = (uint32_t)(c - pv.cbeg[p]);
+        const char *pb = pv.objects + pv.begin[oid];
+        const char *pe = pb + pv.size[oid];
+        uint64_t buf[MAXC / 8];
+        rule_populate_simple(rule, pb, pe, (char *)buf, cid);
+        uint32_t sz = osize[i];
+        if (sz > MAXC) {
+            prim::set_error(err, QUIDS_ERR_SIZE_BOUND);
+            sz = MAXC;
         }
-        __syncthreads();
+        const uint64_t ob = obegin[i], oe = obegin[i + 1];
+        char *dst = objects + ob;
+        copy_bytes(dst, (const char *)buf, sz);
+        for (uint64_t q = ob + sz; q < oe; ++q) objects[q] = 0;
+        if (f != 1.0) {
+            double2 m = omag[i];
+            omag[i] = make_double2(__ddiv_rn(m.x, f), __ddiv_rn(m.y, f));
+        }
     }
 }
 
@@ -755,12 +740,12 @@ inline int radix_select(quids_gpu_ctx *ctx, const uint64_t *d_n, uint64_t n_host
     QD_CUDA(cudaMemsetAsync(ctx->d_hist, 0, 256 * sizeof(unsigned long long), ctx->stream));
     for (int shift = 56; shift >= 0; shift -= 8) {
         prim::k_radix_hist<<<grid, prim::kThreads, 0, ctx->stream>>>(k1, d_n, ctx->d_sel, shift, ctx->d_hist);
-        prim::k_radix_pick<<<1, 32, 0, ctx->stream>>>(ctx->d_sel, ctx->d_hist, shift, true);
+        prim::k_radix_pick<<<1, 256, 0, ctx->stream>>>(ctx->d_sel, ctx->d_hist, shift, true);
     }
     k_select_ties_init<<<1, 1, 0, ctx->stream>>>(ctx->d_sel);
     for (int shift = 56; shift >= 0; shift -= 8) {
         prim::k_radix_hist<<<grid, prim::kThreads, 0, ctx->stream>>>(k2, d_n, ctx->d_sel + 1, shift, ctx->d_hist);
-        prim::k_radix_pick<<<1, 32, 0, ctx->stream>>>(ctx->d_sel + 1, ctx->d_hist, shift, tie_descending);
+        prim::k_radix_pick<<<1, 256, 0, ctx->stream>>>(ctx->d_sel + 1, ctx->d_hist, shift, tie_descending);
     }
     return launched(ctx, 34);
 }
@@ -784,25 +769,23 @@ inline int launch_symbolic(quids_gpu_ctx *ctx, const Rule &rule, const parents_v
     if constexpr (has_hash_child<Rule>::value) {
         if (fast) {
             k_symbolic<Rule, 8, true><<<grid, prim::kThreads, smem, ctx->stream>>>(
-                rule, pv, d_nc, bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG), bufp<uint32_t>(ctx, B_CSIZE),
-                d_maxabs, err, rc);
+                rule, pv, bufp<uint64_t>(ctx, B_TILEPAR), d_nc, bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG),
+                bufp<uint32_t>(ctx, B_CSIZE), bufp<uint32_t>(ctx, B_CPAR), d_maxabs, err, rc);
             return launched(ctx);
         }
     }
     k_symbolic<Rule, MAXC, false><<<grid, prim::kThreads, smem, ctx->stream>>>(
-        rule, pv, d_nc, bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG), bufp<uint32_t>(ctx, B_CSIZE), d_maxabs,
-        err, rc);
+        rule, pv, bufp<uint64_t>(ctx, B_TILEPAR), d_nc, bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG),
+        bufp<uint32_t>(ctx, B_CSIZE), bufp<uint32_t>(ctx, B_CPAR), d_maxabs, err, rc);
     return launched(ctx);
 }
 
 template <class Rule, int MAXC>
 inline int launch_populate(quids_gpu_ctx *ctx, const Rule &rule, const parents_view &pv, uint64_t ns,
                            quids_gpu_state *out) {
-    uint64_t tiles = (ns + kTileChildren - 1) / kTileChildren;
-    unsigned grid = (unsigned)(tiles < (uint64_t)ctx->num_sms * 8 ? tiles : (uint64_t)ctx->num_sms * 8);
-    if (grid < 1) grid = 1;
-    k_populate<Rule, MAXC><<<grid, prim::kThreads, 0, ctx->stream>>>(
-        rule, pv, bufp<uint64_t>(ctx, B_SCHILD), ctx->d_words + W_NS, (const uint64_t *)out->begin.p,
+    k_populate<Rule, MAXC><<<grid_for(ctx, ns), prim::kThreads, 0, ctx->stream>>>(
+        rule, pv, bufp<uint64_t>(ctx, B_SCHILD), bufp<uint32_t>(ctx, B_CPAR), ctx->d_words + W_NS,
+        (const uint64_t *)out->begin.p,
         (const uint32_t *)out->size.p, (char *)out->objects.p, (double2 *)out->mag.p,
         (const double *)(ctx->d_words + W_FACTOR), (int *)(ctx->d_words + W_STATUS));
     return launched(ctx);
@@ -952,7 +935,7 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, qui
 
     uint64_t M = (uint64_t)((double)NC / load) + 1;
     if (M < 1024) M = 1024;
-    if (M >= 0xfffffff0ull) return QUIDS_ERR_OOM;  // slot indices (and the extra slots) are u32
+    if (M >= 0x7ffffff0ull) return QUIDS_ERR_OOM;  // slot indices are 31-bit (the top bit marks joiners)
     s.table_capacity = M;
     // tables larger than a share of L2 are filled region by region
     const double table_bytes = 44.0 * (double)M;
@@ -996,8 +979,15 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, qui
         QD_CUDA(cudaMemsetAsync(ctx->buf[B_RHIST].p, 0, R * sizeof(unsigned int), ctx->stream));
     }
 
+    const uint64_t sym_tiles = (NC + kTileChildren - 1) / kTileChildren;
+    QD_TRY(ensure(ctx->buf[B_TILEPAR], (sym_tiles + 1) * sizeof(uint64_t)));
+    QD_TRY(ensure(ctx->buf[B_CPAR], NC * sizeof(uint32_t)));
+
     // ---- stage 1: symbolic iteration (src/quids.hpp:647-721)
     begin_stage(1);
+    k_tile_parents<<<grid_for(ctx, NP), prim::kThreads, 0, ctx->stream>>>(bufp<uint64_t>(ctx, B_CBEGIN), NP, sym_tiles,
+                                                                         bufp<uint64_t>(ctx, B_TILEPAR));
+    QD_TRY(launched(ctx));
     region_count rc{M, regions ? R : 0u, regions ? bufp<unsigned int>(ctx, B_RHIST) : nullptr};
     if (maxsize <= 256) {
         QD_TRY((launch_symbolic<Rule, 256>(ctx, rule, pv, NC, fast, rc)));
@@ -1017,7 +1007,7 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, qui
     if (!regions) {
         direct_src src{bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG)};
         prim::k_table_claim<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
-            tb, src, ctx->d_words + W_NC, bufp<uint32_t>(ctx, B_SLOT), err);
+            tb, src, ctx->d_words + W_NC, d_maxabs, bufp<uint32_t>(ctx, B_SLOT), err);
         prim::k_table_accumulate<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
             tb, src, bufp<uint32_t>(ctx, B_SLOT), ctx->d_words + W_NC, d_maxabs);
         QD_TRY(launched(ctx, 2));
@@ -1033,7 +1023,7 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, qui
             bufp<uint32_t>(ctx, B_RIDX), bufp<double2>(ctx, B_RMAG), err);
         region_src src{bufp<uint64_t>(ctx, B_RHASH), bufp<uint32_t>(ctx, B_RIDX), bufp<double2>(ctx, B_RMAG)};
         prim::k_table_claim<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
-            tb, src, ctx->d_words + W_NC, bufp<uint32_t>(ctx, B_RSLOT), err);
+            tb, src, ctx->d_words + W_NC, d_maxabs, bufp<uint32_t>(ctx, B_RSLOT), err);
         prim::k_table_accumulate<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
             tb, src, bufp<uint32_t>(ctx, B_RSLOT), ctx->d_words + W_NC, d_maxabs);
         QD_TRY(launched(ctx, 4));

@@ -260,24 +260,35 @@ __global__ void __launch_bounds__(kThreads) k_radix_hist(K kf, const uint64_t *d
         if (sh[i]) atomicAdd(&hist[i], (unsigned long long)sh[i]);
 }
 
-static __global__ void k_radix_pick(select_state *st, unsigned long long *hist, int shift, bool descending) {
-    // one warp: cumulative counts in preference order
-    if (threadIdx.x != 0) return;
+// picks the digit holding the k-th item in preference order (256 threads:
+// the 256 bins are scanned in parallel)
+static __global__ void __launch_bounds__(256) k_radix_pick(select_state *st, unsigned long long *hist, int shift,
+                                                            bool descending) {
+    __shared__ uint64_t sm[256];
     if (!st->active) return;
-    uint64_t above = 0;
-    int d = 0;
-    for (int s = 0; s < 256; ++s) {
-        d = descending ? 255 - s : s;
-        uint64_t c = hist[d];
-        if (above + c >= st->k_rem) break;
-        above += c;
+    const int t = threadIdx.x;
+    const int d = descending ? 255 - t : t;  // t-th bin in preference order
+    const uint64_t c = hist[d];
+    sm[t] = c;
+    __syncthreads();
+    for (int o = 1; o < 256; o <<= 1) {  // inclusive scan
+        uint64_t v = t >= o ? sm[t - o] : 0;
+        __syncthreads();
+        sm[t] += v;
+        __syncthreads();
     }
-    st->prefix |= (uint64_t)d << shift;
-    st->mask |= 255ull << shift;
-    st->n_better += above;
-    st->k_rem -= above;
-    st->n_equal = hist[d];
-    for (int s = 0; s < 256; ++s) hist[s] = 0;
+    const uint64_t incl = sm[t], excl = incl - c;
+    const uint64_t k = st->k_rem;
+    __syncthreads();
+    if (excl < k && k <= incl) {  // exactly one bin holds the k-th item
+        select_state *w = st;
+        w->prefix |= (uint64_t)d << shift;
+        w->mask |= 255ull << shift;
+        w->n_better += excl;
+        w->k_rem = k - excl;
+        w->n_equal = c;
+    }
+    hist[d] = 0;
 }
 
 // ---------------------------------------------------- collision table
@@ -310,15 +321,22 @@ __device__ __forceinline__ void fix_atomic_add(unsigned long long *w, fix128 v) 
 }
 
 // Pass 1: every child item (src.hash(k)) finds or claims the slot of its
-// hash; slot_out[k] = slot, or 0xffffffff at the probe limit
-// (QUIDS_ERR_TABLE_FULL).
+// hash.  The claiming thread initialises the group with its own child (rep =
+// its index, acc = its magnitude); slot_out[k] = slot | kJoin for the others,
+// which pass 2 adds in.  0xffffffff at the probe limit (QUIDS_ERR_TABLE_FULL).
+constexpr uint32_t kJoin = 0x80000000u;
+constexpr uint32_t kNoSlot = 0xffffffffu;
+
 template <class Src>
-__global__ void __launch_bounds__(kThreads) k_table_claim(table t, Src src, const uint64_t *d_n, uint32_t *slot_out,
+__global__ void __launch_bounds__(kThreads) k_table_claim(table t, Src src, const uint64_t *d_n,
+                                                           const unsigned long long *d_maxabs, uint32_t *slot_out,
                                                            int *err) {
     const uint64_t n = *d_n;
+    const int F = fix_scale(__longlong_as_double((long long)*d_maxabs), n);
     for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t h = src.hash(k);
         uint64_t s;
+        bool claimed = false;
         if (h == kEmptyKey) {
             s = t.m;
         } else {
@@ -329,11 +347,17 @@ __global__ void __launch_bounds__(kThreads) k_table_claim(table t, Src src, cons
                 if (key == h) break;
                 if (key == kEmptyKey) {
                     key = atomicCAS((unsigned long long *)&t.keys[s], kEmptyKey, h);
-                    if (key == kEmptyKey) {  // claimed: initialise the slot's group
-                        ulonglong4_32a zero;
-                        zero.x = zero.y = zero.z = zero.w = 0;
-                        t.rep[s] = 0xffffffffu;
-                        *(ulonglong4_32a *)&t.acc[4 * s] = zero;
+                    if (key == kEmptyKey) {  // claimed: the group starts with this child
+                        const double2 m = src.mag(k);
+                        const fix128 re = to_fix(m.x, F), im = to_fix(m.y, F);
+                        ulonglong4_32a a;
+                        a.x = re.lo;
+                        a.y = re.hi;
+                        a.z = im.lo;
+                        a.w = im.hi;
+                        t.rep[s] = (uint32_t)src.child(k);
+                        *(ulonglong4_32a *)&t.acc[4 * s] = a;
+                        claimed = true;
                         break;
                     }
                     if (key == h) break;
@@ -346,22 +370,25 @@ __global__ void __launch_bounds__(kThreads) k_table_claim(table t, Src src, cons
                 }
             }
         }
-        slot_out[k] = (uint32_t)s;
+        slot_out[k] = s == ~0ull ? kNoSlot : (claimed ? (uint32_t)s : (uint32_t)s | kJoin);
     }
 }
 
-// Pass 2: rep = minimum child index of the group; acc += magnitude as an
-// exact 128-bit fixed-point sum per component (scale 2^-F, F from the largest
-// component and the child count), independent of the order of the atomics.
+// Pass 2: the joiners: rep = minimum child index of the group; acc +=
+// magnitude as an exact 128-bit fixed-point sum per component (scale 2^-F, F
+// from the largest component and the child count), independent of the order
+// of the atomics.  Clears the join marks.
 template <class Src>
-__global__ void __launch_bounds__(kThreads) k_table_accumulate(table t, Src src, const uint32_t *slot_of,
+__global__ void __launch_bounds__(kThreads) k_table_accumulate(table t, Src src, uint32_t *slot_of,
                                                                 const uint64_t *d_n,
                                                                 const unsigned long long *d_maxabs) {
     const uint64_t n = *d_n;
     const int F = fix_scale(__longlong_as_double((long long)*d_maxabs), n);
     for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t s = slot_of[k];
-        if (s == 0xffffffffu) continue;
+        uint32_t s = slot_of[k];
+        if (s == kNoSlot || !(s & kJoin)) continue;
+        s &= ~kJoin;
+        slot_of[k] = s;
         atomicMin(&t.rep[s], (uint32_t)src.child(k));
         const double2 m = src.mag(k);
         fix_atomic_add(&t.acc[4ull * s + 0], to_fix(m.x, F));
