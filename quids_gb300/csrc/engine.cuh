@@ -48,8 +48,8 @@ enum qd_buf_id {
     B_RIDX,        // u32 [NC] child indices in table-region order
     B_RMAG,        // double2 [NC] child magnitudes in table-region order
     B_RSLOT,       // u32 [NC] table slot of each region-ordered child
-    B_FLAG,        // u8 [NC] child represents a kept group (region path)
-    B_GMAG,        // double2 [NC] summed magnitude of a kept group, at its representative (region path)
+    B_NOTREP,      // u8 [NC] child is not its group's representative
+    B_HASJOIN,     // u8 [NC] child's group has more than one member (for the representative)
     B_RHIST,       // u32 [R] children per table region
     B_ROFF,        // u64 [R+1] region offsets
     B_RCUR,        // u64 [R] region write cursors
@@ -494,9 +494,13 @@ __device__ __forceinline__ uint32_t padded_size(uint32_t sz, uint32_t align) {
 // A child represents its group when it is the group's lowest symbolic index
 // (src/quids.hpp:785-809 keeps one member per hash); the group survives zero
 // elimination when its summed norm is above tolerance (src/quids.hpp:819-823).
+// A group of one keeps its member's own magnitude; larger groups read their
+// exact fixed-point sum.
 struct group_view {
-    const uint32_t *slot_of;
-    const uint32_t *rep;
+    const uint32_t *slot_of;  // by child index
+    const uint8_t *not_rep;
+    const uint8_t *has_join;
+    const double2 *cmag;
     const unsigned long long *acc;
     const uint64_t *d_nc;
     const unsigned long long *d_maxabs;
@@ -506,12 +510,20 @@ struct group_view {
         const ulonglong4_32a a = *(const ulonglong4_32a *)&acc[4ull * s];
         return mag_t{from_fix(fix128{a.x, a.y}, F), from_fix(fix128{a.z, a.w}, F)};
     }
-    __device__ __forceinline__ bool kept(uint64_t c, mag_t &m) const {
+    // the group magnitude if c is a representative, else false
+    __device__ __forceinline__ bool rep_mag(uint64_t c, mag_t &m) const {
+        if (not_rep[c]) return false;
         const uint32_t s = slot_of[c];
-        if (s == 0xffffffffu || rep[s] != (uint32_t)c) return false;
-        m = sum(s);
-        return cnorm(m) > tolerance;
+        if (s == prim::kNoSlot) return false;
+        if (has_join[c]) {
+            m = sum(s);
+        } else {
+            const double2 v = cmag[c];
+            m = mag_t{v.x, v.y};
+        }
+        return true;
     }
+    __device__ __forceinline__ bool kept(uint64_t c, mag_t &m) const { return rep_mag(c, m) && cnorm(m) > tolerance; }
 };
 
 // items of the collision-table insert: children in index order ...
@@ -532,66 +544,6 @@ struct region_src {
     __device__ __forceinline__ double2 mag(uint64_t k) const { return rmag[k]; }
 };
 
-// Region path: in region order (the table region in L2), each representative
-// of a group above tolerance marks itself and stores the group's magnitude at
-// its child index, for an index-ordered compaction afterwards.
-static __global__ void __launch_bounds__(prim::kThreads)
-    k_region_groups(group_view g, const uint32_t *rslot, const uint32_t *ridx, uint8_t *flag, double2 *gmag) {
-    const uint64_t n = *g.d_nc;
-    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t s = rslot[k];
-        if (s == 0xffffffffu) continue;
-        const uint32_t c = ridx[k];
-        if (g.rep[s] != c) continue;
-        const mag_t m = g.sum(s);
-        if (cnorm(m) > g.tolerance) {
-            flag[c] = 1;
-            gmag[c] = make_double2(m.re, m.im);
-        }
-    }
-}
-
-struct flags_layout {
-    const uint8_t *flag;
-    const double2 *gmag;
-    const uint32_t *csize;
-    uint32_t align;
-    double2 *omag;
-    uint32_t *osize;
-    uint64_t *obegin;
-    uint64_t *schild;
-    __device__ bool select(uint64_t c) const { return flag[c] != 0; }
-    __device__ uint64_t bytes(uint64_t c) const { return padded_size(csize[c], align); }
-    __device__ double norm(uint64_t c) const {
-        const double2 m = gmag[c];
-        return cnorm(mag_t{m.x, m.y});
-    }
-    __device__ void emit(uint64_t c, uint64_t j, uint64_t off) const {
-        omag[j] = gmag[c];
-        osize[j] = csize[c];
-        obegin[j] = off;
-        schild[j] = c;
-    }
-};
-
-struct flags_collect {
-    const uint8_t *flag;
-    const double2 *gmag;
-    const uint64_t *hash;
-    uint64_t *uchild;
-    double2 *umag;
-    uint64_t *unorm;
-    uint64_t *uhash;
-    __device__ bool select(uint64_t c) const { return flag[c] != 0; }
-    __device__ void emit(uint64_t c, uint64_t j) const {
-        const double2 m = gmag[c];
-        uchild[j] = c;
-        umag[j] = m;
-        unorm[j] = (uint64_t)__double_as_longlong(cnorm(mag_t{m.x, m.y}));
-        uhash[j] = hash[c];
-    }
-};
-
 // no truncation possible: survivors straight into the output layout
 struct groups_layout {
     group_view g;
@@ -606,9 +558,14 @@ struct groups_layout {
         return g.kept(c, m);
     }
     __device__ uint64_t bytes(uint64_t c) const { return padded_size(csize[c], align); }
-    __device__ double norm(uint64_t c) const { return cnorm(g.sum(g.slot_of[c])); }
+    __device__ double norm(uint64_t c) const {
+        mag_t m;
+        g.rep_mag(c, m);
+        return cnorm(m);
+    }
     __device__ void emit(uint64_t c, uint64_t j, uint64_t off) const {
-        const mag_t m = g.sum(g.slot_of[c]);
+        mag_t m;
+        g.rep_mag(c, m);
         omag[j] = make_double2(m.re, m.im);
         osize[j] = csize[c];
         obegin[j] = off;
@@ -629,7 +586,8 @@ struct groups_collect {
         return g.kept(c, m);
     }
     __device__ void emit(uint64_t c, uint64_t j) const {
-        const mag_t m = g.sum(g.slot_of[c]);
+        mag_t m;
+        g.rep_mag(c, m);
         uchild[j] = c;
         umag[j] = make_double2(m.re, m.im);
         unorm[j] = (uint64_t)__double_as_longlong(cnorm(m));
@@ -729,6 +687,14 @@ struct keep_parents {
     }
     __device__ void emit(uint64_t i, uint64_t j) const { pidx[j] = i; }
 };
+
+// region path: slot of each child back in child order
+static __global__ void __launch_bounds__(prim::kThreads)
+    k_unpermute_slots(const uint32_t *rslot, const uint32_t *ridx, const uint64_t *d_n, uint32_t *slot_of) {
+    const uint64_t n = *d_n;
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x)
+        slot_of[ridx[k]] = rslot[k];
+}
 
 // ------------------------------------------------------------ radix select
 // Runs the 8 passes of a top-k selection (and the tie passes) on the stream.
@@ -942,14 +908,18 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, qui
     uint32_t R = (uint32_t)(table_bytes / (32.0 * 1024 * 1024)) + 1;
     if (R < 4) R = 1;
     if (R > prim::kMaxRegions) R = prim::kMaxRegions;
-    if (prm.flags & QUIDS_FLAG_NO_REGIONS) R = 1;
-    if ((prm.flags & QUIDS_FLAG_REGIONS) && R < 4) R = 4;
+    // region order pays for its scatter only where the table traffic is latency
+    // bound; measured on GB300 it breaks even, so it is opt-in
+    if (!(prm.flags & QUIDS_FLAG_REGIONS)) R = 1;
+    else if (R < 4) R = 4;
     const bool regions = R > 1;
     const uint64_t tiles_nc = (NC + prim::kTile - 1) / prim::kTile;
     QD_TRY(ensure(ctx->buf[B_HASH], NC * sizeof(uint64_t)));
     QD_TRY(ensure(ctx->buf[B_CMAG], NC * sizeof(double2)));
     QD_TRY(ensure(ctx->buf[B_CSIZE], NC * sizeof(uint32_t)));
     QD_TRY(ensure(ctx->buf[B_SLOT], NC * sizeof(uint32_t)));
+    QD_TRY(ensure(ctx->buf[B_NOTREP], NC));
+    QD_TRY(ensure(ctx->buf[B_HASJOIN], NC));
     QD_TRY(ensure(ctx->buf[B_KEYS], M * sizeof(uint64_t)));
     QD_TRY(ensure(ctx->buf[B_REP], (M + 1) * sizeof(uint32_t)));
     QD_TRY(ensure(ctx->buf[B_ACC], 4 * (M + 1) * sizeof(uint64_t)));
@@ -971,8 +941,6 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, qui
         QD_TRY(ensure(ctx->buf[B_RIDX], NC * sizeof(uint32_t)));
         QD_TRY(ensure(ctx->buf[B_RMAG], NC * sizeof(double2)));
         QD_TRY(ensure(ctx->buf[B_RSLOT], NC * sizeof(uint32_t)));
-        QD_TRY(ensure(ctx->buf[B_FLAG], NC));
-        QD_TRY(ensure(ctx->buf[B_GMAG], NC * sizeof(double2)));
         QD_TRY(ensure(ctx->buf[B_RHIST], R * sizeof(unsigned int)));
         QD_TRY(ensure(ctx->buf[B_ROFF], (R + 1) * sizeof(uint64_t)));
         QD_TRY(ensure(ctx->buf[B_RCUR], R * sizeof(uint64_t)));
@@ -1003,13 +971,16 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, qui
     QD_CUDA(cudaMemsetAsync(tb.keys, 0xff, M * sizeof(uint64_t), ctx->stream));
     QD_CUDA(cudaMemsetAsync(tb.rep + M, 0xff, sizeof(uint32_t), ctx->stream));  // the extra slot
     QD_CUDA(cudaMemsetAsync(tb.acc + 4 * M, 0, 4 * sizeof(uint64_t), ctx->stream));
+    QD_CUDA(cudaMemsetAsync(ctx->buf[B_NOTREP].p, 0, NC, ctx->stream));
+    QD_CUDA(cudaMemsetAsync(ctx->buf[B_HASJOIN].p, 0, NC, ctx->stream));
+    uint8_t *not_rep = bufp<uint8_t>(ctx, B_NOTREP), *has_join = bufp<uint8_t>(ctx, B_HASJOIN);
     const unsigned long long *d_maxabs = (const unsigned long long *)(ctx->d_words + W_MAXABS);
     if (!regions) {
         direct_src src{bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG)};
         prim::k_table_claim<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
             tb, src, ctx->d_words + W_NC, d_maxabs, bufp<uint32_t>(ctx, B_SLOT), err);
         prim::k_table_accumulate<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
-            tb, src, bufp<uint32_t>(ctx, B_SLOT), ctx->d_words + W_NC, d_maxabs);
+            tb, src, bufp<uint32_t>(ctx, B_SLOT), ctx->d_words + W_NC, d_maxabs, not_rep, has_join);
         QD_TRY(launched(ctx, 2));
     } else {
         prim::k_region_offsets<<<1, 1024, 0, ctx->stream>>>(bufp<unsigned int>(ctx, B_RHIST), R,
@@ -1025,61 +996,40 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, qui
         prim::k_table_claim<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
             tb, src, ctx->d_words + W_NC, d_maxabs, bufp<uint32_t>(ctx, B_RSLOT), err);
         prim::k_table_accumulate<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
-            tb, src, bufp<uint32_t>(ctx, B_RSLOT), ctx->d_words + W_NC, d_maxabs);
-        QD_TRY(launched(ctx, 4));
+            tb, src, bufp<uint32_t>(ctx, B_RSLOT), ctx->d_words + W_NC, d_maxabs, not_rep, has_join);
+        k_unpermute_slots<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
+            bufp<uint32_t>(ctx, B_RSLOT), bufp<uint32_t>(ctx, B_RIDX), ctx->d_words + W_NC,
+            bufp<uint32_t>(ctx, B_SLOT));
+        QD_TRY(launched(ctx, 5));
     }
     end_stage(2);
 
     // ---- stage 3 (+4): representatives above tolerance (src/quids.hpp:819-823),
     // truncation (src/quids.hpp:866-900, ties by lower hash) and the output
     // layout (src/quids.hpp:927-948), with per-tile norm sums for normalize
-    group_view gv{bufp<uint32_t>(ctx, B_SLOT), bufp<uint32_t>(ctx, B_REP), bufp<unsigned long long>(ctx, B_ACC),
-                  ctx->d_words + W_NC, d_maxabs, prm.tolerance};
+    group_view gv{bufp<uint32_t>(ctx, B_SLOT), not_rep, has_join, bufp<double2>(ctx, B_CMAG),
+                  bufp<unsigned long long>(ctx, B_ACC), ctx->d_words + W_NC, d_maxabs, prm.tolerance};
     const uint32_t align = prm.align_byte_length;
     double *tile_norm = bufp<double>(ctx, B_TILENORM);
     begin_stage(3);
-    if (regions) {  // mark representatives in region order, compact in index order
-        QD_CUDA(cudaMemsetAsync(ctx->buf[B_FLAG].p, 0, NC, ctx->stream));
-        k_region_groups<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
-            gv, bufp<uint32_t>(ctx, B_RSLOT), bufp<uint32_t>(ctx, B_RIDX), bufp<uint8_t>(ctx, B_FLAG),
-            bufp<double2>(ctx, B_GMAG));
-        QD_TRY(launched(ctx));
-    }
     if (!may_truncate) {
         prim::lookback lbc, lbb;
         QD_TRY(lookback_chain(ctx, NC, 0, lbc));
         QD_TRY(lookback_chain(ctx, NC, 1, lbb));
-        if (regions) {
-            flags_layout f{bufp<uint8_t>(ctx, B_FLAG), bufp<double2>(ctx, B_GMAG), bufp<uint32_t>(ctx, B_CSIZE), align,
-                           (double2 *)out->mag.p, (uint32_t *)out->size.p, (uint64_t *)out->begin.p,
-                           bufp<uint64_t>(ctx, B_SCHILD)};
-            prim::k_compact_layout<<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
-                f, ctx->d_words + W_NC, ctx->d_words + W_NS, ctx->d_words + W_OUTBYTES, (uint64_t *)out->begin.p,
-                tile_norm, lbc, lbb);
-        } else {
-            groups_layout f{gv, bufp<uint32_t>(ctx, B_CSIZE), align, (double2 *)out->mag.p, (uint32_t *)out->size.p,
-                            (uint64_t *)out->begin.p, bufp<uint64_t>(ctx, B_SCHILD)};
-            prim::k_compact_layout<<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
-                f, ctx->d_words + W_NC, ctx->d_words + W_NS, ctx->d_words + W_OUTBYTES, (uint64_t *)out->begin.p,
-                tile_norm, lbc, lbb);
-        }
+        groups_layout f{gv, bufp<uint32_t>(ctx, B_CSIZE), align, (double2 *)out->mag.p, (uint32_t *)out->size.p,
+                        (uint64_t *)out->begin.p, bufp<uint64_t>(ctx, B_SCHILD)};
+        prim::k_compact_layout<<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
+            f, ctx->d_words + W_NC, ctx->d_words + W_NS, ctx->d_words + W_OUTBYTES, (uint64_t *)out->begin.p,
+            tile_norm, lbc, lbb);
         QD_TRY(launched(ctx));
         end_stage(3);
     } else {
         prim::lookback lb;
         QD_TRY(lookback_chain(ctx, NC, 0, lb));
-        if (regions) {
-            flags_collect f{bufp<uint8_t>(ctx, B_FLAG), bufp<double2>(ctx, B_GMAG), bufp<uint64_t>(ctx, B_HASH),
-                            bufp<uint64_t>(ctx, B_UCHILD), bufp<double2>(ctx, B_UMAG), bufp<uint64_t>(ctx, B_UNORM),
-                            bufp<uint64_t>(ctx, B_UHASH)};
-            prim::k_compact<<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(f, ctx->d_words + W_NC,
-                                                                                       ctx->d_words + W_NU, lb);
-        } else {
-            groups_collect f{gv, bufp<uint64_t>(ctx, B_HASH), bufp<uint64_t>(ctx, B_UCHILD),
-                             bufp<double2>(ctx, B_UMAG), bufp<uint64_t>(ctx, B_UNORM), bufp<uint64_t>(ctx, B_UHASH)};
-            prim::k_compact<<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(f, ctx->d_words + W_NC,
-                                                                                       ctx->d_words + W_NU, lb);
-        }
+        groups_collect f{gv, bufp<uint64_t>(ctx, B_HASH), bufp<uint64_t>(ctx, B_UCHILD), bufp<double2>(ctx, B_UMAG),
+                         bufp<uint64_t>(ctx, B_UNORM), bufp<uint64_t>(ctx, B_UHASH)};
+        prim::k_compact<<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(f, ctx->d_words + W_NC,
+                                                                                   ctx->d_words + W_NU, lb);
         QD_TRY(launched(ctx));
         end_stage(3);
         begin_stage(4);

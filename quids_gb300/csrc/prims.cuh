@@ -377,11 +377,15 @@ __global__ void __launch_bounds__(kThreads) k_table_claim(table t, Src src, cons
 // Pass 2: the joiners: rep = minimum child index of the group; acc +=
 // magnitude as an exact 128-bit fixed-point sum per component (scale 2^-F, F
 // from the largest component and the child count), independent of the order
-// of the atomics.  Clears the join marks.
+// of the atomics.  Clears the join marks.  Each atomicMin compares two
+// members: the larger is marked not_rep, the smaller has_join; at the end the
+// representative is the one member never marked not_rep, and it is marked
+// has_join exactly when its group has more than one member.
 template <class Src>
 __global__ void __launch_bounds__(kThreads) k_table_accumulate(table t, Src src, uint32_t *slot_of,
                                                                 const uint64_t *d_n,
-                                                                const unsigned long long *d_maxabs) {
+                                                                const unsigned long long *d_maxabs,
+                                                                uint8_t *not_rep, uint8_t *has_join) {
     const uint64_t n = *d_n;
     const int F = fix_scale(__longlong_as_double((long long)*d_maxabs), n);
     for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
@@ -389,7 +393,12 @@ __global__ void __launch_bounds__(kThreads) k_table_accumulate(table t, Src src,
         if (s == kNoSlot || !(s & kJoin)) continue;
         s &= ~kJoin;
         slot_of[k] = s;
-        atomicMin(&t.rep[s], (uint32_t)src.child(k));
+        const uint32_t c = (uint32_t)src.child(k);
+        const uint32_t old = atomicMin(&t.rep[s], c);
+        if (old != 0xffffffffu) {  // slot M starts without a member
+            not_rep[old > c ? old : c] = 1;
+            has_join[old < c ? old : c] = 1;
+        }
         const double2 m = src.mag(k);
         fix_atomic_add(&t.acc[4ull * s + 0], to_fix(m.x, F));
         fix_atomic_add(&t.acc[4ull * s + 2], to_fix(m.y, F));

@@ -249,10 +249,10 @@ def test_run_gate_list_equals_per_call(ctx):
     assert final.total_proba == a.total_proba
 
 
-def test_large_steps_region_path(ctx, port):
-    """The 8.4M-child Hadamard applications of the 24-qubit circuit (the table
-    is filled region by region there) against the oracle from identical
-    inputs, with truncation to 2^22."""
+def test_large_steps(ctx, port):
+    """The 8.4M-child Hadamard applications of the 24-qubit circuit against the
+    oracle from identical inputs, with truncation to 2^22; each also with the
+    collision table filled region by region."""
     from tests.parity import assert_fixed_state_parity
     port.set_globals(1e-18, True, 8)
     gates = [g for layer in W.circuit_layers(0) for g in layer]
@@ -274,6 +274,11 @@ def test_large_steps_region_path(ctx, port):
             assert (sy.num_object, sy.num_object_after_interferences) == (nc, nu)
             assert_fixed_state_parity(nxt.download(), b.store(), truncated=nu > (1 << 22), what=f"H{g.params}")
             assert nxt.total_proba == pytest.approx(b.total_proba, rel=1e-12)
+            # the same step with the table filled in region order gives the same state
+            ra, rb, rsy = quids.it_t(ctx, inp), quids.it_t(ctx), quids.sy_it_t()
+            quids.simulate(ra, r, rb, rsy, 1 << 22, flags=capi.FLAG_REGIONS)
+            for u, v in zip(rb.download(), nxt.download()):
+                assert np.array_equal(u, v)
             checked += 1
             if checked == 3:
                 break
