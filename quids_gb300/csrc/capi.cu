@@ -97,7 +97,7 @@ int quids_gpu_ctx_create(int device, quids_gpu_ctx **out) {
     if (!rc) rc = cuda_status(cudaMalloc(&ctx->d_words, W_COUNT_WORDS * sizeof(uint64_t)));
     if (!rc) rc = cuda_status(cudaMallocHost(&ctx->h_words, W_COUNT_WORDS * sizeof(uint64_t)));
     if (!rc) rc = cuda_status(cudaMalloc(&ctx->d_sel, 2 * sizeof(qd::prim::select_state)));
-    if (!rc) rc = cuda_status(cudaMalloc(&ctx->d_hist, 256 * sizeof(unsigned long long)));
+    if (!rc) rc = cuda_status(cudaMalloc(&ctx->d_hist, qd::prim::kBins * sizeof(unsigned long long)));
     if (!rc) rc = cuda_status(cudaEventCreate(&ctx->ev0));
     if (!rc) rc = cuda_status(cudaEventCreate(&ctx->ev1));
     for (int k = 0; k < 16 && !rc; ++k) rc = cuda_status(cudaEventCreate(&ctx->ev_stage[k]));

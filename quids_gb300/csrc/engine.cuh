@@ -34,8 +34,7 @@ enum qd_buf_id {
     B_CMAG,        // double2 [NC] child magnitudes
     B_CSIZE,       // u32 [NC] child sizes
     B_SLOT,        // u32 [NC] collision-table slot of each child
-    B_KEYS,        // u64 [M] table keys
-    B_REP,         // u32 [M+1] group representative (minimum child index)
+    B_KEYS,        // table_slot [M+1] table keys and group representatives
     B_ACC,         // u64 [4(M+1)] group magnitude sums, 128-bit fixed point
     B_UCHILD,      // u64 [NU] groups kept after zero elimination (truncation path)
     B_UMAG,        // double2 [NU]
@@ -703,17 +702,17 @@ inline int radix_select(quids_gpu_ctx *ctx, const uint64_t *d_n, uint64_t n_host
                         bool tie_descending) {
     unsigned grid = grid_for(ctx, n_host);
     k_select_init<<<1, 1, 0, ctx->stream>>>(ctx->d_sel, d_n, k);
-    QD_CUDA(cudaMemsetAsync(ctx->d_hist, 0, 256 * sizeof(unsigned long long), ctx->stream));
-    for (int shift = 56; shift >= 0; shift -= 8) {
+    QD_CUDA(cudaMemsetAsync(ctx->d_hist, 0, prim::kBins * sizeof(unsigned long long), ctx->stream));
+    for (int shift = 64 - prim::kDigitBits; shift >= 0; shift -= prim::kDigitBits) {
         prim::k_radix_hist<<<grid, prim::kThreads, 0, ctx->stream>>>(k1, d_n, ctx->d_sel, shift, ctx->d_hist);
-        prim::k_radix_pick<<<1, 256, 0, ctx->stream>>>(ctx->d_sel, ctx->d_hist, shift, true);
+        prim::k_radix_pick<<<1, 1024, 0, ctx->stream>>>(ctx->d_sel, ctx->d_hist, shift, true);
     }
     k_select_ties_init<<<1, 1, 0, ctx->stream>>>(ctx->d_sel);
-    for (int shift = 56; shift >= 0; shift -= 8) {
+    for (int shift = 64 - prim::kDigitBits; shift >= 0; shift -= prim::kDigitBits) {
         prim::k_radix_hist<<<grid, prim::kThreads, 0, ctx->stream>>>(k2, d_n, ctx->d_sel + 1, shift, ctx->d_hist);
-        prim::k_radix_pick<<<1, 256, 0, ctx->stream>>>(ctx->d_sel + 1, ctx->d_hist, shift, tie_descending);
+        prim::k_radix_pick<<<1, 1024, 0, ctx->stream>>>(ctx->d_sel + 1, ctx->d_hist, shift, tie_descending);
     }
-    return launched(ctx, 34);
+    return launched(ctx, 2 + 4 * 64 / prim::kDigitBits);
 }
 
 inline uint64_t next_pow2(uint64_t v) {
@@ -920,8 +919,7 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, qui
     QD_TRY(ensure(ctx->buf[B_SLOT], NC * sizeof(uint32_t)));
     QD_TRY(ensure(ctx->buf[B_NOTREP], NC));
     QD_TRY(ensure(ctx->buf[B_HASJOIN], NC));
-    QD_TRY(ensure(ctx->buf[B_KEYS], M * sizeof(uint64_t)));
-    QD_TRY(ensure(ctx->buf[B_REP], (M + 1) * sizeof(uint32_t)));
+    QD_TRY(ensure(ctx->buf[B_KEYS], (M + 1) * sizeof(prim::table_slot)));
     QD_TRY(ensure(ctx->buf[B_ACC], 4 * (M + 1) * sizeof(uint64_t)));
     QD_TRY(ensure(ctx->buf[B_SCHILD], NSB * sizeof(uint64_t)));
     QD_TRY(ensure(ctx->buf[B_TILENORM], tiles_nc * sizeof(double)));
@@ -966,11 +964,9 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, qui
 
     // ---- stage 2: collision table (src/quids.hpp:726-809)
     begin_stage(2);
-    prim::table tb{bufp<uint64_t>(ctx, B_KEYS), bufp<uint32_t>(ctx, B_REP), bufp<unsigned long long>(ctx, B_ACC), M,
-                   65536u};
-    QD_CUDA(cudaMemsetAsync(tb.keys, 0xff, M * sizeof(uint64_t), ctx->stream));
-    QD_CUDA(cudaMemsetAsync(tb.rep + M, 0xff, sizeof(uint32_t), ctx->stream));  // the extra slot
-    QD_CUDA(cudaMemsetAsync(tb.acc + 4 * M, 0, 4 * sizeof(uint64_t), ctx->stream));
+    prim::table tb{bufp<prim::table_slot>(ctx, B_KEYS), bufp<unsigned long long>(ctx, B_ACC), M, 65536u};
+    QD_CUDA(cudaMemsetAsync(tb.slots, 0xff, (M + 1) * sizeof(prim::table_slot), ctx->stream));
+    QD_CUDA(cudaMemsetAsync(tb.acc + 4 * M, 0, 4 * sizeof(uint64_t), ctx->stream));  // the extra slot
     QD_CUDA(cudaMemsetAsync(ctx->buf[B_NOTREP].p, 0, NC, ctx->stream));
     QD_CUDA(cudaMemsetAsync(ctx->buf[B_HASJOIN].p, 0, NC, ctx->stream));
     uint8_t *not_rep = bufp<uint8_t>(ctx, B_NOTREP), *has_join = bufp<uint8_t>(ctx, B_HASJOIN);

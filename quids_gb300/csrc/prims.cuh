@@ -218,8 +218,11 @@ __global__ void __launch_bounds__(kThreads) k_compact(P p, const uint64_t *d_n, 
 }
 
 // --------------------------------------------------------- radix select
-// Top-k selection on 64-bit keys, 8 bits per pass from the top.  State is
-// device resident so the passes need no host round trip.
+// Top-k selection on 64-bit keys, 16 bits per pass from the top (4 passes).
+// State is device resident so the passes need no host round trip.
+constexpr int kDigitBits = 16;
+constexpr int kBins = 1 << kDigitBits;
+
 struct select_state {
     uint64_t prefix;     // key bits fixed so far
     uint64_t mask;       // which bits of prefix are fixed
@@ -230,81 +233,95 @@ struct select_state {
     uint32_t pad;
 };
 
-// descending = true: keep the k largest keys; false: the k smallest.
-// K::key(i) -> u64, K::eligible(i) -> bool (restricts the population)
+// K::key(i) -> u64, K::eligible(i) -> bool (restricts the population).
+// Lanes holding the same digit aggregate their count (keys often share
+// their leading bits, so a few bins take most items).
 template <class K>
 __global__ void __launch_bounds__(kThreads) k_radix_hist(K kf, const uint64_t *d_n, const select_state *st,
                                                           int shift, unsigned long long *hist) {
-    __shared__ unsigned int sh[256];
     if (!st->active) return;
-    for (int i = threadIdx.x; i < 256; i += blockDim.x) sh[i] = 0;
-    __syncthreads();
     const uint64_t n = *d_n, prefix = st->prefix, mask = st->mask;
     const int lane = threadIdx.x & 31;
     const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
     const uint64_t warp = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    // warp-uniform loop; lanes holding the same digit aggregate their count
-    // (the keys' leading bits are often identical: one bin takes most items)
     for (uint64_t base = warp * 32; base < n; base += warps * 32) {
         const uint64_t i = base + lane;
-        unsigned d = 256;
+        unsigned d = kBins;
         if (i < n && kf.eligible(i)) {
             uint64_t k = kf.key(i);
-            if ((k & mask) == prefix) d = (unsigned)((k >> shift) & 255);
+            if ((k & mask) == prefix) d = (unsigned)((k >> shift) & (kBins - 1));
         }
         const unsigned same = __match_any_sync(0xffffffffu, d);
-        if (d < 256 && lane == __ffs(same) - 1) atomicAdd(&sh[d], (unsigned)__popc(same));
+        if (d < (unsigned)kBins && lane == __ffs(same) - 1)
+            atomicAdd(&hist[d], (unsigned long long)__popc(same));
     }
-    __syncthreads();
-    for (int i = threadIdx.x; i < 256; i += blockDim.x)
-        if (sh[i]) atomicAdd(&hist[i], (unsigned long long)sh[i]);
 }
 
-// picks the digit holding the k-th item in preference order (256 threads:
-// the 256 bins are scanned in parallel)
-static __global__ void __launch_bounds__(256) k_radix_pick(select_state *st, unsigned long long *hist, int shift,
-                                                            bool descending) {
-    __shared__ uint64_t sm[256];
-    if (!st->active) return;
+// picks the digit holding the k-th item in preference order and clears the
+// histogram (one block: 1024 threads x 64 bins)
+static __global__ void __launch_bounds__(1024) k_radix_pick(select_state *st, unsigned long long *hist, int shift,
+                                                             bool descending) {
+    constexpr int per = kBins / 1024;
+    __shared__ uint64_t sm[1024];
     const int t = threadIdx.x;
-    const int d = descending ? 255 - t : t;  // t-th bin in preference order
-    const uint64_t c = hist[d];
-    sm[t] = c;
+    const bool active = st->active != 0;
+    uint64_t sum = 0;
+    if (active)
+        for (int j = 0; j < per; ++j) {
+            const int r = t * per + j;  // rank in preference order
+            sum += hist[descending ? kBins - 1 - r : r];
+        }
+    sm[t] = sum;
     __syncthreads();
-    for (int o = 1; o < 256; o <<= 1) {  // inclusive scan
+    for (int o = 1; o < 1024; o <<= 1) {
         uint64_t v = t >= o ? sm[t - o] : 0;
         __syncthreads();
         sm[t] += v;
         __syncthreads();
     }
-    const uint64_t incl = sm[t], excl = incl - c;
-    const uint64_t k = st->k_rem;
-    __syncthreads();
-    if (excl < k && k <= incl) {  // exactly one bin holds the k-th item
-        select_state *w = st;
-        w->prefix |= (uint64_t)d << shift;
-        w->mask |= 255ull << shift;
-        w->n_better += excl;
-        w->k_rem = k - excl;
-        w->n_equal = c;
+    if (active) {
+        const uint64_t k = st->k_rem;
+        uint64_t excl = sm[t] - sum;
+        __syncthreads();
+        if (excl < k && k <= excl + sum) {  // the k-th item is in this thread's bins
+            for (int j = 0; j < per; ++j) {
+                const int r = t * per + j;
+                const int d = descending ? kBins - 1 - r : r;
+                const uint64_t c = hist[d];
+                if (k <= excl + c) {
+                    st->prefix |= (uint64_t)d << shift;
+                    st->mask |= (uint64_t)(kBins - 1) << shift;
+                    st->n_better += excl;
+                    st->k_rem = k - excl;
+                    st->n_equal = c;
+                    break;
+                }
+                excl += c;
+            }
+        }
+        __syncthreads();
+        for (int j = 0; j < per; ++j) hist[t * per + j] = 0;
     }
-    hist[d] = 0;
 }
 
 // ---------------------------------------------------- collision table
-// keys[M] (kEmptyKey = free; cleared before each step), rep[M+1] (u32
-// minimum child index) and acc[M+1][4] (re lo, re hi, im lo, im hi: one
-// 32-byte sector per slot).  Pass 1 claims slots (CAS from kEmptyKey) and the
-// claiming thread initialises the slot's rep and acc; pass 2, a separate
-// launch, accumulates, so only the keys need clearing and no fence is needed.
-// Children whose hash is kEmptyKey use the extra slot M (initialised by the
-// host).  M need not be a power of two: the home slot is the high half of
+// slots[M+1] {key, rep} (16 bytes; cleared to all-ones before each step)
+// and acc[M+1][4] (re lo, re hi, im lo, im hi: one 32-byte sector per slot).
+// Pass 1 claims slots (CAS from kEmptyKey) and the claiming thread starts
+// the group with its own child; pass 2, a separate launch, adds the other
+// members, so only the slots need clearing and no fence is needed.
+// Children whose hash is kEmptyKey use the extra slot M.  M need not be a power of two: the home slot is the high half of
 // (mixed hash) * M.
+struct __align__(16) table_slot {
+    unsigned long long key;  // kEmptyKey = free
+    unsigned int rep;        // minimum child index of the group
+    unsigned int pad;
+};
+
 struct table {
-    uint64_t *keys;
-    uint32_t *rep;
+    table_slot *slots;       // [M+1], memset to 0xff before each step
     unsigned long long *acc;
-    uint64_t m;         // slots
+    uint64_t m;              // slots
     uint32_t max_probes;
 };
 
@@ -343,25 +360,21 @@ __global__ void __launch_bounds__(kThreads) k_table_claim(table t, Src src, cons
             s = table_home(h, t.m);
             uint32_t probe = 0;
             while (true) {
-                uint64_t key = ld_volatile_u64(&t.keys[s]);
-                if (key == h) break;
-                if (key == kEmptyKey) {
-                    key = atomicCAS((unsigned long long *)&t.keys[s], kEmptyKey, h);
-                    if (key == kEmptyKey) {  // claimed: the group starts with this child
-                        const double2 m = src.mag(k);
-                        const fix128 re = to_fix(m.x, F), im = to_fix(m.y, F);
-                        ulonglong4_32a a;
-                        a.x = re.lo;
-                        a.y = re.hi;
-                        a.z = im.lo;
-                        a.w = im.hi;
-                        t.rep[s] = (uint32_t)src.child(k);
-                        *(ulonglong4_32a *)&t.acc[4 * s] = a;
-                        claimed = true;
-                        break;
-                    }
-                    if (key == h) break;
+                const unsigned long long key = atomicCAS(&t.slots[s].key, kEmptyKey, h);
+                if (key == kEmptyKey) {  // claimed: the group starts with this child
+                    const double2 m = src.mag(k);
+                    const fix128 re = to_fix(m.x, F), im = to_fix(m.y, F);
+                    ulonglong4_32a a;
+                    a.x = re.lo;
+                    a.y = re.hi;
+                    a.z = im.lo;
+                    a.w = im.hi;
+                    t.slots[s].rep = (uint32_t)src.child(k);
+                    *(ulonglong4_32a *)&t.acc[4 * s] = a;
+                    claimed = true;
+                    break;
                 }
+                if (key == h) break;
                 if (++s == t.m) s = 0;
                 if (++probe >= t.max_probes) {
                     set_error(err, QUIDS_ERR_TABLE_FULL);
@@ -394,7 +407,7 @@ __global__ void __launch_bounds__(kThreads) k_table_accumulate(table t, Src src,
         s &= ~kJoin;
         slot_of[k] = s;
         const uint32_t c = (uint32_t)src.child(k);
-        const uint32_t old = atomicMin(&t.rep[s], c);
+        const uint32_t old = atomicMin(&t.slots[s].rep, c);
         if (old != 0xffffffffu) {  // slot M starts without a member
             not_rep[old > c ? old : c] = 1;
             has_join[old < c ? old : c] = 1;
