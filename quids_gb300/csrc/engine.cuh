@@ -39,7 +39,6 @@ enum qd_buf_id {
     B_UCHILD,      // u64 [NU] groups kept after zero elimination (truncation path)
     B_UMAG,        // double2 [NU]
     B_UNORM,       // u64 [NU] IEEE bits of the group norm
-    B_UHASH,       // u64 [NU]
     B_SCHILD,      // u64 [NS] representative child of each survivor
     B_LOOKBACK,    // u64 [3 (tiles + 2)] look-back chains
     B_TILENORM,    // double [tiles] per-tile norm sums of the survivors
@@ -552,7 +551,8 @@ struct groups_layout {
     uint32_t *osize;
     uint64_t *obegin;
     uint64_t *schild;
-    __device__ bool select(uint64_t c) const {
+    __device__ bool tie(uint64_t) const { return false; }
+    __device__ bool select(uint64_t c, uint64_t) const {
         mag_t m;
         return g.kept(c, m);
     }
@@ -575,11 +575,9 @@ struct groups_layout {
 // truncation possible: keep the groups with their norms for the selection
 struct groups_collect {
     group_view g;
-    const uint64_t *hash;
     uint64_t *uchild;
     double2 *umag;
     uint64_t *unorm;
-    uint64_t *uhash;
     __device__ bool select(uint64_t c) const {
         mag_t m;
         return g.kept(c, m);
@@ -590,7 +588,6 @@ struct groups_collect {
         uchild[j] = c;
         umag[j] = make_double2(m.re, m.im);
         unorm[j] = (uint64_t)__double_as_longlong(cnorm(m));
-        uhash[j] = hash[c];
     }
 };
 
@@ -598,14 +595,6 @@ struct groups_collect {
 struct key_unorm {
     const uint64_t *unorm;
     __device__ uint64_t key(uint64_t i) const { return unorm[i]; }
-    __device__ bool eligible(uint64_t) const { return true; }
-};
-struct key_uhash_ties {
-    const uint64_t *unorm;
-    const uint64_t *uhash;
-    const prim::select_state *first;
-    __device__ uint64_t key(uint64_t i) const { return uhash[i]; }
-    __device__ bool eligible(uint64_t i) const { return unorm[i] == first->prefix; }
 };
 struct key_parent_norm {
     const double2 *mag;
@@ -613,38 +602,17 @@ struct key_parent_norm {
         double2 m = mag[i];
         return (uint64_t)__double_as_longlong(cnorm(mag_t{m.x, m.y}));
     }
-    __device__ bool eligible(uint64_t) const { return true; }
 };
-struct key_parent_index_ties {
-    const double2 *mag;
-    const prim::select_state *first;
-    __device__ uint64_t key(uint64_t i) const { return i; }
-    __device__ bool eligible(uint64_t i) const {
-        double2 m = mag[i];
-        return (uint64_t)__double_as_longlong(cnorm(mag_t{m.x, m.y})) == first->prefix;
-    }
-};
-
 static __global__ void k_select_init(prim::select_state *st, const uint64_t *d_n, uint64_t k) {
     prim::select_state s{};
     s.k_rem = k;
     s.active = k < *d_n ? 1u : 0u;
     st[0] = s;
-    st[1] = prim::select_state{};
 }
-// second selection among threshold ties, only when not all ties are kept
-static __global__ void k_select_ties_init(prim::select_state *st) {
-    prim::select_state s{};
-    s.k_rem = st[0].k_rem;
-    s.active = (st[0].active && st[0].k_rem < st[0].n_equal) ? 1u : 0u;
-    st[1] = s;
-}
-
-// the truncation's survivors (norm above the cutoff, ties by lower hash) into
-// the output layout (src/quids.hpp:866-948)
+// the truncation's survivors (norm above the cutoff; among exact ties at the
+// cutoff, the lower child indices) into the output layout (src/quids.hpp:866-948)
 struct keep_layout {
     const uint64_t *unorm;
-    const uint64_t *uhash;
     const uint64_t *uchild;
     const double2 *umag;
     const prim::select_state *st;
@@ -654,12 +622,13 @@ struct keep_layout {
     uint32_t *osize;
     uint64_t *obegin;
     uint64_t *schild;
-    __device__ bool select(uint64_t i) const {
-        if (!st[0].active) return true;
+    __device__ bool tie(uint64_t i) const { return st->active && unorm[i] == st->prefix; }
+    __device__ bool select(uint64_t i, uint64_t tie_rank) const {
+        if (!st->active) return true;
         uint64_t k = unorm[i];
-        if (k > st[0].prefix) return true;
-        if (k < st[0].prefix) return false;
-        return !st[1].active || uhash[i] <= st[1].prefix;
+        if (k > st->prefix) return true;
+        if (k < st->prefix) return false;
+        return tie_rank < st->k_rem;
     }
     __device__ uint64_t bytes(uint64_t i) const { return padded_size(csize[uchild[i]], align); }
     __device__ double norm(uint64_t i) const { return __longlong_as_double((long long)unorm[i]); }
@@ -676,13 +645,17 @@ struct keep_parents {
     const double2 *mag;
     const prim::select_state *st;
     uint64_t *pidx;
-    __device__ bool select(uint64_t i) const {
-        if (!st[0].active) return true;
+    __device__ uint64_t key(uint64_t i) const {
         double2 m = mag[i];
-        uint64_t k = (uint64_t)__double_as_longlong(cnorm(mag_t{m.x, m.y}));
-        if (k > st[0].prefix) return true;
-        if (k < st[0].prefix) return false;
-        return !st[1].active || i <= st[1].prefix;
+        return (uint64_t)__double_as_longlong(cnorm(mag_t{m.x, m.y}));
+    }
+    __device__ bool tie(uint64_t i) const { return st->active && key(i) == st->prefix; }
+    __device__ bool select(uint64_t i, uint64_t tie_rank) const {
+        if (!st->active) return true;
+        uint64_t k = key(i);
+        if (k > st->prefix) return true;
+        if (k < st->prefix) return false;
+        return tie_rank < st->k_rem;
     }
     __device__ void emit(uint64_t i, uint64_t j) const { pidx[j] = i; }
 };
@@ -696,23 +669,17 @@ static __global__ void __launch_bounds__(prim::kThreads)
 }
 
 // ------------------------------------------------------------ radix select
-// Runs the 8 passes of a top-k selection (and the tie passes) on the stream.
-template <class K1, class K2>
-inline int radix_select(quids_gpu_ctx *ctx, const uint64_t *d_n, uint64_t n_host, uint64_t k, K1 k1, K2 k2,
-                        bool tie_descending) {
+// Runs the 8 passes of a top-k threshold selection on the stream.
+template <class K1>
+inline int radix_select(quids_gpu_ctx *ctx, const uint64_t *d_n, uint64_t n_host, uint64_t k, K1 k1) {
     unsigned grid = grid_for(ctx, n_host);
     k_select_init<<<1, 1, 0, ctx->stream>>>(ctx->d_sel, d_n, k);
     QD_CUDA(cudaMemsetAsync(ctx->d_hist, 0, prim::kBins * sizeof(unsigned long long), ctx->stream));
     for (int shift = 64 - prim::kDigitBits; shift >= 0; shift -= prim::kDigitBits) {
         prim::k_radix_hist<<<grid, prim::kThreads, 0, ctx->stream>>>(k1, d_n, ctx->d_sel, shift, ctx->d_hist);
-        prim::k_radix_pick<<<1, 1024, 0, ctx->stream>>>(ctx->d_sel, ctx->d_hist, shift, true);
+        prim::k_radix_pick<<<1, prim::kBins, 0, ctx->stream>>>(ctx->d_sel, ctx->d_hist, shift, true);
     }
-    k_select_ties_init<<<1, 1, 0, ctx->stream>>>(ctx->d_sel);
-    for (int shift = 64 - prim::kDigitBits; shift >= 0; shift -= prim::kDigitBits) {
-        prim::k_radix_hist<<<grid, prim::kThreads, 0, ctx->stream>>>(k2, d_n, ctx->d_sel + 1, shift, ctx->d_hist);
-        prim::k_radix_pick<<<1, 1024, 0, ctx->stream>>>(ctx->d_sel + 1, ctx->d_hist, shift, tie_descending);
-    }
-    return launched(ctx, 2 + 4 * 64 / prim::kDigitBits);
+    return launched(ctx, 1 + 2 * 64 / prim::kDigitBits);
 }
 
 inline uint64_t next_pow2(uint64_t v) {
@@ -860,13 +827,13 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, qui
     if (maxn < N) {
         QD_TRY(ensure(ctx->buf[B_PIDX], maxn * sizeof(uint64_t)));
         key_parent_norm k1{(const double2 *)in->mag.p};
-        key_parent_index_ties k2{(const double2 *)in->mag.p, ctx->d_sel};
-        QD_TRY(radix_select(ctx, ctx->d_words + W_N, N, maxn, k1, k2, false));
-        prim::lookback lb;
+        QD_TRY(radix_select(ctx, ctx->d_words + W_N, N, maxn, k1));
+        prim::lookback lb, lbt;
         QD_TRY(lookback_chain(ctx, N, 0, lb));
+        QD_TRY(lookback_chain(ctx, N, 2, lbt));
         keep_parents kp{(const double2 *)in->mag.p, ctx->d_sel, bufp<uint64_t>(ctx, B_PIDX)};
-        prim::k_compact<<<lookback_grid(ctx, N), prim::kThreads, 0, ctx->stream>>>(kp, ctx->d_words + W_N,
-                                                                                  ctx->d_words + W_NP, lb);
+        prim::k_compact_ranked<<<lookback_grid(ctx, N), prim::kThreads, 0, ctx->stream>>>(
+            kp, ctx->d_words + W_N, ctx->d_words + W_NP, lb, lbt);
         QD_TRY(launched(ctx));
         NP = maxn;
         pidx = bufp<uint64_t>(ctx, B_PIDX);
@@ -932,7 +899,6 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, qui
         QD_TRY(ensure(ctx->buf[B_UCHILD], NC * sizeof(uint64_t)));
         QD_TRY(ensure(ctx->buf[B_UMAG], NC * sizeof(double2)));
         QD_TRY(ensure(ctx->buf[B_UNORM], NC * sizeof(uint64_t)));
-        QD_TRY(ensure(ctx->buf[B_UHASH], NC * sizeof(uint64_t)));
     }
     if (regions) {
         QD_TRY(ensure(ctx->buf[B_RHASH], NC * sizeof(uint64_t)));
@@ -1014,34 +980,32 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, qui
         QD_TRY(lookback_chain(ctx, NC, 1, lbb));
         groups_layout f{gv, bufp<uint32_t>(ctx, B_CSIZE), align, (double2 *)out->mag.p, (uint32_t *)out->size.p,
                         (uint64_t *)out->begin.p, bufp<uint64_t>(ctx, B_SCHILD)};
-        prim::k_compact_layout<<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
+        prim::k_compact_layout<groups_layout, false><<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
             f, ctx->d_words + W_NC, ctx->d_words + W_NS, ctx->d_words + W_OUTBYTES, (uint64_t *)out->begin.p,
-            tile_norm, lbc, lbb);
+            tile_norm, lbc, lbb, lbb);
         QD_TRY(launched(ctx));
         end_stage(3);
     } else {
         prim::lookback lb;
         QD_TRY(lookback_chain(ctx, NC, 0, lb));
-        groups_collect f{gv, bufp<uint64_t>(ctx, B_HASH), bufp<uint64_t>(ctx, B_UCHILD), bufp<double2>(ctx, B_UMAG),
-                         bufp<uint64_t>(ctx, B_UNORM), bufp<uint64_t>(ctx, B_UHASH)};
+        groups_collect f{gv, bufp<uint64_t>(ctx, B_UCHILD), bufp<double2>(ctx, B_UMAG), bufp<uint64_t>(ctx, B_UNORM)};
         prim::k_compact<<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(f, ctx->d_words + W_NC,
                                                                                    ctx->d_words + W_NU, lb);
         QD_TRY(launched(ctx));
         end_stage(3);
         begin_stage(4);
         key_unorm k1{bufp<uint64_t>(ctx, B_UNORM)};
-        key_uhash_ties k2{bufp<uint64_t>(ctx, B_UNORM), bufp<uint64_t>(ctx, B_UHASH), ctx->d_sel};
-        QD_TRY(radix_select(ctx, ctx->d_words + W_NU, NC, maxn, k1, k2, false));
-        prim::lookback lbc, lbb;
+        QD_TRY(radix_select(ctx, ctx->d_words + W_NU, NC, maxn, k1));
+        prim::lookback lbc, lbb, lbt;
+        QD_TRY(lookback_chain(ctx, NC, 0, lbt));
         QD_TRY(lookback_chain(ctx, NC, 1, lbc));
         QD_TRY(lookback_chain(ctx, NC, 2, lbb));
-        keep_layout kl{bufp<uint64_t>(ctx, B_UNORM), bufp<uint64_t>(ctx, B_UHASH), bufp<uint64_t>(ctx, B_UCHILD),
-                       bufp<double2>(ctx, B_UMAG), ctx->d_sel, bufp<uint32_t>(ctx, B_CSIZE), align,
-                       (double2 *)out->mag.p, (uint32_t *)out->size.p, (uint64_t *)out->begin.p,
-                       bufp<uint64_t>(ctx, B_SCHILD)};
-        prim::k_compact_layout<<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
+        keep_layout kl{bufp<uint64_t>(ctx, B_UNORM), bufp<uint64_t>(ctx, B_UCHILD), bufp<double2>(ctx, B_UMAG),
+                       ctx->d_sel, bufp<uint32_t>(ctx, B_CSIZE), align, (double2 *)out->mag.p,
+                       (uint32_t *)out->size.p, (uint64_t *)out->begin.p, bufp<uint64_t>(ctx, B_SCHILD)};
+        prim::k_compact_layout<keep_layout, true><<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
             kl, ctx->d_words + W_NU, ctx->d_words + W_NS, ctx->d_words + W_OUTBYTES, (uint64_t *)out->begin.p,
-            tile_norm, lbc, lbb);
+            tile_norm, lbc, lbb, lbt);
         QD_TRY(launched(ctx));
         end_stage(4);
     }

@@ -217,14 +217,69 @@ __global__ void __launch_bounds__(kThreads) k_compact(P p, const uint64_t *d_n, 
     }
 }
 
+// Compaction like k_compact where P::select(i, tie_rank) also sees the rank
+// of the item among the ties (P::tie(i)) in item order.
+template <class P>
+__global__ void __launch_bounds__(kThreads) k_compact_ranked(P p, const uint64_t *d_n, uint64_t *d_count,
+                                                              lookback lb, lookback lb_ties) {
+    __shared__ uint64_t sm[kThreads / 32 + 1];
+    __shared__ uint64_t bcast;
+    __shared__ uint32_t sm_tile;
+    const uint64_t n = *d_n;
+    const uint64_t ntiles = (n + kTile - 1) / kTile;
+    if (n == 0) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) *d_count = 0;
+        return;
+    }
+    while (true) {
+        uint32_t tile = next_tile(lb, &sm_tile);
+        if (tile >= ntiles) break;
+        const uint64_t base = (uint64_t)tile * kTile + (uint64_t)threadIdx.x * kItems;
+        uint32_t ties = 0;
+        uint64_t tcnt = 0;
+#pragma unroll
+        for (int k = 0; k < kItems; ++k) {
+            uint64_t i = base + k;
+            if (i < n && p.tie(i)) {
+                ties |= 1u << k;
+                ++tcnt;
+            }
+        }
+        uint64_t agg_t;
+        uint64_t excl_t = block_excl_scan(tcnt, sm, agg_t);
+        uint64_t rank = tile_prefix(lb_ties, tile, agg_t, &bcast) + excl_t;
+        uint32_t flags = 0;
+        uint64_t cnt = 0;
+#pragma unroll
+        for (int k = 0; k < kItems; ++k) {
+            uint64_t i = base + k;
+            if (i < n && p.select(i, rank)) {
+                flags |= 1u << k;
+                ++cnt;
+            }
+            if (ties & (1u << k)) ++rank;
+        }
+        uint64_t agg;
+        uint64_t texcl = block_excl_scan(cnt, sm, agg);
+        uint64_t prefix = tile_prefix(lb, tile, agg, &bcast);
+        uint64_t j = prefix + texcl;
+#pragma unroll
+        for (int k = 0; k < kItems; ++k)
+            if (flags & (1u << k)) p.emit(base + k, j++);
+        if (tile == ntiles - 1 && threadIdx.x == kThreads - 1) *d_count = prefix + agg;
+    }
+}
+
 // --------------------------------------------------------- radix select
-// Top-k selection on 64-bit keys, 16 bits per pass from the top (4 passes).
-// State is device resident so the passes need no host round trip.
-constexpr int kDigitBits = 16;
+// Threshold of a top-k selection on 64-bit keys, 8 bits per pass from the top
+// (8 passes).  State is device resident so the passes need no host round trip.
+// Afterwards: keys > prefix are kept, and k_rem of the n_equal keys equal to
+// prefix (the ties), taken in item order by the keep compaction.
+constexpr int kDigitBits = 8;
 constexpr int kBins = 1 << kDigitBits;
 
 struct select_state {
-    uint64_t prefix;     // key bits fixed so far
+    uint64_t prefix;     // key bits fixed so far (the threshold at the end)
     uint64_t mask;       // which bits of prefix are fixed
     uint64_t k_rem;      // how many items still to take among those matching prefix
     uint64_t n_better;   // items strictly better than the threshold
@@ -233,13 +288,15 @@ struct select_state {
     uint32_t pad;
 };
 
-// K::key(i) -> u64, K::eligible(i) -> bool (restricts the population).
-// Lanes holding the same digit aggregate their count (keys often share
-// their leading bits, so a few bins take most items).
+// K::key(i) -> u64.  Shared-memory histogram; lanes holding the same digit
+// aggregate their count (keys often share their leading bits).
 template <class K>
 __global__ void __launch_bounds__(kThreads) k_radix_hist(K kf, const uint64_t *d_n, const select_state *st,
                                                           int shift, unsigned long long *hist) {
+    __shared__ unsigned int sh[kBins];
     if (!st->active) return;
+    for (int i = threadIdx.x; i < kBins; i += blockDim.x) sh[i] = 0;
+    __syncthreads();
     const uint64_t n = *d_n, prefix = st->prefix, mask = st->mask;
     const int lane = threadIdx.x & 31;
     const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
@@ -247,61 +304,46 @@ __global__ void __launch_bounds__(kThreads) k_radix_hist(K kf, const uint64_t *d
     for (uint64_t base = warp * 32; base < n; base += warps * 32) {
         const uint64_t i = base + lane;
         unsigned d = kBins;
-        if (i < n && kf.eligible(i)) {
+        if (i < n) {
             uint64_t k = kf.key(i);
             if ((k & mask) == prefix) d = (unsigned)((k >> shift) & (kBins - 1));
         }
         const unsigned same = __match_any_sync(0xffffffffu, d);
-        if (d < (unsigned)kBins && lane == __ffs(same) - 1)
-            atomicAdd(&hist[d], (unsigned long long)__popc(same));
+        if (d < (unsigned)kBins && lane == __ffs(same) - 1) atomicAdd(&sh[d], (unsigned)__popc(same));
     }
+    __syncthreads();
+    for (int i = threadIdx.x; i < kBins; i += blockDim.x)
+        if (sh[i]) atomicAdd(&hist[i], (unsigned long long)sh[i]);
 }
 
 // picks the digit holding the k-th item in preference order and clears the
-// histogram (one block: 1024 threads x 64 bins)
-static __global__ void __launch_bounds__(1024) k_radix_pick(select_state *st, unsigned long long *hist, int shift,
-                                                             bool descending) {
-    constexpr int per = kBins / 1024;
-    __shared__ uint64_t sm[1024];
+// histogram (256 threads scan the 256 bins)
+static __global__ void __launch_bounds__(kBins) k_radix_pick(select_state *st, unsigned long long *hist, int shift,
+                                                              bool descending) {
+    __shared__ uint64_t sm[kBins];
+    if (!st->active) return;
     const int t = threadIdx.x;
-    const bool active = st->active != 0;
-    uint64_t sum = 0;
-    if (active)
-        for (int j = 0; j < per; ++j) {
-            const int r = t * per + j;  // rank in preference order
-            sum += hist[descending ? kBins - 1 - r : r];
-        }
-    sm[t] = sum;
+    const int d = descending ? kBins - 1 - t : t;  // t-th bin in preference order
+    const uint64_t c = hist[d];
+    sm[t] = c;
     __syncthreads();
-    for (int o = 1; o < 1024; o <<= 1) {
+    for (int o = 1; o < kBins; o <<= 1) {
         uint64_t v = t >= o ? sm[t - o] : 0;
         __syncthreads();
         sm[t] += v;
         __syncthreads();
     }
-    if (active) {
-        const uint64_t k = st->k_rem;
-        uint64_t excl = sm[t] - sum;
-        __syncthreads();
-        if (excl < k && k <= excl + sum) {  // the k-th item is in this thread's bins
-            for (int j = 0; j < per; ++j) {
-                const int r = t * per + j;
-                const int d = descending ? kBins - 1 - r : r;
-                const uint64_t c = hist[d];
-                if (k <= excl + c) {
-                    st->prefix |= (uint64_t)d << shift;
-                    st->mask |= (uint64_t)(kBins - 1) << shift;
-                    st->n_better += excl;
-                    st->k_rem = k - excl;
-                    st->n_equal = c;
-                    break;
-                }
-                excl += c;
-            }
-        }
-        __syncthreads();
-        for (int j = 0; j < per; ++j) hist[t * per + j] = 0;
+    const uint64_t incl = sm[t], excl = incl - c;
+    const uint64_t k = st->k_rem;
+    __syncthreads();
+    if (excl < k && k <= incl) {  // exactly one bin holds the k-th item
+        st->prefix |= (uint64_t)d << shift;
+        st->mask |= (uint64_t)(kBins - 1) << shift;
+        st->n_better += excl;
+        st->k_rem = k - excl;
+        st->n_equal = c;
     }
+    hist[d] = 0;
 }
 
 // ---------------------------------------------------- collision table
@@ -515,16 +557,19 @@ static __global__ void __launch_bounds__(kThreads)
 
 // --------------------------------------------- compaction + byte offsets
 // Order-preserving compaction that also lays out the selected items'
-// variable-size payloads: P::select(i) -> bool, P::bytes(i) -> padded size,
-// P::norm(i) -> double, P::emit(i, j, byte_offset).  Two look-back chains
-// (count, bytes) in one pass; per tile, the sum of the selected norms in item
-// order goes to tile_norm[tile] (a fixed decomposition: deterministic).
-// At the end: *d_count, *d_bytes and begin_out[count] = total bytes.
-template <class P>
+// variable-size payloads: P::select(i, tie_rank) -> bool, P::bytes(i) ->
+// padded size, P::norm(i) -> double, P::emit(i, j, byte_offset).  With TIES,
+// P::tie(i) -> bool marks the items equal to a selection threshold and
+// tie_rank is the item's rank among them in item order (a third look-back
+// chain), so a selection can take the first ties.  Per tile, the sum of the
+// selected norms in item order goes to tile_norm[tile] (a fixed
+// decomposition: deterministic).  At the end: *d_count, *d_bytes and
+// begin_out[count] = total bytes.
+template <class P, bool TIES>
 __global__ void __launch_bounds__(kThreads) k_compact_layout(P p, const uint64_t *d_n, uint64_t *d_count,
                                                               uint64_t *d_bytes, uint64_t *begin_out,
                                                               double *tile_norm, lookback lb_count,
-                                                              lookback lb_bytes) {
+                                                              lookback lb_bytes, lookback lb_ties) {
     __shared__ uint64_t sm[kThreads / 32 + 1];
     __shared__ double smd[kThreads];
     __shared__ uint64_t bcast;
@@ -543,18 +588,35 @@ __global__ void __launch_bounds__(kThreads) k_compact_layout(P p, const uint64_t
         uint32_t tile = next_tile(lb_count, &sm_tile);
         if (tile >= ntiles) break;
         const uint64_t base = (uint64_t)tile * kTile + (uint64_t)threadIdx.x * kItems;
+        uint64_t rank = 0;
+        uint32_t ties = 0;
+        if constexpr (TIES) {
+            uint64_t tcnt = 0;
+#pragma unroll
+            for (int k = 0; k < kItems; ++k) {
+                uint64_t i = base + k;
+                if (i < n && p.tie(i)) {
+                    ties |= 1u << k;
+                    ++tcnt;
+                }
+            }
+            uint64_t agg_t;
+            uint64_t excl_t = block_excl_scan(tcnt, sm, agg_t);
+            rank = tile_prefix(lb_ties, tile, agg_t, &bcast) + excl_t;
+        }
         uint32_t flags = 0;
         uint64_t cnt = 0, bytes = 0;
         double nrm = 0;
 #pragma unroll
         for (int k = 0; k < kItems; ++k) {
             uint64_t i = base + k;
-            if (i < n && p.select(i)) {
+            if (i < n && p.select(i, rank)) {
                 flags |= 1u << k;
                 ++cnt;
                 bytes += p.bytes(i);
                 nrm = dadd(nrm, p.norm(i));
             }
+            if (ties & (1u << k)) ++rank;
         }
         // deterministic per-tile norm sum: fixed tree over threads
         smd[threadIdx.x] = nrm;
