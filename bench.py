@@ -51,19 +51,30 @@ def workload(name):
                                        "(H on a seeded random half + 24 CNOT/Z), max_num_object 2^22",
                                        "qubits": 24, "layers": 6, "max_num_object": MAX24, "seed": 0,
                                        "tolerance": 1e-18, "align_byte_length": 8}}
-    if name == "qcgd12":
-        return {"name": name, "init": None, "gates": W.qcgd_step_rules(), "max": 1 << 24, "tolerance": 1e-18,
-                "align": 8, "config": {"workload": "QCGD step (step, coin, split_merge, erase_create) on the "
-                                       "state after step 0 of a 12-node cycle graph, max_num_object 2^24",
-                                       "nodes": 12, "seed": 1, "max_num_object": 1 << 24}}
+    if name in ("qcgd12", "qcgd10"):
+        nodes, seed, cap = (12, 1, 1 << 24) if name == "qcgd12" else (10, 3, 1 << 22)
+        return {"name": name, "init": None, "nodes": nodes, "seed": seed, "gates": W.qcgd_step_rules(), "max": cap,
+                "tolerance": 1e-18, "align": 8,
+                "config": {"workload": f"QCGD step 1 (step, coin(pi/4), split_merge(pi/4,0,-pi/2), "
+                                       f"erase_create(pi/3,pi/5,0)) of a {nodes}-node cycle graph, from the "
+                                       f"state after step 0, max_num_object 2^{cap.bit_length() - 1}",
+                           "nodes": nodes, "seed": seed, "max_num_object": cap, "tolerance": 1e-18,
+                           "align_byte_length": 8}}
     raise SystemExit(f"unknown config {name}")
 
 
-def qcgd12_initial(port=None):
-    """State after the first QCGD step of the 12-node graph (computed with the
-    GPU path when no oracle is given)."""
+def qcgd_initial_cpu(wl, o):
+    """State after QCGD step 0 (computed by the CPU oracle, for its own timing)."""
     from quids_gb300 import workloads as W
-    return W.qcgd_single_state(12, seed=1)
+    s = o.new_state(W.qcgd_single_state(wl["nodes"], seed=wl["seed"]))
+    for g in wl["gates"]:
+        if g.kind == "mod":
+            o.modifier(s, g.code, g.params)
+        else:
+            t = o.new_state()
+            o.simulate(s, g.code, g.params, t, wl["max"])
+            s = t
+    return s.store()
 
 
 # ------------------------------------------------------------------ helpers
@@ -180,11 +191,12 @@ def ours(args, rank, world):
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.int32, device=f"cuda:{dev}")
 
     init_packed = wl["init"]
-    if init_packed is None:  # qcgd12: state after step 0, computed on the GPU
+    if init_packed is None:  # QCGD: the state after step 0, computed on the GPU
         from quids_gb300 import workloads as W
-        it = quids.it_t(ctx, W.qcgd_single_state(12, seed=1))
+        it = quids.it_t(ctx, W.qcgd_single_state(wl["nodes"], seed=wl["seed"]))
         _, it = run_step_gpu(ctx, quids, wl, it)
         init_packed = it.download()
+        wl.pop("_spare", None)
     init = quids.it_t(ctx, init_packed)
 
     # warm-up
@@ -280,7 +292,7 @@ def ours(args, rank, world):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(wl, init_packed, samples=1)
+        cpu = cpu_baseline(wl, init_packed, samples=1, warm=wl["name"] == "circuit24")
 
     if rank == 0:
         line = {
@@ -305,7 +317,7 @@ def ours(args, rank, world):
         print(json.dumps(line), flush=True)
 
 
-def cpu_baseline(wl, init_packed, samples=1):
+def cpu_baseline(wl, init_packed, samples=1, warm=True):
     """The oracle port (the reference algorithm restated, OpenMP) on all host cores."""
     from oracle.oracle import Oracle
     o = Oracle("port")
@@ -325,7 +337,8 @@ def cpu_baseline(wl, init_packed, samples=1):
                 s = t
         return ch
 
-    one()  # warm-up
+    if warm:
+        one()  # warm-up (skipped for the long QCGD steps)
     t0 = time.perf_counter()
     ch = sum(one() for _ in range(samples))
     dt = time.perf_counter() - t0
@@ -337,15 +350,12 @@ def reference(args, rank, world):
     if rank != 0:
         return
     wl = workload(args.config)
-    init_packed = wl["init"]
-    if init_packed is None:
-        print(json.dumps({"impl": "reference", "unavailable": "qcgd12 reference arm not wired"}))
-        return
     from oracle.oracle import Oracle
     o = Oracle("port")
     cores = os.cpu_count() or 1
     o.set_threads(cores)
     o.set_globals(wl["tolerance"], True, wl["align"])
+    init_packed = wl["init"] if wl["init"] is not None else qcgd_initial_cpu(wl, o)
 
     def one():
         s = o.new_state(init_packed)
@@ -382,7 +392,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="circuit24", choices=["circuit24", "qcgd12"])
+    ap.add_argument("--config", default="circuit24", choices=["circuit24", "qcgd12", "qcgd10"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -113,3 +113,49 @@ def assert_fixed_state_parity(got, exp, truncated=False, what=""):
     tol = REL * np.maximum(np.maximum(np.abs(a), np.abs(b)), FLOOR)
     bad = np.abs(a - b) > tol
     assert not bad.any(), f"{what}: {int(bad.sum())} magnitudes differ"
+
+
+def assert_hashed_state_parity(ctx, got_it, exp_packed, hash_rule, qcgd=True, truncated=False, what="",
+                               sample=2000):
+    """Large-state parity through hashes: both states are hashed on the GPU
+    with the rule's hasher (pinned to the reference's by the golden vectors),
+    compared as (hash -> magnitude) maps with the tie band, and a random
+    sample of objects is compared byte for byte."""
+    import quids_gb300 as quids
+    exp_it = quids.it_t(ctx, exp_packed)
+    gh = quids.state_hash(got_it, hash_rule)
+    eh = quids.state_hash(exp_it, hash_rule)
+    got = got_it.download()
+    gm, em = np.asarray(got[3]), np.asarray(exp_packed[3])
+    assert len(gh) == len(eh), f"{what}: {len(gh)} objects, expected {len(eh)}"
+    go, eo = np.argsort(gh, kind="stable"), np.argsort(eh, kind="stable")
+    gh, eh, gm, em = gh[go], eh[eo], gm[go], em[eo]
+    assert (np.diff(gh.astype(np.uint64)) != 0).all(), f"{what}: duplicate hashes in the result"
+    if truncated and len(em):
+        en = np.abs(em) ** 2
+        tau = en.min()
+        kg = np.abs(np.abs(gm) ** 2 - tau) > REL * tau * 4
+        ke = np.abs(en - tau) > REL * tau * 4
+        assert kg.sum() == ke.sum() and (gh[kg] == eh[ke]).all(), f"{what}: sets differ outside the tie band"
+        gm, em = gm[kg], em[ke]
+        gsel, esel = go[kg], eo[ke]
+    else:
+        assert (gh == eh).all(), f"{what}: object sets differ"
+        gsel, esel = go, eo
+    tol = REL * np.maximum(np.maximum(np.abs(gm), np.abs(em)), FLOOR)
+    bad = np.abs(gm - em) > tol
+    assert not bad.any(), f"{what}: {int(bad.sum())} magnitudes differ"
+    rng = np.random.default_rng(0)
+    pick = rng.choice(len(gsel), size=min(sample, len(gsel)), replace=False) if len(gsel) else []
+    gobj, gbeg, gsz = got[0], got[1], got[2]
+    eobj, ebeg, esz = exp_packed[0], exp_packed[1], exp_packed[2]
+    for k in pick:
+        a, b = int(gsel[k]), int(esel[k])
+        x = gobj[int(gbeg[a]): int(gbeg[a]) + int(gsz[a])].tobytes()
+        y = eobj[int(ebeg[b]): int(ebeg[b]) + int(esz[b])].tobytes()
+        assert len(x) == len(y), f"{what}: object sizes differ"
+        if qcgd:
+            mk = W.graph_padding_mask(y)
+            assert (np.frombuffer(x, np.uint8)[mk] == np.frombuffer(y, np.uint8)[mk]).all(), f"{what}: bytes differ"
+        else:
+            assert x == y, f"{what}: bytes differ"

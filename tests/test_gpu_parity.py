@@ -284,3 +284,50 @@ def test_large_steps(ctx, port):
                 break
         it = nxt
     assert checked == 3
+
+
+def _qcgd_large(ctx, port, nodes, seed, cap, what):
+    from tests.parity import assert_hashed_state_parity
+    port.set_globals(1e-18, True, 8)
+    it = quids.it_t(ctx, W.qcgd_single_state(nodes, seed=seed))
+    for step in range(2):
+        for g in W.qcgd_step_rules():
+            r = quids.rule_from(g.kind == "rule", g.code, g.params)
+            if g.kind == "mod":
+                quids.simulate(it, r)
+                continue
+            nxt, sy = quids.it_t(ctx), quids.sy_it_t()
+            if step == 1:
+                inp = it.download()
+            quids.simulate(it, r, nxt, sy, cap)
+            if step == 1:
+                a, b = port.new_state(inp), port.new_state()
+                nc, nu = port.simulate(a, g.code, g.params, b, cap)
+                assert (sy.num_object, sy.num_object_after_interferences) == (nc, nu), f"{what} rule {g.code}"
+                assert_hashed_state_parity(ctx, nxt, b.store(), rules.coin(0.5), truncated=nu > cap,
+                                           what=f"{what} rule {g.code}")
+                assert nxt.total_proba == pytest.approx(b.total_proba, rel=1e-12)
+            it = nxt
+
+
+def test_qcgd_step1_10_nodes(ctx, port):
+    """QCGD step 1 of a 10-node graph (6.4e7 children, 2^22 cap) per rule
+    application against the oracle from identical inputs."""
+    _qcgd_large(ctx, port, 10, 3, 1 << 22, "qcgd10")
+
+
+def _host_ram_gb():
+    with open("/proc/meminfo") as f:
+        for line in f:
+            if line.startswith("MemTotal:"):
+                return int(line.split()[1]) / 2**20
+    return 0.0
+
+
+def test_qcgd_step1_12_nodes(ctx, port):
+    """The 2^24-object QCGD step: step 1 of a 12-node graph (coin 1.0e7,
+    split_merge 1.0e8, erase_create ~5.7e8 children, 2^24 cap) against the
+    oracle from identical inputs.  The oracle needs ~60 GB of host memory."""
+    if _host_ram_gb() < 200:
+        pytest.skip("the CPU oracle of this step needs more host memory")
+    _qcgd_large(ctx, port, 12, 1, 1 << 24, "qcgd12")
