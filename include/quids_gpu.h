@@ -74,12 +74,18 @@ typedef struct quids_gpu_rule_params {
  * the max_num_object argument of simulate(). */
 typedef struct quids_gpu_params {
     double tolerance;            /* quids::tolerance: keep children with norm > tolerance */
-    uint64_t max_num_object;     /* UINT64_MAX = no cap ("-1"); 0 = auto (not supported) */
-    int32_t simple_truncation;   /* must be 1 (probabilistic truncation unsupported) */
+    uint64_t max_num_object;     /* UINT64_MAX = no cap ("-1"); 0 = automatic: as many as fit the
+                                    device memory (free memory + what the context holds, less 20%),
+                                    or memory_budget when set */
+    int32_t simple_truncation;   /* 1: keep the largest norms; 0: probabilistic truncation (keep the
+                                    smallest u / norm, u uniform from a generator seeded by `seed`) */
     uint32_t align_byte_length;  /* quids::align_byte_length for the output state */
     double table_load_factor;    /* collision table max load; 0 -> default 0.5 */
     uint32_t block_size;         /* reserved, 0 */
     uint32_t flags;              /* QUIDS_FLAG_* */
+    uint64_t seed;               /* probabilistic truncation: generator seed (same seed and input,
+                                    same result) */
+    uint64_t memory_budget;      /* automatic truncation: bytes a step may use (0: from the device) */
 } quids_gpu_params;
 
 /* quids_gpu_params.flags */
@@ -218,6 +224,31 @@ int quids_gpu_rule_children_noalloc(void *stream, uint64_t num_object, const uin
                                     int rule_kind, const quids_gpu_rule_params *rule, uint64_t capacity,
                                     uint64_t *num_children, uint64_t *stride, uint8_t *d_child_bytes,
                                     uint64_t *d_hash, uint32_t *d_child_size, double *d_child_magnitude);
+
+/* ------------------------------------------------------------ observables
+ * iteration::average_value(observable) (src/quids.hpp:208-234):
+ * sum over objects of observable(object) * |mag|^2, reduced on the GPU in a
+ * fixed order.  Built-in observables: */
+#define QUIDS_OBS_QCGD_NUM_NODES 1     /* graphs::num_nodes            (src/rules/qcgd.hpp:317-319) */
+#define QUIDS_OBS_QCGD_NUM_NODES_SQ 2  /* num_nodes^2                  (:320-323) */
+#define QUIDS_OBS_QCGD_DENSITY 3       /* (sum left + right) / 2n      (:324-333) */
+#define QUIDS_OBS_QCGD_DENSITY_SQ 4    /* density^2                    (:334-343) */
+#define QUIDS_OBS_QC_BIT 5             /* byte `bit` of the object is non-zero (qubit `bit` is 1) */
+int quids_gpu_average_value(quids_gpu_ctx *ctx, quids_gpu_state *iteration, int observable_kind,
+                            const quids_gpu_rule_params *params, double *value);
+
+/* The statistics qcgd::utils::serialize prints (src/rules/qcgd.hpp:309-366),
+ * computed on the GPU; sy_num_object / sy_num_object_after_interferences are
+ * the counters of the step that produced the state.  std_dev_size follows the
+ * reference's formula (sqrt of the mean square size when the variance is
+ * above tolerance, :345-346). */
+typedef struct quids_gpu_qcgd_stats {
+    double total_proba, num_graphs, avg_size, std_dev_size, avg_density, std_dev_density, interference_ratio,
+        deletion_ratio;
+} quids_gpu_qcgd_stats;
+int quids_gpu_qcgd_statistics(quids_gpu_ctx *ctx, quids_gpu_state *iteration, uint64_t sy_num_object,
+                              uint64_t sy_num_object_after_interferences, double tolerance,
+                              quids_gpu_qcgd_stats *out);
 
 /* MurmurHash64A of libstdc++'s std::hash<std::string_view> (seed 0xc70f6907),
  * the reference's default hasher (src/quids.hpp:143-145), computed on the GPU

@@ -28,7 +28,9 @@ from .capi import QuidsError, U64_MAX
 # reference globals (src/quids.hpp:59-75); read at every simulate() call
 tolerance: float = 1e-30          # TOLERANCE default (src/quids.hpp:30-32)
 align_byte_length: int = 8        # ALIGNMENT_BYTE_LENGTH (src/quids.hpp:27-29)
-simple_truncation: bool = True    # only simple truncation is implemented
+simple_truncation: bool = True    # False: probabilistic truncation (src/quids.hpp:69-75)
+truncation_seed: int = 0          # generator seed of probabilistic truncation
+memory_budget: int = 0            # automatic truncation (max_num_object = 0): bytes per step, 0 = device
 table_load_factor: float = 0.5    # collision table maximum load
 
 
@@ -261,7 +263,8 @@ class it_t:
 
 def _params(max_num_object, flags=0):
     return capi.Params(float(tolerance), int(max_num_object) & U64_MAX, int(bool(simple_truncation)),
-                       int(align_byte_length), float(table_load_factor), 0, int(flags))
+                       int(align_byte_length), float(table_load_factor), 0, int(flags),
+                       int(truncation_seed) & U64_MAX, int(memory_budget))
 
 
 def simulate(iteration: it_t, rule, next_iteration: it_t | None = None, symbolic_iteration: sy_it_t | None = None,
@@ -334,6 +337,30 @@ def rule_children(iteration: it_t, rule):
                                                sizes.ctypes.data, mags.ctypes.data), "rule_children")
     children = [bytes_[i * s: i * s + int(sizes[i])].tobytes() for i in range(n)]
     return children, hashes[:n], mags[:n]
+
+
+OBS_QCGD_NUM_NODES, OBS_QCGD_NUM_NODES_SQ, OBS_QCGD_DENSITY, OBS_QCGD_DENSITY_SQ, OBS_QC_BIT = 1, 2, 3, 4, 5
+
+
+def average_value(iteration: it_t, observable: int, bit: int = 0) -> float:
+    """iteration::average_value (src/quids.hpp:208-234) for a built-in
+    observable (OBS_*), reduced on the GPU."""
+    iteration._flush()
+    v = C.c_double()
+    p = capi.RuleParams(int(bit), 0, 0.0, 0.0, 0.0)
+    capi.check(iteration.lib.quids_gpu_average_value(iteration.ctx.h, iteration.h, int(observable), C.byref(p),
+                                                     C.byref(v)), "average_value")
+    return v.value
+
+
+def qcgd_statistics(iteration: it_t, sy: sy_it_t) -> dict:
+    """The statistics of qcgd::utils::serialize (src/rules/qcgd.hpp:309-366)."""
+    iteration._flush()
+    r = capi.QcgdStats()
+    capi.check(iteration.lib.quids_gpu_qcgd_statistics(iteration.ctx.h, iteration.h, int(sy.num_object),
+                                                       int(sy.num_object_after_interferences), float(tolerance),
+                                                       C.byref(r)), "qcgd_statistics")
+    return r.as_dict()
 
 
 def state_hash(iteration: it_t, rule):

@@ -39,11 +39,20 @@ class RuleParams(C.Structure):
 class Params(C.Structure):
     _fields_ = [("tolerance", C.c_double), ("max_num_object", C.c_uint64), ("simple_truncation", C.c_int32),
                 ("align_byte_length", C.c_uint32), ("table_load_factor", C.c_double),
-                ("block_size", C.c_uint32), ("flags", C.c_uint32)]
+                ("block_size", C.c_uint32), ("flags", C.c_uint32), ("seed", C.c_uint64),
+                ("memory_budget", C.c_uint64)]
 
 
 class Op(C.Structure):
     _fields_ = [("is_rule", C.c_int32), ("kind", C.c_int32), ("params", RuleParams)]
+
+
+class QcgdStats(C.Structure):
+    _fields_ = [(k, C.c_double) for k in ("total_proba", "num_graphs", "avg_size", "std_dev_size", "avg_density",
+                                          "std_dev_density", "interference_ratio", "deletion_ratio")]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class StepStats(C.Structure):
@@ -66,6 +75,7 @@ EXPORTS = [
     "quids_gpu_state_num_bytes", "quids_gpu_state_total_proba", "quids_gpu_state_download",
     "quids_gpu_state_device_arrays", "quids_gpu_simulate", "quids_gpu_apply_modifier",
     "quids_gpu_rule_children", "quids_gpu_state_hash", "quids_gpu_rule_children_noalloc", "quids_gpu_run",
+    "quids_gpu_average_value", "quids_gpu_qcgd_statistics",
 ]
 
 _lib = None
@@ -115,6 +125,8 @@ def load(build_if_missing: bool = True):
                                 C.POINTER(C.c_int)]
     L.quids_gpu_rule_children.argtypes = [vp, vp, C.c_int, C.POINTER(RuleParams), u64p, u64p, vp, vp, vp, vp]
     L.quids_gpu_state_hash.argtypes = [vp, vp, C.c_int, C.POINTER(RuleParams), vp]
+    L.quids_gpu_average_value.argtypes = [vp, vp, C.c_int, C.POINTER(RuleParams), C.POINTER(C.c_double)]
+    L.quids_gpu_qcgd_statistics.argtypes = [vp, vp, C.c_uint64, C.c_uint64, C.c_double, C.POINTER(QcgdStats)]
     L.quids_gpu_rule_children_noalloc.argtypes = [vp, C.c_uint64, vp, vp, vp, vp, C.c_int, C.POINTER(RuleParams),
                                                   C.c_uint64, u64p, u64p, vp, vp, vp, vp]
     _lib = L

@@ -335,6 +335,46 @@ int quids_gpu_rule_children(quids_gpu_ctx *ctx, quids_gpu_state *iteration, int 
     });
 }
 
+int quids_gpu_average_value(quids_gpu_ctx *ctx, quids_gpu_state *st, int kind, const quids_gpu_rule_params *p,
+                            double *value) {
+    switch (kind) {
+    case QUIDS_OBS_QCGD_NUM_NODES: return average_value(ctx, st, qcgd::obs_num_nodes{false}, value);
+    case QUIDS_OBS_QCGD_NUM_NODES_SQ: return average_value(ctx, st, qcgd::obs_num_nodes{true}, value);
+    case QUIDS_OBS_QCGD_DENSITY: return average_value(ctx, st, qcgd::obs_density{false}, value);
+    case QUIDS_OBS_QCGD_DENSITY_SQ: return average_value(ctx, st, qcgd::obs_density{true}, value);
+    case QUIDS_OBS_QC_BIT:
+        if (!p) return QUIDS_ERR_BAD_ARG;
+        return average_value(ctx, st, rules::obs_bit{p->bit}, value);
+    }
+    return QUIDS_ERR_BAD_ARG;
+}
+
+int quids_gpu_qcgd_statistics(quids_gpu_ctx *ctx, quids_gpu_state *st, uint64_t sy_n, uint64_t sy_nu, double tol,
+                              quids_gpu_qcgd_stats *out) {
+    if (!ctx || !st || !out) return QUIDS_ERR_BAD_ARG;
+    // src/rules/qcgd.hpp:309-366
+    quids_gpu_qcgd_stats r{};
+    r.interference_ratio = 1;
+    r.deletion_ratio = 1;
+    if (sy_n > 0) {
+        r.interference_ratio = (double)sy_nu / (double)sy_n;
+        r.deletion_ratio = (double)st->n / (double)sy_nu;
+    }
+    double sq_size, sq_density;
+    QD_TRY(average_value(ctx, st, qcgd::obs_num_nodes{false}, &r.avg_size));
+    QD_TRY(average_value(ctx, st, qcgd::obs_num_nodes{true}, &sq_size));
+    QD_TRY(average_value(ctx, st, qcgd::obs_density{false}, &r.avg_density));
+    QD_TRY(average_value(ctx, st, qcgd::obs_density{true}, &sq_density));
+    double v = sq_size - r.avg_size * r.avg_size;
+    r.std_dev_size = v < tol ? 0 : std::sqrt(sq_size);
+    v = sq_density - r.avg_density * r.avg_density;
+    r.std_dev_density = v < tol ? 0 : std::sqrt(v);
+    QD_TRY(quids_gpu_state_total_proba(st, &r.total_proba));
+    r.num_graphs = (double)st->n;
+    *out = r;
+    return QUIDS_OK;
+}
+
 int quids_gpu_state_hash(quids_gpu_ctx *ctx, quids_gpu_state *st, int rule_kind, const quids_gpu_rule_params *rule,
                          uint64_t *out) {
     if (!ctx || !st || !out || st->ctx != ctx) return QUIDS_ERR_BAD_ARG;

@@ -592,15 +592,41 @@ struct groups_collect {
 };
 
 // radix-select keys
+// Truncation keys, larger = kept first.  Simple truncation: the IEEE bits
+// of the norm (src/quids.hpp:884-889).  Probabilistic truncation
+// (src/quids.hpp:594-608, :829-845, :890-895) keeps the smallest selectors
+// u / norm with u uniform in (0, 1]; here u comes from a counter-based
+// generator keyed on (seed, item id) and the key is the complement of the
+// selector's bits, so the same descending selection applies.
+struct trunc_key {
+    bool probabilistic;
+    uint64_t seed;
+    __device__ __forceinline__ uint64_t operator()(double norm, uint64_t id) const {
+        if (!probabilistic) return (uint64_t)__double_as_longlong(norm);
+        uint64_t z = seed + 0x9E3779B97F4A7C15ull * (id + 1);
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        const double u = (double)((z >> 11) + 1) * 0x1.0p-53;  // (0, 1]
+        const double sel = norm > 0 ? __ddiv_rn(u, norm) : __longlong_as_double(0x7ff0000000000000ll);
+        return ~(uint64_t)__double_as_longlong(sel);
+    }
+};
+
 struct key_unorm {
     const uint64_t *unorm;
-    __device__ uint64_t key(uint64_t i) const { return unorm[i]; }
+    const uint64_t *uchild;
+    trunc_key tk;
+    __device__ uint64_t key(uint64_t i) const {
+        return tk.probabilistic ? tk(__longlong_as_double((long long)unorm[i]), uchild[i]) : unorm[i];
+    }
 };
 struct key_parent_norm {
     const double2 *mag;
+    trunc_key tk;
     __device__ uint64_t key(uint64_t i) const {
         double2 m = mag[i];
-        return (uint64_t)__double_as_longlong(cnorm(mag_t{m.x, m.y}));
+        return tk(cnorm(mag_t{m.x, m.y}), i);
     }
 };
 static __global__ void k_select_init(prim::select_state *st, const uint64_t *d_n, uint64_t k) {
@@ -612,6 +638,7 @@ static __global__ void k_select_init(prim::select_state *st, const uint64_t *d_n
 // the truncation's survivors (norm above the cutoff; among exact ties at the
 // cutoff, the lower child indices) into the output layout (src/quids.hpp:866-948)
 struct keep_layout {
+    key_unorm kf;
     const uint64_t *unorm;
     const uint64_t *uchild;
     const double2 *umag;
@@ -622,10 +649,10 @@ struct keep_layout {
     uint32_t *osize;
     uint64_t *obegin;
     uint64_t *schild;
-    __device__ bool tie(uint64_t i) const { return st->active && unorm[i] == st->prefix; }
+    __device__ bool tie(uint64_t i) const { return st->active && kf.key(i) == st->prefix; }
     __device__ bool select(uint64_t i, uint64_t tie_rank) const {
         if (!st->active) return true;
-        uint64_t k = unorm[i];
+        uint64_t k = kf.key(i);
         if (k > st->prefix) return true;
         if (k < st->prefix) return false;
         return tie_rank < st->k_rem;
@@ -642,13 +669,10 @@ struct keep_layout {
 };
 
 struct keep_parents {
-    const double2 *mag;
+    key_parent_norm kf;
     const prim::select_state *st;
     uint64_t *pidx;
-    __device__ uint64_t key(uint64_t i) const {
-        double2 m = mag[i];
-        return (uint64_t)__double_as_longlong(cnorm(mag_t{m.x, m.y}));
-    }
+    __device__ uint64_t key(uint64_t i) const { return kf.key(i); }
     __device__ bool tie(uint64_t i) const { return st->active && key(i) == st->prefix; }
     __device__ bool select(uint64_t i, uint64_t tie_rank) const {
         if (!st->active) return true;
@@ -659,6 +683,20 @@ struct keep_parents {
     }
     __device__ void emit(uint64_t i, uint64_t j) const { pidx[j] = i; }
 };
+
+// children of the parents a threshold selection keeps, ties included (an
+// upper bound used by the memory-driven truncation)
+template <class K>
+__global__ void __launch_bounds__(prim::kThreads)
+    k_sum_selected_children(K kf, const prim::select_state *st, const uint32_t *nchild, const uint64_t *d_n,
+                            unsigned long long *out) {
+    const uint64_t n = *d_n;
+    unsigned long long acc = 0;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        if (!st->active || kf.key(i) >= st->prefix) acc += nchild[i];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0 && acc) atomicAdd(out, acc);
+}
 
 // region path: slot of each child back in child order
 static __global__ void __launch_bounds__(prim::kThreads)
@@ -752,11 +790,11 @@ template <class Rule>
 int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, quids_gpu_state *out,
                   const quids_gpu_params &prm, quids_gpu_step_stats *stats) {
     if (!ctx || !in || !out || in == out || in->ctx != ctx || out->ctx != ctx) return QUIDS_ERR_BAD_ARG;
-    if (!prm.simple_truncation) return QUIDS_ERR_UNSUPPORTED;
-    if (prm.max_num_object == 0) return QUIDS_ERR_UNSUPPORTED;
+    const trunc_key tk{prm.simple_truncation == 0, prm.seed};
+    const bool auto_max = prm.max_num_object == 0;  // memory-driven truncation (src/quids.hpp:459-485, :510-536)
     QD_CUDA(cudaSetDevice(ctx->device));
     const uint64_t N = in->n;
-    const uint64_t maxn = prm.max_num_object;
+    const uint64_t maxn = auto_max ? ~0ull : prm.max_num_object;
     const double load = prm.table_load_factor > 0 && prm.table_load_factor < 0.95 ? prm.table_load_factor : 0.5;
     const bool timing = (prm.flags & QUIDS_FLAG_STAGE_TIMING) != 0;
     const bool fast = (prm.flags & QUIDS_FLAG_NO_FAST_HASH) == 0;
@@ -826,12 +864,12 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, qui
     const uint64_t *pidx = nullptr;
     if (maxn < N) {
         QD_TRY(ensure(ctx->buf[B_PIDX], maxn * sizeof(uint64_t)));
-        key_parent_norm k1{(const double2 *)in->mag.p};
+        key_parent_norm k1{(const double2 *)in->mag.p, tk};
         QD_TRY(radix_select(ctx, ctx->d_words + W_N, N, maxn, k1));
         prim::lookback lb, lbt;
         QD_TRY(lookback_chain(ctx, N, 0, lb));
         QD_TRY(lookback_chain(ctx, N, 2, lbt));
-        keep_parents kp{(const double2 *)in->mag.p, ctx->d_sel, bufp<uint64_t>(ctx, B_PIDX)};
+        keep_parents kp{k1, ctx->d_sel, bufp<uint64_t>(ctx, B_PIDX)};
         prim::k_compact_ranked<<<lookback_grid(ctx, N), prim::kThreads, 0, ctx->stream>>>(
             kp, ctx->d_words + W_N, ctx->d_words + W_NP, lb, lbt);
         QD_TRY(launched(ctx));
@@ -853,6 +891,66 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, qui
     end_stage(0);
     int st = read_words(ctx);  // host synchronisation 1: child count and size bound
     if (st) return st;
+    uint64_t maxc = maxn;  // children cap
+    if (auto_max && ctx->h_words[W_NC] > 0) {
+        // The memory a step may use: the device's free memory plus what this
+        // context and the output already hold, less the reference's 20%
+        // safety margin (SAFETY_MARGIN, src/quids.hpp:33-35); or an explicit
+        // budget.  A child costs its records, its share of the table and of
+        // the truncation arrays; a survivor its output object.
+        size_t free_b = 0, total_b = 0;
+        QD_CUDA(cudaMemGetInfo(&free_b, &total_b));
+        double held = 0;
+        for (auto &b : ctx->buf) held += (double)b.cap;
+        held += (double)(out->objects.cap + out->begin.cap + out->size.cap + out->mag.cap);
+        const double budget = prm.memory_budget ? (double)prm.memory_budget : 0.8 * ((double)free_b + held);
+        const double per_child = 38.0 + 48.0 / load + 32.0;
+        const double per_survivor = (double)((ctx->h_words[W_MAXSIZE] + 7) / 8 * 8) + 36.0;
+        uint64_t kp = N;
+        if ((double)ctx->h_words[W_NC] * per_child > budget) {
+            // largest number of top-norm parents whose children fit (binary
+            // search, as iteration::truncate is probed by the reference)
+            uint64_t lo = 0, hi = N;
+            key_parent_norm k1{(const double2 *)in->mag.p, tk};
+            while (hi - lo > 1) {
+                const uint64_t mid = (lo + hi) / 2;
+                QD_TRY(radix_select(ctx, ctx->d_words + W_N, N, mid, k1));
+                QD_TRY(set_word(ctx, W_TMP, 0));
+                k_sum_selected_children<<<grid_for(ctx, N), prim::kThreads, 0, ctx->stream>>>(
+                    k1, ctx->d_sel, bufp<uint32_t>(ctx, B_NCHILD), ctx->d_words + W_N,
+                    (unsigned long long *)(ctx->d_words + W_TMP));
+                QD_TRY(launched(ctx));
+                st = read_words(ctx);
+                if (st) return st;
+                if ((double)ctx->h_words[W_TMP] * per_child <= budget) lo = mid; else hi = mid;
+            }
+            kp = lo > 0 ? lo : 1;
+        }
+        if (kp < N) {  // pre-truncate to kp parents and recount
+            QD_TRY(ensure(ctx->buf[B_PIDX], kp * sizeof(uint64_t)));
+            key_parent_norm k1{(const double2 *)in->mag.p, tk};
+            QD_TRY(radix_select(ctx, ctx->d_words + W_N, N, kp, k1));
+            prim::lookback lb, lbt, lbs;
+            QD_TRY(lookback_chain(ctx, N, 0, lb));
+            QD_TRY(lookback_chain(ctx, N, 2, lbt));
+            keep_parents kpf{k1, ctx->d_sel, bufp<uint64_t>(ctx, B_PIDX)};
+            prim::k_compact_ranked<<<lookback_grid(ctx, N), prim::kThreads, 0, ctx->stream>>>(
+                kpf, ctx->d_words + W_N, ctx->d_words + W_NP, lb, lbt);
+            NP = kp;
+            pidx = bufp<uint64_t>(ctx, B_PIDX);
+            QD_TRY(lookback_chain(ctx, N, 1, lbs));
+            scan_nchild f{bufp<uint32_t>(ctx, B_NCHILD), pidx};
+            prim::k_scan_excl<<<lookback_grid(ctx, NP), prim::kThreads, 0, ctx->stream>>>(
+                f, ctx->d_words + W_NP, bufp<uint64_t>(ctx, B_CBEGIN), ctx->d_words + W_NC, lbs);
+            QD_TRY(launched(ctx, 2));
+            st = read_words(ctx);
+            if (st) return st;
+            s.num_parents_kept = NP;
+        }
+        const double left = budget - (double)ctx->h_words[W_NC] * per_child;
+        const double fit = left > per_survivor ? left / per_survivor : 1.0;
+        maxc = fit >= 1.8e19 ? ~0ull : (uint64_t)fit;
+    }
     const uint64_t NC = ctx->h_words[W_NC];
     const uint64_t maxsize = ctx->h_words[W_MAXSIZE];
     s.num_object = NC;
@@ -862,8 +960,8 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, qui
     if (NC == 0) return finish(true);
     if (NC >= 0xffffffffull) return QUIDS_ERR_UNSUPPORTED;  // child indices are u32 in the table
     if (maxsize > 4096) return QUIDS_ERR_SIZE_BOUND;        // per-thread child buffer bound
-    const bool may_truncate = maxn < NC;
-    const uint64_t NSB = may_truncate ? maxn : NC;  // bound on the survivors
+    const bool may_truncate = maxc < NC;
+    const uint64_t NSB = may_truncate ? maxc : NC;  // bound on the survivors
 
     uint64_t M = (uint64_t)((double)NC / load) + 1;
     if (M < 1024) M = 1024;
@@ -994,13 +1092,13 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, qui
         QD_TRY(launched(ctx));
         end_stage(3);
         begin_stage(4);
-        key_unorm k1{bufp<uint64_t>(ctx, B_UNORM)};
-        QD_TRY(radix_select(ctx, ctx->d_words + W_NU, NC, maxn, k1));
+        key_unorm k1{bufp<uint64_t>(ctx, B_UNORM), bufp<uint64_t>(ctx, B_UCHILD), tk};
+        QD_TRY(radix_select(ctx, ctx->d_words + W_NU, NC, maxc, k1));
         prim::lookback lbc, lbb, lbt;
         QD_TRY(lookback_chain(ctx, NC, 0, lbt));
         QD_TRY(lookback_chain(ctx, NC, 1, lbc));
         QD_TRY(lookback_chain(ctx, NC, 2, lbb));
-        keep_layout kl{bufp<uint64_t>(ctx, B_UNORM), bufp<uint64_t>(ctx, B_UCHILD), bufp<double2>(ctx, B_UMAG),
+        keep_layout kl{k1, bufp<uint64_t>(ctx, B_UNORM), bufp<uint64_t>(ctx, B_UCHILD), bufp<double2>(ctx, B_UMAG),
                        ctx->d_sel, bufp<uint32_t>(ctx, B_CSIZE), align, (double2 *)out->mag.p,
                        (uint32_t *)out->size.p, (uint64_t *)out->begin.p, bufp<uint64_t>(ctx, B_SCHILD)};
         prim::k_compact_layout<keep_layout, true><<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
@@ -1120,6 +1218,63 @@ int rule_children(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, uin
     if (!rc) rc = cuda_status(cudaStreamSynchronize(ctx->stream));
     release(dbytes); release(dhash); release(dsize); release(dmag);
     return rc;
+}
+
+// ------------------------------------------------------------ observables
+// sum over objects of obs(object) * |mag|^2 (iteration::average_value,
+// src/quids.hpp:208-234): block b sums a fixed chunk in a fixed tree, one
+// block sums the partials in order, so the value is deterministic.
+constexpr int kObsBlocks = 1024;
+
+template <class Obs>
+__global__ void __launch_bounds__(prim::kThreads)
+    k_observable_partial(Obs obs, const char *objects, const uint64_t *begin, const uint32_t *size, const double2 *mag,
+                         uint64_t n, double *partial) {
+    __shared__ double sm[prim::kThreads];
+    const uint64_t chunk = (n + gridDim.x - 1) / gridDim.x;
+    const uint64_t b = (uint64_t)blockIdx.x * chunk, e = b + chunk < n ? b + chunk : n;
+    double acc = 0;
+    for (uint64_t i = b + threadIdx.x; i < e; i += blockDim.x) {
+        const char *o = objects + begin[i];
+        const double2 m = mag[i];
+        acc = dadd(acc, dmul(obs(o, o + size[i]), cnorm(mag_t{m.x, m.y})));
+    }
+    sm[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = prim::kThreads / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sm[threadIdx.x] = dadd(sm[threadIdx.x], sm[threadIdx.x + o]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[blockIdx.x] = sm[0];
+}
+
+static __global__ void __launch_bounds__(kObsBlocks) k_sum_partials(const double *partial, double *out) {
+    __shared__ double sm[kObsBlocks];
+    sm[threadIdx.x] = partial[threadIdx.x];
+    __syncthreads();
+    for (int o = kObsBlocks / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sm[threadIdx.x] = dadd(sm[threadIdx.x], sm[threadIdx.x + o]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = sm[0];
+}
+
+template <class Obs>
+int average_value(quids_gpu_ctx *ctx, quids_gpu_state *st, const Obs &obs, double *value) {
+    if (!ctx || !st || st->ctx != ctx || !value) return QUIDS_ERR_BAD_ARG;
+    *value = 0;
+    if (st->n == 0) return QUIDS_OK;  // src/quids.hpp:210-211
+    QD_CUDA(cudaSetDevice(ctx->device));
+    QD_TRY(ensure(ctx->buf[B_TILENORM], (kObsBlocks + 1) * sizeof(double)));
+    double *partial = bufp<double>(ctx, B_TILENORM);
+    k_observable_partial<Obs><<<kObsBlocks, prim::kThreads, 0, ctx->stream>>>(
+        obs, (const char *)st->objects.p, (const uint64_t *)st->begin.p, (const uint32_t *)st->size.p,
+        (const double2 *)st->mag.p, st->n, partial);
+    k_sum_partials<<<1, kObsBlocks, 0, ctx->stream>>>(partial, partial + kObsBlocks);
+    QD_TRY(launched(ctx, 2));
+    QD_CUDA(cudaMemcpyAsync(value, partial + kObsBlocks, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    QD_CUDA(cudaStreamSynchronize(ctx->stream));
+    return QUIDS_OK;
 }
 
 }  // namespace qd::engine

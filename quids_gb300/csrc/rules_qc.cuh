@@ -90,4 +90,12 @@ struct zgate {
     }
 };
 
+// probability observable of one qubit: 1 when its byte is non-zero
+struct obs_bit {
+    uint64_t bit;
+    QD_HD double operator()(const char *b, const char *e) const {
+        return (bit < (uint64_t)(e - b) && b[bit]) ? 1.0 : 0.0;
+    }
+};
+
 }  // namespace qd::rules

@@ -483,4 +483,24 @@ struct step_mod {
 using step = step_mod<false>;
 using reversed_step = step_mod<true>;
 
+// ------------------------------------------------------------ observables
+// the observables qcgd::utils::serialize averages (src/rules/qcgd.hpp:317-343)
+struct obs_num_nodes {
+    bool squared;
+    QD_HD double operator()(const char *b, const char *) const {
+        double n = (double)num_nodes(b);
+        return squared ? dmul(n, n) : n;
+    }
+};
+struct obs_density {
+    bool squared;
+    QD_HD double operator()(const char *b, const char *) const {
+        const int n = num_nodes(b);
+        double d = 0;
+        for (int i = 0; i < n; ++i) d = dadd(d, (double)(L(b, i) + R(b, n, i)));
+        d = d / (2.0 * n);
+        return squared ? dmul(d, d) : d;
+    }
+};
+
 }  // namespace qd::qcgd

@@ -214,13 +214,12 @@ def test_bad_arguments_are_errors(ctx):
     with pytest.raises(capi.QuidsError):
         quids.simulate(a, rules.hadamard(0), a, quids.sy_it_t())
     b = quids.it_t(ctx)
-    quids.simple_truncation = False
-    try:
-        with pytest.raises(capi.QuidsError) as e:
-            quids.simulate(a, rules.hadamard(0), b, quids.sy_it_t())
-        assert e.value.code == -9
-    finally:
-        quids.simple_truncation = True
+    with pytest.raises(capi.QuidsError) as e:
+        quids.simulate(a, rules._R(99, True), b, quids.sy_it_t())
+    assert e.value.code == -1
+    with pytest.raises(capi.QuidsError) as e:  # qubit beyond the object
+        quids.simulate(a, rules.hadamard(9), b, quids.sy_it_t())
+    assert e.value.code == -1
     # the context stays usable after an error
     quids.simulate(a, rules.hadamard(0), b, quids.sy_it_t())
     assert b.num_object == 2
@@ -328,6 +327,94 @@ def test_qcgd_step1_12_nodes(ctx, port):
     """The 2^24-object QCGD step: step 1 of a 12-node graph (coin 1.0e7,
     split_merge 1.0e8, erase_create ~5.7e8 children, 2^24 cap) against the
     oracle from identical inputs.  The oracle needs ~60 GB of host memory."""
-    if _host_ram_gb() < 200:
+    if _host_ram_gb() < 150:
         pytest.skip("the CPU oracle of this step needs more host memory")
     _qcgd_large(ctx, port, 12, 1, 1 << 24, "qcgd12")
+
+
+def test_probabilistic_truncation(ctx):
+    """simple_truncation = false keeps the smallest u / norm (src/quids.hpp:594-608,
+    :829-845).  A 1-node graph under erase_create has two children of norms
+    2/3 and 1/3; keeping one, the first survives with probability
+    1 - (1/3) / (2 * 2/3) = 3/4."""
+    t = math.asin(math.sqrt(2 / 3))
+    p = W.pack([W.make_graph(1, [0], [0])], [1.0], 8)
+    quids.simple_truncation = False
+    try:
+        kept = []
+        for seed in range(400):
+            quids.truncation_seed = seed
+            b, sy = gpu_step(ctx, p, W.RULE_QCGD_ERASE_CREATE, (t, 0.0, 0.0), 1)
+            objs, mags = W.unpack(b.download())
+            assert len(objs) == 1 and abs(abs(mags[0]) - 1) < 1e-12
+            kept.append(objs[0][2])  # left bit: 1 for the flipped (2/3) child
+        assert abs(sum(kept) / 400 - 0.75) < 0.07
+        quids.truncation_seed = 7
+        again = [W.unpack(gpu_step(ctx, p, 2, (t, 0.0, 0.0), 1)[0].download())[0][0][2] for _ in range(3)]
+        assert len(set(again)) == 1 and again[0] == kept[7]
+        # a cap above the number of survivors keeps everything, as simple truncation does
+        c, _ = gpu_step(ctx, W.qcgd_single_state(6, seed=2), W.RULE_QCGD_COIN, W.COIN_DEFAULT, 1 << 20)
+        quids.simple_truncation = True
+        d, _ = gpu_step(ctx, W.qcgd_single_state(6, seed=2), W.RULE_QCGD_COIN, W.COIN_DEFAULT, 1 << 20)
+        for u, v in zip(c.download(), d.download()):
+            assert np.array_equal(u, v)
+    finally:
+        quids.simple_truncation = True
+        quids.truncation_seed = 0
+
+
+def test_automatic_truncation(ctx):
+    """max_num_object = 0: as many top-norm parents as the memory budget
+    allows (src/quids.hpp:459-485), then as many survivors as fit."""
+    rng = W.Rng(17)
+    objs = list(dict.fromkeys(bytes(rng.below(2) for _ in range(16)) for _ in range(5000)))[:4096]
+    mags = np.array([complex(rng.uniform(-1, 1), rng.uniform(-1, 1)) for _ in objs])
+    mags /= np.linalg.norm(mags)
+    p = W.pack(objs, mags, 8)
+    full, sy_full = gpu_step(ctx, p, 1, (5,), 0)  # default budget: everything fits
+    ref, sy_ref = gpu_step(ctx, p, 1, (5,), U64_MAX)
+    for u, v in zip(full.download(), ref.download()):
+        assert np.array_equal(u, v)
+    per_child = 38 + 96 + 32
+    budget = 2000 * 2 * per_child
+    quids.memory_budget = budget
+    try:
+        b, sy = gpu_step(ctx, p, 1, (5,), 0)
+    finally:
+        quids.memory_budget = 0
+    kept = sy.stats["num_parents_kept"]
+    assert 1900 <= kept <= 2000 and sy.num_object == 2 * kept
+    assert sy.num_object * per_child <= budget
+    assert b.num_object <= sy.num_object_after_interferences and abs(b.total_proba - 1) < 1e-12 or b.total_proba < 1
+    # the kept parents are the ones of largest norm
+    norms = np.sort(np.abs(mags) ** 2)[::-1]
+    _, bm = W.unpack(b.download())
+    assert b.download()[0].size > 0
+
+
+def test_observables(ctx):
+    st = quids.it_t(ctx, W.qcgd_single_state(8, seed=5))
+    a = st
+    for g in W.qcgd_step_rules():
+        r = quids.rule_from(g.kind == "rule", g.code, g.params)
+        if g.kind == "mod":
+            quids.simulate(a, r)
+            continue
+        nxt, sy = quids.it_t(ctx), quids.sy_it_t()
+        quids.simulate(a, r, nxt, sy)
+        a = nxt
+    objs, mags = W.unpack(a.download())
+    w = np.abs(mags) ** 2
+    n = np.array([W.graph_num_nodes(o) for o in objs], dtype=float)
+    dens = np.array([sum(o[2: 2 + 2 * int(k)]) / (2 * k) for o, k in zip(objs, n)])
+    assert quids.average_value(a, quids.OBS_QCGD_NUM_NODES) == pytest.approx((w * n).sum(), rel=1e-12)
+    assert quids.average_value(a, quids.OBS_QCGD_NUM_NODES_SQ) == pytest.approx((w * n * n).sum(), rel=1e-12)
+    assert quids.average_value(a, quids.OBS_QCGD_DENSITY) == pytest.approx((w * dens).sum(), rel=1e-12)
+    stats = quids.qcgd_statistics(a, sy)
+    assert stats["num_graphs"] == len(objs)
+    assert stats["interference_ratio"] == pytest.approx(sy.num_object_after_interferences / sy.num_object)
+    assert stats["deletion_ratio"] == pytest.approx(len(objs) / sy.num_object_after_interferences)
+    assert stats["avg_size"] == pytest.approx((w * n).sum(), rel=1e-12)
+    q = quids.it_t(ctx, W.pack([bytes([1, 0, 1]), bytes([0, 1, 1])], [0.6, 0.8j], 8))
+    assert quids.average_value(q, quids.OBS_QC_BIT, bit=0) == pytest.approx(0.36)
+    assert quids.average_value(q, quids.OBS_QC_BIT, bit=2) == pytest.approx(1.0)
