@@ -187,6 +187,42 @@ int quids_gpu_run(quids_gpu_ctx *ctx, quids_gpu_state *a, quids_gpu_state *b, co
                   uint64_t n_ops, const quids_gpu_params *params, quids_gpu_step_stats *rule_stats,
                   int *final_index);
 
+/* ------------------------------------------------------------ batched form
+ * No counterpart in the reference, which steps one state per call: the
+ * loop `for each instance: quids::simulate(...)` over many independent
+ * states (different graphs, different angles), in one pipeline per step.
+ * A batched state holds n_inst instances, each a contiguous run of objects
+ * [inst_begin[g], inst_begin[g+1]).  quids_gpu_simulate_batched applies, to
+ * every instance g, quids::simulate with rule parameters rules[g] and the
+ * same params (max_num_object caps every instance; 0, the memory-driven cap,
+ * is QUIDS_ERR_UNSUPPORTED here), and normalises each instance by its own
+ * total probability (its value before normalisation is returned by
+ * quids_gpu_state_instances).  Each instance's survivors and magnitudes are
+ * those of quids_gpu_simulate on that instance alone (magnitudes within the
+ * 1e-12 relative tolerance of the normalisation sums); the probabilistic
+ * truncation draws differ.  Modifiers (quids_gpu_apply_modifier) act on
+ * every object and keep the instances.  A plain step of a batched state
+ * gives a plain state. */
+#define QUIDS_MAX_INSTANCES 65536u
+int quids_gpu_state_upload_batched(quids_gpu_state *st, uint64_t num_object, const uint8_t *objects,
+                                   const uint64_t *begin, const uint32_t *size, const double *magnitude,
+                                   uint64_t num_bytes, uint32_t n_inst, const uint64_t *inst_begin);
+/* *n_inst = 0 for a plain state.  inst_begin (n_inst + 1 entries) and
+ * inst_total (n_inst) may be NULL. */
+int quids_gpu_state_instances(quids_gpu_state *st, uint32_t *n_inst, uint64_t *inst_begin, double *inst_total);
+/* rules: n_inst entries.  inst_stats: NULL or 3 * n_inst entries, per instance
+ * {symbolic num_object, num_object_after_interferences, survivors}. */
+int quids_gpu_simulate_batched(quids_gpu_ctx *ctx, quids_gpu_state *iteration, int rule_kind,
+                               const quids_gpu_rule_params *rules, quids_gpu_state *next_iteration,
+                               const quids_gpu_params *params, uint64_t *inst_stats,
+                               quids_gpu_step_stats *stats);
+/* quids_gpu_run over a batched state: rule op r takes its per-instance
+ * parameters from inst_params + r * n_inst (or op.params for every instance
+ * when inst_params is NULL); modifiers take op.params. */
+int quids_gpu_run_batched(quids_gpu_ctx *ctx, quids_gpu_state *a, quids_gpu_state *b, const quids_gpu_op *ops,
+                          uint64_t n_ops, const quids_gpu_rule_params *inst_params, const quids_gpu_params *params,
+                          quids_gpu_step_stats *rule_stats, int *final_index);
+
 /* ------------------------------------------------------ rule-level access
  * Materialises every child of every parent of `iteration` (the symbolic
  * iteration of src/quids.hpp:647-721 with the child bytes kept): children

@@ -251,6 +251,72 @@ class it_t:
         b = int(begin[oid])
         return objects[b: b + int(size[oid])].tobytes(), complex(mag[oid])
 
+    # ---- batched states (no counterpart in the reference)
+    def upload_batched(self, states):
+        """Uploads independent states (a list of packed tuples) as the
+        instances of one batched state; each instance's bytes are padded to a
+        multiple of 8 so every object keeps its alignment."""
+        objs, begins, sizes, mags, inst_begin = [], [], [], [], [0]
+        off = 0
+        for objects, begin, size, mag in states:
+            objects = np.asarray(objects, dtype=np.uint8)
+            n = len(size)
+            nb = int(objects.shape[0])
+            pad = (-nb) % 8
+            objs.append(objects)
+            if pad:
+                objs.append(np.zeros(pad, np.uint8))
+            begins.append(np.asarray(begin[:n], dtype=np.uint64) + np.uint64(off))
+            sizes.append(np.asarray(size, dtype=np.uint32))
+            mags.append(np.asarray(mag, dtype=np.complex128))
+            off += nb + pad
+            inst_begin.append(inst_begin[-1] + n)
+        n = inst_begin[-1]
+        objects = np.ascontiguousarray(np.concatenate(objs) if objs else np.zeros(0, np.uint8))
+        begin = np.ascontiguousarray(np.concatenate(begins + [np.array([off], np.uint64)]))
+        size = np.ascontiguousarray(np.concatenate(sizes) if sizes else np.zeros(0, np.uint32))
+        mag = np.ascontiguousarray(np.concatenate(mags) if mags else np.zeros(0, np.complex128))
+        ib = np.ascontiguousarray(np.asarray(inst_begin, dtype=np.uint64))
+        capi.check(self.lib.quids_gpu_state_upload_batched(
+            self.h, n, objects.ctypes.data if off else None, begin.ctypes.data, size.ctypes.data,
+            mag.ctypes.data, off, len(states), ib.ctypes.data), "state_upload_batched")
+        self._pending = []
+
+    @property
+    def num_instances(self) -> int:
+        g = C.c_uint32()
+        capi.check(self.lib.quids_gpu_state_instances(self.h, C.byref(g), None, None), "state_instances")
+        return int(g.value)
+
+    def instances(self):
+        """(inst_begin u64[n_inst + 1], inst_total f64[n_inst]): instance
+        offsets, and each instance's total probability before the last
+        step normalised it."""
+        g = self.num_instances
+        ib = np.zeros(g + 1, np.uint64)
+        tot = np.zeros(max(g, 1), np.float64)
+        n = C.c_uint32()
+        capi.check(self.lib.quids_gpu_state_instances(self.h, C.byref(n), ib.ctypes.data, tot.ctypes.data),
+                   "state_instances")
+        return ib, tot[:g]
+
+    def download_instances(self):
+        """The instances as a list of packed tuples (begin rebased per instance)."""
+        objects, begin, size, mag = self.download()
+        ib, _ = self.instances()
+        out = []
+        for g in range(len(ib) - 1):
+            a, b = int(ib[g]), int(ib[g + 1])
+            if a == b:
+                out.append((np.zeros(0, np.uint8), np.zeros(1, np.uint64), np.zeros(0, np.uint32),
+                            np.zeros(0, np.complex128)))
+                continue
+            lo = int(begin[a])
+            hi = int(begin[b]) if b < len(size) else int(begin[len(size)])
+            out.append((objects[lo:hi].copy(), (begin[a:b + 1] - np.uint64(lo)).astype(np.uint64),
+                        size[a:b].copy(), mag[a:b].copy()))
+        return out
+
     def average_value(self, observable) -> float:
         """iteration::average_value (src/quids.hpp:208-234), evaluated on the host."""
         objects, begin, size, mag = self.download()
@@ -313,6 +379,63 @@ def run(a: it_t, b: it_t, ops, max_num_object: int = U64_MAX, flags: int = 0):
     b._pending = []
     rc = a.lib.quids_gpu_run(a.ctx.h, a.h, b.h, arr, len(ops), C.byref(prm), stats, C.byref(fin))
     capi.check(rc, "run")
+    return (a if fin.value == 0 else b), [stats[i].as_dict() for i in range(n_rules)]
+
+
+def simulate_batched(iteration: it_t, rules_per_instance, next_iteration: it_t, max_num_object: int = U64_MAX,
+                     flags: int = 0):
+    """One rule step of every instance of a batched state: instance g steps
+    with rules_per_instance[g] (all of one kind).  Returns (step stats,
+    per-instance u64[n_inst, 3] {num_object, num_object_after_interferences,
+    survivors})."""
+    iteration._flush()
+    g = iteration.num_instances
+    if len(rules_per_instance) != g:
+        raise QuidsError(-1, f"simulate_batched: {len(rules_per_instance)} rules for {g} instances")
+    kinds = {r.kind for r in rules_per_instance}
+    if len(kinds) != 1 or not rules_per_instance[0].is_rule:
+        raise QuidsError(-1, "simulate_batched: one rule kind for every instance")
+    arr = (capi.RuleParams * g)(*[r.params() for r in rules_per_instance])
+    inst = np.zeros((g, 3), np.uint64)
+    stats = capi.StepStats()
+    prm = _params(max_num_object, flags)
+    next_iteration._pending = []
+    capi.check(iteration.lib.quids_gpu_simulate_batched(iteration.ctx.h, iteration.h, kinds.pop(), arr,
+                                                        next_iteration.h, C.byref(prm), inst.ctypes.data,
+                                                        C.byref(stats)), "simulate_batched")
+    return stats.as_dict(), inst
+
+
+def run_batched(a: it_t, b: it_t, ops, max_num_object: int = U64_MAX, flags: int = 0):
+    """run() over a batched state.  A rule op is one rule (every instance) or
+    a list of rules of one kind, one per instance; modifiers act on every
+    object.  Returns (final it_t, per-rule stats)."""
+    a._flush()
+    g = a.num_instances
+    arr = (capi.Op * max(len(ops), 1))()
+    per = []
+    n_rules = 0
+    for i, r in enumerate(ops):
+        if isinstance(r, (list, tuple)):
+            if len(r) != g or len({x.kind for x in r}) != 1:
+                raise QuidsError(-1, "run_batched: a per-instance op needs one rule of one kind per instance")
+            head = r[0]
+            per.extend(x.params() for x in r)
+        else:
+            head = r
+            if r.is_rule:
+                per.extend(r.params() for _ in range(g))
+        arr[i].is_rule = int(head.is_rule)
+        arr[i].kind = head.kind
+        arr[i].params = head.params()
+        n_rules += int(head.is_rule)
+    inst = (capi.RuleParams * max(len(per), 1))(*per)
+    stats = (capi.StepStats * max(n_rules, 1))()
+    fin = C.c_int(0)
+    prm = _params(max_num_object, flags)
+    b._pending = []
+    capi.check(a.lib.quids_gpu_run_batched(a.ctx.h, a.h, b.h, arr, len(ops), inst, C.byref(prm), stats,
+                                           C.byref(fin)), "run_batched")
     return (a if fin.value == 0 else b), [stats[i].as_dict() for i in range(n_rules)]
 
 

@@ -75,7 +75,8 @@ EXPORTS = [
     "quids_gpu_state_num_bytes", "quids_gpu_state_total_proba", "quids_gpu_state_download",
     "quids_gpu_state_device_arrays", "quids_gpu_simulate", "quids_gpu_apply_modifier",
     "quids_gpu_rule_children", "quids_gpu_state_hash", "quids_gpu_rule_children_noalloc", "quids_gpu_run",
-    "quids_gpu_average_value", "quids_gpu_qcgd_statistics",
+    "quids_gpu_average_value", "quids_gpu_qcgd_statistics", "quids_gpu_state_upload_batched",
+    "quids_gpu_state_instances", "quids_gpu_simulate_batched", "quids_gpu_run_batched",
 ]
 
 _lib = None
@@ -129,6 +130,12 @@ def load(build_if_missing: bool = True):
     L.quids_gpu_qcgd_statistics.argtypes = [vp, vp, C.c_uint64, C.c_uint64, C.c_double, C.POINTER(QcgdStats)]
     L.quids_gpu_rule_children_noalloc.argtypes = [vp, C.c_uint64, vp, vp, vp, vp, C.c_int, C.POINTER(RuleParams),
                                                   C.c_uint64, u64p, u64p, vp, vp, vp, vp]
+    L.quids_gpu_state_upload_batched.argtypes = [vp, C.c_uint64, vp, vp, vp, vp, C.c_uint64, C.c_uint32, vp]
+    L.quids_gpu_state_instances.argtypes = [vp, C.POINTER(C.c_uint32), vp, vp]
+    L.quids_gpu_simulate_batched.argtypes = [vp, vp, C.c_int, C.POINTER(RuleParams), vp, C.POINTER(Params), vp,
+                                             C.POINTER(StepStats)]
+    L.quids_gpu_run_batched.argtypes = [vp, vp, vp, C.POINTER(Op), C.c_uint64, C.POINTER(RuleParams),
+                                        C.POINTER(Params), C.POINTER(StepStats), C.POINTER(C.c_int)]
     _lib = L
     return L
 

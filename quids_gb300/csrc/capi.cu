@@ -1,8 +1,7 @@
 // capi.cu -- the extern "C" entry points of include/quids_gpu.h.
 //
 // Built-in rules are instantiated here; the rule and modifier objects are
-// formed on the host from quids_gpu_rule_params exactly as the reference's
-// constructors form them (src/rules/quantum_computer.hpp, src/rules/qcgd.hpp).
+// formed on the host from quids_gpu_rule_params (factories.cuh).
 #include <cmath>
 #include <complex>
 #include <cstring>
@@ -12,44 +11,13 @@
 #include "engine.cuh"
 #include "rules_qc.cuh"
 #include "rules_qcgd.cuh"
+#include "factories.cuh"
 
 using namespace qd;
 using namespace qd::engine;
+using qd::host::dispatch_rule;
 
 namespace {
-
-qcgd::factors make_factors(const quids_gpu_rule_params *p) {
-    // src/rules/qcgd.hpp:466-471
-    std::complex<double> d = std::polar(std::sin(p->theta), p->phi);
-    std::complex<double> dn = std::polar(std::cos(p->theta), p->xi);
-    std::complex<double> dc = std::conj(d), dnc = std::conj(dn);
-    std::complex<double> ndnc = -dnc;
-    qcgd::factors f;
-    f.d = {d.real(), d.imag()};
-    f.dc = {dc.real(), dc.imag()};
-    f.dn = {dn.real(), dn.imag()};
-    f.ndnc = {ndnc.real(), ndnc.imag()};
-    return f;
-}
-
-rules::hadamard make_hadamard(const quids_gpu_rule_params *p) {
-    rules::hadamard h;
-    h.bit = p->bit;
-    h.inv_sqrt2 = 1 / std::sqrt(2);  // quantum_computer.hpp:41
-    return h;
-}
-
-template <class F>
-int dispatch_rule(int kind, const quids_gpu_rule_params *p, F &&f) {
-    if (!p) return QUIDS_ERR_BAD_ARG;
-    switch (kind) {
-    case QUIDS_RULE_HADAMARD: return f(make_hadamard(p));
-    case QUIDS_RULE_QCGD_ERASE_CREATE: return f(qcgd::erase_create{make_factors(p)});
-    case QUIDS_RULE_QCGD_COIN: return f(qcgd::coin{make_factors(p)});
-    case QUIDS_RULE_QCGD_SPLIT_MERGE: return f(qcgd::split_merge{make_factors(p)});
-    }
-    return QUIDS_ERR_BAD_ARG;
-}
 
 __global__ void k_set_words_zero(uint64_t *w, int n) {
     for (int i = threadIdx.x; i < n; i += blockDim.x) w[i] = 0;
@@ -118,13 +86,7 @@ int quids_gpu_ctx_destroy(quids_gpu_ctx *ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     for (quids_gpu_state *st : ctx->states) {
-        release(st->objects);
-        release(st->begin);
-        release(st->size);
-        release(st->mag);
-        release(st->d_total);
-        st->n = st->nbytes = 0;
-        st->total_pending = false;
+        release_state(st);
         st->ctx = nullptr;
     }
     ctx->states.clear();
@@ -187,11 +149,7 @@ int quids_gpu_state_destroy(quids_gpu_state *st) {
     cudaSetDevice(st->ctx->device);
     cudaStreamSynchronize(st->ctx->stream);
     st->ctx->states.erase(st);
-    release(st->objects);
-    release(st->begin);
-    release(st->size);
-    release(st->mag);
-    release(st->d_total);
+    release_state(st);
     delete st;
     return QUIDS_OK;
 }
@@ -220,6 +178,8 @@ int quids_gpu_state_upload(quids_gpu_state *st, uint64_t n, const uint8_t *objec
     st->nbytes = num_bytes;
     st->total_proba = 1;
     st->total_pending = false;
+    st->n_inst = 0;
+    st->h_inst_begin.clear();
     return QUIDS_OK;
 }
 

@@ -41,7 +41,7 @@ enum qd_buf_id {
     B_UNORM,       // u64 [NU] IEEE bits of the group norm
     B_SCHILD,      // u64 [NS] representative child of each survivor
     B_LOOKBACK,    // u64 [3 (tiles + 2)] look-back chains
-    B_TILENORM,    // double [tiles] per-tile norm sums of the survivors
+    B_TILENORM,    // double [blocks] per-block partial sums of an observable
     B_RHASH,       // u64 [NC] child hashes in table-region order
     B_RIDX,        // u32 [NC] child indices in table-region order
     B_RMAG,        // double2 [NC] child magnitudes in table-region order
@@ -54,6 +54,16 @@ enum qd_buf_id {
     B_TILEPAR,     // u64 [tiles+1] first parent of each tile of children
     B_CPAR,        // u32 [NC] kept-parent index of each child
     B_MODSTATUS,   // int: sticky error of modifier launches (reported by the next step)
+    // batched steps
+    B_RULES,       // Rule [G] per-instance rules
+    B_BCOUNT,      // u64 [4G] per-instance tie counts and fixed-point totals
+    B_BSEL,        // select_state [G]
+    B_BHIST,       // u32 [256 G] per-instance radix histograms
+    B_BOFF,        // u64 [G+1] per-instance tie offsets
+    B_UINST,       // u32 [NU] instance of each group kept after zero elimination
+    B_UBEGIN,      // u64 [G+1] instance offsets over the groups
+    B_PBEGIN,      // u64 [G+1] instance offsets over the kept parents
+    B_BFACTOR,     // double [G] per-instance sqrt(total)
     B_COUNT
 };
 
@@ -71,6 +81,8 @@ enum qd_word {
     W_TOTAL,      // total probability (double)
     W_FACTOR,     // sqrt(total) (double)
     W_TMP,
+    W_MAXNORM,    // bit pattern of the largest survivor norm
+    W_ACC,        // 2 words: fixed-point total probability
     W_COUNT_WORDS = 16
 };
 
@@ -100,6 +112,14 @@ struct quids_gpu_state {
     mutable double total_proba = 1;
     mutable bool total_pending = false;
     qd_dbuf objects, begin, size, mag, d_total;
+    // batched state: n_inst independent instances, each a contiguous run of
+    // objects (inst: instance of each object; inst_begin: u64 [n_inst+1]
+    // offsets, mirrored in h_inst_begin; inst_total: double [n_inst] total
+    // probability of each instance before its normalisation).  n_inst = 0:
+    // a plain state.
+    uint32_t n_inst = 0;
+    qd_dbuf inst, inst_begin, inst_total;
+    std::vector<uint64_t> h_inst_begin;
 };
 
 namespace qd::engine {
@@ -145,6 +165,15 @@ inline void release(qd_dbuf &b) {
     if (b.p) cudaFree(b.p);
     b.p = nullptr;
     b.cap = 0;
+}
+inline void release_state(quids_gpu_state *st) {
+    for (qd_dbuf *b : {&st->objects, &st->begin, &st->size, &st->mag, &st->d_total, &st->inst, &st->inst_begin,
+                       &st->inst_total})
+        release(*b);
+    st->n = st->nbytes = 0;
+    st->n_inst = 0;
+    st->h_inst_begin.clear();
+    st->total_pending = false;
 }
 
 template <class T>
@@ -245,13 +274,36 @@ QD_HD void rule_populate_simple(const R &r, const char *pb, const char *pe, char
     }
 }
 
-// ------------------------------------------------------- per-rule kernels
+// ------------------------------------------------------- rule sources
+// The rule of a parent: one rule for every parent, or (batched states) one
+// rule per instance, looked up by the parent's instance.  Child hashes are
+// tagged with the instance so that groups never span instances.
 template <class Rule>
+struct single_rule {
+    using rule_type = Rule;
+    Rule r;
+    __device__ __forceinline__ const Rule &get(uint64_t) const { return r; }
+    __device__ __forceinline__ uint64_t tag(uint64_t h, uint64_t) const { return h; }
+};
+template <class Rule>
+struct instance_rules {
+    using rule_type = Rule;
+    const Rule *rules;    // [instances]
+    const uint32_t *inst; // instance of each parent
+    __device__ __forceinline__ Rule get(uint64_t parent) const { return rules[inst[parent]]; }
+    __device__ __forceinline__ uint64_t tag(uint64_t h, uint64_t parent) const {
+        return h ^ (0x9E3779B97F4A7C15ull * ((uint64_t)inst[parent] + 1));
+    }
+};
+
+// ------------------------------------------------------- per-rule kernels
+template <class RS>
 __global__ void __launch_bounds__(prim::kThreads)
-    k_num_child(Rule rule, const char *objects, const uint64_t *begin, const uint32_t *size, uint64_t n,
+    k_num_child(RS rs, const char *objects, const uint64_t *begin, const uint32_t *size, uint64_t n,
                 uint32_t *nchild, unsigned long long *d_maxsize, int *err) {
     uint32_t mx = 0;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const auto &rule = rs.get(i);
         const char *pb = objects + begin[i];
         if (!object_fits(rule, size[i])) {
             nchild[i] = 0;
@@ -319,9 +371,9 @@ static __global__ void __launch_bounds__(prim::kThreads)
 // size, hash and parent.  FAST: the rule's hash_child; otherwise
 // populate_child into a per-thread buffer of MAXC bytes followed by the
 // rule's hasher.
-template <class Rule, int MAXC, bool FAST>
+template <class RS, int MAXC, bool FAST>
 __global__ void __launch_bounds__(prim::kThreads)
-    k_symbolic(Rule rule, parents_view pv, const uint64_t *tile_first, const uint64_t *d_nc, uint64_t *hash,
+    k_symbolic(RS rs, parents_view pv, const uint64_t *tile_first, const uint64_t *d_nc, uint64_t *hash,
                double2 *cmag, uint32_t *csize, uint32_t *cpar, unsigned long long *d_maxabs, int *err,
                region_count rc) {
     __shared__ uint64_t s_cb[kStagedParents + 1];
@@ -361,6 +413,7 @@ __global__ void __launch_bounds__(prim::kThreads)
             mag_t m{pm.x, pm.y};
             uint32_t sz = 0;
             uint64_t h;
+            const auto &rule = rs.get(oid);
             if constexpr (FAST) {
                 h = rule.hash_child(pb, pe, cid, sz, m);
             } else {
@@ -372,6 +425,7 @@ __global__ void __launch_bounds__(prim::kThreads)
                 }
                 h = rule_hash(rule, (const char *)buf, (const char *)buf + sz);
             }
+            h = rs.tag(h, oid);
             hash[c] = h;
             cmag[c] = make_double2(m.re, m.im);
             csize[c] = sz;
@@ -395,13 +449,13 @@ __global__ void __launch_bounds__(prim::kThreads)
 // Finalize (src/quids.hpp:958-967) fused with normalisation (:1008-1013):
 // populate_child_simple of each survivor into the packed output (padding
 // zeroed) and mag /= sqrt(total) when that factor is not 1.
-template <class Rule, int MAXC>
+template <class RS, int MAXC>
 __global__ void __launch_bounds__(prim::kThreads)
-    k_populate(Rule rule, parents_view pv, const uint64_t *schild, const uint32_t *cpar, const uint64_t *d_ns,
+    k_populate(RS rs, parents_view pv, const uint64_t *schild, const uint32_t *cpar, const uint64_t *d_ns,
                const uint64_t *obegin, const uint32_t *osize, char *objects, double2 *omag, const double *d_factor,
-               int *err) {
+               const uint32_t *finst, int *err) {
     const uint64_t ns = *d_ns;
-    const double f = *d_factor;
+    const double f0 = finst ? 1.0 : *d_factor;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ns; i += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t c = schild[i];
         const uint64_t p = cpar[c];
@@ -410,7 +464,7 @@ __global__ void __launch_bounds__(prim::kThreads)
         const char *pb = pv.objects + pv.begin[oid];
         const char *pe = pb + pv.size[oid];
         uint64_t buf[MAXC / 8];
-        rule_populate_simple(rule, pb, pe, (char *)buf, cid);
+        rule_populate_simple(rs.get(oid), pb, pe, (char *)buf, cid);
         uint32_t sz = osize[i];
         if (sz > MAXC) {
             prim::set_error(err, QUIDS_ERR_SIZE_BOUND);
@@ -420,6 +474,7 @@ __global__ void __launch_bounds__(prim::kThreads)
         char *dst = objects + ob;
         copy_bytes(dst, (const char *)buf, sz);
         for (uint64_t q = ob + sz; q < oe; ++q) objects[q] = 0;
+        const double f = finst ? d_factor[finst[i]] : f0;  // batched: the survivor's instance factor
         if (f != 1.0) {
             double2 m = omag[i];
             omag[i] = make_double2(__ddiv_rn(m.x, f), __ddiv_rn(m.y, f));
@@ -727,9 +782,10 @@ inline uint64_t next_pow2(uint64_t v) {
 }
 
 // ------------------------------------------------------------- the step
-template <class Rule, int MAXC>
-inline int launch_symbolic(quids_gpu_ctx *ctx, const Rule &rule, const parents_view &pv, uint64_t nc, bool fast,
+template <class RS, int MAXC>
+inline int launch_symbolic(quids_gpu_ctx *ctx, const RS &rule, const parents_view &pv, uint64_t nc, bool fast,
                            region_count rc) {
+    using Rule = typename RS::rule_type;
     uint64_t tiles = (nc + kTileChildren - 1) / kTileChildren;
     unsigned grid = (unsigned)(tiles < (uint64_t)ctx->num_sms * 8 ? tiles : (uint64_t)ctx->num_sms * 8);
     uint64_t *d_nc = ctx->d_words + W_NC;
@@ -738,26 +794,26 @@ inline int launch_symbolic(quids_gpu_ctx *ctx, const Rule &rule, const parents_v
     const size_t smem = rc.r * sizeof(unsigned int);
     if constexpr (has_hash_child<Rule>::value) {
         if (fast) {
-            k_symbolic<Rule, 8, true><<<grid, prim::kThreads, smem, ctx->stream>>>(
+            k_symbolic<RS, 8, true><<<grid, prim::kThreads, smem, ctx->stream>>>(
                 rule, pv, bufp<uint64_t>(ctx, B_TILEPAR), d_nc, bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG),
                 bufp<uint32_t>(ctx, B_CSIZE), bufp<uint32_t>(ctx, B_CPAR), d_maxabs, err, rc);
             return launched(ctx);
         }
     }
-    k_symbolic<Rule, MAXC, false><<<grid, prim::kThreads, smem, ctx->stream>>>(
+    k_symbolic<RS, MAXC, false><<<grid, prim::kThreads, smem, ctx->stream>>>(
         rule, pv, bufp<uint64_t>(ctx, B_TILEPAR), d_nc, bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG),
         bufp<uint32_t>(ctx, B_CSIZE), bufp<uint32_t>(ctx, B_CPAR), d_maxabs, err, rc);
     return launched(ctx);
 }
 
-template <class Rule, int MAXC>
-inline int launch_populate(quids_gpu_ctx *ctx, const Rule &rule, const parents_view &pv, uint64_t ns,
+template <class RS, int MAXC>
+inline int launch_populate(quids_gpu_ctx *ctx, const RS &rule, const parents_view &pv, uint64_t ns,
                            quids_gpu_state *out) {
-    k_populate<Rule, MAXC><<<grid_for(ctx, ns), prim::kThreads, 0, ctx->stream>>>(
+    k_populate<RS, MAXC><<<grid_for(ctx, ns), prim::kThreads, 0, ctx->stream>>>(
         rule, pv, bufp<uint64_t>(ctx, B_SCHILD), bufp<uint32_t>(ctx, B_CPAR), ctx->d_words + W_NS,
         (const uint64_t *)out->begin.p,
         (const uint32_t *)out->size.p, (char *)out->objects.p, (double2 *)out->mag.p,
-        (const double *)(ctx->d_words + W_FACTOR), (int *)(ctx->d_words + W_STATUS));
+        (const double *)(ctx->d_words + W_FACTOR), nullptr, (int *)(ctx->d_words + W_STATUS));
     return launched(ctx);
 }
 
@@ -787,8 +843,9 @@ inline unsigned lookback_grid(quids_gpu_ctx *ctx, uint64_t n) {
 }
 
 template <class Rule>
-int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, quids_gpu_state *out,
+int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, quids_gpu_state *out,
                   const quids_gpu_params &prm, quids_gpu_step_stats *stats) {
+    const single_rule<Rule> rule{rule_};
     if (!ctx || !in || !out || in == out || in->ctx != ctx || out->ctx != ctx) return QUIDS_ERR_BAD_ARG;
     const trunc_key tk{prm.simple_truncation == 0, prm.seed};
     const bool auto_max = prm.max_num_object == 0;  // memory-driven truncation (src/quids.hpp:459-485, :510-536)
@@ -813,6 +870,8 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, qui
         if (timing) cudaEventRecord(ctx->ev_stage[2 * k + 1], ctx->stream);
     };
     auto finish = [&](bool empty) -> int {
+        out->n_inst = 0;  // a plain step makes a plain state
+        out->h_inst_begin.clear();
         if (empty) {
             out->n = 0;
             out->nbytes = 0;
@@ -856,7 +915,7 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, qui
     QD_TRY(set_word(ctx, W_N, N));
     QD_TRY(ensure(ctx->buf[B_NCHILD], N * sizeof(uint32_t)));
     QD_TRY(ensure(ctx->buf[B_LOOKBACK], 3 * ((N + prim::kTile - 1) / prim::kTile + 2) * sizeof(uint64_t)));
-    k_num_child<Rule><<<grid_for(ctx, N), prim::kThreads, 0, ctx->stream>>>(
+    k_num_child<<<grid_for(ctx, N), prim::kThreads, 0, ctx->stream>>>(
         rule, (const char *)in->objects.p, (const uint64_t *)in->begin.p, (const uint32_t *)in->size.p, N,
         bufp<uint32_t>(ctx, B_NCHILD), (unsigned long long *)(ctx->d_words + W_MAXSIZE), err);
     QD_TRY(launched(ctx));
@@ -987,7 +1046,6 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, qui
     QD_TRY(ensure(ctx->buf[B_KEYS], (M + 1) * sizeof(prim::table_slot)));
     QD_TRY(ensure(ctx->buf[B_ACC], 4 * (M + 1) * sizeof(uint64_t)));
     QD_TRY(ensure(ctx->buf[B_SCHILD], NSB * sizeof(uint64_t)));
-    QD_TRY(ensure(ctx->buf[B_TILENORM], tiles_nc * sizeof(double)));
     QD_TRY(ensure(ctx->buf[B_LOOKBACK], 3 * (tiles_nc + 2) * sizeof(uint64_t)));
     QD_TRY(ensure(out->begin, (NSB + 1) * sizeof(uint64_t)));
     QD_TRY(ensure(out->size, NSB * sizeof(uint32_t)));
@@ -1020,9 +1078,9 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, qui
     QD_TRY(launched(ctx));
     region_count rc{M, regions ? R : 0u, regions ? bufp<unsigned int>(ctx, B_RHIST) : nullptr};
     if (maxsize <= 256) {
-        QD_TRY((launch_symbolic<Rule, 256>(ctx, rule, pv, NC, fast, rc)));
+        QD_TRY((launch_symbolic<single_rule<Rule>, 256>(ctx, rule, pv, NC, fast, rc)));
     } else {
-        QD_TRY((launch_symbolic<Rule, 4096>(ctx, rule, pv, NC, fast, rc)));
+        QD_TRY((launch_symbolic<single_rule<Rule>, 4096>(ctx, rule, pv, NC, fast, rc)));
     }
     end_stage(1);
 
@@ -1065,12 +1123,12 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, qui
     end_stage(2);
 
     // ---- stage 3 (+4): representatives above tolerance (src/quids.hpp:819-823),
-    // truncation (src/quids.hpp:866-900, ties by lower hash) and the output
-    // layout (src/quids.hpp:927-948), with per-tile norm sums for normalize
+    // truncation (src/quids.hpp:866-900, ties by lower child index) and the
+    // output layout (src/quids.hpp:927-948), with the largest survivor norm
     group_view gv{bufp<uint32_t>(ctx, B_SLOT), not_rep, has_join, bufp<double2>(ctx, B_CMAG),
                   bufp<unsigned long long>(ctx, B_ACC), ctx->d_words + W_NC, d_maxabs, prm.tolerance};
     const uint32_t align = prm.align_byte_length;
-    double *tile_norm = bufp<double>(ctx, B_TILENORM);
+    unsigned long long *d_maxnorm = (unsigned long long *)(ctx->d_words + W_MAXNORM);
     begin_stage(3);
     if (!may_truncate) {
         prim::lookback lbc, lbb;
@@ -1080,7 +1138,7 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, qui
                         (uint64_t *)out->begin.p, bufp<uint64_t>(ctx, B_SCHILD)};
         prim::k_compact_layout<groups_layout, false><<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
             f, ctx->d_words + W_NC, ctx->d_words + W_NS, ctx->d_words + W_OUTBYTES, (uint64_t *)out->begin.p,
-            tile_norm, lbc, lbb, lbb);
+            d_maxnorm, lbc, lbb, lbb);
         QD_TRY(launched(ctx));
         end_stage(3);
     } else {
@@ -1103,7 +1161,7 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, qui
                        (uint32_t *)out->size.p, (uint64_t *)out->begin.p, bufp<uint64_t>(ctx, B_SCHILD)};
         prim::k_compact_layout<keep_layout, true><<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
             kl, ctx->d_words + W_NU, ctx->d_words + W_NS, ctx->d_words + W_OUTBYTES, (uint64_t *)out->begin.p,
-            tile_norm, lbc, lbb, lbt);
+            d_maxnorm, lbc, lbb, lbt);
         QD_TRY(launched(ctx));
         end_stage(4);
     }
@@ -1116,12 +1174,14 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, qui
     if (NS == 0) return finish(true);
     QD_TRY(ensure(out->objects, outbytes));
 
-    // ---- stage 5: total probability (src/quids.hpp:1002-1008), in a fixed order
+    // ---- stage 5: total probability (src/quids.hpp:1002-1008), exact
     begin_stage(5);
-    prim::k_norm_from_tiles<<<1, 1024, 0, ctx->stream>>>(tile_norm, ctx->d_words + (may_truncate ? W_NU : W_NC),
-                                                        (double *)(ctx->d_words + W_TOTAL),
-                                                        (double *)(ctx->d_words + W_FACTOR));
-    QD_TRY(launched(ctx));
+    prim::k_fix_total<<<grid_for(ctx, NS, 4), prim::kThreads, 0, ctx->stream>>>(
+        (const double2 *)out->mag.p, ctx->d_words + W_NS, d_maxnorm, (unsigned long long *)(ctx->d_words + W_ACC));
+    prim::k_fix_finalize<<<1, 1, 0, ctx->stream>>>((const unsigned long long *)(ctx->d_words + W_ACC),
+                                                   ctx->d_words + W_NS, d_maxnorm, (double *)(ctx->d_words + W_TOTAL),
+                                                   (double *)(ctx->d_words + W_FACTOR));
+    QD_TRY(launched(ctx, 2));
     QD_CUDA(cudaMemcpyAsync(out->d_total.p, ctx->d_words + W_TOTAL, sizeof(double), cudaMemcpyDeviceToDevice,
                             ctx->stream));
     end_stage(5);
@@ -1129,9 +1189,9 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, qui
     // ---- stage 6: finalize populate (src/quids.hpp:958-967) + normalisation
     begin_stage(6);
     if (maxsize <= 256) {
-        QD_TRY((launch_populate<Rule, 256>(ctx, rule, pv, NS, out)));
+        QD_TRY((launch_populate<single_rule<Rule>, 256>(ctx, rule, pv, NS, out)));
     } else {
-        QD_TRY((launch_populate<Rule, 4096>(ctx, rule, pv, NS, out)));
+        QD_TRY((launch_populate<single_rule<Rule>, 4096>(ctx, rule, pv, NS, out)));
     }
     end_stage(6);
     out->n = NS;
@@ -1176,10 +1236,10 @@ int rule_children(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, uin
     QD_TRY(set_word(ctx, W_NP, N));
     QD_TRY(ensure(ctx->buf[B_NCHILD], N * sizeof(uint32_t)));
     QD_TRY(ensure(ctx->buf[B_LOOKBACK], 3 * ((N + prim::kTile - 1) / prim::kTile + 2) * sizeof(uint64_t)));
-    k_num_child<Rule><<<grid_for(ctx, N), prim::kThreads, 0, ctx->stream>>>(
-        rule, (const char *)in->objects.p, (const uint64_t *)in->begin.p, (const uint32_t *)in->size.p, N,
-        bufp<uint32_t>(ctx, B_NCHILD), (unsigned long long *)(ctx->d_words + W_MAXSIZE),
-        (int *)(ctx->d_words + W_STATUS));
+    k_num_child<<<grid_for(ctx, N), prim::kThreads, 0, ctx->stream>>>(
+        single_rule<Rule>{rule}, (const char *)in->objects.p, (const uint64_t *)in->begin.p,
+        (const uint32_t *)in->size.p, N, bufp<uint32_t>(ctx, B_NCHILD),
+        (unsigned long long *)(ctx->d_words + W_MAXSIZE), (int *)(ctx->d_words + W_STATUS));
     QD_TRY(launched(ctx));
     QD_TRY(ensure(ctx->buf[B_CBEGIN], (N + 1) * sizeof(uint64_t)));
     {

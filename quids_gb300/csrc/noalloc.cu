@@ -132,7 +132,7 @@ extern "C" int quids_gpu_rule_children_noalloc(void *stream, uint64_t num_object
     unsigned scan_grid = (unsigned)(tiles < (uint64_t)sms * 4 ? tiles : (uint64_t)sms * 4);
     int rc = with_rule(rule_kind, rule, [&](auto r) {
         k_num_child<<<grid_of(sms, num_object), prim::kThreads, 0, s>>>(
-            r, (const char *)d_objects, d_begin, d_size, num_object, nchild, (unsigned long long *)(words + 2),
+            single_rule<decltype(r)>{r}, (const char *)d_objects, d_begin, d_size, num_object, nchild, (unsigned long long *)(words + 2),
             (int *)(words + 3));
         prim::k_scan_excl<<<scan_grid, prim::kThreads, 0, s>>>(scan_nchild{nchild, nullptr}, words + 0, cbegin,
                                                                words + 1, lb);

@@ -561,17 +561,15 @@ static __global__ void __launch_bounds__(kThreads)
 // padded size, P::norm(i) -> double, P::emit(i, j, byte_offset).  With TIES,
 // P::tie(i) -> bool marks the items equal to a selection threshold and
 // tie_rank is the item's rank among them in item order (a third look-back
-// chain), so a selection can take the first ties.  Per tile, the sum of the
-// selected norms in item order goes to tile_norm[tile] (a fixed
-// decomposition: deterministic).  At the end: *d_count, *d_bytes and
-// begin_out[count] = total bytes.
+// chain), so a selection can take the first ties.  The largest selected norm
+// goes to *d_maxnorm (as IEEE bits) when d_maxnorm is not null.  At the end:
+// *d_count, *d_bytes and begin_out[count] = total bytes.
 template <class P, bool TIES>
 __global__ void __launch_bounds__(kThreads) k_compact_layout(P p, const uint64_t *d_n, uint64_t *d_count,
                                                               uint64_t *d_bytes, uint64_t *begin_out,
-                                                              double *tile_norm, lookback lb_count,
+                                                              unsigned long long *d_maxnorm, lookback lb_count,
                                                               lookback lb_bytes, lookback lb_ties) {
     __shared__ uint64_t sm[kThreads / 32 + 1];
-    __shared__ double smd[kThreads];
     __shared__ uint64_t bcast;
     __shared__ uint32_t sm_tile;
     const uint64_t n = *d_n;
@@ -584,6 +582,7 @@ __global__ void __launch_bounds__(kThreads) k_compact_layout(P p, const uint64_t
         }
         return;
     }
+    unsigned long long mx = 0;
     while (true) {
         uint32_t tile = next_tile(lb_count, &sm_tile);
         if (tile >= ntiles) break;
@@ -606,7 +605,6 @@ __global__ void __launch_bounds__(kThreads) k_compact_layout(P p, const uint64_t
         }
         uint32_t flags = 0;
         uint64_t cnt = 0, bytes = 0;
-        double nrm = 0;
 #pragma unroll
         for (int k = 0; k < kItems; ++k) {
             uint64_t i = base + k;
@@ -614,18 +612,11 @@ __global__ void __launch_bounds__(kThreads) k_compact_layout(P p, const uint64_t
                 flags |= 1u << k;
                 ++cnt;
                 bytes += p.bytes(i);
-                nrm = dadd(nrm, p.norm(i));
+                const unsigned long long b = (unsigned long long)__double_as_longlong(p.norm(i));
+                mx = mx > b ? mx : b;
             }
             if (ties & (1u << k)) ++rank;
         }
-        // deterministic per-tile norm sum: fixed tree over threads
-        smd[threadIdx.x] = nrm;
-        __syncthreads();
-        for (int o = kThreads / 2; o > 0; o >>= 1) {
-            if (threadIdx.x < o) smd[threadIdx.x] = dadd(smd[threadIdx.x], smd[threadIdx.x + o]);
-            __syncthreads();
-        }
-        if (threadIdx.x == 0) tile_norm[tile] = smd[0];
         uint64_t agg_c, agg_b;
         uint64_t excl_c = block_excl_scan(cnt, sm, agg_c);
         uint64_t excl_b = block_excl_scan(bytes, sm, agg_b);
@@ -645,31 +636,52 @@ __global__ void __launch_bounds__(kThreads) k_compact_layout(P p, const uint64_t
             begin_out[pre_c + agg_c] = pre_b + agg_b;
         }
     }
+    if (d_maxnorm) {
+        for (int o = 16; o > 0; o >>= 1) {
+            unsigned long long y = __shfl_xor_sync(0xffffffffu, mx, o);
+            mx = mx > y ? mx : y;
+        }
+        if ((threadIdx.x & 31) == 0 && mx) atomicMax(d_maxnorm, mx);
+    }
 }
 
 // --------------------------------------------------------- normalisation
-// total = sum of the per-tile norm sums in tile order (one block, fixed
-// tree); factor = sqrt(total) (src/quids.hpp:1004-1008).
-static __global__ void __launch_bounds__(1024) k_norm_from_tiles(const double *tile_norm, const uint64_t *d_items,
-                                                                  double *d_total, double *d_factor) {
-    __shared__ double sm[1024];
-    const uint64_t nt = (*d_items + kTile - 1) / kTile;
-    const uint64_t per = (nt + 1023) / 1024;
-    double s = 0;
-    for (uint64_t k = 0; k < per; ++k) {
-        uint64_t t = (uint64_t)threadIdx.x * per + k;
-        if (t < nt) s = dadd(s, tile_norm[t]);
+// Total probability (src/quids.hpp:1002-1008) of the n magnitudes, exact:
+// every norm is converted to 128-bit fixed point with F = fix_scale(max
+// norm, n) and the integers are summed (any order gives the same bits).
+// One fixed-point atomic add per block into acc[2] (zero beforehand).
+static __global__ void __launch_bounds__(kThreads) k_fix_total(const double2 *mag, const uint64_t *d_n,
+                                                                const unsigned long long *d_maxnorm,
+                                                                unsigned long long *acc) {
+    __shared__ fix128 sm[kThreads / 32];
+    const uint64_t n = *d_n;
+    const int F = fix_scale(__longlong_as_double((long long)*d_maxnorm), n);
+    fix128 a{0, 0};
+    for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (uint64_t)gridDim.x * blockDim.x) {
+        const double2 m = mag[j];
+        a = fix_add(a, to_fix(cnorm(mag_t{m.x, m.y}), F));
     }
-    sm[threadIdx.x] = s;
+    for (int o = 16; o > 0; o >>= 1) {
+        const uint64_t lo = __shfl_xor_sync(0xffffffffu, a.lo, o);
+        const uint64_t hi = __shfl_xor_sync(0xffffffffu, a.hi, o);
+        a = fix_add(a, fix128{lo, hi});
+    }
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = a;
     __syncthreads();
-    for (int o = 512; o > 0; o >>= 1) {
-        if (threadIdx.x < o) sm[threadIdx.x] = dadd(sm[threadIdx.x], sm[threadIdx.x + o]);
-        __syncthreads();
-    }
     if (threadIdx.x == 0) {
-        *d_total = sm[0];
-        *d_factor = __dsqrt_rn(sm[0]);
+        fix128 t{0, 0};
+        for (int w = 0; w < kThreads / 32; ++w) t = fix_add(t, sm[w]);
+        fix_atomic_add(acc, t);
     }
+}
+
+// total = acc * 2^-F, factor = sqrt(total)
+static __global__ void k_fix_finalize(const unsigned long long *acc, const uint64_t *d_n,
+                                      const unsigned long long *d_maxnorm, double *d_total, double *d_factor) {
+    const int F = fix_scale(__longlong_as_double((long long)*d_maxnorm), *d_n);
+    const double t = from_fix(fix128{acc[0], acc[1]}, F);
+    *d_total = t;
+    *d_factor = __dsqrt_rn(t);
 }
 
 }  // namespace qd::prim

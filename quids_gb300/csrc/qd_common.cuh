@@ -210,6 +210,13 @@ QD_HD double u64_to_double_rn(uint64_t v) {
 #endif
 }
 
+QD_HD fix128 fix_add(fix128 a, fix128 b) {
+    fix128 r;
+    r.lo = a.lo + b.lo;
+    r.hi = a.hi + b.hi + (r.lo < a.lo ? 1ull : 0ull);
+    return r;
+}
+
 // correctly rounded (hi:lo) * 2^-F
 QD_HD double from_fix(fix128 v, int F) {
     bool neg = (v.hi >> 63) != 0;
