@@ -12,6 +12,15 @@ the step time.
 erase_create) on a 12-node cycle graph, starting from the state after the
 first step (the reference needs ~60 s on 8 cores for it).
 
+"batch256": the batched form -- 256 independent QCGD instances (cycle
+graphs of U[4,16] nodes, Bernoulli(0.5) bits, per-instance split_merge and
+erase_create angles, seed 2), max_num_object 2^18 per instance; one bench
+step is the first QCGD step of every instance in one pipeline per rule
+(quids_gpu_run_batched).  The same step run instance by instance through
+the plain path is timed beside it ("plain_instance_by_instance").  Later
+steps do not fit one GPU: the coin rule of the second step has more than
+2^32 children (about 4.7e10).
+
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--config NAME]
 
 --impl reference times the CPU restatement of the reference algorithm
@@ -59,6 +68,15 @@ def workload(name):
                                        f"erase_create(pi/3,pi/5,0)) of a {nodes}-node cycle graph, from the "
                                        f"state after step 0, max_num_object 2^{cap.bit_length() - 1}",
                            "nodes": nodes, "seed": seed, "max_num_object": cap, "tolerance": 1e-18,
+                           "align_byte_length": 8}}
+    if name == "batch256":
+        insts = W.qcgd_batch_instances(256, 2, 4, 16)
+        return {"name": name, "insts": insts, "max": 1 << 18, "tolerance": 1e-18, "align": 8,
+                "config": {"workload": "batched QCGD: 256 instances (cycle graphs, U[4,16] nodes, per-instance "
+                                       "split_merge/erase_create angles, seed 2), first step (step, coin, "
+                                       "split_merge, erase_create) of all instances in one pipeline per rule, "
+                                       "max_num_object 2^18 per instance",
+                           "instances": 256, "seed": 2, "max_num_object": 1 << 18, "tolerance": 1e-18,
                            "align_byte_length": 8}}
     raise SystemExit(f"unknown config {name}")
 
@@ -156,8 +174,7 @@ def stage_bytes(st):
     sbar_p = sp / NP if NP else 0
     sbar_c = st["out_bytes"] / NS if NS else 0
     M = st["table_capacity"]
-    regions = int(44.0 * M / (32 * 1024 * 1024)) + 1 >= 4   # the library's region rule
-    if regions:   # scatter (24 in, 28 out), insert (28 in, 4 out); mark (8 in, 17 out per rep); flags + gathers
+    if st.get("_regions"):   # scatter (24 in, 28 out), insert (28 in, 4 out); mark (8 in, 17 out per rep); flags + gathers
         s2 = 8.0 * M + 84.0 * NC
         s3 = 9.0 * NC + 17.0 * NU
     else:         # insert (24 in, 4 out); per child slot + rep, per rep its sum
@@ -171,7 +188,7 @@ def stage_bytes(st):
         2: s2,
         3: s3 + (40.0 * NU if trunc else out_layout),
         4: (8.0 * NU + 40.0 * NU + out_layout) if trunc else 0.0,       # select (first pass), keep + layout
-        5: 8.0 * (NC / 2048.0),                                         # per-tile norm sums
+        5: 16.0 * NS,                                                   # exact total: survivor magnitudes
         6: NS * (sbar_p + sbar_c + 48.0),                               # populate + normalise magnitudes
         7: 0.0,
     }
@@ -317,6 +334,171 @@ def ours(args, rank, world):
         print(json.dumps(line), flush=True)
 
 
+def batch_ops(quids, wl):
+    from quids_gb300 import workloads as W
+    insts = wl["insts"]
+    return [quids.rules.step, quids.rule_from(True, W.RULE_QCGD_COIN, W.COIN_DEFAULT),
+            [quids.rule_from(True, W.RULE_QCGD_SPLIT_MERGE, sm) for _, sm, _ in insts],
+            [quids.rule_from(True, W.RULE_QCGD_ERASE_CREATE, ec) for _, _, ec in insts]]
+
+
+def instance_ops(quids, sm, ec):
+    from quids_gb300 import workloads as W
+    return [quids.rules.step, quids.rule_from(True, W.RULE_QCGD_COIN, W.COIN_DEFAULT),
+            quids.rule_from(True, W.RULE_QCGD_SPLIT_MERGE, sm), quids.rule_from(True, W.RULE_QCGD_ERASE_CREATE, ec)]
+
+
+def ours_batched(args, rank, world):
+    """The batched form: one QCGD step of 256 instances per bench step."""
+    import torch
+    import quids_gb300 as quids
+    from quids_gb300 import capi, workloads as W
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    wl = workload(args.config)
+    quids.tolerance, quids.align_byte_length = wl["tolerance"], wl["align"]
+    ctx = quids.Context(dev)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=f"cuda:{dev}")
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.int32, device=f"cuda:{dev}")
+    packed = [W.pack([g], [1.0 + 0j], 8) for g, _, _ in wl["insts"]]
+    ops = batch_ops(quids, wl)
+    spare = [quids.it_t(ctx)]
+
+    def step(src):
+        fin, st = quids.run_batched(src, spare[0], ops, wl["max"])
+        if fin is spare[0]:
+            spare[0] = src
+        return sum(x["num_object"] for x in st), sum(x["algorithmic_bytes"] for x in st), fin
+
+    def fresh():
+        a = quids.it_t(ctx)
+        a.upload_batched(packed)
+        return a
+
+    for _ in range(args.warmup):
+        step(fresh())
+    ctx.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    launches0 = ctx.lib.quids_gpu_ctx_launch_count(ctx.h)
+    ms, children, abytes = [], 0, 0.0
+    t_wall0 = time.perf_counter()
+    with Clocks(dev) as clk:
+        for _ in range(args.steps):
+            src = fresh()
+            with torch.cuda.stream(stream):
+                flush.fill_(1)
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+            c, b, _ = step(src)
+            with torch.cuda.stream(stream):
+                e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+            children += c
+            abytes += b
+    ctx.synchronize()
+    t_wall = time.perf_counter() - t_wall0
+    launches = ctx.lib.quids_gpu_ctx_launch_count(ctx.h) - launches0
+    total_ms = sum(ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device=f"cuda:{dev}")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * children / (total_ms / 1e3)
+
+    # the same step, instance by instance through the plain path
+    plain_ms = []
+    for _ in range(max(1, min(args.steps, 3))):
+        with torch.cuda.stream(stream):
+            flush.fill_(1)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+        pc = 0
+        for (g, sm, ec), p in zip(wl["insts"], packed):
+            fin, st = quids.run(quids.it_t(ctx, p), quids.it_t(ctx), instance_ops(quids, sm, ec), wl["max"])
+            pc += sum(x["num_object"] for x in st)
+        with torch.cuda.stream(stream):
+            e1.record(stream)
+        e1.synchronize()
+        plain_ms.append(e0.elapsed_time(e1))
+    plain_value = pc / (statistics.mean(plain_ms) / 1e3)
+
+    # e2e: host instances in, final batched state out, copies inside the timed region
+    e2e = None
+    if rank == 0 or world > 1:
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        e2e_children, h2d, d2h = 0, 0, 0
+        for _ in range(args.steps):
+            src = fresh()
+            h2d = sum(sum(a.nbytes for a in p) for p in packed)
+            c, _, out = step(src)
+            e2e_children += c
+            got = out.download()
+            d2h = sum(a.nbytes for a in got)
+        ctx.synchronize()
+        t_e2e = time.perf_counter() - t0
+        e2e = {"value": e2e_children / t_e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h), "ms_per_step": 1e3 * t_e2e / args.steps}
+
+    peak, peak_kind = peaks()
+    achieved = abytes / (total_ms / 1e3) / 1e9
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline_batched(wl, packed)
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded generators; the reference publishes no dataset)",
+            "config": dict(wl["config"], parallelism=f"replicas x{world}",
+                           l2="flushed before every step (256 MiB write)",
+                           children_per_step=children // args.steps),
+            "plain_instance_by_instance": {"value": plain_value, "unit": UNIT,
+                                           "ms_per_step": statistics.mean(plain_ms),
+                                           "batched_over_plain": value / plain_value},
+            "e2e": e2e,
+            "gpu_launches": int(launches),
+            "roofline": {"bound": "hbm", "kernel": "whole batched step (all kernels)", "achieved": achieved,
+                         "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                         "traffic": None},
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "wall_s_timed": t_wall,
+        }
+        print(json.dumps(line), flush=True)
+
+
+def cpu_baseline_batched(wl, packed):
+    """The oracle port on all host cores, instance after instance."""
+    from oracle.oracle import Oracle
+    from quids_gb300 import workloads as W
+    o = Oracle("port")
+    cores = os.cpu_count() or 1
+    o.set_threads(cores)
+    o.set_globals(wl["tolerance"], True, wl["align"])
+    t0 = time.perf_counter()
+    ch = 0
+    for (g, sm, ec), p in zip(wl["insts"], packed):
+        s = o.new_state(p)
+        o.modifier(s, W.MOD_QCGD_STEP, ())
+        for kind, prm in ((W.RULE_QCGD_COIN, W.COIN_DEFAULT), (W.RULE_QCGD_SPLIT_MERGE, sm),
+                          (W.RULE_QCGD_ERASE_CREATE, ec)):
+            t = o.new_state()
+            ch += o.simulate(s, kind, prm, t, wl["max"])[0]
+            s = t
+    dt = time.perf_counter() - t0
+    return {"value": ch / dt, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"the first step of all {len(packed)} instances, one after another ({ch} children, "
+                      f"{dt:.2f} s)"}
+
+
 def cpu_baseline(wl, init_packed, samples=1, warm=True):
     """The oracle port (the reference algorithm restated, OpenMP) on all host cores."""
     from oracle.oracle import Oracle
@@ -350,6 +532,22 @@ def reference(args, rank, world):
     if rank != 0:
         return
     wl = workload(args.config)
+    if wl["name"] == "batch256":  # the reference steps one state per call: instances one by one
+        from quids_gb300 import workloads as W
+        packed = [W.pack([g], [1.0 + 0j], 8) for g, _, _ in wl["insts"]]
+        for _ in range(args.warmup):
+            cpu_baseline_batched(wl, packed)
+        vals = [cpu_baseline_batched(wl, packed) for _ in range(args.steps)]
+        v = statistics.mean(x["value"] for x in vals)
+        print(json.dumps({
+            "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": dict(wl["config"], parallelism="host cores, instances one after another"),
+            "cpu_baseline": dict(vals[-1], value=v),
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }), flush=True)
+        return
     from oracle.oracle import Oracle
     o = Oracle("port")
     cores = os.cpu_count() or 1
@@ -392,7 +590,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="circuit24", choices=["circuit24", "qcgd12", "qcgd10"])
+    ap.add_argument("--config", default="circuit24", choices=["circuit24", "qcgd12", "qcgd10", "batch256"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -403,6 +601,8 @@ def main():
     try:
         if args.impl == "reference":
             reference(args, rank, world)
+        elif args.config == "batch256":
+            ours_batched(args, rank, world)
         else:
             ours(args, rank, world)
     finally:

@@ -286,6 +286,46 @@ int quids_gpu_qcgd_statistics(quids_gpu_ctx *ctx, quids_gpu_state *iteration, ui
                               uint64_t sy_num_object_after_interferences, double tolerance,
                               quids_gpu_qcgd_stats *out);
 
+/* ---------------------------------------------------------------- adjoint
+ * No counterpart in the reference.  Reverse mode through a run of rule and
+ * modifier ops with respect to the rule angles (theta, phi, xi of the QCGD
+ * rules), with every step's structure held fixed: the same children,
+ * collisions, zero elimination and truncation as the forward run.
+ *
+ * quids_gpu_forward runs `ops` from `initial` (as quids_gpu_run does) and
+ * records a tape: the state at the start of every segment of
+ * checkpoint_every rule applications, and the rule inputs of the last
+ * segment.  The final state is copied to final_out when not NULL.  Modifiers
+ * must be X, CNOT, QCGD step or reversed_step (they move bytes and keep
+ * magnitudes); max_num_object must not be 0 (the memory-driven cap depends
+ * on free memory, so a replay could differ).
+ *
+ * quids_gpu_simulate_backward: loss_adjoint (2 * n doubles, n = objects of
+ * the final state) is a = 2 dL/d(conj m) of a real loss L of the final
+ * magnitudes m (for L = sum w_s |m_s|^2, a_s = 2 w_s m_s).  The backward
+ * recomputes each segment's states from its checkpoint, replays every rule
+ * step and gathers the adjoint from survivors to children to parents.
+ * grad_angles receives 3 * n_ops doubles: dL/dtheta, dL/dphi, dL/dxi of
+ * each op (zero for modifiers and the Hadamard rule).
+ * quids_gpu_simulate_backward_observable takes L = average_value of a
+ * built-in observable of the final state (QUIDS_OBS_*), computed with its
+ * adjoint on the GPU, and returns L in *loss.
+ * quids_gpu_observable_adjoint: L and a for one state (adjoint may be NULL). */
+typedef struct quids_gpu_tape quids_gpu_tape;
+int quids_gpu_tape_create(quids_gpu_ctx *ctx, quids_gpu_tape **out);
+int quids_gpu_tape_destroy(quids_gpu_tape *tape);
+int quids_gpu_forward(quids_gpu_ctx *ctx, quids_gpu_tape *tape, quids_gpu_state *initial, const quids_gpu_op *ops,
+                      uint64_t n_ops, const quids_gpu_params *params, uint64_t checkpoint_every,
+                      quids_gpu_state *final_out, quids_gpu_step_stats *rule_stats);
+int quids_gpu_tape_final_state(quids_gpu_tape *tape, quids_gpu_state *out);
+int quids_gpu_simulate_backward(quids_gpu_ctx *ctx, quids_gpu_tape *tape, const double *loss_adjoint,
+                                double *grad_angles);
+int quids_gpu_simulate_backward_observable(quids_gpu_ctx *ctx, quids_gpu_tape *tape, int observable_kind,
+                                           const quids_gpu_rule_params *params, double *loss,
+                                           double *grad_angles);
+int quids_gpu_observable_adjoint(quids_gpu_ctx *ctx, quids_gpu_state *iteration, int observable_kind,
+                                 const quids_gpu_rule_params *params, double *value, double *adjoint);
+
 /* MurmurHash64A of libstdc++'s std::hash<std::string_view> (seed 0xc70f6907),
  * the reference's default hasher (src/quids.hpp:143-145), computed on the GPU
  * for `n` byte strings of one state.  out = n u64. */

@@ -439,6 +439,80 @@ def run_batched(a: it_t, b: it_t, ops, max_num_object: int = U64_MAX, flags: int
     return (a if fin.value == 0 else b), [stats[i].as_dict() for i in range(n_rules)]
 
 
+class Tape:
+    """A forward run of rules and modifiers recorded for simulate_backward
+    (no counterpart in the reference): reverse mode with respect to the rule
+    angles, each step's structure (children, collisions, truncation) held
+    fixed.  Checkpoints every `checkpoint_every` rule applications."""
+
+    def __init__(self, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        self.lib = self.ctx.lib
+        h = C.c_void_p()
+        capi.check(self.lib.quids_gpu_tape_create(self.ctx.h, C.byref(h)), "tape_create")
+        self.h = h
+        self.n_ops = 0
+
+    def __del__(self):
+        try:
+            if self.h:
+                self.lib.quids_gpu_tape_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+    def forward(self, initial: it_t, ops, max_num_object: int = U64_MAX, checkpoint_every: int = 1, flags: int = 0):
+        """Runs ops from `initial`; returns (final it_t, per-rule stats)."""
+        initial._flush()
+        arr = (capi.Op * max(len(ops), 1))()
+        n_rules = 0
+        for i, r in enumerate(ops):
+            arr[i].is_rule = int(r.is_rule)
+            arr[i].kind = r.kind
+            arr[i].params = r.params()
+            n_rules += int(r.is_rule)
+        stats = (capi.StepStats * max(n_rules, 1))()
+        out = it_t(self.ctx)
+        prm = _params(max_num_object, flags)
+        capi.check(self.lib.quids_gpu_forward(self.ctx.h, self.h, initial.h, arr, len(ops), C.byref(prm),
+                                              int(checkpoint_every), out.h, stats), "forward")
+        self.n_ops = len(ops)
+        return out, [stats[i].as_dict() for i in range(n_rules)]
+
+    def backward(self, loss_adjoint):
+        """loss_adjoint: complex array a = 2 dL/d(conj m) over the final
+        state's objects.  Returns dL/d(theta, phi, xi) per op, shape (n_ops, 3)."""
+        a = np.ascontiguousarray(loss_adjoint, dtype=np.complex128)
+        g = np.zeros((max(self.n_ops, 1), 3), np.float64)
+        capi.check(self.lib.quids_gpu_simulate_backward(self.ctx.h, self.h, a.ctypes.data if len(a) else None,
+                                                        g.ctypes.data), "simulate_backward")
+        return g[: self.n_ops]
+
+    def backward_observable(self, observable: int, bit: int = 0):
+        """L = the final state's average_value of a built-in observable;
+        returns (L, dL/d(theta, phi, xi) per op)."""
+        g = np.zeros((max(self.n_ops, 1), 3), np.float64)
+        loss = C.c_double()
+        p = capi.RuleParams(int(bit), 0, 0.0, 0.0, 0.0)
+        capi.check(self.lib.quids_gpu_simulate_backward_observable(self.ctx.h, self.h, int(observable), C.byref(p),
+                                                                   C.byref(loss), g.ctypes.data),
+                   "simulate_backward_observable")
+        return float(loss.value), g[: self.n_ops]
+
+
+def observable_adjoint(iteration: it_t, observable: int, bit: int = 0):
+    """(L, a): L = average_value of a built-in observable and its adjoint
+    a = 2 dL/d(conj m) over the state's objects."""
+    iteration._flush()
+    n = iteration.num_object
+    a = np.zeros(max(n, 1), np.complex128)
+    v = C.c_double()
+    p = capi.RuleParams(int(bit), 0, 0.0, 0.0, 0.0)
+    capi.check(iteration.lib.quids_gpu_observable_adjoint(iteration.ctx.h, iteration.h, int(observable), C.byref(p),
+                                                          C.byref(v), a.ctypes.data), "observable_adjoint")
+    return float(v.value), a[:n]
+
+
 def rule_children(iteration: it_t, rule):
     """Every child of every parent with its bytes, hash, size and magnitude
     (the symbolic iteration with the child bytes kept)."""

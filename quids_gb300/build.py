@@ -17,7 +17,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libquids_gb300.so")
-SOURCES = ["capi.cu", "noalloc.cu", "batch.cu"]
+SOURCES = ["capi.cu", "noalloc.cu", "batch.cu", "adjoint.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -76,7 +76,9 @@ EXPORTS = [
     "quids_gpu_state_device_arrays", "quids_gpu_simulate", "quids_gpu_apply_modifier",
     "quids_gpu_rule_children", "quids_gpu_state_hash", "quids_gpu_rule_children_noalloc", "quids_gpu_run",
     "quids_gpu_average_value", "quids_gpu_qcgd_statistics", "quids_gpu_state_upload_batched",
-    "quids_gpu_state_instances", "quids_gpu_simulate_batched", "quids_gpu_run_batched",
+    "quids_gpu_state_instances", "quids_gpu_simulate_batched", "quids_gpu_run_batched", "quids_gpu_tape_create",
+    "quids_gpu_tape_destroy", "quids_gpu_forward", "quids_gpu_tape_final_state", "quids_gpu_simulate_backward",
+    "quids_gpu_simulate_backward_observable", "quids_gpu_observable_adjoint",
 ]
 
 _lib = None
@@ -136,6 +138,15 @@ def load(build_if_missing: bool = True):
                                              C.POINTER(StepStats)]
     L.quids_gpu_run_batched.argtypes = [vp, vp, vp, C.POINTER(Op), C.c_uint64, C.POINTER(RuleParams),
                                         C.POINTER(Params), C.POINTER(StepStats), C.POINTER(C.c_int)]
+    L.quids_gpu_tape_create.argtypes = [vp, C.POINTER(vp)]
+    L.quids_gpu_tape_destroy.argtypes = [vp]
+    L.quids_gpu_forward.argtypes = [vp, vp, vp, C.POINTER(Op), C.c_uint64, C.POINTER(Params), C.c_uint64, vp,
+                                    C.POINTER(StepStats)]
+    L.quids_gpu_tape_final_state.argtypes = [vp, vp]
+    L.quids_gpu_simulate_backward.argtypes = [vp, vp, vp, vp]
+    L.quids_gpu_simulate_backward_observable.argtypes = [vp, vp, C.c_int, C.POINTER(RuleParams),
+                                                         C.POINTER(C.c_double), vp]
+    L.quids_gpu_observable_adjoint.argtypes = [vp, vp, C.c_int, C.POINTER(RuleParams), C.POINTER(C.c_double), vp]
     _lib = L
     return L
 

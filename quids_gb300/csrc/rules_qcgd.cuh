@@ -205,6 +205,23 @@ struct factors {
     mag_t d, dc, dn, ndnc;
 };
 
+// A rule multiplies a child's magnitude by a product of the four factors.
+// The rules name the factor they apply (F_D .. F_NDNC); with a magnitude the
+// factor's value multiplies it, with a factor_count (used by the adjoint)
+// the factor's occurrence is counted instead.
+enum { F_D = 0, F_DC = 1, F_DN = 2, F_NDNC = 3 };
+struct factor_count {
+    uint16_t n[4];
+};
+QD_HD void mulf(mag_t *m, const factors &f, int k) {
+    if (!m) return;
+    const mag_t &v = k == F_D ? f.d : k == F_DC ? f.dc : k == F_DN ? f.dn : f.ndnc;
+    *m = cmul(*m, v);
+}
+QD_HD void mulf(factor_count *m, const factors &, int k) {
+    if (m) ++m->n[k];
+}
+
 // ---------------------------------------------------- erase_create / coin
 // erase_create (:459-532): a site is a node with left == right;
 // coin (:534-605): a site is a node with left != right.  Children = 2^sites
@@ -228,22 +245,22 @@ struct flip_rule {
             if (site(L(pb, i), R(pb, n, i))) nc *= 2;
         num_child = nc;
     }
-    QD_HD void apply(const char *pb, int n, uint32_t cid, mag_t *mag, char *cb, uint64_t *lh,
-                     uint64_t *rh) const {
+    template <class M>
+    QD_HD void apply(const char *pb, int n, uint32_t cid, M *mag, char *cb, uint64_t *lh, uint64_t *rh) const {
         for (int i = 0; i < n; ++i) {
             bool l = L(pb, i), r = R(pb, n, i);
             if (site(l, r)) {
                 bool c = conj_of(l, r);
                 if (cid & 1) {
-                    if (mag) *mag = cmul(*mag, c ? f.dc : f.d);
+                    mulf(mag, f, c ? F_DC : F_D);
                     l = !l;
                     r = !r;
                     if (cb) {
                         cb[2 + i] = l;
                         cb[2 + n + i] = r;
                     }
-                } else if (mag) {
-                    *mag = cmul(*mag, c ? f.ndnc : f.dn);
+                } else {
+                    mulf(mag, f, c ? F_NDNC : F_DN);
                 }
                 cid >>= 1;
             }
@@ -262,7 +279,10 @@ struct flip_rule {
     QD_HD void populate_child_simple(const char *pb, const char *pe, char *cb,
                                      uint32_t child_id) const {
         copy_bytes(cb, pb, (uint32_t)(pe - pb));
-        apply(pb, num_nodes(pb), child_id, nullptr, cb, nullptr, nullptr);
+        apply(pb, num_nodes(pb), child_id, (mag_t *)nullptr, cb, nullptr, nullptr);
+    }
+    QD_HD void factor_counts(const char *pb, const char *, uint32_t child_id, factor_count &fc) const {
+        apply(pb, num_nodes(pb), child_id, &fc, nullptr, nullptr, nullptr);
     }
     QD_HD uint64_t hasher(const char *b, const char *) const { return hash_graph(b); }
     QD_HD uint64_t hash_child(const char *pb, const char *pe, uint32_t child_id, uint32_t &size,
@@ -318,22 +338,23 @@ struct split_merge {
         int n, cn;
         uint32_t cid;  // child id with the wrap bits consumed
     };
-    QD_HD plan make_plan(const char *p, uint32_t cid, mag_t *mag) const {
+    template <class M>
+    QD_HD plan make_plan(const char *p, uint32_t cid, M *mag) const {
         plan pl;
         int n = pl.n = num_nodes(p);
         bool fs, lm;
         wrap_sites(p, n, fs, lm);
         fs = fs && (cid & 1);
         if (fs) {
-            if (mag) *mag = cmul(*mag, f.d);
+            mulf(mag, f, F_D);
             cid >>= 1;
         }
         if (lm) {
             if (cid & 1) {
-                if (mag) *mag = cmul(*mag, f.dc);
+                mulf(mag, f, F_DC);
             } else {
                 lm = false;
-                if (mag) *mag = cmul(*mag, f.ndnc);
+                mulf(mag, f, F_NDNC);
             }
             cid >>= 1;
         }
@@ -345,9 +366,9 @@ struct split_merge {
             if (!(s || m)) continue;
             if (bits & 1) {
                 cn += (int)s - (int)m;
-                if (mag) *mag = cmul(*mag, s ? f.d : f.dc);
-            } else if (mag) {
-                *mag = cmul(*mag, s ? f.dn : f.ndnc);
+                mulf(mag, f, s ? F_D : F_DC);
+            } else {
+                mulf(mag, f, s ? F_DN : F_NDNC);
             }
             bits >>= 1;
         }
@@ -448,6 +469,9 @@ struct split_merge {
     }
     QD_HD void populate_child_simple(const char *pb, const char *, char *cb, uint32_t child_id) const {
         build(pb, cb, child_id, nullptr, nullptr);
+    }
+    QD_HD void factor_counts(const char *pb, const char *, uint32_t child_id, factor_count &fc) const {
+        make_plan(pb, child_id, &fc);
     }
     QD_HD uint64_t hasher(const char *b, const char *) const { return hash_graph(b); }
     QD_HD uint64_t hash_child(const char *pb, const char *, uint32_t child_id, uint32_t &size,

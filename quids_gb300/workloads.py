@@ -217,3 +217,27 @@ def qcgd_batch_instances(n_inst: int = 256, seed: int = 2, lo: int = 4, hi: int 
         ec = (rng.uniform(0, math.pi), rng.uniform(0, 2 * math.pi), rng.uniform(0, 2 * math.pi))
         out.append((g, sm, ec))
     return out
+
+
+def qcgd_adjoint_workload(n_nodes: int = 10, seed: int = 3):
+    """Adjoint workload: a cycle graph of n_nodes with Bernoulli(0.5) bits and
+    six angles U(0, pi) -- split_merge (theta1, phi1, xi1) and erase_create
+    (theta2, phi2, xi2) -- drawn from one generator of `seed`, bits first."""
+    rng = Rng(seed)
+    g = random_graph(n_nodes, rng)
+    angles = [rng.uniform(0, math.pi) for _ in range(6)]
+    return pack([g], [1.0 + 0j], 8), angles
+
+
+def qcgd_adjoint_ops(angles, n_steps: int):
+    """(ops, slots): n_steps of step, coin, split_merge(angles[0:3]),
+    erase_create(angles[3:6]) as Gate tuples; slots maps (op index,
+    component 0..2) -> angle index for the rule ops carrying the angles."""
+    ops, slots = [], []
+    for _ in range(n_steps):
+        base = len(ops)
+        ops += [Gate("mod", MOD_QCGD_STEP, ()), Gate("rule", RULE_QCGD_COIN, tuple(COIN_DEFAULT)),
+                Gate("rule", RULE_QCGD_SPLIT_MERGE, tuple(angles[0:3])),
+                Gate("rule", RULE_QCGD_ERASE_CREATE, tuple(angles[3:6]))]
+        slots += [(base + 2, k, k) for k in range(3)] + [(base + 3, k, 3 + k) for k in range(3)]
+    return ops, slots
