@@ -21,6 +21,13 @@ the plain path is timed beside it ("plain_instance_by_instance").  Later
 steps do not fit one GPU: the coin rule of the second step has more than
 2^32 children (about 4.7e10).
 
+"adjoint10": the adjoint -- a 10-node cycle graph (seed 3), T = 20 QCGD
+steps with split_merge / erase_create angles U(0, pi) from seed 3,
+max_num_object 2^22; one bench step is the taped forward plus
+simulate_backward of the expected node count (checkpoints every 5 QCGD
+steps); the value counts the forward's children per second of the whole
+forward + backward, and the plain forward is timed beside it.
+
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--config NAME]
 
 --impl reference times the CPU restatement of the reference algorithm
@@ -78,6 +85,15 @@ def workload(name):
                                        "max_num_object 2^18 per instance",
                            "instances": 256, "seed": 2, "max_num_object": 1 << 18, "tolerance": 1e-18,
                            "align_byte_length": 8}}
+    if name == "adjoint10":
+        init, angles = W.qcgd_adjoint_workload(10, seed=3)
+        return {"name": name, "init": init, "angles": angles, "T": 20, "every": 15, "max": 1 << 22,
+                "tolerance": 1e-18, "align": 8,
+                "config": {"workload": "adjoint: gradient of the expected node count after 20 QCGD steps (step, "
+                                       "coin, split_merge, erase_create) of a 10-node cycle graph with respect to "
+                                       "the 6 split_merge/erase_create angles, max_num_object 2^22, checkpoints "
+                                       "every 5 steps", "nodes": 10, "seed": 3, "T": 20,
+                           "max_num_object": 1 << 22, "tolerance": 1e-18, "align_byte_length": 8}}
     raise SystemExit(f"unknown config {name}")
 
 
@@ -428,7 +444,9 @@ def ours_batched(args, rank, world):
         plain_ms.append(e0.elapsed_time(e1))
     plain_value = pc / (statistics.mean(plain_ms) / 1e3)
 
-    # e2e: host instances in, final batched state out, copies inside the timed region
+    # e2e: host instances in, each instance's object count and total
+    # probability out (the full final state is 7.9 GB), copies inside the
+    # timed region
     e2e = None
     if rank == 0 or world > 1:
         ctx.synchronize()
@@ -439,8 +457,8 @@ def ours_batched(args, rank, world):
             h2d = sum(sum(a.nbytes for a in p) for p in packed)
             c, _, out = step(src)
             e2e_children += c
-            got = out.download()
-            d2h = sum(a.nbytes for a in got)
+            ib, tot = out.instances()
+            d2h = ib.nbytes + tot.nbytes
         ctx.synchronize()
         t_e2e = time.perf_counter() - t0
         e2e = {"value": e2e_children / t_e2e, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
@@ -473,6 +491,104 @@ def ours_batched(args, rank, world):
             "wall_s_timed": t_wall,
         }
         print(json.dumps(line), flush=True)
+
+
+def ours_adjoint(args, rank, world):
+    """The adjoint: taped forward + simulate_backward per bench step."""
+    import torch
+    import quids_gb300 as quids
+    from quids_gb300 import workloads as W
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    wl = workload(args.config)
+    quids.tolerance, quids.align_byte_length = wl["tolerance"], wl["align"]
+    ctx = quids.Context(dev)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=f"cuda:{dev}")
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.int32, device=f"cuda:{dev}")
+    gates, slots = W.qcgd_adjoint_ops(wl["angles"], wl["T"])
+    ops = [quids.rule_from(g.kind == "rule", g.code, g.params) for g in gates]
+    tape = quids.Tape(ctx)
+
+    def step():
+        final, st = tape.forward(quids.it_t(ctx, wl["init"]), ops, wl["max"], wl["every"])
+        loss, g = tape.backward_observable(quids.OBS_QCGD_NUM_NODES)
+        grad = [0.0] * 6
+        for oi, comp, ai in slots:
+            grad[ai] += float(g[oi, comp])
+        return sum(x["num_object"] for x in st), sum(x["algorithmic_bytes"] for x in st), loss, grad
+
+    def timed(fn):
+        with torch.cuda.stream(stream):
+            flush.fill_(1)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+        r = fn()
+        with torch.cuda.stream(stream):
+            e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1), r
+
+    for _ in range(args.warmup):
+        step()
+    ctx.synchronize()
+    torch.cuda.synchronize()
+    launches0 = ctx.lib.quids_gpu_ctx_launch_count(ctx.h)
+    ms, children, abytes = [], 0, 0.0
+    t_wall0 = time.perf_counter()
+    with Clocks(dev) as clk:
+        for _ in range(args.steps):
+            t, (c, b, loss, grad) = timed(step)
+            ms.append(t)
+            children += c
+            abytes += b
+    t_wall = time.perf_counter() - t_wall0
+    launches = ctx.lib.quids_gpu_ctx_launch_count(ctx.h) - launches0
+    total_ms = sum(ms)
+    value = world * children / (total_ms / 1e3)
+
+    def plain():
+        fin, st = quids.run(quids.it_t(ctx, wl["init"]), quids.it_t(ctx), ops, wl["max"])
+        return sum(x["num_object"] for x in st)
+    plain_ms = [timed(plain)[0] for _ in range(max(1, min(args.steps, 2)))]
+    fwd_ms = statistics.mean(plain_ms)
+
+    # e2e: initial state from pinned host memory, gradients back to the host
+    objects, begin, size, mag = wl["init"]
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()  # noqa: E731
+    h_in = tuple(pin(a) for a in (objects, begin, size, mag))
+    t0 = time.perf_counter()
+    e2e_children = 0
+    for _ in range(args.steps):
+        final, st = tape.forward(quids.it_t(ctx, h_in), ops, wl["max"], wl["every"])
+        tape.backward_observable(quids.OBS_QCGD_NUM_NODES)
+        e2e_children += sum(x["num_object"] for x in st)
+    t_e2e = time.perf_counter() - t0
+    peak, peak_kind = peaks()
+    achieved = abytes / (total_ms / 1e3) / 1e9
+    if rank == 0:
+        print(json.dumps({
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded generators; the reference publishes no dataset)",
+            "config": dict(wl["config"], parallelism=f"replicas x{world}",
+                           l2="flushed before every step (256 MiB write)",
+                           children_per_step=children // args.steps),
+            "adjoint": {"loss": loss, "grad": grad, "plain_forward_ms": fwd_ms,
+                        "forward_plus_backward_over_forward": (total_ms / args.steps) / fwd_ms},
+            "e2e": {"value": e2e_children / t_e2e, "unit": UNIT,
+                    "h2d_bytes_per_step": int(sum(a.nbytes for a in h_in)), "d2h_bytes_per_step": 6 * 8 + 8,
+                    "ms_per_step": 1e3 * t_e2e / args.steps},
+            "gpu_launches": int(launches),
+            "roofline": {"bound": "hbm", "kernel": "whole forward (all kernels; backward not counted)",
+                         "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "peak_source": peak_kind, "traffic": None},
+            "cpu_baseline": None,
+            "clocks": clk.summary(),
+            "wall_s_timed": t_wall,
+        }), flush=True)
 
 
 def cpu_baseline_batched(wl, packed):
@@ -553,6 +669,10 @@ def reference(args, rank, world):
     cores = os.cpu_count() or 1
     o.set_threads(cores)
     o.set_globals(wl["tolerance"], True, wl["align"])
+    if wl["name"] == "adjoint10":  # no adjoint in the reference: its forward, first 2 of the 20 steps
+        from quids_gb300 import workloads as W
+        wl["gates"] = W.qcgd_adjoint_ops(wl["angles"], 2)[0]
+        wl["config"] = dict(wl["config"], sample="reference forward only, first 2 of the 20 steps")
     init_packed = wl["init"] if wl["init"] is not None else qcgd_initial_cpu(wl, o)
 
     def one():
@@ -590,7 +710,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="circuit24", choices=["circuit24", "qcgd12", "qcgd10", "batch256"])
+    ap.add_argument("--config", default="circuit24", choices=["circuit24", "qcgd12", "qcgd10", "batch256", "adjoint10"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -603,6 +723,8 @@ def main():
             reference(args, rank, world)
         elif args.config == "batch256":
             ours_batched(args, rank, world)
+        elif args.config == "adjoint10":
+            ours_adjoint(args, rank, world)
         else:
             ours(args, rank, world)
     finally:

@@ -254,6 +254,7 @@ struct bkeep_layout {
         const prim::select_state &s = st[uinst[i]];
         return s.active && kf.key(i) == s.prefix;
     }
+    __device__ bool rank_needed() const { return true; }  // ranks are offset per instance
     __device__ bool select(uint64_t i, uint64_t tie_rank) const {
         const uint32_t g = uinst[i];
         const prim::select_state &s = st[g];
@@ -640,17 +641,10 @@ int simulate_batched(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule *rules_
     k_binst_factors<<<(G + 255) / 256, 256, 0, ctx->stream>>>(tot, G, obegin, maxn, (double *)out->inst_total.p,
                                                              bufp<double>(ctx, B_BFACTOR));
     QD_TRY(launched(ctx, 4));
-    if (maxsize <= 256) {
-        k_populate<instance_rules<Rule>, 256><<<grid_for(ctx, NS), prim::kThreads, 0, ctx->stream>>>(
-            rs, pv, bufp<uint64_t>(ctx, B_SCHILD), bufp<uint32_t>(ctx, B_CPAR), ctx->d_words + W_NS,
-            (const uint64_t *)out->begin.p, (const uint32_t *)out->size.p, (char *)out->objects.p,
-            (double2 *)out->mag.p, bufp<double>(ctx, B_BFACTOR), (const uint32_t *)out->inst.p, err);
-    } else {
-        k_populate<instance_rules<Rule>, 4096><<<grid_for(ctx, NS), prim::kThreads, 0, ctx->stream>>>(
-            rs, pv, bufp<uint64_t>(ctx, B_SCHILD), bufp<uint32_t>(ctx, B_CPAR), ctx->d_words + W_NS,
-            (const uint64_t *)out->begin.p, (const uint32_t *)out->size.p, (char *)out->objects.p,
-            (double2 *)out->mag.p, bufp<double>(ctx, B_BFACTOR), (const uint32_t *)out->inst.p, err);
-    }
+    k_populate<instance_rules<Rule>, no_post><<<grid_for(ctx, NS), prim::kThreads, 0, ctx->stream>>>(
+        rs, pv, bufp<uint64_t>(ctx, B_SCHILD), bufp<uint32_t>(ctx, B_CPAR), ctx->d_words + W_NS,
+        (const uint64_t *)out->begin.p, (const uint32_t *)out->size.p, (char *)out->objects.p, (double2 *)out->mag.p,
+        bufp<double>(ctx, B_BFACTOR), (const uint32_t *)out->inst.p, err, no_post{});
     QD_TRY(launched(ctx));
     if (inst_stats) {
         k_binst_stats<<<(G + 255) / 256, 256, 0, ctx->stream>>>(bufp<uint64_t>(ctx, B_CBEGIN), pbegin, ubegin,

@@ -19,6 +19,43 @@ using qd::host::dispatch_rule;
 
 namespace {
 
+// The modifiers that follow a rule in a run, applied to each survivor
+// right after its populate (in order, like the separate modifier launches
+// they replace).  An object a modifier does not fit sets the sticky modifier
+// status, as a separate modifier launch does.
+struct mod_chain {
+    static constexpr bool active = true;
+    static constexpr int kMax = 16;
+    int n = 0;
+    int32_t kind[kMax];
+    uint64_t bit[kMax], control[kMax];
+    int *status = nullptr;
+
+    template <class M>
+    __device__ static void apply(const M &mod, char *b, char *e, mag_t &m, int *err) {
+        if (!object_fits(mod, (uint32_t)(e - b))) {
+            prim::set_error(err, QUIDS_ERR_BAD_ARG);
+            return;
+        }
+        mod(b, e, m);
+    }
+    __device__ void operator()(char *b, char *e, mag_t &m, int *) const {
+        int *err = status;
+        for (int k = 0; k < n; ++k) {
+            switch (kind[k]) {
+            case QUIDS_MOD_CNOT: apply(rules::cnot{control[k], bit[k]}, b, e, m, err); break;
+            case QUIDS_MOD_X: apply(rules::xgate{bit[k]}, b, e, m, err); break;
+            case QUIDS_MOD_Y: apply(rules::ygate{bit[k]}, b, e, m, err); break;
+            case QUIDS_MOD_Z: apply(rules::zgate{bit[k]}, b, e, m, err); break;
+            case QUIDS_MOD_QCGD_STEP: apply(qcgd::step{}, b, e, m, err); break;
+            case QUIDS_MOD_QCGD_REVERSED_STEP: apply(qcgd::reversed_step{}, b, e, m, err); break;
+            }
+        }
+    }
+};
+
+bool chainable(int kind) { return kind >= QUIDS_MOD_CNOT && kind <= QUIDS_MOD_QCGD_REVERSED_STEP; }
+
 __global__ void k_set_words_zero(uint64_t *w, int n) {
     for (int i = threadIdx.x; i < n; i += blockDim.x) w[i] = 0;
 }
@@ -63,7 +100,12 @@ int quids_gpu_ctx_create(int device, quids_gpu_ctx **out) {
     if (!rc) ctx->num_sms = prop.multiProcessorCount;
     if (!rc) rc = cuda_status(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
     if (!rc) rc = cuda_status(cudaMalloc(&ctx->d_words, W_COUNT_WORDS * sizeof(uint64_t)));
-    if (!rc) rc = cuda_status(cudaMallocHost(&ctx->h_words, W_COUNT_WORDS * sizeof(uint64_t)));
+    if (!rc) rc = cuda_status(cudaHostAlloc((void **)&ctx->h_words, (W_COUNT_WORDS + 1) * sizeof(uint64_t),
+                                            cudaHostAllocMapped));
+    if (!rc) {
+        std::memset(ctx->h_words, 0, (W_COUNT_WORDS + 1) * sizeof(uint64_t));
+        rc = cuda_status(cudaHostGetDevicePointer((void **)&ctx->h_words_dev, ctx->h_words, 0));
+    }
     if (!rc) rc = cuda_status(cudaMalloc(&ctx->d_sel, 2 * sizeof(qd::prim::select_state)));
     if (!rc) rc = cuda_status(cudaMalloc(&ctx->d_hist, qd::prim::kBins * sizeof(unsigned long long)));
     if (!rc) rc = cuda_status(cudaEventCreate(&ctx->ev0));
@@ -268,13 +310,38 @@ int quids_gpu_run(quids_gpu_ctx *ctx, quids_gpu_state *a, quids_gpu_state *b, co
     if (!ctx || !a || !b || a == b || (!ops && n_ops) || !params || !final_index) return QUIDS_ERR_BAD_ARG;
     quids_gpu_state *cur = a, *other = b;
     uint64_t r = 0;
+    const quids_gpu_params prm = *params;
     for (uint64_t i = 0; i < n_ops; ++i) {
         const quids_gpu_op &op = ops[i];
         int rc;
         if (op.is_rule) {
-            rc = quids_gpu_simulate(ctx, cur, op.kind, &op.params, other, params, rule_stats ? rule_stats + r : nullptr);
+            // the modifiers up to the next rule run inside this rule's populate
+            mod_chain chain;
+            uint64_t j = i + 1;
+            while (j < n_ops && !ops[j].is_rule && chainable(ops[j].kind) && chain.n < mod_chain::kMax) {
+                chain.kind[chain.n] = ops[j].kind;
+                chain.bit[chain.n] = ops[j].params.bit;
+                chain.control[chain.n] = ops[j].params.control;
+                ++chain.n;
+                ++j;
+            }
+            if (chain.n) {
+                if (!ctx->buf[B_MODSTATUS].p) {
+                    QD_TRY(ensure(ctx->buf[B_MODSTATUS], sizeof(uint64_t)));
+                    QD_CUDA(cudaMemsetAsync(ctx->buf[B_MODSTATUS].p, 0, sizeof(uint64_t), ctx->stream));
+                }
+                chain.status = bufp<int>(ctx, B_MODSTATUS);
+            }
+            quids_gpu_step_stats *st = rule_stats ? rule_stats + r : nullptr;
+            rc = dispatch_rule(op.kind, &op.params, [&](auto rule) {
+                return chain.n ? simulate_rule(ctx, cur, rule, other, prm, st, chain)
+                               : simulate_rule(ctx, cur, rule, other, prm, st);
+            });
             ++r;
-            if (!rc) std::swap(cur, other);
+            if (!rc) {
+                std::swap(cur, other);
+                i = j - 1;
+            }
         } else {
             rc = quids_gpu_apply_modifier(ctx, cur, op.kind, &op.params);
         }

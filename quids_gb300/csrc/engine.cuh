@@ -7,6 +7,8 @@
 // members (see rules_qc.cuh); `simulate_rule<Rule>` instantiates the step
 // for it.
 #pragma once
+#include <algorithm>
+#include <atomic>
 #include <cstdint>
 #include <cstring>
 #include <limits>
@@ -83,6 +85,7 @@ enum qd_word {
     W_TMP,
     W_MAXNORM,    // bit pattern of the largest survivor norm
     W_ACC,        // 2 words: fixed-point total probability
+    W_DONE = W_ACC + 2,  // blocks done with the total (u32)
     W_COUNT_WORDS = 16
 };
 
@@ -92,7 +95,9 @@ struct quids_gpu_ctx {
     cudaStream_t stream = nullptr;
     qd_dbuf buf[B_COUNT];
     uint64_t *d_words = nullptr;             // W_COUNT_WORDS
-    uint64_t *h_words = nullptr;             // pinned mirror
+    uint64_t *h_words = nullptr;             // mapped pinned mirror: W_COUNT_WORDS words + a sequence word
+    uint64_t *h_words_dev = nullptr;         // its device address
+    uint64_t publish_seq = 0;
     qd::prim::select_state *d_sel = nullptr; // two states
     unsigned long long *d_hist = nullptr;    // 256
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -189,12 +194,38 @@ inline unsigned grid_for(quids_gpu_ctx *ctx, uint64_t n, int per_sm = 8) {
     return (unsigned)g;
 }
 
+// The step's words on the host, without a stream synchronisation: a
+// one-warp kernel copies them into mapped pinned memory and then writes a
+// sequence number; the host waits for that number (checking the stream for
+// errors as it waits) and reads the words.  The stream keeps running.
+static __global__ void k_publish_words(const uint64_t *w, volatile uint64_t *h, uint64_t seq) {
+    if (threadIdx.x < W_COUNT_WORDS) h[threadIdx.x] = w[threadIdx.x];
+    __threadfence_system();
+    __syncwarp();
+    if (threadIdx.x == 0) h[W_COUNT_WORDS] = seq;
+}
+
 inline int read_words(quids_gpu_ctx *ctx) {
-    QD_CUDA(cudaMemcpyAsync(ctx->h_words, ctx->d_words, W_COUNT_WORDS * sizeof(uint64_t),
-                            cudaMemcpyDeviceToHost, ctx->stream));
-    QD_CUDA(cudaStreamSynchronize(ctx->stream));
-    int st = (int)(int64_t)ctx->h_words[W_STATUS];
-    return st;
+    const uint64_t seq = ++ctx->publish_seq;
+    k_publish_words<<<1, 32, 0, ctx->stream>>>(ctx->d_words, ctx->h_words_dev, seq);
+    ctx->launches += 1;
+    QD_CUDA(cudaGetLastError());
+    volatile uint64_t *hw = ctx->h_words;
+    for (uint64_t it = 1; hw[W_COUNT_WORDS] != seq; ++it) {
+        if ((it & 1023) == 0) {
+            const cudaError_t e = cudaStreamQuery(ctx->stream);
+            if (e == cudaSuccess) {
+                if (hw[W_COUNT_WORDS] != seq) {  // the stream is done: read the words directly
+                    QD_CUDA(cudaMemcpy((void *)ctx->h_words, ctx->d_words, W_COUNT_WORDS * sizeof(uint64_t),
+                                       cudaMemcpyDeviceToHost));
+                }
+                break;
+            }
+            if (e != cudaErrorNotReady) return cuda_status(e);
+        }
+    }
+    std::atomic_thread_fence(std::memory_order_acquire);
+    return (int)(int64_t)hw[W_STATUS];
 }
 
 // bookkeeping after a launch: count it, report a launch error
@@ -217,6 +248,53 @@ static __global__ void k_take_status(int *src, uint64_t *status_word) {
 // stream-ordered write of one device word (no host synchronisation)
 inline int set_word(quids_gpu_ctx *ctx, qd_word w, uint64_t v) {
     k_set_word<<<1, 1, 0, ctx->stream>>>(ctx->d_words + w, v);
+    return launched(ctx);
+}
+
+// Start of a step, one launch: the step's words (zero but the parent
+// counts, and a sticky modifier status moved in) and `nzero` zeroed words of
+// look-back chains.
+static __global__ void __launch_bounds__(256)
+    k_step_begin(uint64_t *words, uint64_t n, uint64_t np, int *modstatus, uint64_t *zero, uint64_t nzero) {
+    const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid < W_COUNT_WORDS) {
+        uint64_t v = 0;
+        if (tid == W_N) v = n;
+        if (tid == W_NP) v = np;
+        if (tid == W_STATUS && modstatus) {
+            v = (uint64_t)(uint32_t)*modstatus;
+            *modstatus = 0;
+        }
+        words[tid] = v;
+    }
+    for (uint64_t i = tid; i < nzero; i += (uint64_t)gridDim.x * blockDim.x) zero[i] = 0;
+}
+
+// Several byte fills in one launch (regions 16-byte aligned).
+struct fill_set {
+    static constexpr int kMax = 6;
+    unsigned char *p[kMax];
+    uint64_t n[kMax];
+    uint32_t v[kMax];  // the byte replicated
+    int count;
+};
+static __global__ void __launch_bounds__(256) k_fill(fill_set f) {
+    const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (uint64_t)gridDim.x * blockDim.x;
+    for (int r = 0; r < f.count; ++r) {
+        const uint32_t w = f.v[r] * 0x01010101u;
+        const uint4 q = make_uint4(w, w, w, w);
+        const uint64_t n16 = f.n[r] / 16;
+        for (uint64_t i = tid; i < n16; i += stride) ((uint4 *)f.p[r])[i] = q;
+        for (uint64_t i = n16 * 16 + tid; i < f.n[r]; i += stride) f.p[r][i] = (unsigned char)f.v[r];
+    }
+}
+inline int fill(quids_gpu_ctx *ctx, const fill_set &f) {
+    uint64_t most = 0;
+    for (int r = 0; r < f.count; ++r) most = f.n[r] > most ? f.n[r] : most;
+    uint64_t g = (most / 16 + 255) / 256;
+    const uint64_t cap = (uint64_t)ctx->num_sms * 8;
+    g = g < 1 ? 1 : (g > cap ? cap : g);
+    k_fill<<<(unsigned)g, 256, 0, ctx->stream>>>(f);
     return launched(ctx);
 }
 
@@ -367,6 +445,22 @@ static __global__ void __launch_bounds__(prim::kThreads)
     }
 }
 
+// the same map written by the child-offset scan as each parent's offset is
+// known (entries beyond `cap` are left to k_tile_parents)
+struct tile_parents_epilogue {
+    uint64_t *tile_first;
+    uint64_t cap;  // entries
+    __device__ __forceinline__ void operator()(uint64_t p, uint64_t lo, uint64_t cnt, uint64_t np) const {
+        const uint64_t hi = lo + cnt;
+        for (uint64_t t = (lo + kTileChildren - 1) / kTileChildren; t * kTileChildren < hi && t < cap; ++t)
+            tile_first[t] = p;
+        if (p == np - 1) {
+            const uint64_t tiles = (hi + kTileChildren - 1) / kTileChildren;
+            if (tiles < cap) tile_first[tiles] = np - 1;
+        }
+    }
+};
+
 // Symbolic iteration (src/quids.hpp:705-719): per child, its magnitude,
 // size, hash and parent.  FAST: the rule's hash_child; otherwise
 // populate_child into a per-thread buffer of MAXC bytes followed by the
@@ -446,14 +540,22 @@ __global__ void __launch_bounds__(prim::kThreads)
     if ((threadIdx.x & 31) == 0 && bits) atomicMax(d_maxabs, bits);
 }
 
+// What runs on each survivor right after populate (the modifiers that
+// follow a rule in a run); nothing by default.
+struct no_post {
+    static constexpr bool active = false;
+    __device__ __forceinline__ void operator()(char *, char *, mag_t &, int *) const {}
+};
+
 // Finalize (src/quids.hpp:958-967) fused with normalisation (:1008-1013):
-// populate_child_simple of each survivor into the packed output (padding
-// zeroed) and mag /= sqrt(total) when that factor is not 1.
-template <class RS, int MAXC>
+// populate_child_simple of each survivor straight into its slot of the
+// packed output (padding zeroed), mag /= sqrt(total) when that factor is
+// not 1 (batched: the survivor's instance factor), then `post`.
+template <class RS, class Post>
 __global__ void __launch_bounds__(prim::kThreads)
     k_populate(RS rs, parents_view pv, const uint64_t *schild, const uint32_t *cpar, const uint64_t *d_ns,
                const uint64_t *obegin, const uint32_t *osize, char *objects, double2 *omag, const double *d_factor,
-               const uint32_t *finst, int *err) {
+               const uint32_t *finst, int *err, Post post) {
     const uint64_t ns = *d_ns;
     const double f0 = finst ? 1.0 : *d_factor;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ns; i += (uint64_t)gridDim.x * blockDim.x) {
@@ -463,21 +565,18 @@ __global__ void __launch_bounds__(prim::kThreads)
         const uint32_t cid = (uint32_t)(c - pv.cbeg[p]);
         const char *pb = pv.objects + pv.begin[oid];
         const char *pe = pb + pv.size[oid];
-        uint64_t buf[MAXC / 8];
-        rule_populate_simple(rs.get(oid), pb, pe, (char *)buf, cid);
-        uint32_t sz = osize[i];
-        if (sz > MAXC) {
-            prim::set_error(err, QUIDS_ERR_SIZE_BOUND);
-            sz = MAXC;
-        }
         const uint64_t ob = obegin[i], oe = obegin[i + 1];
+        const uint32_t sz = osize[i];
         char *dst = objects + ob;
-        copy_bytes(dst, (const char *)buf, sz);
+        rule_populate_simple(rs.get(oid), pb, pe, dst, cid);
         for (uint64_t q = ob + sz; q < oe; ++q) objects[q] = 0;
         const double f = finst ? d_factor[finst[i]] : f0;  // batched: the survivor's instance factor
-        if (f != 1.0) {
-            double2 m = omag[i];
-            omag[i] = make_double2(__ddiv_rn(m.x, f), __ddiv_rn(m.y, f));
+        if (f != 1.0 || Post::active) {
+            const double2 m = omag[i];
+            mag_t mm{m.x, m.y};
+            if (f != 1.0) mm = mag_t{__ddiv_rn(mm.re, f), __ddiv_rn(mm.im, f)};
+            post(dst, dst + sz, mm, err);
+            omag[i] = make_double2(mm.re, mm.im);
         }
     }
 }
@@ -705,6 +804,7 @@ struct keep_layout {
     uint64_t *obegin;
     uint64_t *schild;
     __device__ bool tie(uint64_t i) const { return st->active && kf.key(i) == st->prefix; }
+    __device__ bool rank_needed() const { return st->active && st->n_equal > st->k_rem; }
     __device__ bool select(uint64_t i, uint64_t tie_rank) const {
         if (!st->active) return true;
         uint64_t k = kf.key(i);
@@ -806,14 +906,14 @@ inline int launch_symbolic(quids_gpu_ctx *ctx, const RS &rule, const parents_vie
     return launched(ctx);
 }
 
-template <class RS, int MAXC>
+template <class RS, class Post>
 inline int launch_populate(quids_gpu_ctx *ctx, const RS &rule, const parents_view &pv, uint64_t ns,
-                           quids_gpu_state *out) {
-    k_populate<RS, MAXC><<<grid_for(ctx, ns), prim::kThreads, 0, ctx->stream>>>(
+                           quids_gpu_state *out, const Post &post) {
+    k_populate<RS, Post><<<grid_for(ctx, ns), prim::kThreads, 0, ctx->stream>>>(
         rule, pv, bufp<uint64_t>(ctx, B_SCHILD), bufp<uint32_t>(ctx, B_CPAR), ctx->d_words + W_NS,
         (const uint64_t *)out->begin.p,
         (const uint32_t *)out->size.p, (char *)out->objects.p, (double2 *)out->mag.p,
-        (const double *)(ctx->d_words + W_FACTOR), nullptr, (int *)(ctx->d_words + W_STATUS));
+        (const double *)(ctx->d_words + W_FACTOR), nullptr, (int *)(ctx->d_words + W_STATUS), post);
     return launched(ctx);
 }
 
@@ -836,15 +936,24 @@ inline int lookback_chain(quids_gpu_ctx *ctx, uint64_t n_cap, int slot, prim::lo
     lb.err = (int *)(ctx->d_words + W_STATUS);
     return QUIDS_OK;
 }
+// chain `slot` of a region zeroed beforehand (k_step_begin, k_fill)
+inline void lookback_view(quids_gpu_ctx *ctx, uint64_t n_cap, int slot, prim::lookback &lb) {
+    const uint64_t words = (n_cap + prim::kTile - 1) / prim::kTile + 2;
+    uint64_t *ws = bufp<uint64_t>(ctx, B_LOOKBACK) + (uint64_t)slot * words;
+    lb.status = ws + 1;
+    lb.counter = (uint32_t *)ws;
+    lb.err = (int *)(ctx->d_words + W_STATUS);
+}
+inline uint64_t lookback_words(uint64_t n_cap) { return 3 * ((n_cap + prim::kTile - 1) / prim::kTile + 2); }
 inline unsigned lookback_grid(quids_gpu_ctx *ctx, uint64_t n) {
     uint64_t tiles = (n + prim::kTile - 1) / prim::kTile;
     uint64_t cap = (uint64_t)ctx->num_sms * 4;
     return (unsigned)(tiles < 1 ? 1 : (tiles < cap ? tiles : cap));
 }
 
-template <class Rule>
+template <class Rule, class Post = no_post>
 int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, quids_gpu_state *out,
-                  const quids_gpu_params &prm, quids_gpu_step_stats *stats) {
+                  const quids_gpu_params &prm, quids_gpu_step_stats *stats, const Post &post = Post{}) {
     const single_rule<Rule> rule{rule_};
     if (!ctx || !in || !out || in == out || in->ctx != ctx || out->ctx != ctx) return QUIDS_ERR_BAD_ARG;
     const trunc_key tk{prm.simple_truncation == 0, prm.seed};
@@ -901,20 +1010,21 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, qu
         return QUIDS_OK;
     };
     if (timing) QD_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
-    QD_CUDA(cudaMemsetAsync(ctx->d_words, 0, W_COUNT_WORDS * sizeof(uint64_t), ctx->stream));
-    if (ctx->buf[B_MODSTATUS].p) {  // an earlier modifier met an unfit object
-        k_take_status<<<1, 1, 0, ctx->stream>>>(bufp<int>(ctx, B_MODSTATUS), ctx->d_words + W_STATUS);
-        QD_TRY(launched(ctx));
-    }
+    // the step's words, the sticky status of earlier modifiers (an unfit
+    // object), and the zeroed look-back chains of stage 0, in one launch
+    QD_TRY(ensure(ctx->buf[B_NCHILD], (N ? N : 1) * sizeof(uint32_t)));
+    QD_TRY(ensure(ctx->buf[B_LOOKBACK], lookback_words(N) * sizeof(uint64_t)));
+    const uint64_t nzero0 = N ? lookback_words(N) : 0;
+    k_step_begin<<<(unsigned)std::min<uint64_t>((nzero0 + 255) / 256 + 1, (uint64_t)ctx->num_sms * 4), 256, 0,
+                   ctx->stream>>>(
+        ctx->d_words, N, maxn < N ? 0 : N, bufp<int>(ctx, B_MODSTATUS), bufp<uint64_t>(ctx, B_LOOKBACK), nzero0);
+    QD_TRY(launched(ctx));
     if (N == 0) return finish(true);
     int *err = (int *)(ctx->d_words + W_STATUS);
 
     // ---- stage 0: num_child (src/quids.hpp:548-569), parent pre-truncation
     // (src/quids.hpp:613-642, ties by lower index), child offsets (:666-673)
     begin_stage(0);
-    QD_TRY(set_word(ctx, W_N, N));
-    QD_TRY(ensure(ctx->buf[B_NCHILD], N * sizeof(uint32_t)));
-    QD_TRY(ensure(ctx->buf[B_LOOKBACK], 3 * ((N + prim::kTile - 1) / prim::kTile + 2) * sizeof(uint64_t)));
     k_num_child<<<grid_for(ctx, N), prim::kThreads, 0, ctx->stream>>>(
         rule, (const char *)in->objects.p, (const uint64_t *)in->begin.p, (const uint32_t *)in->size.p, N,
         bufp<uint32_t>(ctx, B_NCHILD), (unsigned long long *)(ctx->d_words + W_MAXSIZE), err);
@@ -926,25 +1036,28 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, qu
         key_parent_norm k1{(const double2 *)in->mag.p, tk};
         QD_TRY(radix_select(ctx, ctx->d_words + W_N, N, maxn, k1));
         prim::lookback lb, lbt;
-        QD_TRY(lookback_chain(ctx, N, 0, lb));
-        QD_TRY(lookback_chain(ctx, N, 2, lbt));
+        lookback_view(ctx, N, 0, lb);
+        lookback_view(ctx, N, 2, lbt);
         keep_parents kp{k1, ctx->d_sel, bufp<uint64_t>(ctx, B_PIDX)};
         prim::k_compact_ranked<<<lookback_grid(ctx, N), prim::kThreads, 0, ctx->stream>>>(
             kp, ctx->d_words + W_N, ctx->d_words + W_NP, lb, lbt);
         QD_TRY(launched(ctx));
         NP = maxn;
         pidx = bufp<uint64_t>(ctx, B_PIDX);
-    } else {
-        QD_TRY(set_word(ctx, W_NP, N));
     }
     s.num_parents_kept = NP;
     QD_TRY(ensure(ctx->buf[B_CBEGIN], (NP + 1) * sizeof(uint64_t)));
+    // the scan also writes the symbolic pass's tile -> first parent map, as
+    // far as the map's buffer already reaches
+    uint64_t *tile_map = bufp<uint64_t>(ctx, B_TILEPAR);
+    uint64_t tile_map_cap = ctx->buf[B_TILEPAR].cap / sizeof(uint64_t);
     {
         prim::lookback lb;
-        QD_TRY(lookback_chain(ctx, N, 1, lb));
+        lookback_view(ctx, N, 1, lb);
         scan_nchild f{bufp<uint32_t>(ctx, B_NCHILD), pidx};
         prim::k_scan_excl<<<lookback_grid(ctx, NP), prim::kThreads, 0, ctx->stream>>>(
-            f, ctx->d_words + W_NP, bufp<uint64_t>(ctx, B_CBEGIN), ctx->d_words + W_NC, lb);
+            f, ctx->d_words + W_NP, bufp<uint64_t>(ctx, B_CBEGIN), ctx->d_words + W_NC, lb,
+            tile_parents_epilogue{tile_map, tile_map_cap});
         QD_TRY(launched(ctx));
     }
     end_stage(0);
@@ -1001,6 +1114,7 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, qu
             scan_nchild f{bufp<uint32_t>(ctx, B_NCHILD), pidx};
             prim::k_scan_excl<<<lookback_grid(ctx, NP), prim::kThreads, 0, ctx->stream>>>(
                 f, ctx->d_words + W_NP, bufp<uint64_t>(ctx, B_CBEGIN), ctx->d_words + W_NC, lbs);
+            tile_map_cap = 0;  // the map of the first scan is stale
             QD_TRY(launched(ctx, 2));
             st = read_words(ctx);
             if (st) return st;
@@ -1046,7 +1160,7 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, qu
     QD_TRY(ensure(ctx->buf[B_KEYS], (M + 1) * sizeof(prim::table_slot)));
     QD_TRY(ensure(ctx->buf[B_ACC], 4 * (M + 1) * sizeof(uint64_t)));
     QD_TRY(ensure(ctx->buf[B_SCHILD], NSB * sizeof(uint64_t)));
-    QD_TRY(ensure(ctx->buf[B_LOOKBACK], 3 * (tiles_nc + 2) * sizeof(uint64_t)));
+    QD_TRY(ensure(ctx->buf[B_LOOKBACK], 4 * (tiles_nc + 2) * sizeof(uint64_t)));
     QD_TRY(ensure(out->begin, (NSB + 1) * sizeof(uint64_t)));
     QD_TRY(ensure(out->size, NSB * sizeof(uint32_t)));
     QD_TRY(ensure(out->mag, NSB * sizeof(double2)));
@@ -1073,9 +1187,11 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, qu
 
     // ---- stage 1: symbolic iteration (src/quids.hpp:647-721)
     begin_stage(1);
-    k_tile_parents<<<grid_for(ctx, NP), prim::kThreads, 0, ctx->stream>>>(bufp<uint64_t>(ctx, B_CBEGIN), NP, sym_tiles,
-                                                                         bufp<uint64_t>(ctx, B_TILEPAR));
-    QD_TRY(launched(ctx));
+    if (sym_tiles + 1 > tile_map_cap || bufp<uint64_t>(ctx, B_TILEPAR) != tile_map) {
+        k_tile_parents<<<grid_for(ctx, NP), prim::kThreads, 0, ctx->stream>>>(bufp<uint64_t>(ctx, B_CBEGIN), NP,
+                                                                             sym_tiles, bufp<uint64_t>(ctx, B_TILEPAR));
+        QD_TRY(launched(ctx));
+    }
     region_count rc{M, regions ? R : 0u, regions ? bufp<unsigned int>(ctx, B_RHIST) : nullptr};
     if (maxsize <= 256) {
         QD_TRY((launch_symbolic<single_rule<Rule>, 256>(ctx, rule, pv, NC, fast, rc)));
@@ -1087,10 +1203,16 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, qu
     // ---- stage 2: collision table (src/quids.hpp:726-809)
     begin_stage(2);
     prim::table tb{bufp<prim::table_slot>(ctx, B_KEYS), bufp<unsigned long long>(ctx, B_ACC), M, 65536u};
-    QD_CUDA(cudaMemsetAsync(tb.slots, 0xff, (M + 1) * sizeof(prim::table_slot), ctx->stream));
-    QD_CUDA(cudaMemsetAsync(tb.acc + 4 * M, 0, 4 * sizeof(uint64_t), ctx->stream));  // the extra slot
-    QD_CUDA(cudaMemsetAsync(ctx->buf[B_NOTREP].p, 0, NC, ctx->stream));
-    QD_CUDA(cudaMemsetAsync(ctx->buf[B_HASJOIN].p, 0, NC, ctx->stream));
+    {  // table slots free, the extra slot's sum, the group marks, the look-back chains of stages 3-4
+        fill_set f{};
+        f.p[0] = (unsigned char *)tb.slots, f.n[0] = (M + 1) * sizeof(prim::table_slot), f.v[0] = 0xff;
+        f.p[1] = (unsigned char *)(tb.acc + 4 * M), f.n[1] = 4 * sizeof(uint64_t), f.v[1] = 0;
+        f.p[2] = bufp<unsigned char>(ctx, B_NOTREP), f.n[2] = NC, f.v[2] = 0;
+        f.p[3] = bufp<unsigned char>(ctx, B_HASJOIN), f.n[3] = NC, f.v[3] = 0;
+        f.p[4] = bufp<unsigned char>(ctx, B_LOOKBACK), f.n[4] = 4 * (tiles_nc + 2) * sizeof(uint64_t), f.v[4] = 0;
+        f.count = 5;
+        QD_TRY(fill(ctx, f));
+    }
     uint8_t *not_rep = bufp<uint8_t>(ctx, B_NOTREP), *has_join = bufp<uint8_t>(ctx, B_HASJOIN);
     const unsigned long long *d_maxabs = (const unsigned long long *)(ctx->d_words + W_MAXABS);
     if (!regions) {
@@ -1132,8 +1254,8 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, qu
     begin_stage(3);
     if (!may_truncate) {
         prim::lookback lbc, lbb;
-        QD_TRY(lookback_chain(ctx, NC, 0, lbc));
-        QD_TRY(lookback_chain(ctx, NC, 1, lbb));
+        lookback_view(ctx, NC, 0, lbc);
+        lookback_view(ctx, NC, 1, lbb);
         groups_layout f{gv, bufp<uint32_t>(ctx, B_CSIZE), align, (double2 *)out->mag.p, (uint32_t *)out->size.p,
                         (uint64_t *)out->begin.p, bufp<uint64_t>(ctx, B_SCHILD)};
         prim::k_compact_layout<groups_layout, false><<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
@@ -1143,7 +1265,7 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, qu
         end_stage(3);
     } else {
         prim::lookback lb;
-        QD_TRY(lookback_chain(ctx, NC, 0, lb));
+        lookback_view(ctx, NC, 3, lb);
         groups_collect f{gv, bufp<uint64_t>(ctx, B_UCHILD), bufp<double2>(ctx, B_UMAG), bufp<uint64_t>(ctx, B_UNORM)};
         prim::k_compact<<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(f, ctx->d_words + W_NC,
                                                                                    ctx->d_words + W_NU, lb);
@@ -1153,9 +1275,9 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, qu
         key_unorm k1{bufp<uint64_t>(ctx, B_UNORM), bufp<uint64_t>(ctx, B_UCHILD), tk};
         QD_TRY(radix_select(ctx, ctx->d_words + W_NU, NC, maxc, k1));
         prim::lookback lbc, lbb, lbt;
-        QD_TRY(lookback_chain(ctx, NC, 0, lbt));
-        QD_TRY(lookback_chain(ctx, NC, 1, lbc));
-        QD_TRY(lookback_chain(ctx, NC, 2, lbb));
+        lookback_view(ctx, NC, 0, lbt);
+        lookback_view(ctx, NC, 1, lbc);
+        lookback_view(ctx, NC, 2, lbb);
         keep_layout kl{k1, bufp<uint64_t>(ctx, B_UNORM), bufp<uint64_t>(ctx, B_UCHILD), bufp<double2>(ctx, B_UMAG),
                        ctx->d_sel, bufp<uint32_t>(ctx, B_CSIZE), align, (double2 *)out->mag.p,
                        (uint32_t *)out->size.p, (uint64_t *)out->begin.p, bufp<uint64_t>(ctx, B_SCHILD)};
@@ -1177,22 +1299,17 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, qu
     // ---- stage 5: total probability (src/quids.hpp:1002-1008), exact
     begin_stage(5);
     prim::k_fix_total<<<grid_for(ctx, NS, 4), prim::kThreads, 0, ctx->stream>>>(
-        (const double2 *)out->mag.p, ctx->d_words + W_NS, d_maxnorm, (unsigned long long *)(ctx->d_words + W_ACC));
-    prim::k_fix_finalize<<<1, 1, 0, ctx->stream>>>((const unsigned long long *)(ctx->d_words + W_ACC),
-                                                   ctx->d_words + W_NS, d_maxnorm, (double *)(ctx->d_words + W_TOTAL),
-                                                   (double *)(ctx->d_words + W_FACTOR));
-    QD_TRY(launched(ctx, 2));
+        (const double2 *)out->mag.p, ctx->d_words + W_NS, d_maxnorm, (unsigned long long *)(ctx->d_words + W_ACC),
+        (unsigned int *)(ctx->d_words + W_DONE), (double *)(ctx->d_words + W_TOTAL),
+        (double *)(ctx->d_words + W_FACTOR));
+    QD_TRY(launched(ctx));
     QD_CUDA(cudaMemcpyAsync(out->d_total.p, ctx->d_words + W_TOTAL, sizeof(double), cudaMemcpyDeviceToDevice,
                             ctx->stream));
     end_stage(5);
 
     // ---- stage 6: finalize populate (src/quids.hpp:958-967) + normalisation
     begin_stage(6);
-    if (maxsize <= 256) {
-        QD_TRY((launch_populate<single_rule<Rule>, 256>(ctx, rule, pv, NS, out)));
-    } else {
-        QD_TRY((launch_populate<single_rule<Rule>, 4096>(ctx, rule, pv, NS, out)));
-    }
+    QD_TRY((launch_populate<single_rule<Rule>, Post>(ctx, rule, pv, NS, out, post)));
     end_stage(6);
     out->n = NS;
     out->nbytes = outbytes;

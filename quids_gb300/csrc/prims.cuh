@@ -122,6 +122,59 @@ static __device__ uint64_t tile_prefix(const lookback &lb, uint32_t tile, uint64
     return p;
 }
 
+// Exclusive prefixes of one tile on two chains at once: warp 0 looks back on
+// chain a while warp 1 looks back on chain b.
+static __device__ void tile_prefix2(const lookback &la, uint64_t agg_a, const lookback &lbb, uint64_t agg_b,
+                                    uint32_t tile, uint64_t *bcast2, uint64_t &pa, uint64_t &pb) {
+    const int warp = threadIdx.x >> 5;
+    if (warp < 2) {
+        const lookback &lb = warp == 0 ? la : lbb;
+        const uint64_t aggregate = warp == 0 ? agg_a : agg_b;
+        const int lane = threadIdx.x & 31;
+        uint64_t prefix = 0;
+        if (tile == 0) {
+            if (lane == 0) st_volatile_u64(&lb.status[0], kFlagInc | (aggregate & kValMask));
+        } else {
+            if (lane == 0) st_volatile_u64(&lb.status[tile], kFlagAgg | (aggregate & kValMask));
+            int64_t base = (int64_t)tile - 1;
+            bool failed = false;
+            while (true) {
+                int64_t j = base - lane;
+                uint64_t s = kFlagInc;
+                if (j >= 0) {
+                    uint32_t it = 0;
+                    s = ld_volatile_u64(&lb.status[j]);
+                    while ((s >> 62) == 0 && ++it < kSpinLimit) {
+                        __nanosleep(64);
+                        s = ld_volatile_u64(&lb.status[j]);
+                    }
+                    if ((s >> 62) == 0) {
+                        failed = true;
+                        s = kFlagInc;
+                    }
+                }
+                unsigned inc = __ballot_sync(0xffffffffu, (s >> 62) == 2);
+                uint64_t v = s & kValMask;
+                if (inc) {
+                    int first = __ffs(inc) - 1;
+                    if (lane > first) v = 0;
+                    prefix += warp_sum(v);
+                    break;
+                }
+                prefix += warp_sum(v);
+                base -= 32;
+            }
+            if (__any_sync(0xffffffffu, failed) && lane == 0) set_error(lb.err, QUIDS_ERR_TIMEOUT);
+            if (lane == 0) st_volatile_u64(&lb.status[tile], kFlagInc | ((prefix + aggregate) & kValMask));
+        }
+        if (lane == 0) bcast2[warp] = prefix;
+    }
+    __syncthreads();
+    pa = bcast2[0];
+    pb = bcast2[1];
+    __syncthreads();
+}
+
 __device__ __forceinline__ uint32_t next_tile(const lookback &lb, uint32_t *sm_tile) {
     if (threadIdx.x == 0) *sm_tile = atomicAdd(lb.counter, 1u);
     __syncthreads();
@@ -133,9 +186,14 @@ __device__ __forceinline__ uint32_t next_tile(const lookback &lb, uint32_t *sm_t
 // --------------------------------------------------------------- scan
 // out[i] = sum_{j<i} f(j) for i in [0, n], *total = sum; f(i) is called
 // exactly once per item (it may have side effects, e.g. gathers).
-template <class F>
+struct no_epilogue {
+    __device__ __forceinline__ void operator()(uint64_t, uint64_t, uint64_t, uint64_t) const {}
+};
+
+// E::operator()(i, out[i], f(i), n) runs once per item after its prefix is known.
+template <class F, class E = no_epilogue>
 __global__ void __launch_bounds__(kThreads) k_scan_excl(F f, const uint64_t *d_n, uint64_t *out,
-                                                         uint64_t *d_total, lookback lb) {
+                                                         uint64_t *d_total, lookback lb, E epi = E{}) {
     __shared__ uint64_t sm[kThreads / 32 + 1];
     __shared__ uint64_t bcast;
     __shared__ uint32_t sm_tile;
@@ -167,7 +225,10 @@ __global__ void __launch_bounds__(kThreads) k_scan_excl(F f, const uint64_t *d_n
 #pragma unroll
         for (int k = 0; k < kItems; ++k) {
             uint64_t i = base + k;
-            if (i < n) out[i] = run;
+            if (i < n) {
+                out[i] = run;
+                epi(i, run, v[k], n);
+            }
             run += v[k];
         }
         if (tile == ntiles - 1 && threadIdx.x == kThreads - 1) {
@@ -561,7 +622,9 @@ static __global__ void __launch_bounds__(kThreads)
 // padded size, P::norm(i) -> double, P::emit(i, j, byte_offset).  With TIES,
 // P::tie(i) -> bool marks the items equal to a selection threshold and
 // tie_rank is the item's rank among them in item order (a third look-back
-// chain), so a selection can take the first ties.  The largest selected norm
+// chain), so a selection can take the first ties; P::rank_needed() -> bool
+// (the same for every thread) skips the ranking when the selection keeps
+// every tie, and select then gets tie_rank 0.  The largest selected norm
 // goes to *d_maxnorm (as IEEE bits) when d_maxnorm is not null.  At the end:
 // *d_count, *d_bytes and begin_out[count] = total bytes.
 template <class P, bool TIES>
@@ -582,14 +645,17 @@ __global__ void __launch_bounds__(kThreads) k_compact_layout(P p, const uint64_t
         }
         return;
     }
+    __shared__ uint64_t bcast2[2];
     unsigned long long mx = 0;
+    bool ranked = false;
+    if constexpr (TIES) ranked = p.rank_needed();  // uniform over the launch
     while (true) {
         uint32_t tile = next_tile(lb_count, &sm_tile);
         if (tile >= ntiles) break;
         const uint64_t base = (uint64_t)tile * kTile + (uint64_t)threadIdx.x * kItems;
         uint64_t rank = 0;
         uint32_t ties = 0;
-        if constexpr (TIES) {
+        if (ranked) {
             uint64_t tcnt = 0;
 #pragma unroll
             for (int k = 0; k < kItems; ++k) {
@@ -620,8 +686,8 @@ __global__ void __launch_bounds__(kThreads) k_compact_layout(P p, const uint64_t
         uint64_t agg_c, agg_b;
         uint64_t excl_c = block_excl_scan(cnt, sm, agg_c);
         uint64_t excl_b = block_excl_scan(bytes, sm, agg_b);
-        uint64_t pre_c = tile_prefix(lb_count, tile, agg_c, &bcast);
-        uint64_t pre_b = tile_prefix(lb_bytes, tile, agg_b, &bcast);
+        uint64_t pre_c, pre_b;
+        tile_prefix2(lb_count, agg_c, lb_bytes, agg_b, tile, bcast2, pre_c, pre_b);
         uint64_t j = pre_c + excl_c, off = pre_b + excl_b;
 #pragma unroll
         for (int k = 0; k < kItems; ++k)
@@ -649,11 +715,14 @@ __global__ void __launch_bounds__(kThreads) k_compact_layout(P p, const uint64_t
 // Total probability (src/quids.hpp:1002-1008) of the n magnitudes, exact:
 // every norm is converted to 128-bit fixed point with F = fix_scale(max
 // norm, n) and the integers are summed (any order gives the same bits).
-// One fixed-point atomic add per block into acc[2] (zero beforehand).
-static __global__ void __launch_bounds__(kThreads) k_fix_total(const double2 *mag, const uint64_t *d_n,
-                                                                const unsigned long long *d_maxnorm,
-                                                                unsigned long long *acc) {
+// One fixed-point atomic add per block into acc[2] (zero beforehand); the
+// last block to finish (ticket from *done, zero beforehand) converts the
+// sum: total = acc 2^-F, factor = sqrt(total).
+static __global__ void __launch_bounds__(kThreads)
+    k_fix_total(const double2 *mag, const uint64_t *d_n, const unsigned long long *d_maxnorm,
+                unsigned long long *acc, unsigned int *done, double *d_total, double *d_factor) {
     __shared__ fix128 sm[kThreads / 32];
+    __shared__ bool last;
     const uint64_t n = *d_n;
     const int F = fix_scale(__longlong_as_double((long long)*d_maxnorm), n);
     fix128 a{0, 0};
@@ -672,16 +741,17 @@ static __global__ void __launch_bounds__(kThreads) k_fix_total(const double2 *ma
         fix128 t{0, 0};
         for (int w = 0; w < kThreads / 32; ++w) t = fix_add(t, sm[w]);
         fix_atomic_add(acc, t);
+        __threadfence();
+        last = atomicAdd(done, 1u) == gridDim.x - 1;
     }
-}
-
-// total = acc * 2^-F, factor = sqrt(total)
-static __global__ void k_fix_finalize(const unsigned long long *acc, const uint64_t *d_n,
-                                      const unsigned long long *d_maxnorm, double *d_total, double *d_factor) {
-    const int F = fix_scale(__longlong_as_double((long long)*d_maxnorm), *d_n);
-    const double t = from_fix(fix128{acc[0], acc[1]}, F);
-    *d_total = t;
-    *d_factor = __dsqrt_rn(t);
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        __threadfence();
+        const fix128 tot{atomicAdd(&acc[0], 0ull), atomicAdd(&acc[1], 0ull)};
+        const double t = from_fix(tot, F);
+        *d_total = t;
+        *d_factor = __dsqrt_rn(t);
+    }
 }
 
 }  // namespace qd::prim
