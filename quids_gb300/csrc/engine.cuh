@@ -56,6 +56,7 @@ enum qd_buf_id {
     B_TILEPAR,     // u64 [tiles+1] first parent of each tile of children
     B_CPAR,        // u32 [NC] kept-parent index of each child
     B_MODSTATUS,   // int: sticky error of modifier launches (reported by the next step)
+    B_LBEG,        // u64 [NP+1] leader offsets of the grouped symbolic pass
     // batched steps
     B_RULES,       // Rule [G] per-instance rules
     B_BCOUNT,      // u64 [4G] per-instance tie counts and fixed-point totals
@@ -300,6 +301,13 @@ inline int fill(quids_gpu_ctx *ctx, const fill_set &f) {
 
 
 // ---------------------------------------------------------- rule traits
+// rules whose children come in groups sharing factor prefixes
+// (grouped_children = true, template expand_group<H>(pb, pe, e, s, mag, emit))
+template <class R, class = void>
+struct has_grouped : std::false_type {};
+template <class R>
+struct has_grouped<R, std::void_t<decltype(R::grouped_children)>> : std::bool_constant<R::grouped_children> {};
+
 template <class R, class = void>
 struct has_hash_child : std::false_type {};
 template <class R>
@@ -447,19 +455,20 @@ static __global__ void __launch_bounds__(prim::kThreads)
 
 // the same map written by the child-offset scan as each parent's offset is
 // known (entries beyond `cap` are left to k_tile_parents)
-struct tile_parents_epilogue {
+template <uint64_t TILE>
+struct tile_map_epilogue {
     uint64_t *tile_first;
     uint64_t cap;  // entries
     __device__ __forceinline__ void operator()(uint64_t p, uint64_t lo, uint64_t cnt, uint64_t np) const {
         const uint64_t hi = lo + cnt;
-        for (uint64_t t = (lo + kTileChildren - 1) / kTileChildren; t * kTileChildren < hi && t < cap; ++t)
-            tile_first[t] = p;
+        for (uint64_t t = (lo + TILE - 1) / TILE; t * TILE < hi && t < cap; ++t) tile_first[t] = p;
         if (p == np - 1) {
-            const uint64_t tiles = (hi + kTileChildren - 1) / kTileChildren;
+            const uint64_t tiles = (hi + TILE - 1) / TILE;
             if (tiles < cap) tile_first[tiles] = np - 1;
         }
     }
 };
+using tile_parents_epilogue = tile_map_epilogue<kTileChildren>;
 
 // Symbolic iteration (src/quids.hpp:705-719): per child, its magnitude,
 // size, hash and parent.  FAST: the rule's hash_child; otherwise
@@ -546,6 +555,97 @@ struct no_post {
     static constexpr bool active = false;
     __device__ __forceinline__ void operator()(char *, char *, mag_t &, int *) const {}
 };
+
+// Grouped symbolic iteration for rules with grouped_children: a parent
+// with 2^s children (one factor per site) is handled by "leaders", each
+// expanding the 2^H children whose ids share their low s-H bits
+// (expand_group); parents with fewer than H sites have one leader that
+// walks its children one by one.  The leaders of each parent come from a
+// scan of leader counts (lbeg).  The output is that of k_symbolic.
+constexpr int kGroupBits = 2;
+constexpr int kLeaderTile = prim::kThreads;          // leaders per tile
+constexpr int kStagedLeaderParents = 4 * kLeaderTile;
+struct scan_leaders {
+    const uint32_t *nchild;
+    const uint64_t *pidx;
+    __device__ uint64_t operator()(uint64_t i) const {
+        const uint32_t nc = nchild[pidx ? pidx[i] : i];
+        if (nc == 0) return 0;
+        const int s = __ffs((int)nc) - 1;  // nc = 2^s
+        return s >= kGroupBits ? (uint64_t)(nc >> kGroupBits) : 1;
+    }
+};
+using leader_tile_epilogue = tile_map_epilogue<kLeaderTile>;
+
+template <class RS>
+__global__ void __launch_bounds__(prim::kThreads)
+    k_symbolic_grouped(RS rs, parents_view pv, const uint64_t *lbeg, const uint64_t *tile_first, const uint64_t *d_nl,
+                       uint64_t *hash, double2 *cmag, uint32_t *csize, uint32_t *cpar,
+                       unsigned long long *d_maxabs) {
+    using Rule = typename RS::rule_type;
+    constexpr int H = kGroupBits;
+    __shared__ uint64_t s_lb[kStagedLeaderParents + 1];
+    const uint64_t nl = *d_nl;
+    const uint64_t ntiles = (nl + kLeaderTile - 1) / kLeaderTile;
+    unsigned long long mx = 0;  // IEEE bits of the largest |component| (ordered like the values)
+    for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const uint64_t plo = tile_first[t], phi = tile_first[t + 1];
+        const int count = phi - plo + 1 <= (uint64_t)kStagedLeaderParents ? (int)(phi - plo + 1) : -1;
+        __syncthreads();  // the previous tile is done with s_lb
+        for (int k = threadIdx.x; k <= count; k += blockDim.x) s_lb[k] = lbeg[plo + k];
+        __syncthreads();
+        const uint64_t l = t * kLeaderTile + threadIdx.x;
+        if (l >= nl) continue;
+        uint64_t p;
+        if (count > 0) {
+            int lo = 0, hi = count;  // s_lb[lo] <= l < s_lb[hi]
+            while (hi - lo > 1) {
+                const int mid = (lo + hi) >> 1;
+                if (s_lb[mid] <= l) lo = mid; else hi = mid;
+            }
+            p = plo + (uint64_t)lo;
+        } else {
+            p = parent_of(lbeg, pv.np, l);
+        }
+        const uint64_t oid = pv.pidx ? pv.pidx[p] : p;
+        const uint64_t c0 = pv.cbeg[p];
+        const uint64_t nch = pv.cbeg[p + 1] - c0;
+        const int s = __ffsll((long long)nch) - 1;
+        const uint32_t e = (uint32_t)(l - lbeg[p]);
+        const char *pb = pv.objects + pv.begin[oid];
+        const char *pe = pb + pv.size[oid];
+        const double2 pm = pv.mag[oid];
+        const Rule &rule = rs.get(oid);
+        auto out = [&](uint64_t c, uint64_t h, const mag_t &m, uint32_t sz) {
+            hash[c] = rs.tag(h, oid);
+            cmag[c] = make_double2(m.re, m.im);
+            csize[c] = sz;
+            cpar[c] = (uint32_t)p;
+            const unsigned long long a = (unsigned long long)__double_as_longlong(m.re) & 0x7fffffffffffffffull;
+            const unsigned long long b = (unsigned long long)__double_as_longlong(m.im) & 0x7fffffffffffffffull;
+            const unsigned long long ab = a > b ? a : b;
+            mx = mx > ab ? mx : ab;
+        };
+        if (s >= H) {
+            rule.template expand_group<H>(pb, pe, e, s, mag_t{pm.x, pm.y},
+                                          [&](uint32_t j, uint64_t h, const mag_t &m, uint32_t sz) {
+                                              out(c0 + e + ((uint64_t)j << (s - H)), h, m, sz);
+                                          });
+        } else {
+            for (uint32_t cid = 0; cid < (uint32_t)nch; ++cid) {
+                mag_t m{pm.x, pm.y};
+                uint32_t sz = 0;
+                const uint64_t h = rule.hash_child(pb, pe, cid, sz, m);
+                out(c0 + cid, h, m, sz);
+            }
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long y = __shfl_xor_sync(0xffffffffu, mx, o);
+        mx = mx > y ? mx : y;
+    }
+    if ((threadIdx.x & 31) == 0 && mx) atomicMax(d_maxabs, mx);
+}
 
 // Finalize (src/quids.hpp:958-967) fused with normalisation (:1008-1013):
 // populate_child_simple of each survivor straight into its slot of the
@@ -1187,16 +1287,38 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, qu
 
     // ---- stage 1: symbolic iteration (src/quids.hpp:647-721)
     begin_stage(1);
-    if (sym_tiles + 1 > tile_map_cap || bufp<uint64_t>(ctx, B_TILEPAR) != tile_map) {
-        k_tile_parents<<<grid_for(ctx, NP), prim::kThreads, 0, ctx->stream>>>(bufp<uint64_t>(ctx, B_CBEGIN), NP,
-                                                                             sym_tiles, bufp<uint64_t>(ctx, B_TILEPAR));
-        QD_TRY(launched(ctx));
+    bool grouped = false;
+    if constexpr (has_grouped<Rule>::value) grouped = fast && !regions;
+    if constexpr (has_grouped<Rule>::value) if (grouped) {  // leader offsets and tile map, then the grouped pass
+        const uint64_t ltiles_cap = NC / kLeaderTile + 2;  // leaders <= children
+        QD_TRY(ensure(ctx->buf[B_LBEG], (NP + 1) * sizeof(uint64_t)));
+        QD_TRY(ensure(ctx->buf[B_TILEPAR], ltiles_cap * sizeof(uint64_t)));
+        prim::lookback lb;
+        QD_TRY(lookback_chain(ctx, NP, 0, lb));
+        scan_leaders f{bufp<uint32_t>(ctx, B_NCHILD), pidx};
+        prim::k_scan_excl<<<lookback_grid(ctx, NP), prim::kThreads, 0, ctx->stream>>>(
+            f, ctx->d_words + W_NP, bufp<uint64_t>(ctx, B_LBEG), ctx->d_words + W_TMP, lb,
+            leader_tile_epilogue{bufp<uint64_t>(ctx, B_TILEPAR), ltiles_cap});
+        const uint64_t est_tiles = (NC / (1u << kGroupBits)) / kLeaderTile + 1;
+        const unsigned g = (unsigned)std::min<uint64_t>(std::max<uint64_t>(est_tiles, 1), (uint64_t)ctx->num_sms * 8);
+        k_symbolic_grouped<single_rule<Rule>><<<g, prim::kThreads, 0, ctx->stream>>>(
+            rule, pv, bufp<uint64_t>(ctx, B_LBEG), bufp<uint64_t>(ctx, B_TILEPAR), ctx->d_words + W_TMP,
+            bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG), bufp<uint32_t>(ctx, B_CSIZE),
+            bufp<uint32_t>(ctx, B_CPAR), (unsigned long long *)(ctx->d_words + W_MAXABS));
+        QD_TRY(launched(ctx, 2));
     }
-    region_count rc{M, regions ? R : 0u, regions ? bufp<unsigned int>(ctx, B_RHIST) : nullptr};
-    if (maxsize <= 256) {
-        QD_TRY((launch_symbolic<single_rule<Rule>, 256>(ctx, rule, pv, NC, fast, rc)));
-    } else {
-        QD_TRY((launch_symbolic<single_rule<Rule>, 4096>(ctx, rule, pv, NC, fast, rc)));
+    if (!grouped) {
+        if (sym_tiles + 1 > tile_map_cap || bufp<uint64_t>(ctx, B_TILEPAR) != tile_map) {
+            k_tile_parents<<<grid_for(ctx, NP), prim::kThreads, 0, ctx->stream>>>(
+                bufp<uint64_t>(ctx, B_CBEGIN), NP, sym_tiles, bufp<uint64_t>(ctx, B_TILEPAR));
+            QD_TRY(launched(ctx));
+        }
+        region_count rc{M, regions ? R : 0u, regions ? bufp<unsigned int>(ctx, B_RHIST) : nullptr};
+        if (maxsize <= 256) {
+            QD_TRY((launch_symbolic<single_rule<Rule>, 256>(ctx, rule, pv, NC, fast, rc)));
+        } else {
+            QD_TRY((launch_symbolic<single_rule<Rule>, 4096>(ctx, rule, pv, NC, fast, rc)));
+        }
     }
     end_stage(1);
 

@@ -30,6 +30,16 @@ QD_HD void hash_combine(uint64_t &seed, uint64_t v) {
     seed += 0xe6546b64ull;
 }
 
+// trailing zeros of v > 0 (small v; constant once unrolled)
+QD_HD constexpr int ctz_small(int v) {
+    int c = 0;
+    while (!(v & 1)) {
+        v >>= 1;
+        ++c;
+    }
+    return c;
+}
+
 // ---- accessors (n passed explicitly: the count is read once per object)
 QD_HD int num_nodes(const char *o) { return ld_u16(o); }
 QD_HD bool L(const char *o, int i) { return o[2 + i] != 0; }
@@ -232,6 +242,7 @@ QD_HD void mulf(factor_count *m, const factors &, int k) {
 template <bool ON_XOR>
 struct flip_rule {
     factors f;
+    static constexpr bool grouped_children = true;  // 2^sites children, one factor per site
 
     QD_HD static bool site(bool l, bool r) { return ON_XOR ? (l != r) : (l == r); }
     QD_HD static bool conj_of(bool l, bool r) { return ON_XOR ? l : (l && r); }
@@ -285,6 +296,93 @@ struct flip_rule {
         apply(pb, num_nodes(pb), child_id, &fc, nullptr, nullptr, nullptr);
     }
     QD_HD uint64_t hasher(const char *b, const char *) const { return hash_graph(b); }
+
+    // The 2^H children of a parent with s >= H sites whose child ids share
+    // the low s-H bits `e` (children e + j 2^(s-H), j < 2^H), as hash_child
+    // computes them, bit for bit: a child's magnitude is the parent's times
+    // one factor per site in site order, so these children share the
+    // products over the first s-H sites, and the last H sites form a binary
+    // tree walked with the j bits reversed, so consecutive children redo
+    // only the products that differ (2^(H+1) - 2 complex products for
+    // 2^H children instead of H 2^H).  The left/right hashes share their
+    // prefixes the same way.  emit(j, hash, magnitude, size).
+    struct walk_state {
+        mag_t m;
+        uint64_t lh, rh;
+    };
+    template <int H, class Emit>
+    QD_HD void expand_group(const char *pb, const char *pe, uint32_t e, int s, mag_t pm, Emit &&emit) const {
+        const uint32_t size = (uint32_t)(pe - pb);
+        const int n = num_nodes(pb);
+        const char *nm = names(pb, n);
+        uint64_t nh = 0;
+        for (int i = 0; i < n; ++i) hash_combine(nh, node_hash(nm, name_begin(pb, n, i)));
+        // shared prefix: the nodes before the first of the last H sites
+        walk_state w{pm, 0, 0};
+        int i = 0, k = 0;
+        uint32_t bits = e;
+        for (; i < n; ++i) {
+            bool l = L(pb, i), r = R(pb, n, i);
+            if (site(l, r)) {
+                if (k == s - H) break;
+                const bool c = conj_of(l, r);
+                if (bits & 1) {
+                    mulf(&w.m, f, c ? F_DC : F_D);
+                    l = !l;
+                    r = !r;
+                } else {
+                    mulf(&w.m, f, c ? F_NDNC : F_DN);
+                }
+                bits >>= 1;
+                ++k;
+            }
+            if (l) hash_combine(w.lh, (uint64_t)i);
+            if (r) hash_combine(w.rh, (uint64_t)i);
+        }
+        int q[H + 1];  // node index of each suffix site, then n
+        {
+            int x = i, m = 0;
+            for (; x < n && m < H; ++x)
+                if (site(L(pb, x), R(pb, n, x))) q[m++] = x;
+            q[H] = n;
+        }
+        walk_state P[H + 1];  // P[lv]: the state before suffix site lv (P[H] is the child's)
+        P[0] = w;
+#pragma unroll
+        for (int t = 0; t < (1 << H); ++t) {
+            int j = 0;
+#pragma unroll
+            for (int b = 0; b < H; ++b) j |= ((t >> b) & 1) << (H - 1 - b);
+            const int k0 = t == 0 ? 0 : H - 1 - ctz_small(t);
+#pragma unroll
+            for (int lv = 0; lv < H; ++lv) {
+                if (lv < k0) continue;
+                walk_state x = P[lv];
+                const int node = q[lv];
+                bool l = L(pb, node), r = R(pb, n, node);
+                const bool c = conj_of(l, r);
+                if ((j >> lv) & 1) {
+                    mulf(&x.m, f, c ? F_DC : F_D);
+                    l = !l;
+                    r = !r;
+                } else {
+                    mulf(&x.m, f, c ? F_NDNC : F_DN);
+                }
+                if (l) hash_combine(x.lh, (uint64_t)node);
+                if (r) hash_combine(x.rh, (uint64_t)node);
+                for (int y = node + 1; y < q[lv + 1]; ++y) {
+                    if (L(pb, y)) hash_combine(x.lh, (uint64_t)y);
+                    if (R(pb, n, y)) hash_combine(x.rh, (uint64_t)y);
+                }
+                P[lv + 1] = x;
+            }
+            uint64_t hh = nh;
+            hash_combine(hh, P[H].lh);
+            hash_combine(hh, P[H].rh);
+            emit((uint32_t)j, hh, P[H].m, size);
+        }
+    }
+
     QD_HD uint64_t hash_child(const char *pb, const char *pe, uint32_t child_id, uint32_t &size,
                               mag_t &mag) const {
         size = (uint32_t)(pe - pb);

@@ -55,6 +55,30 @@ uint64_t shim_hash_child(int kind, const double *p, const uint8_t *o, uint32_t s
     });
     return h;
 }
+// the grouped expansion of the flip rules (kind 2, 3) with H = h (2 or 3)
+// for the children whose ids share the low s-h bits e: writes 2^h hashes and
+// 2^(h+1) doubles (child e + j 2^(s-h) at slot j); returns s, or -1
+int shim_expand_group(int kind, int h, const double *p, const uint8_t *o, uint32_t sz, uint32_t e,
+                      const double *mag, uint64_t *hashes, double *mags) {
+    auto run = [&](auto r) {
+        uint32_t nc, mcs;
+        r.get_num_child((const char *)o, (const char *)o + sz, nc, mcs);
+        int s = 0;
+        while ((1u << s) < nc) ++s;
+        auto emit = [&](uint32_t j, uint64_t hv, const mag_t &m, uint32_t) {
+            hashes[j] = hv;
+            mags[2 * j] = m.re;
+            mags[2 * j + 1] = m.im;
+        };
+        const mag_t pm{mag[0], mag[1]};
+        if (h == 2) r.template expand_group<2>((const char *)o, (const char *)o + sz, e, s, pm, emit);
+        else r.template expand_group<3>((const char *)o, (const char *)o + sz, e, s, pm, emit);
+        return s;
+    };
+    if (kind == 2) return run(qcgd::erase_create{factors(p)});
+    if (kind == 3) return run(qcgd::coin{factors(p)});
+    return -1;
+}
 uint64_t shim_murmur(const uint8_t *b, uint64_t len) { return murmur64a((const char *)b, len); }
 uint64_t shim_hash_graph(const uint8_t *b) { return qcgd::hash_graph((const char *)b); }
 int shim_modifier(int kind, const double *p, uint8_t *o, uint32_t sz, double *mag) {

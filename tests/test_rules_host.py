@@ -27,6 +27,8 @@ def shim():
     S = C.CDLL(SHIM_SO)
     for f in ("shim_hash_child", "shim_hash_graph", "shim_murmur"):
         getattr(S, f).restype = C.c_uint64
+    S.shim_expand_group.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32,
+                                    C.c_void_p, C.c_void_p, C.c_void_p]
     S.shim_murmur.argtypes = [C.c_void_p, C.c_uint64]
     return S
 
@@ -140,3 +142,39 @@ def test_modifiers_match_oracle(shim, port):
             keep, p = _dp(())
             shim.shim_modifier(kind, p, b, len(o), mm)
             assert bytes(b)[: len(o)] == xo
+
+
+@pytest.mark.parametrize("h", [2, 3])
+@pytest.mark.parametrize("kind", [W.RULE_QCGD_ERASE_CREATE, W.RULE_QCGD_COIN])
+def test_grouped_expansion_is_hash_child_bit_for_bit(shim, kind, h):
+    """The grouped symbolic pass (children sharing factor prefixes share
+    their products) gives every child's hash and magnitude bit for bit as
+    hash_child does, child by child."""
+    rng = W.Rng(11)
+    keep, pp = _dp((1.1, 0.7, 2.3))
+    checked = 0
+    for trial in range(60):
+        n = 4 + rng.below(13)
+        g = W.random_graph(n, rng)
+        a, b = C.c_uint32(), C.c_uint32()
+        shim.shim_num_child(kind, pp, _buf(g), len(g), C.byref(a), C.byref(b))
+        nc = a.value
+        if nc < (1 << h):
+            continue
+        s = nc.bit_length() - 1
+        pm = np.array([0.3 + 0.01 * trial, -0.2], np.float64)
+        pmp = pm.ctypes.data_as(C.POINTER(C.c_double))
+        for e in range(0, 1 << (s - h), max(1, (1 << (s - h)) // 5)):
+            hs = np.zeros(1 << h, np.uint64)
+            ms = np.zeros(2 << h, np.float64)
+            assert shim.shim_expand_group(kind, h, pp, _buf(g), len(g), e, pmp, hs.ctypes.data,
+                                          ms.ctypes.data) == s
+            for j in range(1 << h):
+                cid = e + (j << (s - h))
+                mm = (C.c_double * 2)(pm[0], pm[1])
+                sz = C.c_uint32()
+                hv = shim.shim_hash_child(kind, pp, _buf(g), len(g), cid, C.byref(sz), mm)
+                assert hv == int(hs[j]), (trial, e, j)
+                assert (mm[0], mm[1]) == (ms[2 * j], ms[2 * j + 1]), (trial, e, j)
+                checked += 1
+    assert checked > 500
