@@ -553,14 +553,23 @@ int simulate_batched(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule *rules_
     QD_TRY(ensure(out->d_total, sizeof(double)));
 
     // ---- symbolic iteration (src/quids.hpp:705-719), instance-tagged hashes
-    k_tile_parents<<<grid_for(ctx, NP), prim::kThreads, 0, ctx->stream>>>(bufp<uint64_t>(ctx, B_CBEGIN), NP,
-                                                                         sym_tiles, bufp<uint64_t>(ctx, B_TILEPAR));
-    QD_TRY(launched(ctx));
-    const region_count rc{M, 0u, nullptr};
-    if (maxsize <= 256) {
-        QD_TRY((launch_symbolic<instance_rules<Rule>, 256>(ctx, rs, pv, NC, fast, rc)));
-    } else {
-        QD_TRY((launch_symbolic<instance_rules<Rule>, 4096>(ctx, rs, pv, NC, fast, rc)));
+    bool grouped = false;
+    if constexpr (has_grouped<Rule>::value) {
+        if (fast) {
+            QD_TRY(launch_symbolic_grouped(ctx, rs, pv, NC));
+            grouped = true;
+        }
+    }
+    if (!grouped) {
+        k_tile_parents<<<grid_for(ctx, NP), prim::kThreads, 0, ctx->stream>>>(
+            bufp<uint64_t>(ctx, B_CBEGIN), NP, sym_tiles, bufp<uint64_t>(ctx, B_TILEPAR));
+        QD_TRY(launched(ctx));
+        const region_count rc{M, 0u, nullptr};
+        if (maxsize <= 256) {
+            QD_TRY((launch_symbolic<instance_rules<Rule>, 256>(ctx, rs, pv, NC, fast, rc)));
+        } else {
+            QD_TRY((launch_symbolic<instance_rules<Rule>, 4096>(ctx, rs, pv, NC, fast, rc)));
+        }
     }
 
     // ---- collision elimination (src/quids.hpp:785-809)

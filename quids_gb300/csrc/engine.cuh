@@ -762,17 +762,14 @@ struct group_view {
         const ulonglong4_32a a = *(const ulonglong4_32a *)&acc[4ull * s];
         return mag_t{from_fix(fix128{a.x, a.y}, F), from_fix(fix128{a.z, a.w}, F)};
     }
-    // the group magnitude if c is a representative, else false
+    // the group magnitude if c is a representative, else false (the child's
+    // own records are loaded before any branch)
     __device__ __forceinline__ bool rep_mag(uint64_t c, mag_t &m) const {
-        if (not_rep[c]) return false;
+        const uint8_t nr = not_rep[c], hj = has_join[c];
         const uint32_t s = slot_of[c];
-        if (s == prim::kNoSlot) return false;
-        if (has_join[c]) {
-            m = sum(s);
-        } else {
-            const double2 v = cmag[c];
-            m = mag_t{v.x, v.y};
-        }
+        const double2 v = cmag[c];
+        if (nr || s == prim::kNoSlot) return false;
+        m = hj ? sum(s) : mag_t{v.x, v.y};
         return true;
     }
     __device__ __forceinline__ bool kept(uint64_t c, mag_t &m) const { return rep_mag(c, m) && cnorm(m) > tolerance; }
@@ -1051,6 +1048,29 @@ inline unsigned lookback_grid(quids_gpu_ctx *ctx, uint64_t n) {
     return (unsigned)(tiles < 1 ? 1 : (tiles < cap ? tiles : cap));
 }
 
+// leader offsets and their tile map (one scan), then the grouped pass
+template <class RS>
+inline int launch_symbolic_grouped(quids_gpu_ctx *ctx, const RS &rs, const parents_view &pv, uint64_t nc) {
+    const uint64_t np = pv.np;
+    const uint64_t ltiles_cap = nc / kLeaderTile + 2;  // leaders <= children
+    QD_TRY(ensure(ctx->buf[B_LBEG], (np + 1) * sizeof(uint64_t)));
+    QD_TRY(ensure(ctx->buf[B_TILEPAR], ltiles_cap * sizeof(uint64_t)));
+    prim::lookback lb;
+    QD_TRY(lookback_chain(ctx, np, 0, lb));
+    scan_leaders f{bufp<uint32_t>(ctx, B_NCHILD), pv.pidx};
+    prim::k_scan_excl<<<lookback_grid(ctx, np), prim::kThreads, 0, ctx->stream>>>(
+        f, ctx->d_words + W_NP, bufp<uint64_t>(ctx, B_LBEG), ctx->d_words + W_TMP, lb,
+        leader_tile_epilogue{bufp<uint64_t>(ctx, B_TILEPAR), ltiles_cap});
+    const uint64_t est_tiles = (nc >> kGroupBits) / kLeaderTile + 1;
+    const unsigned g = (unsigned)std::min<uint64_t>(est_tiles, (uint64_t)ctx->num_sms * 8);
+    k_symbolic_grouped<RS><<<g, prim::kThreads, 0, ctx->stream>>>(
+        rs, pv, bufp<uint64_t>(ctx, B_LBEG), bufp<uint64_t>(ctx, B_TILEPAR), ctx->d_words + W_TMP,
+        bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG), bufp<uint32_t>(ctx, B_CSIZE),
+        bufp<uint32_t>(ctx, B_CPAR), (unsigned long long *)(ctx->d_words + W_MAXABS));
+    return launched(ctx, 2);
+}
+
+
 template <class Rule, class Post = no_post>
 int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, quids_gpu_state *out,
                   const quids_gpu_params &prm, quids_gpu_step_stats *stats, const Post &post = Post{}) {
@@ -1289,24 +1309,7 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, qu
     begin_stage(1);
     bool grouped = false;
     if constexpr (has_grouped<Rule>::value) grouped = fast && !regions;
-    if constexpr (has_grouped<Rule>::value) if (grouped) {  // leader offsets and tile map, then the grouped pass
-        const uint64_t ltiles_cap = NC / kLeaderTile + 2;  // leaders <= children
-        QD_TRY(ensure(ctx->buf[B_LBEG], (NP + 1) * sizeof(uint64_t)));
-        QD_TRY(ensure(ctx->buf[B_TILEPAR], ltiles_cap * sizeof(uint64_t)));
-        prim::lookback lb;
-        QD_TRY(lookback_chain(ctx, NP, 0, lb));
-        scan_leaders f{bufp<uint32_t>(ctx, B_NCHILD), pidx};
-        prim::k_scan_excl<<<lookback_grid(ctx, NP), prim::kThreads, 0, ctx->stream>>>(
-            f, ctx->d_words + W_NP, bufp<uint64_t>(ctx, B_LBEG), ctx->d_words + W_TMP, lb,
-            leader_tile_epilogue{bufp<uint64_t>(ctx, B_TILEPAR), ltiles_cap});
-        const uint64_t est_tiles = (NC / (1u << kGroupBits)) / kLeaderTile + 1;
-        const unsigned g = (unsigned)std::min<uint64_t>(std::max<uint64_t>(est_tiles, 1), (uint64_t)ctx->num_sms * 8);
-        k_symbolic_grouped<single_rule<Rule>><<<g, prim::kThreads, 0, ctx->stream>>>(
-            rule, pv, bufp<uint64_t>(ctx, B_LBEG), bufp<uint64_t>(ctx, B_TILEPAR), ctx->d_words + W_TMP,
-            bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG), bufp<uint32_t>(ctx, B_CSIZE),
-            bufp<uint32_t>(ctx, B_CPAR), (unsigned long long *)(ctx->d_words + W_MAXABS));
-        QD_TRY(launched(ctx, 2));
-    }
+    if constexpr (has_grouped<Rule>::value) if (grouped) QD_TRY(launch_symbolic_grouped(ctx, rule, pv, NC));
     if (!grouped) {
         if (sym_tiles + 1 > tile_map_cap || bufp<uint64_t>(ctx, B_TILEPAR) != tile_map) {
             k_tile_parents<<<grid_for(ctx, NP), prim::kThreads, 0, ctx->stream>>>(

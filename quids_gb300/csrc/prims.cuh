@@ -671,17 +671,28 @@ __global__ void __launch_bounds__(kThreads) k_compact_layout(P p, const uint64_t
         }
         uint32_t flags = 0;
         uint64_t cnt = 0, bytes = 0;
+        // the selection of the thread's items, with every load unguarded (an
+        // item past the end reads item n-1 and is dropped), so the loads of
+        // all items are in flight together
+        bool sel[kItems];
+        uint64_t ib[kItems];
 #pragma unroll
         for (int k = 0; k < kItems; ++k) {
-            uint64_t i = base + k;
-            if (i < n && p.select(i, rank)) {
+            const uint64_t i = base + k;
+            const uint64_t ic = i < n ? i : n - 1;
+            sel[k] = p.select(ic, rank) && i < n;
+            ib[k] = p.bytes(ic);
+            if (ties & (1u << k)) ++rank;
+        }
+#pragma unroll
+        for (int k = 0; k < kItems; ++k) {
+            if (sel[k]) {
                 flags |= 1u << k;
                 ++cnt;
-                bytes += p.bytes(i);
-                const unsigned long long b = (unsigned long long)__double_as_longlong(p.norm(i));
+                bytes += ib[k];
+                const unsigned long long b = (unsigned long long)__double_as_longlong(p.norm(base + k));
                 mx = mx > b ? mx : b;
             }
-            if (ties & (1u << k)) ++rank;
         }
         uint64_t agg_c, agg_b;
         uint64_t excl_c = block_excl_scan(cnt, sm, agg_c);

@@ -259,8 +259,7 @@ QD_HD int fix_scale(double maxabs, uint64_t n) {
     uint64_t bits;
     memcpy(&bits, &maxabs, 8);
     int e = (int)((bits >> 52) & 0x7ff) - 1022;  // maxabs < 2^e
-    int ln = 0;
-    while (ln < 64 && (1ull << ln) < n) ++ln;     // n <= 2^ln
+    const int ln = n <= 1 ? 0 : 64 - clz64(n - 1);  // n <= 2^ln
     return 124 - e - ln;
 }
 
