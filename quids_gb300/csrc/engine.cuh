@@ -87,7 +87,9 @@ enum qd_word {
     W_MAXNORM,    // bit pattern of the largest survivor norm
     W_ACC,        // 2 words: fixed-point total probability
     W_DONE = W_ACC + 2,  // blocks done with the total (u32)
-    W_COUNT_WORDS = 16
+    W_DONE_SCAN,         // blocks done with the child-offset scan (u32)
+    W_DONE_LAYOUT,       // blocks done with the layout compaction (u32)
+    W_COUNT_WORDS = 24
 };
 
 struct quids_gpu_ctx {
@@ -206,11 +208,19 @@ static __global__ void k_publish_words(const uint64_t *w, volatile uint64_t *h, 
     if (threadIdx.x == 0) h[W_COUNT_WORDS] = seq;
 }
 
-inline int read_words(quids_gpu_ctx *ctx) {
-    const uint64_t seq = ++ctx->publish_seq;
-    k_publish_words<<<1, 32, 0, ctx->stream>>>(ctx->d_words, ctx->h_words_dev, seq);
-    ctx->launches += 1;
-    QD_CUDA(cudaGetLastError());
+// the publication a kernel's last block makes of the step's words (the
+// host then waits with wait_words(ctx, pb.seq))
+inline prim::publish publish_words(quids_gpu_ctx *ctx, qd_word done) {
+    prim::publish pb;
+    pb.words = ctx->d_words;
+    pb.host = ctx->h_words_dev;
+    pb.count = W_COUNT_WORDS;
+    pb.seq = ++ctx->publish_seq;
+    pb.done = (unsigned int *)(ctx->d_words + done);
+    return pb;
+}
+
+inline int wait_words(quids_gpu_ctx *ctx, uint64_t seq) {
     volatile uint64_t *hw = ctx->h_words;
     for (uint64_t it = 1; hw[W_COUNT_WORDS] != seq; ++it) {
         if ((it & 1023) == 0) {
@@ -227,6 +237,14 @@ inline int read_words(quids_gpu_ctx *ctx) {
     }
     std::atomic_thread_fence(std::memory_order_acquire);
     return (int)(int64_t)hw[W_STATUS];
+}
+
+inline int read_words(quids_gpu_ctx *ctx) {
+    const uint64_t seq = ++ctx->publish_seq;
+    k_publish_words<<<1, 32, 0, ctx->stream>>>(ctx->d_words, ctx->h_words_dev, seq);
+    ctx->launches += 1;
+    QD_CUDA(cudaGetLastError());
+    return wait_words(ctx, seq);
 }
 
 // bookkeeping after a launch: count it, report a launch error
@@ -1171,17 +1189,18 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, qu
     // far as the map's buffer already reaches
     uint64_t *tile_map = bufp<uint64_t>(ctx, B_TILEPAR);
     uint64_t tile_map_cap = ctx->buf[B_TILEPAR].cap / sizeof(uint64_t);
+    const prim::publish pb0 = publish_words(ctx, W_DONE_SCAN);
     {
         prim::lookback lb;
         lookback_view(ctx, N, 1, lb);
         scan_nchild f{bufp<uint32_t>(ctx, B_NCHILD), pidx};
         prim::k_scan_excl<<<lookback_grid(ctx, NP), prim::kThreads, 0, ctx->stream>>>(
             f, ctx->d_words + W_NP, bufp<uint64_t>(ctx, B_CBEGIN), ctx->d_words + W_NC, lb,
-            tile_parents_epilogue{tile_map, tile_map_cap});
+            tile_parents_epilogue{tile_map, tile_map_cap}, pb0);
         QD_TRY(launched(ctx));
     }
     end_stage(0);
-    int st = read_words(ctx);  // host synchronisation 1: child count and size bound
+    int st = wait_words(ctx, pb0.seq);  // host wait 1: child count and size bound
     if (st) return st;
     uint64_t maxc = maxn;  // children cap
     if (auto_max && ctx->h_words[W_NC] > 0) {
@@ -1376,6 +1395,7 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, qu
                   bufp<unsigned long long>(ctx, B_ACC), ctx->d_words + W_NC, d_maxabs, prm.tolerance};
     const uint32_t align = prm.align_byte_length;
     unsigned long long *d_maxnorm = (unsigned long long *)(ctx->d_words + W_MAXNORM);
+    const prim::publish pb1 = publish_words(ctx, W_DONE_LAYOUT);
     begin_stage(3);
     if (!may_truncate) {
         prim::lookback lbc, lbb;
@@ -1385,7 +1405,7 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, qu
                         (uint64_t *)out->begin.p, bufp<uint64_t>(ctx, B_SCHILD)};
         prim::k_compact_layout<groups_layout, false><<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
             f, ctx->d_words + W_NC, ctx->d_words + W_NS, ctx->d_words + W_OUTBYTES, (uint64_t *)out->begin.p,
-            d_maxnorm, lbc, lbb, lbb);
+            d_maxnorm, lbc, lbb, lbb, pb1);
         QD_TRY(launched(ctx));
         end_stage(3);
     } else {
@@ -1408,11 +1428,11 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, qu
                        (uint32_t *)out->size.p, (uint64_t *)out->begin.p, bufp<uint64_t>(ctx, B_SCHILD)};
         prim::k_compact_layout<keep_layout, true><<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
             kl, ctx->d_words + W_NU, ctx->d_words + W_NS, ctx->d_words + W_OUTBYTES, (uint64_t *)out->begin.p,
-            d_maxnorm, lbc, lbb, lbt);
+            d_maxnorm, lbc, lbb, lbt, pb1);
         QD_TRY(launched(ctx));
         end_stage(4);
     }
-    st = read_words(ctx);  // host synchronisation 2: survivors and their bytes
+    st = wait_words(ctx, pb1.seq);  // host wait 2: survivors and their bytes
     if (st) return st;
     const uint64_t NS = ctx->h_words[W_NS];
     const uint64_t NU = may_truncate ? ctx->h_words[W_NU] : NS;

@@ -186,6 +186,36 @@ __device__ __forceinline__ uint32_t next_tile(const lookback &lb, uint32_t *sm_t
 // --------------------------------------------------------------- scan
 // out[i] = sum_{j<i} f(j) for i in [0, n], *total = sum; f(i) is called
 // exactly once per item (it may have side effects, e.g. gathers).
+// A kernel's last block to finish copies `count` words of the step into
+// mapped host memory and then writes `seq` after them, so the host learns
+// the step's counts without a separate launch (host == nullptr: nothing).
+// `done` is a block counter zeroed beforehand.
+struct publish {
+    const uint64_t *words = nullptr;
+    volatile uint64_t *host = nullptr;
+    uint32_t count = 0;
+    uint64_t seq = 0;
+    unsigned int *done = nullptr;
+};
+__device__ __forceinline__ void publish_at_exit(const publish &pb) {
+    __shared__ bool last;
+    if (!pb.host) return;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        last = atomicAdd(pb.done, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (last) {
+        __threadfence();
+        for (uint32_t i = threadIdx.x; i < pb.count; i += blockDim.x)
+            pb.host[i] = ((const volatile uint64_t *)pb.words)[i];
+        __threadfence_system();
+        __syncthreads();
+        if (threadIdx.x == 0) pb.host[pb.count] = pb.seq;
+    }
+}
+
 struct no_epilogue {
     __device__ __forceinline__ void operator()(uint64_t, uint64_t, uint64_t, uint64_t) const {}
 };
@@ -193,20 +223,18 @@ struct no_epilogue {
 // E::operator()(i, out[i], f(i), n) runs once per item after its prefix is known.
 template <class F, class E = no_epilogue>
 __global__ void __launch_bounds__(kThreads) k_scan_excl(F f, const uint64_t *d_n, uint64_t *out,
-                                                         uint64_t *d_total, lookback lb, E epi = E{}) {
+                                                         uint64_t *d_total, lookback lb, E epi = E{},
+                                                         publish pb = publish{}) {
     __shared__ uint64_t sm[kThreads / 32 + 1];
     __shared__ uint64_t bcast;
     __shared__ uint32_t sm_tile;
     const uint64_t n = *d_n;
     const uint64_t ntiles = (n + kTile - 1) / kTile;
-    if (n == 0) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-            out[0] = 0;
-            if (d_total) *d_total = 0;
-        }
-        return;
+    if (n == 0 && blockIdx.x == 0 && threadIdx.x == 0) {
+        out[0] = 0;
+        if (d_total) *d_total = 0;
     }
-    while (true) {
+    while (n) {
         uint32_t tile = next_tile(lb, &sm_tile);
         if (tile >= ntiles) break;
         const uint64_t base = (uint64_t)tile * kTile + (uint64_t)threadIdx.x * kItems;
@@ -236,6 +264,7 @@ __global__ void __launch_bounds__(kThreads) k_scan_excl(F f, const uint64_t *d_n
             if (d_total) *d_total = prefix + agg;
         }
     }
+    publish_at_exit(pb);
 }
 
 // ------------------------------------------------------------- compact
@@ -631,7 +660,8 @@ template <class P, bool TIES>
 __global__ void __launch_bounds__(kThreads) k_compact_layout(P p, const uint64_t *d_n, uint64_t *d_count,
                                                               uint64_t *d_bytes, uint64_t *begin_out,
                                                               unsigned long long *d_maxnorm, lookback lb_count,
-                                                              lookback lb_bytes, lookback lb_ties) {
+                                                              lookback lb_bytes, lookback lb_ties,
+                                                              publish pb = publish{}) {
     __shared__ uint64_t sm[kThreads / 32 + 1];
     __shared__ uint64_t bcast;
     __shared__ uint32_t sm_tile;
@@ -643,6 +673,7 @@ __global__ void __launch_bounds__(kThreads) k_compact_layout(P p, const uint64_t
             *d_bytes = 0;
             begin_out[0] = 0;
         }
+        publish_at_exit(pb);
         return;
     }
     __shared__ uint64_t bcast2[2];
@@ -720,6 +751,7 @@ __global__ void __launch_bounds__(kThreads) k_compact_layout(P p, const uint64_t
         }
         if ((threadIdx.x & 31) == 0 && mx) atomicMax(d_maxnorm, mx);
     }
+    publish_at_exit(pb);
 }
 
 // --------------------------------------------------------- normalisation
