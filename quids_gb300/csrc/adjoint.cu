@@ -4,13 +4,14 @@
 //
 // Checkpointing: the ops are cut into segments of `checkpoint_every` rule
 // applications.  The forward keeps the state at the start of every segment
-// and, for the last segment, the input state of each rule.  The backward
-// walks the segments from the last: it recomputes a segment's rule inputs
-// from its checkpoint (the last segment's are kept), then goes through the
-// segment's ops in reverse, replaying each rule step on its input and
-// running the adjoint kernels (adjoint.cuh) on the replay.  Modifiers
-// supported by the backward permute bytes without touching magnitudes
-// (X, CNOT, QCGD step / reversed_step), so the adjoint passes through them.
+// and, for the last segment, the input state and the structure record
+// (adjoint.cuh) of each rule step.  The backward walks the segments from the
+// last: it recomputes a segment's rule steps from its checkpoint, keeping
+// their inputs and records (the last segment's come from the forward), then
+// goes through the segment's ops in reverse, running the adjoint kernels of
+// each rule step on its input and record.  Modifiers supported by the
+// backward permute bytes without touching magnitudes (X, CNOT, QCGD step /
+// reversed_step), so the adjoint passes through them.
 #include <cstring>
 #include <new>
 #include <utility>
@@ -30,6 +31,7 @@ struct quids_gpu_tape {
     std::vector<uint64_t> seg_begin;             // first op of each segment (plus n_ops at the end)
     std::vector<quids_gpu_state *> ckpt;         // state before seg_begin[k] (null for the last segment)
     std::vector<quids_gpu_state *> last_inputs;  // [n_ops] rule inputs of the last segment
+    std::vector<qd::adjoint::step_record> last_records;  // [n_ops] their structure records
     quids_gpu_state *final = nullptr;
     bool ready = false;
     qd::adjoint::scratch sc;
@@ -68,9 +70,11 @@ int copy_state(quids_gpu_ctx *ctx, const quids_gpu_state *src, quids_gpu_state *
 void clear_tape(quids_gpu_tape *t) {
     for (auto *&s : t->ckpt) drop(s);
     for (auto *&s : t->last_inputs) drop(s);
+    for (auto &r : t->last_records) adjoint::release_record(r);
     drop(t->final);
     t->ckpt.clear();
     t->last_inputs.clear();
+    t->last_records.clear();
     t->seg_begin.clear();
     t->ready = false;
 }
@@ -90,8 +94,11 @@ int forward_rule(quids_gpu_tape *t, const quids_gpu_op &op, quids_gpu_state *cur
     });
 }
 
-// the rule inputs of segment k, recomputed from its checkpoint
-int recompute_segment(quids_gpu_tape *t, size_t k, std::vector<quids_gpu_state *> &inputs) {
+// the rule inputs and records of segment k, recomputed from its checkpoint;
+// *last_out: the output of the segment's last rule step (its record points
+// at it)
+int recompute_segment(quids_gpu_tape *t, size_t k, std::vector<quids_gpu_state *> &inputs,
+                      std::vector<adjoint::step_record> &records, quids_gpu_state **last_out) {
     quids_gpu_state *cur = nullptr;
     QD_TRY(new_state(t->ctx, &cur));
     int rc = copy_state(t->ctx, t->ckpt[k], cur);
@@ -99,7 +106,9 @@ int recompute_segment(quids_gpu_tape *t, size_t k, std::vector<quids_gpu_state *
         const quids_gpu_op &op = t->ops[i];
         if (op.is_rule) {
             quids_gpu_state *out = nullptr;
-            rc = forward_rule(t, op, cur, &out, nullptr);
+            quids_gpu_step_stats st{};
+            rc = forward_rule(t, op, cur, &out, &st);
+            if (!rc) rc = adjoint::capture_record(t->ctx, st, cur, out, records[i]);
             if (rc) {
                 drop(out);
                 break;
@@ -110,7 +119,7 @@ int recompute_segment(quids_gpu_tape *t, size_t k, std::vector<quids_gpu_state *
             rc = quids_gpu_apply_modifier(t->ctx, cur, op.kind, &op.params);
         }
     }
-    drop(cur);
+    *last_out = cur;
     return rc;
 }
 
@@ -163,6 +172,7 @@ int quids_gpu_forward(quids_gpu_ctx *ctx, quids_gpu_tape *t, quids_gpu_state *in
     const size_t nseg = t->seg_begin.size() - 1;
     t->ckpt.assign(nseg, nullptr);
     t->last_inputs.assign(n_ops, nullptr);
+    t->last_records.assign(n_ops, adjoint::step_record{});
 
     quids_gpu_state *cur = nullptr;
     QD_TRY(new_state(ctx, &cur));
@@ -179,8 +189,11 @@ int quids_gpu_forward(quids_gpu_ctx *ctx, quids_gpu_tape *t, quids_gpu_state *in
         const quids_gpu_op &op = ops[i];
         if (op.is_rule) {
             quids_gpu_state *out = nullptr;
-            rc = forward_rule(t, op, cur, &out, rule_stats ? rule_stats + r : nullptr);
+            quids_gpu_step_stats st{};
+            rc = forward_rule(t, op, cur, &out, &st);
+            if (rule_stats) rule_stats[r] = st;
             ++r;
+            if (!rc && k + 1 == nseg) rc = adjoint::capture_record(ctx, st, cur, out, t->last_records[i]);
             if (rc) {
                 drop(out);
                 break;
@@ -225,36 +238,37 @@ int backward_from(quids_gpu_tape *t, double *grad_angles) {
     QD_CUDA(cudaMemsetAsync(t->grads.p, 0, (n_ops * 3 + 3) * sizeof(double), ctx->stream));
     double *grads = (double *)t->grads.p;
     const size_t nseg = t->seg_begin.size() - 1;
-    quids_gpu_state *replay = nullptr;
-    QD_TRY(new_state(ctx, &replay));
     int rc = QUIDS_OK;
     for (size_t k = nseg; k-- > 0 && !rc;) {
+        const bool last = k + 1 == nseg;
         std::vector<quids_gpu_state *> inputs(n_ops, nullptr);
-        if (k + 1 == nseg) {
-            inputs = t->last_inputs;  // kept by the forward; released with the tape
-        } else {
-            rc = recompute_segment(t, k, inputs);
+        std::vector<adjoint::step_record> records;
+        quids_gpu_state *seg_out = nullptr;
+        if (!last) {
+            records.assign(n_ops, adjoint::step_record{});
+            rc = recompute_segment(t, k, inputs, records, &seg_out);
         }
+        const std::vector<quids_gpu_state *> &in_of = last ? t->last_inputs : inputs;
+        const std::vector<adjoint::step_record> &rec_of = last ? t->last_records : records;
         for (uint64_t i = t->seg_begin[k + 1]; !rc && i-- > t->seg_begin[k];) {
             const quids_gpu_op &op = t->ops[i];
             if (!op.is_rule) continue;  // magnitude-preserving permutation of the bytes
-            quids_gpu_state *in = inputs[i];
-            quids_gpu_step_stats st{};
+            quids_gpu_state *in = in_of[i];
+            rc = ensure(t->a1, (in->n ? in->n : 1) * sizeof(double2));
+            if (rc) break;
             rc = host::dispatch_rule(op.kind, &op.params, [&](auto r) {
-                int e = simulate_rule(ctx, in, r, replay, t->prm, &st);  // the forward step, replayed
-                if (e) return e;
-                e = ensure(t->a1, (in->n ? in->n : 1) * sizeof(double2));
-                if (e) return e;
                 const adjoint::rule_angles ang{op.params.theta, op.params.phi, op.params.xi};
-                return adjoint::backward_rule(ctx, t->sc, in, r, ang, replay, st, (double2 *)t->a0.p,
+                return adjoint::backward_rule(ctx, t->sc, in, r, ang, rec_of[i], (double2 *)t->a0.p,
                                               (double2 *)t->a1.p, grads + 3 * i);
             });
             std::swap(t->a0, t->a1);
         }
-        if (k + 1 != nseg)
+        if (!last) {
             for (auto *&s : inputs) drop(s);
+            for (auto &r : records) adjoint::release_record(r);
+            drop(seg_out);
+        }
     }
-    drop(replay);
     if (rc) return rc;
     QD_CUDA(cudaMemcpyAsync(grad_angles, grads, n_ops * 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     return cuda_status(cudaStreamSynchronize(ctx->stream));

@@ -21,11 +21,12 @@
 //   collisions: a_v(c) = a_u(group of c), or 0 when the group was dropped
 //   children:   a_m(p) = sum over children c of p of conj(f_c) a_v(c)
 //   angles:     dL/dtheta += Re(conj(a_v(c)) m_p df_c/dtheta), and so on.
-// A backward rule step replays the forward step on its input (the pipeline
-// is deterministic, so the replay has the forward's structure), then runs
-// the kernels below on the replay's buffers.  Every reduction has a fixed
-// order: one warp per parent gathers its children, and the angle sums go
-// through a fixed grid of per-block partials.
+// A backward rule step reads the structure its forward step left (a record:
+// table slots, child offsets, representatives, normalisation factor), taken
+// during the forward or the recomputation of its segment; the pipeline is
+// deterministic, so a recomputed step has the forward's structure.  Every
+// reduction has a fixed order: one warp per parent gathers its children,
+// and the angle sums go through a fixed grid of per-block partials.
 #pragma once
 #include <type_traits>
 
@@ -120,6 +121,50 @@ static __global__ void __launch_bounds__(prim::kThreads)
     }
 }
 
+// Per-block tables for the closed forms: sin^k, cos^k (k <= kMaxSites) and
+// e^{i phi k}, e^{i xi k} (|k| <= kMaxSites).  Beyond them, the direct form.
+constexpr int kMaxSites = 63;
+struct factor_tables {
+    double sp[kMaxSites + 2], cp[kMaxSites + 2];
+    double2 ephi[2 * kMaxSites + 1], exi[2 * kMaxSites + 1];
+};
+__device__ __forceinline__ void fill_tables(factor_tables &t, const rule_angles &ang) {
+    double s, c;
+    sincos(ang.theta, &s, &c);
+    for (int k = threadIdx.x; k < kMaxSites + 2; k += blockDim.x) {
+        t.sp[k] = ipow(s, k);
+        t.cp[k] = ipow(c, k);
+    }
+    for (int k = threadIdx.x; k < 2 * kMaxSites + 1; k += blockDim.x) {
+        double a, b;
+        sincos(ang.phi * (k - kMaxSites), &a, &b);
+        t.ephi[k] = make_double2(b, a);
+        sincos(ang.xi * (k - kMaxSites), &a, &b);
+        t.exi[k] = make_double2(b, a);
+    }
+}
+__device__ __forceinline__ child_factor factor_from_tables(const qcgd::factor_count &fc, const factor_tables &t,
+                                                           double s, double c, const rule_angles &ang) {
+    const int a = fc.n[qcgd::F_D] + fc.n[qcgd::F_DC], b = fc.n[qcgd::F_DN] + fc.n[qcgd::F_NDNC];
+    const int kp = (int)fc.n[qcgd::F_D] - (int)fc.n[qcgd::F_DC];
+    const int kx = (int)fc.n[qcgd::F_DN] - (int)fc.n[qcgd::F_NDNC];
+    if (a > kMaxSites || b > kMaxSites) return factor_of(fc, s, c, ang);
+    const double2 ep = t.ephi[kp + kMaxSites], ex = t.exi[kx + kMaxSites];
+    const double pr = ep.x * ex.x - ep.y * ex.y, pi = ep.x * ex.y + ep.y * ex.x;
+    const double sign = (fc.n[qcgd::F_NDNC] & 1) ? -1.0 : 1.0;
+    const double r = sign * t.sp[a] * t.cp[b];
+    double dr = 0;
+    if (a) dr += a * t.sp[a - 1] * t.cp[b + 1];
+    if (b) dr -= b * t.sp[a + 1] * t.cp[b - 1];
+    dr *= sign;
+    child_factor out;
+    out.f = mag_t{r * pr, r * pi};
+    out.dth = mag_t{dr * pr, dr * pi};
+    out.dph = mag_t{-kp * out.f.im, kp * out.f.re};
+    out.dxi = mag_t{-kx * out.f.im, kx * out.f.re};
+    return out;
+}
+
 // One warp per kept parent: the parent's adjoint from its children (in child
 // order, then a fixed shuffle tree), and the children's angle derivatives.
 // gpartial: [3][kAdjBlocks] per-block angle sums.
@@ -129,10 +174,13 @@ __global__ void __launch_bounds__(prim::kThreads)
                   const double2 *a_u, rule_angles ang, double2 *a_in, double *gpartial) {
     using Rule = typename RS::rule_type;
     __shared__ double sm[3][prim::kThreads / 32];
+    __shared__ factor_tables tab;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
     double s_th, c_th;
     sincos(ang.theta, &s_th, &c_th);
+    if constexpr (has_factor_counts<Rule>::value) fill_tables(tab, ang);
+    __syncthreads();
     double g0 = 0, g1 = 0, g2 = 0;
     for (uint64_t p = (uint64_t)blockIdx.x * (blockDim.x >> 5) + wib; p < pv.np; p += warps) {
         const uint64_t oid = pv.pidx ? pv.pidx[p] : p;
@@ -153,7 +201,7 @@ __global__ void __launch_bounds__(prim::kThreads)
             if constexpr (has_factor_counts<Rule>::value) {
                 qcgd::factor_count fc{};
                 rule.factor_counts(pb, pe, cid, fc);
-                const child_factor cf = factor_of(fc, s_th, c_th, ang);
+                const child_factor cf = factor_from_tables(fc, tab, s_th, c_th, ang);
                 f = cf.f;
                 // Re(conj(a_v) m_p df)
                 const mag_t d0 = cmul(mag_t{pm.x, pm.y}, cf.dth), d1 = cmul(mag_t{pm.x, pm.y}, cf.dph),
@@ -225,40 +273,81 @@ struct scratch {
     qd_dbuf partial;  // double [4 kAdjBlocks + 4]
 };
 
-// The backward rule step: `replay` holds the forward step's output for input
-// `in` (replayed just before, so the context's buffers hold its structure and
-// stats its counters).  a_out: adjoint of replay's magnitudes; a_in: adjoint
-// of in's magnitudes (written for every object); grad3: the three angle
-// derivatives (device).
+// What the backward of one rule step needs from its forward: the children's
+// table slots, the child offsets over the kept parents (and the kept
+// parents), each survivor's representative child, the normalisation factor
+// and the output state (its magnitudes).  Captured right after the step
+// (capture_record), so the backward needs no replay of the step.
+struct step_record {
+    qd_dbuf slot_of, cbeg, pidx, schild, factor;
+    uint64_t N = 0, NP = 0, NC = 0, NS = 0, M = 0;
+    bool has_pidx = false;
+    quids_gpu_state *out = nullptr;  // not owned
+};
+inline void release_record(step_record &r) {
+    for (qd_dbuf *b : {&r.slot_of, &r.cbeg, &r.pidx, &r.schild, &r.factor}) release(*b);
+    r = step_record{};
+}
+inline int capture_record(quids_gpu_ctx *ctx, const quids_gpu_step_stats &st, const quids_gpu_state *in,
+                          quids_gpu_state *out, step_record &r) {
+    r.N = in->n;
+    r.NP = st.num_parents_kept;
+    r.NC = st.num_object;
+    r.NS = out->n;
+    r.M = st.table_capacity;
+    r.out = out;
+    r.has_pidx = r.NP < r.N;
+    if (r.NC == 0 || r.NS == 0) return QUIDS_OK;
+    cudaStream_t s = ctx->stream;
+    QD_TRY(ensure(r.slot_of, r.NC * sizeof(uint32_t)));
+    QD_TRY(ensure(r.cbeg, (r.NP + 1) * sizeof(uint64_t)));
+    QD_TRY(ensure(r.schild, r.NS * sizeof(uint64_t)));
+    QD_TRY(ensure(r.factor, sizeof(double)));
+    QD_CUDA(cudaMemcpyAsync(r.slot_of.p, ctx->buf[B_SLOT].p, r.NC * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
+    QD_CUDA(cudaMemcpyAsync(r.cbeg.p, ctx->buf[B_CBEGIN].p, (r.NP + 1) * sizeof(uint64_t), cudaMemcpyDeviceToDevice,
+                            s));
+    QD_CUDA(cudaMemcpyAsync(r.schild.p, ctx->buf[B_SCHILD].p, r.NS * sizeof(uint64_t), cudaMemcpyDeviceToDevice, s));
+    QD_CUDA(cudaMemcpyAsync(r.factor.p, ctx->d_words + W_FACTOR, sizeof(double), cudaMemcpyDeviceToDevice, s));
+    if (r.has_pidx) {
+        QD_TRY(ensure(r.pidx, r.NP * sizeof(uint64_t)));
+        QD_CUDA(cudaMemcpyAsync(r.pidx.p, ctx->buf[B_PIDX].p, r.NP * sizeof(uint64_t), cudaMemcpyDeviceToDevice, s));
+    }
+    return QUIDS_OK;
+}
+
+// The backward rule step from its forward's record.  a_out: adjoint of the
+// output magnitudes (replaced by the adjoint before normalisation); a_in:
+// adjoint of in's magnitudes (written for every object); grad3: the three
+// angle derivatives (device).
 template <class Rule>
 int backward_rule(quids_gpu_ctx *ctx, scratch &sc, quids_gpu_state *in, const Rule &rule_, const rule_angles &ang,
-                  quids_gpu_state *replay, const quids_gpu_step_stats &st, double2 *a_out, double2 *a_in,
-                  double *grad3) {
-    const uint64_t N = in->n, NS = replay->n, NP = st.num_parents_kept, M = st.table_capacity;
+                  const step_record &r, double2 *a_out, double2 *a_in, double *grad3) {
+    const uint64_t N = in->n, NS = r.NS, NP = r.NP, M = r.M;
     QD_CUDA(cudaMemsetAsync(a_in, 0, (N ? N : 1) * sizeof(double2), ctx->stream));
     QD_CUDA(cudaMemsetAsync(grad3, 0, 3 * sizeof(double), ctx->stream));
-    if (N == 0 || NS == 0 || st.num_object == 0) return QUIDS_OK;
+    if (N == 0 || NS == 0 || r.NC == 0) return QUIDS_OK;
     QD_TRY(ensure(sc.partial, (4 * kAdjBlocks + 4) * sizeof(double)));
     QD_TRY(ensure(sc.surv, (M + 1) * sizeof(uint32_t)));
     double *partial = (double *)sc.partial.p;
     double *dot = partial + 4 * kAdjBlocks;
+    const double2 *mout = (const double2 *)r.out->mag.p;
     // normalize
-    k_dot_partial<<<kAdjBlocks, prim::kThreads, 0, ctx->stream>>>(a_out, (const double2 *)replay->mag.p, NS, partial);
+    k_dot_partial<<<kAdjBlocks, prim::kThreads, 0, ctx->stream>>>(a_out, mout, NS, partial);
     k_sum_partials<<<1, kAdjBlocks, 0, ctx->stream>>>(partial, dot);
-    k_norm_adjoint<<<grid_for(ctx, NS), prim::kThreads, 0, ctx->stream>>>(
-        a_out, (const double2 *)replay->mag.p, NS, dot, (const double *)(ctx->d_words + W_FACTOR));
+    k_norm_adjoint<<<grid_for(ctx, NS), prim::kThreads, 0, ctx->stream>>>(a_out, mout, NS, dot,
+                                                                         (const double *)r.factor.p);
     // collisions and truncation: each slot's survivor
     uint32_t *surv = (uint32_t *)sc.surv.p;
     QD_CUDA(cudaMemsetAsync(surv, 0xff, (M + 1) * sizeof(uint32_t), ctx->stream));
     k_surv_of_slot<<<grid_for(ctx, NS), prim::kThreads, 0, ctx->stream>>>(
-        bufp<uint64_t>(ctx, B_SCHILD), bufp<uint32_t>(ctx, B_SLOT), NS, M + 1, surv);
+        (const uint64_t *)r.schild.p, (const uint32_t *)r.slot_of.p, NS, M + 1, surv);
     // children -> parents, angle derivatives
     parents_view pv{(const char *)in->objects.p, (const uint64_t *)in->begin.p, (const uint32_t *)in->size.p,
-                    (const double2 *)in->mag.p, bufp<uint64_t>(ctx, B_CBEGIN),
-                    NP < N ? bufp<uint64_t>(ctx, B_PIDX) : nullptr, NP};
+                    (const double2 *)in->mag.p, (const uint64_t *)r.cbeg.p,
+                    r.has_pidx ? (const uint64_t *)r.pidx.p : nullptr, NP};
     const single_rule<Rule> rs{rule_};
     k_adj_parents<single_rule<Rule>><<<kAdjBlocks, prim::kThreads, 0, ctx->stream>>>(
-        rs, pv, bufp<uint32_t>(ctx, B_SLOT), surv, M + 1, a_out, ang, a_in, partial);
+        rs, pv, (const uint32_t *)r.slot_of.p, surv, M + 1, a_out, ang, a_in, partial);
     for (int k = 0; k < 3; ++k)
         k_sum_partials<<<1, kAdjBlocks, 0, ctx->stream>>>(partial + (uint64_t)k * kAdjBlocks, grad3 + k);
     return launched(ctx, 9);
