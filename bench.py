@@ -112,6 +112,30 @@ def qcgd_initial_cpu(wl, o):
 
 
 # ------------------------------------------------------------------ helpers
+def max_over_ranks(x, dev=None):
+    """The largest x over the ranks of the process group (NCCL: on the
+    rank's GPU; gloo: on the CPU)."""
+    import torch
+    device = f"cuda:{dev}" if torch.distributed.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(children_per_rank, local_ms, world, dev=None):
+    """Whole-job throughput of `world` replicas that each processed
+    children_per_rank in local_ms: the children of all ranks over the
+    slowest rank's time.  Returns (children/s, that time in ms)."""
+    total_ms = max_over_ranks(local_ms, dev) if world > 1 else float(local_ms)
+    return world * children_per_rank / (total_ms / 1e3), total_ms
+
+
+def barrier(world):
+    if world > 1:
+        import torch
+        torch.distributed.barrier()
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -262,6 +286,7 @@ def ours(args, rank, world):
             ms.append(e0.elapsed_time(e1))
             children += c
     ctx.synchronize()
+    barrier(world)
     t_wall = time.perf_counter() - t_wall0
     launches = ctx.lib.quids_gpu_ctx_launch_count(ctx.h) - launches0
 
@@ -273,12 +298,7 @@ def ours(args, rank, world):
             flush.fill_(1)
         run_step_gpu(ctx, quids, wl, src, stats, flags=capi.FLAG_STAGE_TIMING)
     ctx.synchronize()
-    total_ms = sum(ms)
-    if world > 1:
-        t = torch.tensor([total_ms], device=f"cuda:{dev}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * children / (total_ms / 1e3)
+    value, total_ms = job_value(children, sum(ms), world, dev)
 
     # dominant stage and its roofline (stage times are CUDA events on the library's stream)
     stage_t = [0.0] * 8
@@ -419,12 +439,8 @@ def ours_batched(args, rank, world):
     ctx.synchronize()
     t_wall = time.perf_counter() - t_wall0
     launches = ctx.lib.quids_gpu_ctx_launch_count(ctx.h) - launches0
-    total_ms = sum(ms)
-    if world > 1:
-        t = torch.tensor([total_ms], device=f"cuda:{dev}")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * children / (total_ms / 1e3)
+    barrier(world)
+    value, total_ms = job_value(children, sum(ms), world, dev)
 
     # the same step, instance by instance through the plain path
     plain_ms = []
@@ -545,8 +561,8 @@ def ours_adjoint(args, rank, world):
             abytes += b
     t_wall = time.perf_counter() - t_wall0
     launches = ctx.lib.quids_gpu_ctx_launch_count(ctx.h) - launches0
-    total_ms = sum(ms)
-    value = world * children / (total_ms / 1e3)
+    barrier(world)
+    value, total_ms = job_value(children, sum(ms), world, dev)
 
     def plain():
         fin, st = quids.run(quids.it_t(ctx, wl["init"]), quids.it_t(ctx), ops, wl["max"])
