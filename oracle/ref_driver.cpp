@@ -20,6 +20,7 @@
 #include <limits>
 #include <memory>
 #include <omp.h>
+#include <vector>
 
 #include "oracle_api.h"
 
@@ -182,6 +183,51 @@ uint64_t qo_rule_hash(int rule_kind, const double *params, const uint8_t *obj, u
     auto rule = make_rule(rule_kind, params);
     if (!rule) return 0;
     return rule->hasher((const char *)obj, (const char *)obj + size);
+}
+
+// Reference-only (the QCGD simulation string, src/rules/qcgd.hpp:1086-1166):
+// flags::read_n_iter on `settings` (it seeds rand()) then flags::read_state
+// on `state_arg` into st.
+int qo_ref_read_state(const char *settings, const char *state_arg, void *st) {
+    quids::rules::qcgd::flags::read_n_iter(settings);
+    quids::rules::qcgd::flags::read_state(state_arg, *(quids::it_t *)st);
+    return 0;
+}
+
+// flags::read_rule: per entry its n_iter, whether it is a rule, and for
+// rules the magnitudes of children 0..3 of `probe` (from magnitude 1) under
+// the rule and under its reversed form: out[entry][2][4] complex.
+int qo_ref_read_rules(const char *rules_arg, const uint8_t *probe, uint32_t size, int max_entries, int *n_iter,
+                      int *is_rule, double *out) {
+    auto sim = quids::rules::qcgd::flags::read_rule(rules_arg);
+    int n = 0;
+    for (auto &e : sim) {
+        if (n >= max_entries) break;
+        n_iter[n] = std::get<0>(e);
+        is_rule[n] = std::get<1>(e) ? 1 : 0;
+        if (is_rule[n]) {
+            quids::rule_t *rs[2] = {std::get<3>(e), std::get<5>(e)};
+            for (int v = 0; v < 2; ++v) {
+                uint nc, mcs;
+                rs[v]->get_num_child((const char *)probe, (const char *)probe + size, nc, mcs);
+                std::vector<char> child(mcs + 64);
+                for (uint c = 0; c < 4; ++c) {
+                    double *o = out + ((size_t)n * 8 + v * 4 + c) * 2;
+                    if (c >= nc) {
+                        o[0] = o[1] = 0;
+                        continue;
+                    }
+                    uint sz = 0;
+                    quids::mag_t m(1, 0);
+                    rs[v]->populate_child((const char *)probe, (const char *)probe + size, child.data(), c, sz, m);
+                    o[0] = m.real();
+                    o[1] = m.imag();
+                }
+            }
+        }
+        ++n;
+    }
+    return n;
 }
 
 } // extern "C"
