@@ -81,7 +81,12 @@ typedef struct quids_gpu_params {
                                     smallest u / norm, u uniform from a generator seeded by `seed`) */
     uint32_t align_byte_length;  /* quids::align_byte_length for the output state */
     double table_load_factor;    /* collision table max load; 0 -> default 0.5 */
-    uint32_t block_size;         /* reserved, 0 */
+    uint32_t hash_ranges;        /* 0: one pass when the children fit (2^32 child indices, device memory),
+                                    else as many hash-range passes as they need; k >= 2: at least k
+                                    passes.  Range passes give the one-pass result bit for bit; the
+                                    automatic truncation (max_num_object = 0) never uses them (it
+                                    keeps fewer parents until one pass fits), nor does the adjoint
+                                    forward (QUIDS_ERR_UNSUPPORTED) */
     uint32_t flags;              /* QUIDS_FLAG_* */
     uint64_t seed;               /* probabilistic truncation: generator seed (same seed and input,
                                     same result) */
@@ -117,6 +122,8 @@ typedef struct quids_gpu_step_stats {
      * probability, 6 finalize populate with normalisation, 7 unused */
     float stage_ms[8];
     uint64_t kernel_launches;                /* kernels this step launched */
+    uint64_t hash_ranges;                    /* hash-range passes the step ran in (0: one pass; the
+                                                range passes record ms_total only, no stages) */
 } quids_gpu_step_stats;
 
 typedef struct quids_gpu_ctx quids_gpu_ctx;

@@ -32,6 +32,7 @@ simple_truncation: bool = True    # False: probabilistic truncation (src/quids.h
 truncation_seed: int = 0          # generator seed of probabilistic truncation
 memory_budget: int = 0            # automatic truncation (max_num_object = 0): bytes per step, 0 = device
 table_load_factor: float = 0.5    # collision table maximum load
+hash_ranges: int = 0              # 0: one pass while the children fit; k >= 2: k hash-range passes
 
 
 class rules:
@@ -329,7 +330,7 @@ class it_t:
 
 def _params(max_num_object, flags=0):
     return capi.Params(float(tolerance), int(max_num_object) & U64_MAX, int(bool(simple_truncation)),
-                       int(align_byte_length), float(table_load_factor), 0, int(flags),
+                       int(align_byte_length), float(table_load_factor), int(hash_ranges), int(flags),
                        int(truncation_seed) & U64_MAX, int(memory_budget))
 
 

@@ -39,7 +39,7 @@ class RuleParams(C.Structure):
 class Params(C.Structure):
     _fields_ = [("tolerance", C.c_double), ("max_num_object", C.c_uint64), ("simple_truncation", C.c_int32),
                 ("align_byte_length", C.c_uint32), ("table_load_factor", C.c_double),
-                ("block_size", C.c_uint32), ("flags", C.c_uint32), ("seed", C.c_uint64),
+                ("hash_ranges", C.c_uint32), ("flags", C.c_uint32), ("seed", C.c_uint64),
                 ("memory_budget", C.c_uint64)]
 
 
@@ -60,7 +60,8 @@ class StepStats(C.Structure):
                 ("num_object_after_interferences", C.c_uint64), ("num_object_out", C.c_uint64),
                 ("max_child_size", C.c_uint64), ("table_capacity", C.c_uint64), ("out_bytes", C.c_uint64),
                 ("total_proba", C.c_double), ("algorithmic_bytes", C.c_double), ("ms_total", C.c_float),
-                ("stage_ms", C.c_float * 8), ("kernel_launches", C.c_uint64)]
+                ("stage_ms", C.c_float * 8), ("kernel_launches", C.c_uint64),
+                ("hash_ranges", C.c_uint64)]
 
     def as_dict(self):
         d = {k: getattr(self, k) for k, _ in self._fields_ if k != "stage_ms"}

@@ -88,10 +88,12 @@ bool backward_modifier(int kind) {
 int forward_rule(quids_gpu_tape *t, const quids_gpu_op &op, quids_gpu_state *cur, quids_gpu_state **out,
                  quids_gpu_step_stats *stats) {
     QD_TRY(new_state(t->ctx, out));
-    const quids_gpu_params prm = t->prm;
-    return host::dispatch_rule(op.kind, &op.params, [&](auto r) {
+    quids_gpu_params prm = t->prm;
+    prm.hash_ranges = 0;  // the step records are those of one pass
+    const int rc = host::dispatch_rule(op.kind, &op.params, [&](auto r) {
         return simulate_rule(t->ctx, cur, r, *out, prm, stats);
     });
+    return rc == kNeedRanges ? QUIDS_ERR_UNSUPPORTED : rc;
 }
 
 // the rule inputs and records of segment k, recomputed from its checkpoint;

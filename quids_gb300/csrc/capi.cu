@@ -9,6 +9,7 @@
 #include <utility>
 
 #include "engine.cuh"
+#include "ranges.cuh"
 #include "rules_qc.cuh"
 #include "rules_qcgd.cuh"
 #include "factories.cuh"
@@ -287,7 +288,7 @@ int quids_gpu_simulate(quids_gpu_ctx *ctx, quids_gpu_state *iteration, int rule_
     if (!params) return QUIDS_ERR_BAD_ARG;
     quids_gpu_params prm = *params;
     return dispatch_rule(rule_kind, rule, [&](auto r) {
-        return simulate_rule(ctx, iteration, r, next_iteration, prm, stats);
+        return ranges::simulate_step(ctx, iteration, r, next_iteration, prm, stats);
     });
 }
 
@@ -334,8 +335,8 @@ int quids_gpu_run(quids_gpu_ctx *ctx, quids_gpu_state *a, quids_gpu_state *b, co
             }
             quids_gpu_step_stats *st = rule_stats ? rule_stats + r : nullptr;
             rc = dispatch_rule(op.kind, &op.params, [&](auto rule) {
-                return chain.n ? simulate_rule(ctx, cur, rule, other, prm, st, chain)
-                               : simulate_rule(ctx, cur, rule, other, prm, st);
+                return chain.n ? ranges::simulate_step(ctx, cur, rule, other, prm, st, chain)
+                               : ranges::simulate_step(ctx, cur, rule, other, prm, st);
             });
             ++r;
             if (!rc) {

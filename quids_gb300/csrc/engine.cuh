@@ -145,7 +145,7 @@ inline int cuda_status(cudaError_t e) {
     } while (0)
 #define QD_CUDA(expr) QD_TRY(::qd::engine::cuda_status(expr))
 
-inline int ensure(qd_dbuf &b, size_t bytes) {
+inline int ensure(qd_dbuf &b, size_t bytes, bool headroom = true) {
     if (bytes == 0) bytes = 8;
     if (b.cap >= bytes) return QUIDS_OK;
     if (b.p) {
@@ -154,7 +154,7 @@ inline int ensure(qd_dbuf &b, size_t bytes) {
         b.cap = 0;
         if (e != cudaSuccess) return cuda_status(e);
     }
-    size_t want = bytes + bytes / 4;
+    size_t want = headroom ? bytes + bytes / 4 : bytes;
     cudaError_t e = cudaMalloc(&b.p, want);
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -669,18 +669,39 @@ __global__ void __launch_bounds__(prim::kThreads)
 // populate_child_simple of each survivor straight into its slot of the
 // packed output (padding zeroed), mag /= sqrt(total) when that factor is
 // not 1 (batched: the survivor's instance factor), then `post`.
-template <class RS, class Post>
+// the (kept parent, child id) of each survivor: from its representative
+// child index (schild) and the children's parents (cpar) ...
+struct schild_source {
+    const uint64_t *schild;
+    const uint32_t *cpar;
+    const uint64_t *cbeg;
+    __device__ __forceinline__ void get(uint64_t i, uint64_t &p, uint32_t &cid) const {
+        const uint64_t c = schild[i];
+        p = cpar[c];
+        cid = (uint32_t)(c - cbeg[p]);
+    }
+};
+// ... or stored per survivor
+struct pc_source {
+    const uint32_t *par;
+    const uint32_t *cid;
+    __device__ __forceinline__ void get(uint64_t i, uint64_t &p, uint32_t &c) const {
+        p = par[i];
+        c = cid[i];
+    }
+};
+
+template <class RS, class SS, class Post>
 __global__ void __launch_bounds__(prim::kThreads)
-    k_populate(RS rs, parents_view pv, const uint64_t *schild, const uint32_t *cpar, const uint64_t *d_ns,
-               const uint64_t *obegin, const uint32_t *osize, char *objects, double2 *omag, const double *d_factor,
-               const uint32_t *finst, int *err, Post post) {
+    k_populate(RS rs, parents_view pv, SS ss, const uint64_t *d_ns, const uint64_t *obegin, const uint32_t *osize,
+               char *objects, double2 *omag, const double *d_factor, const uint32_t *finst, int *err, Post post) {
     const uint64_t ns = *d_ns;
     const double f0 = finst ? 1.0 : *d_factor;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ns; i += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t c = schild[i];
-        const uint64_t p = cpar[c];
+        uint64_t p;
+        uint32_t cid;
+        ss.get(i, p, cid);
         const uint64_t oid = pv.pidx ? pv.pidx[p] : p;
-        const uint32_t cid = (uint32_t)(c - pv.cbeg[p]);
         const char *pb = pv.objects + pv.begin[oid];
         const char *pe = pb + pv.size[oid];
         const uint64_t ob = obegin[i], oe = obegin[i + 1];
@@ -1024,9 +1045,9 @@ inline int launch_symbolic(quids_gpu_ctx *ctx, const RS &rule, const parents_vie
 template <class RS, class Post>
 inline int launch_populate(quids_gpu_ctx *ctx, const RS &rule, const parents_view &pv, uint64_t ns,
                            quids_gpu_state *out, const Post &post) {
-    k_populate<RS, Post><<<grid_for(ctx, ns), prim::kThreads, 0, ctx->stream>>>(
-        rule, pv, bufp<uint64_t>(ctx, B_SCHILD), bufp<uint32_t>(ctx, B_CPAR), ctx->d_words + W_NS,
-        (const uint64_t *)out->begin.p,
+    k_populate<RS, schild_source, Post><<<grid_for(ctx, ns), prim::kThreads, 0, ctx->stream>>>(
+        rule, pv, schild_source{bufp<uint64_t>(ctx, B_SCHILD), bufp<uint32_t>(ctx, B_CPAR), pv.cbeg},
+        ctx->d_words + W_NS, (const uint64_t *)out->begin.p,
         (const uint32_t *)out->size.p, (char *)out->objects.p, (double2 *)out->mag.p,
         (const double *)(ctx->d_words + W_FACTOR), nullptr, (int *)(ctx->d_words + W_STATUS), post);
     return launched(ctx);
@@ -1088,6 +1109,11 @@ inline int launch_symbolic_grouped(quids_gpu_ctx *ctx, const RS &rs, const paren
     return launched(ctx, 2);
 }
 
+
+// simulate_rule's answer for a step beyond one pass (2^32 children, or
+// records and table beyond the device memory) or with hash-range passes
+// asked for: nothing of it is done yet, the caller runs the range passes
+constexpr int kNeedRanges = 1;
 
 template <class Rule, class Post = no_post>
 int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, quids_gpu_state *out,
@@ -1270,9 +1296,25 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, qu
     parents_view pv{(const char *)in->objects.p, (const uint64_t *)in->begin.p, (const uint32_t *)in->size.p,
                     (const double2 *)in->mag.p, bufp<uint64_t>(ctx, B_CBEGIN), pidx, NP};
     if (NC == 0) return finish(true);
-    if (NC >= 0xffffffffull) return QUIDS_ERR_UNSUPPORTED;  // child indices are u32 in the table
-    if (maxsize > 4096) return QUIDS_ERR_SIZE_BOUND;        // per-thread child buffer bound
+    if (maxsize > 4096) return QUIDS_ERR_SIZE_BOUND;  // per-thread child buffer bound
     const bool may_truncate = maxc < NC;
+    if (!auto_max) {
+        // one pass holds every child's records and table with 32-bit child
+        // indices; beyond that (or when asked) the step runs in hash ranges
+        if (prm.hash_ranges >= 2 || NC >= 0xffffffffull) return kNeedRanges;
+        if ((double)NC / load + 1 >= (double)0x7ffffff0ull) return kNeedRanges;  // 31-bit table slots
+        const double need = (double)NC * (38.0 + 48.0 / load + (may_truncate ? 32.0 : 0.0));
+        if (need > 1e9) {
+            size_t free_b = 0, total_b = 0;
+            QD_CUDA(cudaMemGetInfo(&free_b, &total_b));
+            double held = 0;
+            for (auto &b : ctx->buf) held += (double)b.cap;
+            // buffers grow with 25 % headroom
+            if (need > 0.7 * ((double)free_b + held)) return kNeedRanges;
+        }
+    } else if (NC >= 0xffffffffull) {
+        return QUIDS_ERR_UNSUPPORTED;  // child indices are u32 in the table
+    }
     const uint64_t NSB = may_truncate ? maxc : NC;  // bound on the survivors
 
     uint64_t M = (uint64_t)((double)NC / load) + 1;

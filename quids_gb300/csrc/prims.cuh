@@ -470,7 +470,9 @@ __device__ __forceinline__ void fix_atomic_add(unsigned long long *w, fix128 v) 
 }
 
 // Pass 1: every child item (src.hash(k)) finds or claims the slot of its
-// hash.  The claiming thread initialises the group with its own child (rep =
+// hash.  The fixed-point scale F comes from the largest component and the
+// child count *d_nf (default: the *d_n items; a hash-range pass gives the
+// whole step's count, so its sums are those of one pass).  The claiming thread initialises the group with its own child (rep =
 // its index, acc = its magnitude); slot_out[k] = slot | kJoin for the others,
 // which pass 2 adds in.  0xffffffff at the probe limit (QUIDS_ERR_TABLE_FULL).
 constexpr uint32_t kJoin = 0x80000000u;
@@ -479,9 +481,9 @@ constexpr uint32_t kNoSlot = 0xffffffffu;
 template <class Src>
 __global__ void __launch_bounds__(kThreads) k_table_claim(table t, Src src, const uint64_t *d_n,
                                                            const unsigned long long *d_maxabs, uint32_t *slot_out,
-                                                           int *err) {
+                                                           int *err, const uint64_t *d_nf = nullptr) {
     const uint64_t n = *d_n;
-    const int F = fix_scale(__longlong_as_double((long long)*d_maxabs), n);
+    const int F = fix_scale(__longlong_as_double((long long)*d_maxabs), d_nf ? *d_nf : n);
     for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t h = src.hash(k);
         uint64_t s;
@@ -530,9 +532,10 @@ template <class Src>
 __global__ void __launch_bounds__(kThreads) k_table_accumulate(table t, Src src, uint32_t *slot_of,
                                                                 const uint64_t *d_n,
                                                                 const unsigned long long *d_maxabs,
-                                                                uint8_t *not_rep, uint8_t *has_join) {
+                                                                uint8_t *not_rep, uint8_t *has_join,
+                                                                const uint64_t *d_nf = nullptr) {
     const uint64_t n = *d_n;
-    const int F = fix_scale(__longlong_as_double((long long)*d_maxabs), n);
+    const int F = fix_scale(__longlong_as_double((long long)*d_maxabs), d_nf ? *d_nf : n);
     for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
         uint32_t s = slot_of[k];
         if (s == kNoSlot || !(s & kJoin)) continue;
