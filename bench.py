@@ -76,6 +76,16 @@ def workload(name):
                                        f"state after step 0, max_num_object 2^{cap.bit_length() - 1}",
                            "nodes": nodes, "seed": seed, "max_num_object": cap, "tolerance": 1e-18,
                            "align_byte_length": 8}}
+    if name == "qcgd12s2":
+        cap = 1 << 24
+        return {"name": name, "init": None, "nodes": 12, "seed": 1, "gates": W.qcgd_step_rules(), "max": cap,
+                "pre_steps": 2, "cpu_sample_objects": 1 << 20, "tolerance": 1e-18, "align": 8,
+                "config": {"workload": "QCGD step 2 (step, coin(pi/4), split_merge(pi/4,0,-pi/2), "
+                                       "erase_create(pi/3,pi/5,0)) of a 12-node cycle graph, from the 2^24-object "
+                                       "state after steps 0-1, max_num_object 2^24: coin has 3.15e9 children "
+                                       "(beyond 2^31 table slots: hash-range passes)",
+                           "nodes": 12, "seed": 1, "max_num_object": cap, "tolerance": 1e-18,
+                           "align_byte_length": 8}}
     if name == "batch256":
         insts = W.qcgd_batch_instances(256, 2, 4, 16)
         return {"name": name, "insts": insts, "max": 1 << 18, "tolerance": 1e-18, "align": 8,
@@ -98,17 +108,29 @@ def workload(name):
 
 
 def qcgd_initial_cpu(wl, o):
-    """State after QCGD step 0 (computed by the CPU oracle, for its own timing)."""
+    """State after the QCGD steps before the timed one (computed by the CPU
+    oracle, for its own timing), cut to the CPU sample."""
     from quids_gb300 import workloads as W
     s = o.new_state(W.qcgd_single_state(wl["nodes"], seed=wl["seed"]))
-    for g in wl["gates"]:
-        if g.kind == "mod":
-            o.modifier(s, g.code, g.params)
-        else:
-            t = o.new_state()
-            o.simulate(s, g.code, g.params, t, wl["max"])
-            s = t
-    return s.store()
+    for _ in range(wl.get("pre_steps", 1)):
+        for g in wl["gates"]:
+            if g.kind == "mod":
+                o.modifier(s, g.code, g.params)
+            else:
+                t = o.new_state()
+                o.simulate(s, g.code, g.params, t, wl["max"])
+                s = t
+    return cpu_sample(wl, s.store())
+
+
+def cpu_sample(wl, packed):
+    """The first cpu_sample_objects objects of a state (the CPU's bounded
+    sample of a workload too large for it), else the state."""
+    n = wl.get("cpu_sample_objects")
+    objects, begin, size, mag = packed
+    if not n or n >= len(size):
+        return packed
+    return (objects[:int(begin[n])].copy(), begin[:n + 1].copy(), size[:n].copy(), mag[:n].copy())
 
 
 # ------------------------------------------------------------------ helpers
@@ -251,8 +273,10 @@ def ours(args, rank, world):
     if init_packed is None:  # QCGD: the state after step 0, computed on the GPU
         from quids_gb300 import workloads as W
         it = quids.it_t(ctx, W.qcgd_single_state(wl["nodes"], seed=wl["seed"]))
-        _, it = run_step_gpu(ctx, quids, wl, it)
+        for _ in range(wl.get("pre_steps", 1)):
+            _, it = run_step_gpu(ctx, quids, wl, it)
         init_packed = it.download()
+        del it
         wl.pop("_spare", None)
     init = quids.it_t(ctx, init_packed)
 
@@ -345,7 +369,7 @@ def ours(args, rank, world):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(wl, init_packed, samples=1, warm=wl["name"] == "circuit24")
+        cpu = cpu_baseline(wl, cpu_sample(wl, init_packed), samples=1, warm=wl["name"] == "circuit24")
 
     if rank == 0:
         line = {
@@ -656,8 +680,9 @@ def cpu_baseline(wl, init_packed, samples=1, warm=True):
     t0 = time.perf_counter()
     ch = sum(one() for _ in range(samples))
     dt = time.perf_counter() - t0
+    part = (f"the first {wl['cpu_sample_objects']} objects of " if wl.get("cpu_sample_objects") else "")
     return {"value": ch / dt, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{samples} full step(s) of the {wl['name']} workload ({ch} children, {dt:.2f} s)"}
+            "sample": f"{samples} step(s) of {part}the {wl['name']} workload ({ch} children, {dt:.2f} s)"}
 
 
 def reference(args, rank, world):
@@ -715,7 +740,10 @@ def reference(args, rank, world):
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": dict(wl["config"], parallelism="host cores"),
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{args.steps} full step(s) of {wl['name']}"},
+                         "sample": f"{args.steps} step(s) of "
+                                   + (f"the first {wl['cpu_sample_objects']} objects of "
+                                      if wl.get("cpu_sample_objects") else "")
+                                   + wl["name"]},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
 
@@ -726,7 +754,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="circuit24", choices=["circuit24", "qcgd12", "qcgd10", "batch256", "adjoint10"])
+    ap.add_argument("--config", default="circuit24", choices=["circuit24", "qcgd12", "qcgd10", "qcgd12s2", "batch256",
+                                                                 "adjoint10"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -123,7 +123,8 @@ typedef struct quids_gpu_step_stats {
     float stage_ms[8];
     uint64_t kernel_launches;                /* kernels this step launched */
     uint64_t hash_ranges;                    /* hash-range passes the step ran in (0: one pass; the
-                                                range passes record ms_total only, no stages) */
+                                                stage times of range passes are summed over the passes,
+                                                stage 4 includes the merge and final selection) */
 } quids_gpu_step_stats;
 
 typedef struct quids_gpu_ctx quids_gpu_ctx;

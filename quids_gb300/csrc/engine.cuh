@@ -595,11 +595,25 @@ struct scan_leaders {
 };
 using leader_tile_epilogue = tile_map_epilogue<kLeaderTile>;
 
-template <class RS>
+// what the grouped pass does with child c (hash already tagged): its
+// records ...
+struct child_records {
+    uint64_t *hash;
+    double2 *cmag;
+    uint32_t *csize;
+    uint32_t *cpar;
+    __device__ __forceinline__ void operator()(uint64_t c, uint64_t h, const mag_t &m, uint32_t sz, uint64_t p) const {
+        hash[c] = h;
+        cmag[c] = make_double2(m.re, m.im);
+        csize[c] = sz;
+        cpar[c] = (uint32_t)p;
+    }
+};
+
+template <class RS, class Out>
 __global__ void __launch_bounds__(prim::kThreads)
     k_symbolic_grouped(RS rs, parents_view pv, const uint64_t *lbeg, const uint64_t *tile_first, const uint64_t *d_nl,
-                       uint64_t *hash, double2 *cmag, uint32_t *csize, uint32_t *cpar,
-                       unsigned long long *d_maxabs) {
+                       Out emit_child, unsigned long long *d_maxabs) {
     using Rule = typename RS::rule_type;
     constexpr int H = kGroupBits;
     __shared__ uint64_t s_lb[kStagedLeaderParents + 1];
@@ -635,10 +649,7 @@ __global__ void __launch_bounds__(prim::kThreads)
         const double2 pm = pv.mag[oid];
         const Rule &rule = rs.get(oid);
         auto out = [&](uint64_t c, uint64_t h, const mag_t &m, uint32_t sz) {
-            hash[c] = rs.tag(h, oid);
-            cmag[c] = make_double2(m.re, m.im);
-            csize[c] = sz;
-            cpar[c] = (uint32_t)p;
+            emit_child(c, rs.tag(h, oid), m, sz, p);
             const unsigned long long a = (unsigned long long)__double_as_longlong(m.re) & 0x7fffffffffffffffull;
             const unsigned long long b = (unsigned long long)__double_as_longlong(m.im) & 0x7fffffffffffffffull;
             const unsigned long long ab = a > b ? a : b;
@@ -1102,10 +1113,11 @@ inline int launch_symbolic_grouped(quids_gpu_ctx *ctx, const RS &rs, const paren
         leader_tile_epilogue{bufp<uint64_t>(ctx, B_TILEPAR), ltiles_cap});
     const uint64_t est_tiles = (nc >> kGroupBits) / kLeaderTile + 1;
     const unsigned g = (unsigned)std::min<uint64_t>(est_tiles, (uint64_t)ctx->num_sms * 8);
-    k_symbolic_grouped<RS><<<g, prim::kThreads, 0, ctx->stream>>>(
-        rs, pv, bufp<uint64_t>(ctx, B_LBEG), bufp<uint64_t>(ctx, B_TILEPAR), ctx->d_words + W_TMP,
-        bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG), bufp<uint32_t>(ctx, B_CSIZE),
-        bufp<uint32_t>(ctx, B_CPAR), (unsigned long long *)(ctx->d_words + W_MAXABS));
+    const child_records rec{bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG), bufp<uint32_t>(ctx, B_CSIZE),
+                            bufp<uint32_t>(ctx, B_CPAR)};
+    k_symbolic_grouped<RS, child_records><<<g, prim::kThreads, 0, ctx->stream>>>(
+        rs, pv, bufp<uint64_t>(ctx, B_LBEG), bufp<uint64_t>(ctx, B_TILEPAR), ctx->d_words + W_TMP, rec,
+        (unsigned long long *)(ctx->d_words + W_MAXABS));
     return launched(ctx, 2);
 }
 

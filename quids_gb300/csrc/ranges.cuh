@@ -37,17 +37,32 @@ __device__ __forceinline__ uint32_t range_of(uint64_t h, uint32_t k) {
 }
 
 // ------------------------------------------------------------------ kernels
-// Pass k of the symbolic iteration: every child of the kept parents is
-// computed (hash_child) and those of range k are written at their rank among
-// them, in child order (blocked items; a look-back chain over tiles of
-// kTileChildren children).  Records past `cap` are not written; *d_count
-// gets the range's full count.  *d_maxabs: the largest |component| over
-// every child of the step (not only the range's).
+// the kept parent holding child c of a tile whose parents' child offsets are
+// staged in s_cb (count + 1 of them), else found in global memory
+__device__ __forceinline__ uint64_t tile_parent(const uint64_t *s_cb, int count, uint64_t plo,
+                                                const parents_view &pv, uint64_t c) {
+    if (count <= 0) return parent_of(pv.cbeg, pv.np, c);
+    int lo = 0, hi = count;  // s_cb[lo] <= c < s_cb[hi]
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (s_cb[mid] <= c) lo = mid; else hi = mid;
+    }
+    return plo + (uint64_t)lo;
+}
+
+// The first pass of the symbolic iteration over the children of the kept
+// parents (rules without grouped children): every child is computed
+// (hash_child; blocked items in child order, a look-back chain over tiles of
+// kTileChildren children), its range stored in rid[c], and the children of
+// range 0 kept: written at their rank among them (records past `cap` are
+// not written; *d_count gets the range's full count).  It also takes the
+// largest |component| over every child of the step into *d_maxabs.
 template <class RS>
 __global__ void __launch_bounds__(prim::kThreads)
-    k_symbolic_range(RS rs, parents_view pv, const uint64_t *tile_first, uint64_t nc, uint32_t k, uint32_t K,
+    k_symbolic_first(RS rs, parents_view pv, const uint64_t *tile_first, uint64_t nc, uint32_t K, uint8_t *rid,
                      uint64_t cap, uint64_t *rhash, double2 *rmag, uint32_t *rsize, uint32_t *rpar, uint32_t *rcid,
                      uint64_t *d_count, prim::lookback lb, unsigned long long *d_maxabs) {
+    static_assert(kSymItems == 4, "one 32-bit word of range ids per thread");
     __shared__ uint64_t s_cb[kStagedParents + 1];
     __shared__ uint64_t sm[prim::kThreads / 32 + 1];
     __shared__ uint64_t bcast;
@@ -58,6 +73,7 @@ __global__ void __launch_bounds__(prim::kThreads)
         const uint32_t tile = prim::next_tile(lb, &sm_tile);
         if (tile >= ntiles) break;
         const uint64_t c0 = (uint64_t)tile * kTileChildren;
+        const uint64_t cb = c0 + (uint64_t)threadIdx.x * kSymItems;  // the thread's first child
         const uint64_t plo = tile_first[tile], phi = tile_first[tile + 1];
         const int count = phi - plo + 1 <= (uint64_t)kStagedParents ? (int)(phi - plo + 1) : -1;
         for (int q = threadIdx.x; q <= count; q += blockDim.x) s_cb[q] = pv.cbeg[plo + q];
@@ -65,23 +81,13 @@ __global__ void __launch_bounds__(prim::kThreads)
         uint64_t hh[kSymItems];
         double2 mm[kSymItems];
         uint32_t ss[kSymItems], pp[kSymItems], cc[kSymItems];
-        uint32_t sel = 0;
+        uint32_t sel = 0, ids = 0;
         uint64_t nsel = 0;
 #pragma unroll
         for (int u = 0; u < kSymItems; ++u) {
-            const uint64_t c = c0 + (uint64_t)threadIdx.x * kSymItems + u;
+            const uint64_t c = cb + u;
             if (c >= nc) break;
-            uint64_t p;
-            if (count > 0) {
-                int lo = 0, hi = count;  // s_cb[lo] <= c < s_cb[hi]
-                while (hi - lo > 1) {
-                    const int mid = (lo + hi) >> 1;
-                    if (s_cb[mid] <= c) lo = mid; else hi = mid;
-                }
-                p = plo + (uint64_t)lo;
-            } else {
-                p = parent_of(pv.cbeg, pv.np, c);
-            }
+            const uint64_t p = tile_parent(s_cb, count, plo, pv, c);
             const uint64_t oid = pv.pidx ? pv.pidx[p] : p;
             const uint32_t cid = (uint32_t)(c - pv.cbeg[p]);
             const char *pb = pv.objects + pv.begin[oid];
@@ -94,15 +100,22 @@ __global__ void __launch_bounds__(prim::kThreads)
             const unsigned long long b = (unsigned long long)__double_as_longlong(m.im) & 0x7fffffffffffffffull;
             mx = mx > a ? mx : a;
             mx = mx > b ? mx : b;
+            const uint32_t r = range_of(h, K);
+            ids |= r << (8 * u);
             hh[u] = h;
             mm[u] = make_double2(m.re, m.im);
             ss[u] = sz;
             pp[u] = (uint32_t)p;
             cc[u] = cid;
-            if (range_of(h, K) == k) {
+            if (r == 0) {
                 sel |= 1u << u;
                 ++nsel;
             }
+        }
+        if (cb + kSymItems <= nc) {
+            *(uint32_t *)(rid + cb) = ids;  // cb is a multiple of 4
+        } else {
+            for (int u = 0; u < kSymItems && cb + u < nc; ++u) rid[cb + u] = (uint8_t)(ids >> (8 * u));
         }
         uint64_t agg;
         const uint64_t excl = prim::block_excl_scan(nsel, sm, agg);  // also orders the reuse of s_cb
@@ -127,6 +140,93 @@ __global__ void __launch_bounds__(prim::kThreads)
         mx = mx > y ? mx : y;
     }
     if ((threadIdx.x & 31) == 0 && mx) atomicMax(d_maxabs, mx);
+}
+
+// the grouped pass's output when it only sorts children into ranges
+struct range_ids {
+    uint8_t *rid;
+    uint32_t K;
+    __device__ __forceinline__ void operator()(uint64_t c, uint64_t h, const mag_t &, uint32_t, uint64_t) const {
+        rid[c] = (uint8_t)range_of(h, K);
+    }
+};
+
+// Pass k over children whose range ids are known: a block takes
+// kListTiles symbolic tiles at a time, lists their children of range k in
+// shared memory (in child order) and computes only those (hash_child),
+// spread over its threads, writing each at its rank among them (a
+// look-back chain over the block tiles).  Records past `cap` are not
+// written; *d_count gets the range's full count.
+constexpr int kListTiles = 8;
+constexpr int kListChildren = kListTiles * kTileChildren;         // 8192 (u16 offsets)
+constexpr int kListPerThread = kListChildren / prim::kThreads;    // 32 range ids per thread
+constexpr int kListStaged = 1024;                                 // parents whose offsets are staged
+template <class RS>
+__global__ void __launch_bounds__(prim::kThreads)
+    k_symbolic_list(RS rs, parents_view pv, const uint64_t *tile_first, uint64_t sym_tiles, uint64_t nc, uint32_t k,
+                    const uint8_t *rid, uint64_t cap, uint64_t *rhash, double2 *rmag, uint32_t *rsize, uint32_t *rpar,
+                    uint32_t *rcid, uint64_t *d_count, prim::lookback lb) {
+    static_assert(kListPerThread == 32, "one 32-bit selection mask per thread");
+    __shared__ uint64_t s_cb[kListStaged + 1];
+    __shared__ uint16_t s_list[kListChildren];
+    __shared__ uint64_t sm[prim::kThreads / 32 + 1];
+    __shared__ uint64_t bcast;
+    __shared__ uint32_t sm_tile;
+    const uint64_t nblk = (nc + kListChildren - 1) / kListChildren;
+    const uint32_t kk = k * 0x01010101u;
+    while (true) {
+        const uint32_t t = prim::next_tile(lb, &sm_tile);
+        if (t >= nblk) break;
+        const uint64_t c0 = (uint64_t)t * kListChildren;
+        const uint64_t t0 = (uint64_t)t * kListTiles;
+        const uint64_t t1 = t0 + kListTiles < sym_tiles ? t0 + kListTiles : sym_tiles;
+        const uint64_t plo = tile_first[t0], phi = tile_first[t1];
+        const int count = phi - plo + 1 <= (uint64_t)kListStaged ? (int)(phi - plo + 1) : -1;
+        for (int q = threadIdx.x; q <= count; q += blockDim.x) s_cb[q] = pv.cbeg[plo + q];
+        const uint64_t cb = c0 + (uint64_t)threadIdx.x * kListPerThread;
+        uint32_t mine = 0;
+        if (cb + kListPerThread <= nc) {
+            const uint4 *w = (const uint4 *)(rid + cb);  // 32-byte aligned
+#pragma unroll
+            for (int v = 0; v < 2; ++v) {
+                const uint4 q = w[v];
+                const uint32_t ws[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+                for (int x = 0; x < 4; ++x) {
+                    const uint32_t eq = __vcmpeq4(ws[x], kk);  // 0xff in each byte equal to k
+#pragma unroll
+                    for (int b = 0; b < 4; ++b) mine |= ((eq >> (8 * b)) & 1u) << (16 * v + 4 * x + b);
+                }
+            }
+        } else {
+            for (int u = 0; u < kListPerThread && cb + u < nc; ++u) mine |= (rid[cb + u] == k ? 1u : 0u) << u;
+        }
+        uint64_t agg;
+        uint64_t e = prim::block_excl_scan((uint64_t)__popc(mine), sm, agg);
+        for (uint32_t m = mine; m; m &= m - 1) s_list[e++] = (uint16_t)(threadIdx.x * kListPerThread + __ffs(m) - 1);
+        const uint64_t pre = prim::tile_prefix(lb, t, agg, &bcast);  // its barriers publish s_list and s_cb
+        for (uint32_t q = threadIdx.x; q < (uint32_t)agg; q += blockDim.x) {
+            const uint64_t c = c0 + s_list[q];
+            const uint64_t p = tile_parent(s_cb, count, plo, pv, c);
+            const uint64_t oid = pv.pidx ? pv.pidx[p] : p;
+            const uint32_t cid = (uint32_t)(c - pv.cbeg[p]);
+            const char *pb = pv.objects + pv.begin[oid];
+            const char *pe = pb + pv.size[oid];
+            const double2 pm = pv.mag[oid];
+            mag_t m{pm.x, pm.y};
+            uint32_t sz = 0;
+            const uint64_t h = rs.tag(rs.get(oid).hash_child(pb, pe, cid, sz, m), oid);
+            const uint64_t j = pre + q;
+            if (j < cap) {
+                rhash[j] = h;
+                rmag[j] = make_double2(m.re, m.im);
+                rsize[j] = sz;
+                rpar[j] = (uint32_t)p;
+                rcid[j] = cid;
+            }
+        }
+        if (t == nblk - 1 && threadIdx.x == 0) *d_count = pre + agg;
+    }
 }
 
 // the groups of a range above tolerance, with their global child index
@@ -270,9 +370,9 @@ struct merged_layout {
 // ------------------------------------------------------------------- the step
 // buffers of the range passes that the context does not keep
 struct range_buffers {
-    qd_dbuf rcid, usize, upar, ucid, cand[6], key[2], perm[2], off, spar, scid;
+    qd_dbuf rid, ltile, rcid, usize, upar, ucid, cand[6], key[2], perm[2], off, spar, scid;
     ~range_buffers() {
-        for (qd_dbuf *b : {&rcid, &usize, &upar, &ucid, &key[0], &key[1], &perm[0], &perm[1], &off, &spar, &scid})
+        for (qd_dbuf *b : {&rid, &ltile, &rcid, &usize, &upar, &ucid, &key[0], &key[1], &perm[0], &perm[1], &off, &spar, &scid})
             release(*b);
         for (auto &b : cand) release(b);
     }
@@ -282,6 +382,32 @@ struct range_buffers {
 // 1/2, kept groups) and per candidate (records and the merge's keys)
 constexpr double kRangeChildBytes = 36.0 + 6.0 + 96.0 + 44.0;
 constexpr double kCandidateBytes = 44.0 + 24.0;
+
+// per-stage device time summed over the passes (QUIDS_FLAG_STAGE_TIMING):
+// events bracket a stage and are read after the host wait that follows
+struct stage_clock {
+    quids_gpu_ctx *ctx;
+    bool on;
+    float *acc;  // [8]
+    bool used[8] = {};
+    void begin(int k) {
+        if (!on) return;
+        cudaEventRecord(ctx->ev_stage[2 * k], ctx->stream);
+        used[k] = true;
+    }
+    void end(int k) {
+        if (on) cudaEventRecord(ctx->ev_stage[2 * k + 1], ctx->stream);
+    }
+    void harvest() {
+        for (int k = 0; on && k < 8; ++k)
+            if (used[k]) {
+                float ms = 0;
+                cudaEventElapsedTime(&ms, ctx->ev_stage[2 * k], ctx->ev_stage[2 * k + 1]);
+                acc[k] += ms;
+                used[k] = false;
+            }
+    }
+};
 
 // zeroed look-back chain of `words` words at word `at` of the chain buffer
 inline int chain_at(quids_gpu_ctx *ctx, uint64_t at, uint64_t words, prim::lookback &lb) {
@@ -311,6 +437,7 @@ int simulate_ranges(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, 
     quids_gpu_step_stats s{};
     s.num_parents = N;
     s.total_proba = std::numeric_limits<double>::quiet_NaN();
+    stage_clock clk{ctx, timing, s.stage_ms};
     // the context's scratch is sized afresh, without headroom (all but the
     // sticky modifier status)
     for (int b = 0; b < B_COUNT; ++b)
@@ -318,6 +445,7 @@ int simulate_ranges(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, 
 
     // ---- num_child, parent pre-truncation, child offsets (as in one pass)
     QD_TRY(ensure(ctx->buf[B_NCHILD], (N ? N : 1) * sizeof(uint32_t)));
+    clk.begin(0);
     QD_TRY(ensure(ctx->buf[B_LOOKBACK], lookback_words(N) * sizeof(uint64_t)));
     const uint64_t nzero0 = N ? lookback_words(N) : 0;
     k_step_begin<<<(unsigned)std::min<uint64_t>((nzero0 + 255) / 256 + 1, (uint64_t)ctx->num_sms * 4), 256, 0,
@@ -356,8 +484,10 @@ int simulate_ranges(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, 
             f, ctx->d_words + W_NP, bufp<uint64_t>(ctx, B_CBEGIN), ctx->d_words + W_NC, lb);
         QD_TRY(launched(ctx));
     }
+    clk.end(0);
     int st = read_words(ctx);
     if (st) return st;
+    clk.harvest();
     const uint64_t NC = ctx->h_words[W_NC], maxsize = ctx->h_words[W_MAXSIZE];
     s.num_object = NC;
     s.max_child_size = maxsize;
@@ -372,12 +502,13 @@ int simulate_ranges(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, 
     QD_CUDA(cudaMemGetInfo(&free_b, &total_b));
     const double out_est = (double)std::min(NC, maxn) * (28.0 + (double)((maxsize + 7) / 8 * 8));
     auto cand_count = [&](uint64_t k) { return maxn >= NC ? NC : std::min<uint64_t>(NC, maxn * k); };
-    const double avail = 0.8 * (double)free_b - out_est;
+    const double avail = 0.8 * (double)free_b - out_est - (double)NC;  // NC: the children's range ids
     uint32_t K = prm.hash_ranges >= 2 ? prm.hash_ranges : 2;
     while (K < (1u << 16) && ((double)NC / K * 1.07 * kRangeChildBytes + (double)cand_count(K) * kCandidateBytes >
                                   avail ||
                               (double)NC / K * 1.07 / load + 4096 >= (double)0x7ff00000ull))
         ++K;
+    if (K > 255) return QUIDS_ERR_OOM;  // range ids are bytes; such a step's ids alone exceed the device
     const uint64_t cand_cap = cand_count(K);
     if (cand_cap >= 0xffffffffull) return QUIDS_ERR_OOM;  // candidate indices are u32
     uint64_t cap = NC / K + NC / K / 16 + 4096;             // a range's share with slack (grown on demand)
@@ -410,6 +541,7 @@ int simulate_ranges(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, 
         return QUIDS_OK;
     };
     QD_TRY(ensure(ctx->buf[B_TILEPAR], (sym_tiles + 1) * sizeof(uint64_t), false));
+    QD_TRY(ensure(rb.rid, (NC + 31) / 32 * 32, false));
     QD_TRY(grow_ranges(cap));
     const size_t cw[6] = {8, 16, 8, 4, 4, 4};
     for (int q = 0; q < 6; ++q) QD_TRY(ensure(rb.cand[q], (cand_cap ? cand_cap : 1) * cw[q], false));
@@ -421,6 +553,31 @@ int simulate_ranges(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, 
     // the step's child count, for the fixed-point scale of the group sums
     QD_TRY(set_word(ctx, W_TMP, NC));
 
+    // ---- the children's ranges: for rules with grouped children, a grouped
+    // pass over every child (leader offsets and their tile map from one
+    // scan, the leader count in W_NU); otherwise the first range pass
+    bool ids_known = false;
+    if constexpr (has_grouped<Rule>::value) {
+        const uint64_t ltiles_cap = NC / kLeaderTile + 2;  // leaders <= children
+        QD_TRY(ensure(ctx->buf[B_LBEG], (NP + 1) * sizeof(uint64_t), false));
+        QD_TRY(ensure(rb.ltile, ltiles_cap * sizeof(uint64_t), false));
+        clk.begin(1);
+        prim::lookback lb;
+        QD_TRY(chain_at(ctx, 0, (NP + prim::kTile - 1) / prim::kTile + 2, lb));
+        scan_leaders f{bufp<uint32_t>(ctx, B_NCHILD), pidx};
+        prim::k_scan_excl<<<lookback_grid(ctx, NP), prim::kThreads, 0, ctx->stream>>>(
+            f, ctx->d_words + W_NP, bufp<uint64_t>(ctx, B_LBEG), ctx->d_words + W_NU, lb,
+            leader_tile_epilogue{(uint64_t *)rb.ltile.p, ltiles_cap});
+        const uint64_t est_tiles = (NC >> kGroupBits) / kLeaderTile + 1;
+        const unsigned g = (unsigned)std::min<uint64_t>(est_tiles, (uint64_t)ctx->num_sms * 8);
+        k_symbolic_grouped<single_rule<Rule>, range_ids><<<g, prim::kThreads, 0, ctx->stream>>>(
+            rs, pv, bufp<uint64_t>(ctx, B_LBEG), (const uint64_t *)rb.ltile.p, ctx->d_words + W_NU,
+            range_ids{(uint8_t *)rb.rid.p, K}, (unsigned long long *)(ctx->d_words + W_MAXABS));
+        QD_TRY(launched(ctx, 2));
+        clk.end(1);
+        ids_known = true;
+    }
+
     // ---- the range passes
     std::vector<uint64_t> run_off(1, 0);
     uint64_t NU = 0, Mmax = 0;
@@ -429,15 +586,29 @@ int simulate_ranges(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, 
         uint64_t nk = 0;
         while (true) {
             prim::lookback lb;
-            QD_TRY(chain_at(ctx, 0, sym_tiles + 2, lb));
-            const unsigned g = (unsigned)std::min<uint64_t>(sym_tiles, (uint64_t)ctx->num_sms * 4);
-            k_symbolic_range<single_rule<Rule>><<<g, prim::kThreads, 0, ctx->stream>>>(
-                rs, pv, bufp<uint64_t>(ctx, B_TILEPAR), NC, k, K, cap, bufp<uint64_t>(ctx, B_HASH),
-                bufp<double2>(ctx, B_CMAG), bufp<uint32_t>(ctx, B_CSIZE), bufp<uint32_t>(ctx, B_CPAR),
-                (uint32_t *)rb.rcid.p, ctx->d_words + W_NC, lb, (unsigned long long *)(ctx->d_words + W_MAXABS));
+            clk.begin(1);
+            if (k == 0 && !ids_known) {
+                QD_TRY(chain_at(ctx, 0, sym_tiles + 2, lb));
+                const unsigned g = (unsigned)std::min<uint64_t>(sym_tiles, (uint64_t)ctx->num_sms * 4);
+                k_symbolic_first<single_rule<Rule>><<<g, prim::kThreads, 0, ctx->stream>>>(
+                    rs, pv, bufp<uint64_t>(ctx, B_TILEPAR), NC, K, (uint8_t *)rb.rid.p, cap,
+                    bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG), bufp<uint32_t>(ctx, B_CSIZE),
+                    bufp<uint32_t>(ctx, B_CPAR), (uint32_t *)rb.rcid.p, ctx->d_words + W_NC, lb,
+                    (unsigned long long *)(ctx->d_words + W_MAXABS));
+            } else {
+                const uint64_t nblk = (NC + kListChildren - 1) / kListChildren;
+                QD_TRY(chain_at(ctx, 0, nblk + 2, lb));
+                const unsigned g = (unsigned)std::min<uint64_t>(nblk, (uint64_t)ctx->num_sms * 8);
+                k_symbolic_list<single_rule<Rule>><<<g, prim::kThreads, 0, ctx->stream>>>(
+                    rs, pv, bufp<uint64_t>(ctx, B_TILEPAR), sym_tiles, NC, k, (const uint8_t *)rb.rid.p, cap,
+                    bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG), bufp<uint32_t>(ctx, B_CSIZE),
+                    bufp<uint32_t>(ctx, B_CPAR), (uint32_t *)rb.rcid.p, ctx->d_words + W_NC, lb);
+            }
             QD_TRY(launched(ctx));
+            clk.end(1);
             st = read_words(ctx);
             if (st) return st;
+            clk.harvest();
             nk = ctx->h_words[W_NC];
             if (nk <= cap) break;
             // a range above its share (large collision groups): its records
@@ -453,6 +624,7 @@ int simulate_ranges(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, 
         Mmax = std::max(Mmax, Mk);
         const prim::table tb{bufp<prim::table_slot>(ctx, B_KEYS), bufp<unsigned long long>(ctx, B_ACC), Mk, 65536u};
         const uint64_t words = (nk + prim::kTile - 1) / prim::kTile + 2;
+        clk.begin(2);
         {
             fill_set f{};
             f.p[0] = (unsigned char *)tb.slots, f.n[0] = (Mk + 1) * sizeof(prim::table_slot), f.v[0] = 0xff;
@@ -471,6 +643,8 @@ int simulate_ranges(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, 
             tb, src, bufp<uint32_t>(ctx, B_SLOT), ctx->d_words + W_NC, d_maxabs, not_rep, has_join,
             ctx->d_words + W_TMP);
         QD_TRY(launched(ctx, 2));
+        clk.end(2);
+        clk.begin(3);
         const group_view gv{bufp<uint32_t>(ctx, B_SLOT), not_rep, has_join, bufp<double2>(ctx, B_CMAG),
                             bufp<unsigned long long>(ctx, B_ACC), ctx->d_words + W_TMP, d_maxabs, prm.tolerance};
         prim::lookback lb0, lb1, lb2;
@@ -491,6 +665,8 @@ int simulate_ranges(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, 
         prim::k_compact<<<lookback_grid(ctx, nk), prim::kThreads, 0, ctx->stream>>>(fc, ctx->d_words + W_NC,
                                                                                    ctx->d_words + W_NU, lb0);
         QD_TRY(launched(ctx));
+        clk.end(3);
+        clk.begin(4);
         // the range's top max_num_object groups, appended to the candidates
         const key_unorm ku{bufp<uint64_t>(ctx, B_UNORM), bufp<uint64_t>(ctx, B_UCHILD), tk};
         QD_TRY(radix_select(ctx, ctx->d_words + W_NU, nk, maxn, ku));
@@ -499,8 +675,10 @@ int simulate_ranges(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, 
         prim::k_compact_ranked<<<lookback_grid(ctx, nk), prim::kThreads, 0, ctx->stream>>>(
             fk, ctx->d_words + W_NU, ctx->d_words + W_NS, lb1, lb2);
         QD_TRY(launched(ctx));
+        clk.end(4);
         st = read_words(ctx);
         if (st) return st;
+        clk.harvest();
         NU += ctx->h_words[W_NU];
         const uint64_t kept = ctx->h_words[W_NS];
         if (run_off.back() + kept > cand_cap) return QUIDS_ERR_CUDA;  // at most max_num_object per range
@@ -517,6 +695,7 @@ int simulate_ranges(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, 
         QD_TRY(ensure(rb.perm[q], (NCAND ? NCAND : 1) * 4, false));
     }
     int cur = 0;
+    clk.begin(4);
     if (NCAND) {
         k_iota_keys<<<grid_for(ctx, NCAND), prim::kThreads, 0, ctx->stream>>>(cand.glob, NCAND, (uint64_t *)rb.key[0].p,
                                                                               (uint32_t *)rb.perm[0].p);
@@ -562,8 +741,10 @@ int simulate_ranges(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, 
             (unsigned long long *)(ctx->d_words + W_MAXNORM), lbc, lbb, lbt);
         QD_TRY(launched(ctx));
     }
+    clk.end(4);
     st = read_words(ctx);
     if (st) return st;
+    clk.harvest();
     const uint64_t NS = ctx->h_words[W_NS], outbytes = ctx->h_words[W_OUTBYTES];
     out->n_inst = 0;
     out->h_inst_begin.clear();
@@ -579,6 +760,7 @@ int simulate_ranges(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, 
         QD_TRY(set_word(ctx, W_ACC, 0));
         QD_TRY(set_word(ctx, (qd_word)(W_ACC + 1), 0));
         QD_TRY(set_word(ctx, W_DONE, 0));
+        clk.begin(5);
         prim::k_fix_total<<<grid_for(ctx, NS, 4), prim::kThreads, 0, ctx->stream>>>(
             (const double2 *)out->mag.p, ctx->d_words + W_NS, (const unsigned long long *)(ctx->d_words + W_MAXNORM),
             (unsigned long long *)(ctx->d_words + W_ACC), (unsigned int *)(ctx->d_words + W_DONE),
@@ -586,11 +768,14 @@ int simulate_ranges(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, 
         QD_TRY(launched(ctx));
         QD_CUDA(cudaMemcpyAsync(out->d_total.p, ctx->d_words + W_TOTAL, sizeof(double), cudaMemcpyDeviceToDevice,
                                 ctx->stream));
+        clk.end(5);
+        clk.begin(6);
         k_populate<single_rule<Rule>, pc_source, Post><<<grid_for(ctx, NS), prim::kThreads, 0, ctx->stream>>>(
             rs, pv, pc_source{(const uint32_t *)rb.spar.p, (const uint32_t *)rb.scid.p}, ctx->d_words + W_NS,
             (const uint64_t *)out->begin.p, (const uint32_t *)out->size.p, (char *)out->objects.p,
             (double2 *)out->mag.p, (const double *)(ctx->d_words + W_FACTOR), nullptr, err, post);
         QD_TRY(launched(ctx));
+        clk.end(6);
         out->n = NS;
         out->nbytes = outbytes;
         out->total_pending = true;
@@ -599,6 +784,7 @@ int simulate_ranges(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, 
     // of the last kernels
     st = read_words(ctx);
     if (st) return st;
+    clk.harvest();
     s.num_object_out = NS;
     s.out_bytes = outbytes;
     if (timing) {
