@@ -581,7 +581,7 @@ int simulate_batched(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule *rules_
     uint8_t *not_rep = bufp<uint8_t>(ctx, B_NOTREP), *has_join = bufp<uint8_t>(ctx, B_HASJOIN);
     const unsigned long long *d_maxabs = (const unsigned long long *)(ctx->d_words + W_MAXABS);
     direct_src src{bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG)};
-    prim::k_table_claim<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(tb, src, ctx->d_words + W_NC, d_maxabs,
+    prim::k_table_claim<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(tb, src, ctx->d_words + W_NC,
                                                                               bufp<uint32_t>(ctx, B_SLOT), err);
     prim::k_table_accumulate<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
         tb, src, bufp<uint32_t>(ctx, B_SLOT), ctx->d_words + W_NC, d_maxabs, not_rep, has_join);

@@ -1416,7 +1416,7 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, qu
     if (!regions) {
         direct_src src{bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG)};
         prim::k_table_claim<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
-            tb, src, ctx->d_words + W_NC, d_maxabs, bufp<uint32_t>(ctx, B_SLOT), err);
+            tb, src, ctx->d_words + W_NC, bufp<uint32_t>(ctx, B_SLOT), err);
         prim::k_table_accumulate<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
             tb, src, bufp<uint32_t>(ctx, B_SLOT), ctx->d_words + W_NC, d_maxabs, not_rep, has_join);
         QD_TRY(launched(ctx, 2));
@@ -1432,7 +1432,7 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, qu
             bufp<uint32_t>(ctx, B_RIDX), bufp<double2>(ctx, B_RMAG), err);
         region_src src{bufp<uint64_t>(ctx, B_RHASH), bufp<uint32_t>(ctx, B_RIDX), bufp<double2>(ctx, B_RMAG)};
         prim::k_table_claim<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
-            tb, src, ctx->d_words + W_NC, d_maxabs, bufp<uint32_t>(ctx, B_RSLOT), err);
+            tb, src, ctx->d_words + W_NC, bufp<uint32_t>(ctx, B_RSLOT), err);
         prim::k_table_accumulate<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
             tb, src, bufp<uint32_t>(ctx, B_RSLOT), ctx->d_words + W_NC, d_maxabs, not_rep, has_join);
         k_unpermute_slots<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(

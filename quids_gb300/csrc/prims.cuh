@@ -437,17 +437,22 @@ static __global__ void __launch_bounds__(kBins) k_radix_pick(select_state *st, u
 }
 
 // ---------------------------------------------------- collision table
-// slots[M+1] {key, rep} (16 bytes; cleared to all-ones before each step)
-// and acc[M+1][4] (re lo, re hi, im lo, im hi: one 32-byte sector per slot).
-// Pass 1 claims slots (CAS from kEmptyKey) and the claiming thread starts
-// the group with its own child; pass 2, a separate launch, adds the other
-// members, so only the slots need clearing and no fence is needed.
-// Children whose hash is kEmptyKey use the extra slot M.  M need not be a power of two: the home slot is the high half of
-// (mixed hash) * M.
+// slots[M+1] {key, rep, claimer} (16 bytes; cleared to all-ones before each
+// step) and acc[M+1][4] (re lo, re hi, im lo, im hi: one 32-byte sector per
+// slot).  Pass 1 claims slots (CAS from kEmptyKey); the claiming item leaves
+// its index in `claimer` and touches nothing else, and every other member
+// (a joiner) clears the group's sum.  Pass 2, a separate launch (no fences),
+// adds the joiners' magnitudes, and the first joiner to take `claimer` adds
+// the claimer's too.  A group of one never touches acc: its representative
+// keeps its own magnitude.  So only the slots need clearing, and a child of
+// a singleton group costs one random 16-byte access.
+// Children whose hash is kEmptyKey use the extra slot M (no claimer; its sum
+// is cleared by the step's fill).  M need not be a power of two: the home
+// slot is the high half of (mixed hash) * M.
 struct __align__(16) table_slot {
     unsigned long long key;  // kEmptyKey = free
     unsigned int rep;        // minimum child index of the group
-    unsigned int pad;
+    unsigned int claimer;    // item that claimed the slot; 0xffffffff once taken by a joiner
 };
 
 struct table {
@@ -470,20 +475,17 @@ __device__ __forceinline__ void fix_atomic_add(unsigned long long *w, fix128 v) 
 }
 
 // Pass 1: every child item (src.hash(k)) finds or claims the slot of its
-// hash.  The fixed-point scale F comes from the largest component and the
-// child count *d_nf (default: the *d_n items; a hash-range pass gives the
-// whole step's count, so its sums are those of one pass).  The claiming thread initialises the group with its own child (rep =
-// its index, acc = its magnitude); slot_out[k] = slot | kJoin for the others,
-// which pass 2 adds in.  0xffffffff at the probe limit (QUIDS_ERR_TABLE_FULL).
+// hash.  The claiming item writes rep = its child index and claimer = its
+// item index; slot_out[k] = slot | kJoin for the others, which clear the
+// group's sum for pass 2.  0xffffffff at the probe limit
+// (QUIDS_ERR_TABLE_FULL).  Item counts stay below 2^32 - 1.
 constexpr uint32_t kJoin = 0x80000000u;
 constexpr uint32_t kNoSlot = 0xffffffffu;
 
 template <class Src>
-__global__ void __launch_bounds__(kThreads) k_table_claim(table t, Src src, const uint64_t *d_n,
-                                                           const unsigned long long *d_maxabs, uint32_t *slot_out,
-                                                           int *err, const uint64_t *d_nf = nullptr) {
+__global__ void __launch_bounds__(kThreads) k_table_claim(table t, Src src, const uint64_t *d_n, uint32_t *slot_out,
+                                                           int *err) {
     const uint64_t n = *d_n;
-    const int F = fix_scale(__longlong_as_double((long long)*d_maxabs), d_nf ? *d_nf : n);
     for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t h = src.hash(k);
         uint64_t s;
@@ -495,20 +497,17 @@ __global__ void __launch_bounds__(kThreads) k_table_claim(table t, Src src, cons
             uint32_t probe = 0;
             while (true) {
                 const unsigned long long key = atomicCAS(&t.slots[s].key, kEmptyKey, h);
-                if (key == kEmptyKey) {  // claimed: the group starts with this child
-                    const double2 m = src.mag(k);
-                    const fix128 re = to_fix(m.x, F), im = to_fix(m.y, F);
-                    ulonglong4_32a a;
-                    a.x = re.lo;
-                    a.y = re.hi;
-                    a.z = im.lo;
-                    a.w = im.hi;
-                    t.slots[s].rep = (uint32_t)src.child(k);
-                    *(ulonglong4_32a *)&t.acc[4 * s] = a;
+                if (key == kEmptyKey) {  // claimed: rep and claimer in one 8-byte store
+                    *(uint2 *)&t.slots[s].rep = make_uint2((uint32_t)src.child(k), (uint32_t)k);
                     claimed = true;
                     break;
                 }
-                if (key == h) break;
+                if (key == h) {  // a joiner: the group's sum starts at zero
+                    ulonglong4_32a z;
+                    z.x = z.y = z.z = z.w = 0;
+                    *(ulonglong4_32a *)&t.acc[4 * s] = z;
+                    break;
+                }
                 if (++s == t.m) s = 0;
                 if (++probe >= t.max_probes) {
                     set_error(err, QUIDS_ERR_TABLE_FULL);
@@ -523,11 +522,15 @@ __global__ void __launch_bounds__(kThreads) k_table_claim(table t, Src src, cons
 
 // Pass 2: the joiners: rep = minimum child index of the group; acc +=
 // magnitude as an exact 128-bit fixed-point sum per component (scale 2^-F, F
-// from the largest component and the child count), independent of the order
-// of the atomics.  Clears the join marks.  Each atomicMin compares two
-// members: the larger is marked not_rep, the smaller has_join; at the end the
-// representative is the one member never marked not_rep, and it is marked
-// has_join exactly when its group has more than one member.
+// from the largest component and the child count *d_nf -- default: the *d_n
+// items; a hash-range pass gives the whole step's count, so its sums are
+// those of one pass), independent of the order of the atomics.  The joiner
+// that takes the slot's claimer adds the claimer's magnitude as well, so
+// every member is added exactly once.  Clears the join marks.  Each
+// atomicMin compares two members: the larger is marked not_rep, the smaller
+// has_join; at the end the representative is the one member never marked
+// not_rep, and it is marked has_join exactly when its group has more than
+// one member.
 template <class Src>
 __global__ void __launch_bounds__(kThreads) k_table_accumulate(table t, Src src, uint32_t *slot_of,
                                                                 const uint64_t *d_n,
@@ -547,9 +550,16 @@ __global__ void __launch_bounds__(kThreads) k_table_accumulate(table t, Src src,
             not_rep[old > c ? old : c] = 1;
             has_join[old < c ? old : c] = 1;
         }
+        const uint32_t k0 = atomicExch(&t.slots[s].claimer, 0xffffffffu);
         const double2 m = src.mag(k);
-        fix_atomic_add(&t.acc[4ull * s + 0], to_fix(m.x, F));
-        fix_atomic_add(&t.acc[4ull * s + 2], to_fix(m.y, F));
+        fix128 re = to_fix(m.x, F), im = to_fix(m.y, F);
+        if (k0 != 0xffffffffu) {
+            const double2 m0 = src.mag(k0);
+            re = fix_add(re, to_fix(m0.x, F));
+            im = fix_add(im, to_fix(m0.y, F));
+        }
+        fix_atomic_add(&t.acc[4ull * s + 0], re);
+        fix_atomic_add(&t.acc[4ull * s + 2], im);
     }
 }
 

@@ -638,7 +638,7 @@ int simulate_ranges(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, 
         const direct_src src{bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG)};
         uint8_t *not_rep = bufp<uint8_t>(ctx, B_NOTREP), *has_join = bufp<uint8_t>(ctx, B_HASJOIN);
         prim::k_table_claim<<<grid_for(ctx, nk), prim::kThreads, 0, ctx->stream>>>(
-            tb, src, ctx->d_words + W_NC, d_maxabs, bufp<uint32_t>(ctx, B_SLOT), err, ctx->d_words + W_TMP);
+            tb, src, ctx->d_words + W_NC, bufp<uint32_t>(ctx, B_SLOT), err);
         prim::k_table_accumulate<<<grid_for(ctx, nk), prim::kThreads, 0, ctx->stream>>>(
             tb, src, bufp<uint32_t>(ctx, B_SLOT), ctx->d_words + W_NC, d_maxabs, not_rep, has_join,
             ctx->d_words + W_TMP);
