@@ -208,16 +208,20 @@ class Clocks:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def run_step_gpu(ctx, quids, wl, init_state, stats_acc=None, flags=0):
+def run_step_gpu(ctx, quids, wl, init_state, stats_acc=None, flags=0, spare=None):
     """One bench step on device-resident input, through quids_gpu_run (the
-    gate list in one library call): returns (children, final it_t)."""
+    gate list in one library call): returns (children, final it_t).  With the
+    same two handles every step (init_state re-uploaded, `spare`), repeated
+    steps are planned runs replayed as a CUDA graph."""
     if "_ops" not in wl:
         wl["_ops"] = [quids.rule_from(g.kind == "rule", g.code, g.params) for g in wl["gates"]]
-    if "_spare" not in wl:
-        wl["_spare"] = quids.it_t(ctx)
+    if spare is None:
+        if "_spare" not in wl:
+            wl["_spare"] = quids.it_t(ctx)
+        spare = wl["_spare"]
     in_bytes = init_state.num_bytes
-    final, stats = quids.run(init_state, wl["_spare"], wl["_ops"], wl["max"], flags)
-    if final is wl["_spare"]:  # keep a free handle for the next step
+    final, stats = quids.run(init_state, spare, wl["_ops"], wl["max"], flags)
+    if final is spare and spare is wl.get("_spare"):  # keep a free handle for the next step
         wl["_spare"] = init_state
     children = 0
     for st in stats:
@@ -278,11 +282,15 @@ def ours(args, rank, world):
         init_packed = it.download()
         del it
         wl.pop("_spare", None)
-    init = quids.it_t(ctx, init_packed)
+    # the two handles of every step: the input is uploaded into `src` before
+    # each step (outside the timed region), `spare` takes the ping-pong
+    src, spare = quids.it_t(ctx), quids.it_t(ctx)
 
-    # warm-up
+    # warm-up (the first run records the steps' sizes, the next ones are
+    # planned runs, captured as a CUDA graph from the third on)
     for _ in range(args.warmup):
-        run_step_gpu(ctx, quids, wl, quids.it_t(ctx, init_packed))
+        src.upload(init_packed)
+        run_step_gpu(ctx, quids, wl, src, spare=spare)
     ctx.synchronize()
 
     # timed: device-resident input, L2 flushed before each step (outside the events)
@@ -291,19 +299,20 @@ def ours(args, rank, world):
     torch.cuda.synchronize()
     ctx.synchronize()
     launches0 = ctx.lib.quids_gpu_ctx_launch_count(ctx.h)
+    runs0 = ctx.run_counts()
     ms = []
     children = 0
     stats = []
     t_wall0 = time.perf_counter()
     with Clocks(dev) as clk:
         for _ in range(args.steps):
-            src = quids.it_t(ctx, init_packed)
+            src.upload(init_packed)
             with torch.cuda.stream(stream):
                 flush.fill_(1)
                 e0 = torch.cuda.Event(enable_timing=True)
                 e1 = torch.cuda.Event(enable_timing=True)
                 e0.record(stream)
-            c, _ = run_step_gpu(ctx, quids, wl, src)
+            c, _ = run_step_gpu(ctx, quids, wl, src, spare=spare)
             with torch.cuda.stream(stream):
                 e1.record(stream)
             e1.synchronize()
@@ -313,14 +322,15 @@ def ours(args, rank, world):
     barrier(world)
     t_wall = time.perf_counter() - t_wall0
     launches = ctx.lib.quids_gpu_ctx_launch_count(ctx.h) - launches0
+    runs = {k: v - runs0[k] for k, v in ctx.run_counts().items()}
 
     # stage timing: the same steps again with CUDA events around every stage
     # of every rule application (live, on the library's stream)
     for _ in range(args.steps):
-        src = quids.it_t(ctx, init_packed)
+        src.upload(init_packed)
         with torch.cuda.stream(stream):
             flush.fill_(1)
-        run_step_gpu(ctx, quids, wl, src, stats, flags=capi.FLAG_STAGE_TIMING)
+        run_step_gpu(ctx, quids, wl, src, stats, flags=capi.FLAG_STAGE_TIMING, spare=spare)
     ctx.synchronize()
     value, total_ms = job_value(children, sum(ms), world, dev)
 
@@ -357,8 +367,8 @@ def ours(args, rank, world):
         t0 = time.perf_counter()
         e2e_children = 0
         for _ in range(args.steps):
-            src = quids.it_t(ctx, h_in)
-            c, out = run_step_gpu(ctx, quids, wl, src)
+            src.upload(h_in)
+            c, out = run_step_gpu(ctx, quids, wl, src, spare=spare)
             e2e_children += c
             capi.check(ctx.lib.quids_gpu_state_download(out.h, h_out[0].data_ptr(), h_out[1].data_ptr(),
                                                         h_out[2].data_ptr(), h_out[3].data_ptr()), "download")
@@ -379,7 +389,8 @@ def ours(args, rank, world):
             "data": "synthetic (seeded generators; the reference publishes no dataset)",
             "config": dict(wl["config"], parallelism=f"replicas x{world}",
                            l2="flushed before every step (256 MiB write)",
-                           children_per_step=children // args.steps),
+                           children_per_step=children // args.steps,
+                           runs_timed=runs),
             "e2e": e2e,
             "gpu_launches": int(launches),
             "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak,

@@ -99,6 +99,7 @@ typedef struct quids_gpu_params {
                                         step, so stats carries timings and total_proba */
 #define QUIDS_FLAG_NO_REGIONS 4u     /* fill the collision table in child order even when it exceeds L2 */
 #define QUIDS_FLAG_REGIONS 8u        /* fill the collision table region by region even when it is small */
+#define QUIDS_FLAG_NO_PLAN 16u       /* quids_gpu_run: always the synchronous steps (no planned run, no graph) */
 
 /* Counters of one rule step (the reference's public counters plus timing). */
 typedef struct quids_gpu_step_stats {
@@ -143,6 +144,10 @@ int quids_gpu_ctx_trim(quids_gpu_ctx *ctx);
 const char *quids_gpu_status_string(int status);
 /* number of kernels launched by this context since its creation */
 uint64_t quids_gpu_ctx_launch_count(quids_gpu_ctx *ctx);
+/* how the context's quids_gpu_run calls ran: synchronous steps (two host
+ * waits per rule step), planned (one host wait per run), and of the planned
+ * ones, replays of a captured CUDA graph.  Any pointer may be NULL. */
+int quids_gpu_ctx_run_counts(quids_gpu_ctx *ctx, uint64_t *sync_runs, uint64_t *planned_runs, uint64_t *graph_runs);
 
 /* ----------------------------------------------------------------- states
  * A state is the device-resident `it_t`.  Handles are not copyable;

@@ -143,6 +143,14 @@ class Context:
     def trim(self):
         capi.check(self.lib.quids_gpu_ctx_trim(self.h), "trim")
 
+    def run_counts(self) -> dict:
+        """How this context's run() calls ran: "sync" (two host waits per
+        rule step), "planned" (one host wait per run) and "graph" (planned
+        runs replayed from a captured CUDA graph)."""
+        v = [C.c_uint64() for _ in range(3)]
+        capi.check(self.lib.quids_gpu_ctx_run_counts(self.h, *[C.byref(x) for x in v]), "run_counts")
+        return {"sync": int(v[0].value), "planned": int(v[1].value), "graph": int(v[2].value)}
+
 
 _default_ctx = None
 
@@ -365,7 +373,14 @@ def run(a: it_t, b: it_t, ops, max_num_object: int = U64_MAX, flags: int = 0):
     """Applies a list of rules and modifiers in one library call (the loop of
     simulate() calls of the reference's examples, ping-ponging between two
     iterations).  ops: rules/modifiers from ``rules``.  Returns
-    (final it_t, list of per-rule stats)."""
+    (final it_t, list of per-rule stats).
+
+    Repeating a run (same ops, knobs and handles, new input uploaded into
+    ``a``) makes it a planned run: the library sizes every step from the
+    earlier run, launches the whole list without host waits and, from the
+    third run on, replays it as a captured CUDA graph.  The results are the
+    synchronous steps' bit for bit; a step beyond its plan falls back to the
+    synchronous steps from there.  flags |= capi.FLAG_NO_PLAN turns this off."""
     a._flush()
     arr = (capi.Op * max(len(ops), 1))()
     n_rules = 0

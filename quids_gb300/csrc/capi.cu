@@ -9,6 +9,7 @@
 #include <utility>
 
 #include "engine.cuh"
+#include "planned.cuh"
 #include "ranges.cuh"
 #include "rules_qc.cuh"
 #include "rules_qcgd.cuh"
@@ -56,6 +57,307 @@ struct mod_chain {
 };
 
 bool chainable(int kind) { return kind >= QUIDS_MOD_CNOT && kind <= QUIDS_MOD_QCGD_REVERSED_STEP; }
+
+// f(modifier) for the modifier of `kind` built from p
+template <class F>
+int dispatch_modifier(int kind, const quids_gpu_rule_params *p, F &&f) {
+    if (!p) return QUIDS_ERR_BAD_ARG;
+    switch (kind) {
+    case QUIDS_MOD_CNOT: return f(rules::cnot{p->control, p->bit});
+    case QUIDS_MOD_X: return f(rules::xgate{p->bit});
+    case QUIDS_MOD_Y: return f(rules::ygate{p->bit});
+    case QUIDS_MOD_Z: return f(rules::zgate{p->bit});
+    case QUIDS_MOD_QCGD_STEP: return f(qcgd::step{});
+    case QUIDS_MOD_QCGD_REVERSED_STEP: return f(qcgd::reversed_step{});
+    }
+    return QUIDS_ERR_BAD_ARG;
+}
+
+// The modifiers after the rule at ops[i], up to the next rule, that run
+// inside its populate; returns the index of the op after them.
+uint64_t gather_chain(const quids_gpu_op *ops, uint64_t n_ops, uint64_t i, mod_chain &chain) {
+    uint64_t j = i + 1;
+    while (j < n_ops && !ops[j].is_rule && chainable(ops[j].kind) && chain.n < mod_chain::kMax) {
+        chain.kind[chain.n] = ops[j].kind;
+        chain.bit[chain.n] = ops[j].params.bit;
+        chain.control[chain.n] = ops[j].params.control;
+        ++chain.n;
+        ++j;
+    }
+    return j;
+}
+
+int ensure_modstatus(quids_gpu_ctx *ctx) {
+    if (!ctx->buf[B_MODSTATUS].p) {
+        QD_TRY(ensure(ctx->buf[B_MODSTATUS], sizeof(uint64_t)));
+        QD_CUDA(cudaMemsetAsync(ctx->buf[B_MODSTATUS].p, 0, sizeof(uint64_t), ctx->stream));
+    }
+    return QUIDS_OK;
+}
+
+// The ops of a run from ops[i0] (rule i0_rule) on, synchronously, from the
+// state `cur` (the other state is written by the next rule).  st: one entry
+// per rule of the whole run.
+int run_sync(quids_gpu_ctx *ctx, quids_gpu_state *&cur, quids_gpu_state *&other, const quids_gpu_op *ops,
+             uint64_t n_ops, uint64_t i0, uint64_t r0, const quids_gpu_params &prm, quids_gpu_step_stats *st) {
+    uint64_t r = r0;
+    for (uint64_t i = i0; i < n_ops; ++i) {
+        const quids_gpu_op &op = ops[i];
+        int rc;
+        if (op.is_rule) {
+            // the modifiers up to the next rule run inside this rule's populate
+            mod_chain chain;
+            const uint64_t j = gather_chain(ops, n_ops, i, chain);
+            if (chain.n) {
+                QD_TRY(ensure_modstatus(ctx));
+                chain.status = bufp<int>(ctx, B_MODSTATUS);
+            }
+            quids_gpu_step_stats *s = st + r;
+            rc = dispatch_rule(op.kind, &op.params, [&](auto rule) {
+                return chain.n ? ranges::simulate_step(ctx, cur, rule, other, prm, s, chain)
+                               : ranges::simulate_step(ctx, cur, rule, other, prm, s);
+            });
+            ++r;
+            if (!rc) {
+                std::swap(cur, other);
+                i = j - 1;
+            }
+        } else {
+            rc = quids_gpu_apply_modifier(ctx, cur, op.kind, &op.params);
+        }
+        if (rc) return rc;
+    }
+    return QUIDS_OK;
+}
+
+// ------------------------------------------------------------ planned runs
+// quids_gpu_run keeps, per context, the plans of the runs it has seen (op
+// list, knobs and state handles): the first run of an op list is
+// synchronous and records each rule step's counts; the next runs are
+// planned (planned.cuh); from the third on, the planned run is a captured
+// CUDA graph, replayed while its buffers and input size are unchanged.
+using planned::app_plan;
+using planned::run_plan;
+constexpr size_t kMaxPlans = 8;
+
+bool plannable(const quids_gpu_params &prm, const quids_gpu_state *a) {
+    return prm.max_num_object != 0 &&
+           !(prm.flags & (QUIDS_FLAG_STAGE_TIMING | QUIDS_FLAG_REGIONS | QUIDS_FLAG_NO_PLAN)) &&
+           prm.hash_ranges < 2 && a->n_inst == 0;
+}
+
+run_plan *find_plan(quids_gpu_ctx *ctx, const quids_gpu_state *a, const quids_gpu_state *b, const quids_gpu_op *ops,
+                    uint64_t n_ops, const quids_gpu_params &prm) {
+    for (run_plan *p : ctx->plans)
+        if (p->a == a && p->b == b && p->ops.size() == n_ops &&
+            (n_ops == 0 || std::memcmp(p->ops.data(), ops, n_ops * sizeof(quids_gpu_op)) == 0) &&
+            std::memcmp(&p->prm, &prm, sizeof(prm)) == 0)
+            return p;
+    return nullptr;
+}
+
+void drop_plan(quids_gpu_ctx *ctx, run_plan *p) {
+    for (size_t k = 0; k < ctx->plans.size(); ++k)
+        if (ctx->plans[k] == p) {
+            ctx->plans.erase(ctx->plans.begin() + (long)k);
+            delete p;
+            return;
+        }
+}
+
+void drop_plans_of(quids_gpu_ctx *ctx, const quids_gpu_state *st) {
+    for (size_t k = ctx->plans.size(); k-- > 0;)
+        if (ctx->plans[k]->a == st || ctx->plans[k]->b == st) {
+            delete ctx->plans[k];
+            ctx->plans.erase(ctx->plans.begin() + (long)k);
+        }
+}
+
+// The bounds of each rule step from a synchronous run's counts (1/16 and a
+// little more of headroom); false when a step cannot be planned (parent
+// pre-truncation, hash-range passes, 32-bit limits).
+bool make_plan(run_plan &p, const quids_gpu_step_stats *st, uint64_t n_rules, const quids_gpu_params &prm) {
+    const double load = prm.table_load_factor > 0 && prm.table_load_factor < 0.95 ? prm.table_load_factor : 0.5;
+    auto pad = [](uint64_t v) { return v + v / 16 + 64; };
+    p.apps.clear();
+    for (uint64_t r = 0; r < n_rules; ++r) {
+        const quids_gpu_step_stats &s = st[r];
+        if (s.num_parents_kept != s.num_parents || s.hash_ranges) return false;
+        app_plan ap;
+        ap.n_cap = pad(s.num_parents);
+        ap.nc_cap = pad(s.num_object);
+        if (ap.nc_cap >= 0xffffffffull || (double)ap.nc_cap / load + 2 >= (double)0x7ffffff0ull) return false;
+        ap.may_truncate = s.num_object > prm.max_num_object;
+        ap.ns_cap = ap.may_truncate ? std::min<uint64_t>(prm.max_num_object, ap.nc_cap) : ap.nc_cap;
+        ap.bytes_cap = pad(s.out_bytes) + 4096;
+        ap.maxsize_lim = s.max_child_size <= 256 ? 256 : 4096;
+        p.apps.push_back(ap);
+    }
+    return true;
+}
+
+// The launches of a planned run on the stream (captured or not).
+int enqueue_planned(quids_gpu_ctx *ctx, run_plan &p, quids_gpu_state *a, quids_gpu_state *b) {
+    const quids_gpu_op *ops = p.ops.data();
+    const uint64_t n_ops = p.ops.size(), R = p.apps.size();
+    planned::k_plan_start<<<1, 1, 0, ctx->stream>>>(ctx->d_words);
+    QD_TRY(launched(ctx));
+    quids_gpu_state *cur = a, *other = b;
+    const uint64_t *cur_meta = nullptr;  // null: the run's input, of known size
+    const uint64_t n0 = a->n;
+    uint64_t r = 0;
+    for (uint64_t i = 0; i < n_ops; ++i) {
+        const quids_gpu_op &op = ops[i];
+        if (op.is_rule) {
+            mod_chain chain;
+            const uint64_t j = gather_chain(ops, n_ops, i, chain);
+            if (chain.n) chain.status = bufp<int>(ctx, B_MODSTATUS);
+            uint64_t *rec = ctx->h_plan_dev + r * planned::R_WORDS;
+            QD_TRY(dispatch_rule(op.kind, &op.params, [&](auto rule) {
+                return chain.n ? planned::simulate_planned(ctx, cur, cur_meta, n0, rule, other, p.prm, p.apps[r],
+                                                           (uint32_t)r, rec, chain)
+                               : planned::simulate_planned(ctx, cur, cur_meta, n0, rule, other, p.prm, p.apps[r],
+                                                           (uint32_t)r, rec);
+            }));
+            std::swap(cur, other);
+            cur_meta = (const uint64_t *)cur->meta.p;
+            ++r;
+            i = j - 1;
+        } else {
+            const uint64_t cap = r == 0 ? n0 : p.apps[r - 1].ns_cap;
+            QD_TRY(dispatch_modifier(op.kind, &op.params, [&](auto mod) {
+                return planned::apply_modifier_planned(ctx, cur, cur_meta, n0, cap, mod);
+            }));
+        }
+    }
+    planned::k_plan_finish<<<1, 1, 0, ctx->stream>>>(ctx->d_words, R >= 2 ? (const uint64_t *)a->meta.p : nullptr,
+                                                     R >= 1 ? (const uint64_t *)b->meta.p : nullptr,
+                                                     ctx->h_plan_dev + R * planned::R_WORDS);
+    return launched(ctx);
+}
+
+// One planned run of p from *a.  Returns QUIDS_OK (stats filled, both
+// states' host sizes updated), an error, or planned::kReplan with *fail_app
+// the rule step to resume from synchronously (its input state intact).
+int run_planned(quids_gpu_ctx *ctx, run_plan &p, quids_gpu_state *a, quids_gpu_state *b, quids_gpu_step_stats *st,
+                uint64_t *fail_app) {
+    const uint64_t R = p.apps.size();
+    const double load = p.prm.table_load_factor > 0 && p.prm.table_load_factor < 0.95 ? p.prm.table_load_factor : 0.5;
+    // every buffer at the plan's bounds before anything is launched
+    if (ensure_modstatus(ctx)) return planned::kNotRun;
+    // (the input state *a keeps its contents; *b is written before it is read)
+    for (uint64_t r = 0; r < R; ++r)
+        if (planned::ensure_planned(ctx, r % 2 ? a : b, p.apps[r], load, r % 2 == 1)) return planned::kNotRun;
+    const size_t words = R * planned::R_WORDS + 8;
+    if (ctx->h_plan_words < words) {
+        if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return QUIDS_ERR_CUDA;
+        if (ctx->h_plan) cudaFreeHost(ctx->h_plan);
+        ctx->h_plan = ctx->h_plan_dev = nullptr;
+        ctx->h_plan_words = 0;
+        const size_t want = words + words / 2;
+        if (cudaHostAlloc((void **)&ctx->h_plan, want * sizeof(uint64_t), cudaHostAllocMapped) != cudaSuccess ||
+            cudaHostGetDevicePointer((void **)&ctx->h_plan_dev, ctx->h_plan, 0) != cudaSuccess) {
+            cudaGetLastError();
+            if (ctx->h_plan) cudaFreeHost(ctx->h_plan);
+            ctx->h_plan = ctx->h_plan_dev = nullptr;
+            return planned::kNotRun;
+        }
+        ctx->h_plan_words = want;
+        g_alloc_epoch.fetch_add(1);  // graphs name the old words
+    }
+    const uint64_t epoch = g_alloc_epoch.load();
+    if (p.exec && !(p.epoch == epoch && p.n0 == a->n && p.bytes0 == a->nbytes)) {
+        cudaGraphExecDestroy(p.exec);
+        p.exec = nullptr;
+    }
+    bool launched_run = false;
+    if (p.exec) {
+        QD_CUDA(cudaGraphLaunch(p.exec, ctx->stream));
+        ctx->launches += p.graph_launches;
+        ++ctx->runs_graph;
+        launched_run = true;
+    } else if (p.runs >= 1) {  // capture the run once a planned run has succeeded
+        const uint64_t l0 = ctx->launches;
+        g_alloc_frozen = true;
+        cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+        int rc = e == cudaSuccess ? enqueue_planned(ctx, p, a, b) : QUIDS_ERR_CUDA;
+        cudaGraph_t g = nullptr;
+        if (e == cudaSuccess) {
+            const cudaError_t e2 = cudaStreamEndCapture(ctx->stream, &g);
+            if (e2 != cudaSuccess && !rc) rc = QUIDS_ERR_CUDA;
+        }
+        g_alloc_frozen = false;
+        const uint64_t n_launch = ctx->launches - l0;
+        ctx->launches = l0;
+        if (!rc && g && cudaGraphInstantiate(&p.exec, g, 0) == cudaSuccess) {
+            p.epoch = epoch;
+            p.n0 = a->n;
+            p.bytes0 = a->nbytes;
+            p.graph_launches = n_launch;
+            QD_CUDA(cudaGraphLaunch(p.exec, ctx->stream));
+            ctx->launches += n_launch;
+            ++ctx->runs_graph;
+            launched_run = true;
+        } else {
+            p.exec = nullptr;
+        }
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();  // a failed capture leaves nothing behind: run uncaptured
+    }
+    if (!launched_run) {
+        const int rc = enqueue_planned(ctx, p, a, b);
+        if (rc) {
+            cudaStreamSynchronize(ctx->stream);
+            return rc;
+        }
+    }
+    ++ctx->runs_planned;
+    QD_CUDA(cudaStreamSynchronize(ctx->stream));  // the run's one host wait
+    const volatile uint64_t *fin = ctx->h_plan + R * planned::R_WORDS;
+    const int status = (int)(uint32_t)fin[0];
+    const uint64_t fa = status ? fin[1] : R;
+    // the counts of the steps done
+    uint64_t in_bytes = a->nbytes;
+    for (uint64_t r = 0; r < fa && r < R; ++r) {
+        const volatile uint64_t *rec = ctx->h_plan + r * planned::R_WORDS;
+        quids_gpu_step_stats s{};
+        s.num_parents = s.num_parents_kept = rec[planned::R_N];
+        s.num_object = rec[planned::R_NC];
+        s.num_object_after_interferences = rec[planned::R_NU];
+        s.num_object_out = rec[planned::R_NS];
+        s.out_bytes = rec[planned::R_BYTES];
+        s.max_child_size = rec[planned::R_MAXSIZE];
+        s.table_capacity = s.num_object ? rec[planned::R_M] : 0;
+        s.total_proba = std::numeric_limits<double>::quiet_NaN();
+        const double N = (double)s.num_parents, NS = (double)s.num_object_out;
+        const double sbar_p = N ? (double)in_bytes / N : 0, sbar_c = NS ? (double)s.out_bytes / NS : 0;
+        s.algorithmic_bytes = (double)in_bytes + 24.0 * N + 72.0 * (double)s.num_object +
+                              24.0 * (double)s.num_object_after_interferences + NS * (sbar_p + sbar_c + 24.0);
+        in_bytes = s.out_bytes;
+        st[r] = s;
+    }
+    auto set_state = [](quids_gpu_state *x, uint64_t n, uint64_t nbytes) {
+        x->n = n;
+        x->nbytes = nbytes;
+        x->total_pending = true;
+        x->n_inst = 0;
+        x->h_inst_begin.clear();
+    };
+    if (!status) {
+        if (R >= 1) set_state(b, fin[4], fin[5]);
+        if (R >= 2) set_state(a, fin[2], fin[3]);
+        ++p.runs;
+        return QUIDS_OK;
+    }
+    // stopped at rule step fa: its input (a for even fa) is intact, the other state is not
+    quids_gpu_state *in = fa % 2 ? b : a, *out = fa % 2 ? a : b;
+    if (fa >= 1) set_state(in, fa % 2 ? fin[4] : fin[2], fa % 2 ? fin[5] : fin[3]);
+    out->n = out->nbytes = 0;
+    out->total_pending = false;
+    out->total_proba = 0;
+    *fail_app = fa;
+    return status;
+}
 
 __global__ void k_set_words_zero(uint64_t *w, int n) {
     for (int i = threadIdx.x; i < n; i += blockDim.x) w[i] = 0;
@@ -133,6 +435,9 @@ int quids_gpu_ctx_destroy(quids_gpu_ctx *ctx) {
         st->ctx = nullptr;
     }
     ctx->states.clear();
+    for (auto *p : ctx->plans) delete p;
+    ctx->plans.clear();
+    if (ctx->h_plan) cudaFreeHost(ctx->h_plan);
     for (auto &b : ctx->buf) release(b);
     if (ctx->d_words) cudaFree(ctx->d_words);
     if (ctx->h_words) cudaFreeHost(ctx->h_words);
@@ -150,6 +455,14 @@ int quids_gpu_ctx_destroy(quids_gpu_ctx *ctx) {
 void *quids_gpu_ctx_stream(quids_gpu_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
 
 uint64_t quids_gpu_ctx_launch_count(quids_gpu_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+int quids_gpu_ctx_run_counts(quids_gpu_ctx *ctx, uint64_t *sync_runs, uint64_t *planned_runs, uint64_t *graph_runs) {
+    if (!ctx) return QUIDS_ERR_BAD_ARG;
+    if (sync_runs) *sync_runs = ctx->runs_sync;
+    if (planned_runs) *planned_runs = ctx->runs_planned;
+    if (graph_runs) *graph_runs = ctx->runs_graph;
+    return QUIDS_OK;
+}
 
 int quids_gpu_ctx_synchronize(quids_gpu_ctx *ctx) {
     if (!ctx) return QUIDS_ERR_BAD_ARG;
@@ -191,6 +504,7 @@ int quids_gpu_state_destroy(quids_gpu_state *st) {
     }
     cudaSetDevice(st->ctx->device);
     cudaStreamSynchronize(st->ctx->stream);
+    drop_plans_of(st->ctx, st);
     st->ctx->states.erase(st);
     release_state(st);
     delete st;
@@ -309,49 +623,73 @@ int quids_gpu_run(quids_gpu_ctx *ctx, quids_gpu_state *a, quids_gpu_state *b, co
                   uint64_t n_ops, const quids_gpu_params *params, quids_gpu_step_stats *rule_stats,
                   int *final_index) {
     if (!ctx || !a || !b || a == b || (!ops && n_ops) || !params || !final_index) return QUIDS_ERR_BAD_ARG;
-    quids_gpu_state *cur = a, *other = b;
-    uint64_t r = 0;
+    if (a->ctx != ctx || b->ctx != ctx) return QUIDS_ERR_BAD_ARG;
+    QD_CUDA(cudaSetDevice(ctx->device));
     const quids_gpu_params prm = *params;
-    for (uint64_t i = 0; i < n_ops; ++i) {
-        const quids_gpu_op &op = ops[i];
-        int rc;
-        if (op.is_rule) {
-            // the modifiers up to the next rule run inside this rule's populate
-            mod_chain chain;
-            uint64_t j = i + 1;
-            while (j < n_ops && !ops[j].is_rule && chainable(ops[j].kind) && chain.n < mod_chain::kMax) {
-                chain.kind[chain.n] = ops[j].kind;
-                chain.bit[chain.n] = ops[j].params.bit;
-                chain.control[chain.n] = ops[j].params.control;
-                ++chain.n;
-                ++j;
-            }
-            if (chain.n) {
-                if (!ctx->buf[B_MODSTATUS].p) {
-                    QD_TRY(ensure(ctx->buf[B_MODSTATUS], sizeof(uint64_t)));
-                    QD_CUDA(cudaMemsetAsync(ctx->buf[B_MODSTATUS].p, 0, sizeof(uint64_t), ctx->stream));
-                }
-                chain.status = bufp<int>(ctx, B_MODSTATUS);
-            }
-            quids_gpu_step_stats *st = rule_stats ? rule_stats + r : nullptr;
-            rc = dispatch_rule(op.kind, &op.params, [&](auto rule) {
-                return chain.n ? ranges::simulate_step(ctx, cur, rule, other, prm, st, chain)
-                               : ranges::simulate_step(ctx, cur, rule, other, prm, st);
-            });
-            ++r;
-            if (!rc) {
-                std::swap(cur, other);
-                i = j - 1;
-            }
-        } else {
-            rc = quids_gpu_apply_modifier(ctx, cur, op.kind, &op.params);
+    uint64_t n_rules = 0;
+    for (uint64_t i = 0; i < n_ops; ++i) n_rules += ops[i].is_rule ? 1 : 0;
+    std::vector<quids_gpu_step_stats> st(n_rules ? n_rules : 1);
+    quids_gpu_state *cur = a, *other = b;
+    uint64_t i0 = 0, r0 = 0;
+    run_plan *p = n_rules && plannable(prm, a) ? find_plan(ctx, a, b, ops, n_ops, prm) : nullptr;
+    bool replan = false;
+    if (p) {
+        uint64_t fa = 0;
+        const int rc = run_planned(ctx, *p, a, b, st.data(), &fa);
+        if (rc == QUIDS_OK) {
+            if (rule_stats) std::memcpy(rule_stats, st.data(), n_rules * sizeof(quids_gpu_step_stats));
+            *final_index = n_rules % 2 ? 1 : 0;
+            return QUIDS_OK;
         }
-        if (rc) {
-            *final_index = cur == a ? 0 : 1;
+        if (rc == planned::kNotRun) {  // the plan's bounds do not fit: synchronous from now on
+            drop_plan(ctx, p);
+            p = nullptr;
+        } else if (rc != planned::kReplan) {
+            *final_index = fa % 2 ? 1 : 0;
+            if (rule_stats) std::memcpy(rule_stats, st.data(), std::min(fa, n_rules) * sizeof(quids_gpu_step_stats));
             return rc;
+        } else {
+            // resume synchronously at rule step fa, from its intact input
+            replan = true;
+            for (uint64_t i = 0, r = 0; i < n_ops; ++i) {
+                if (!ops[i].is_rule) continue;
+                if (r == fa) {
+                    i0 = i;
+                    break;
+                }
+                mod_chain chain;
+                i = gather_chain(ops, n_ops, i, chain) - 1;
+                ++r;
+            }
+            r0 = fa;
+            if (fa % 2) std::swap(cur, other);
         }
     }
+    ++ctx->runs_sync;
+    const int rc = run_sync(ctx, cur, other, ops, n_ops, i0, r0, prm, st.data());
     *final_index = cur == a ? 0 : 1;
+    if (rule_stats) std::memcpy(rule_stats, st.data(), n_rules * sizeof(quids_gpu_step_stats));
+    if (rc) return rc;
+    // a successful run of a plannable op list: (re)make its plan
+    if (n_rules && plannable(prm, a)) {
+        if (!p) {
+            p = new (std::nothrow) run_plan();
+            if (!p) return QUIDS_OK;
+            p->ops.assign(ops, ops + n_ops);
+            p->prm = prm;
+            p->a = a;
+            p->b = b;
+            ctx->plans.push_back(p);
+            if (ctx->plans.size() > kMaxPlans) drop_plan(ctx, ctx->plans.front());
+        }
+        if (!make_plan(*p, st.data(), n_rules, prm)) {
+            drop_plan(ctx, p);
+        } else if (replan) {
+            p->runs = 0;  // the new bounds are tried uncaptured first
+            if (p->exec) cudaGraphExecDestroy(p->exec);
+            p->exec = nullptr;
+        }
+    }
     return QUIDS_OK;
 }
 

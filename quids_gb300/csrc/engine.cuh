@@ -89,8 +89,14 @@ enum qd_word {
     W_DONE = W_ACC + 2,  // blocks done with the total (u32)
     W_DONE_SCAN,         // blocks done with the child-offset scan (u32)
     W_DONE_LAYOUT,       // blocks done with the layout compaction (u32)
+    W_FAILAPP,           // planned run: the step at which it stopped (~0: none)
+    W_M,                 // planned run: collision table slots of the step
     W_COUNT_WORDS = 24
 };
+
+namespace qd::planned {
+struct run_plan;
+}
 
 struct quids_gpu_ctx {
     int device = 0;
@@ -109,6 +115,12 @@ struct quids_gpu_ctx {
     // live states: destroying the context releases their device memory and
     // orphans them, so states may be destroyed after their context
     std::unordered_set<struct quids_gpu_state *> states;
+    // planned runs of quids_gpu_run (most recent last), and the mapped host
+    // words their steps report into
+    std::vector<qd::planned::run_plan *> plans;
+    uint64_t *h_plan = nullptr, *h_plan_dev = nullptr;
+    size_t h_plan_words = 0;
+    uint64_t runs_sync = 0, runs_planned = 0, runs_graph = 0;
 };
 
 struct quids_gpu_state {
@@ -120,6 +132,9 @@ struct quids_gpu_state {
     mutable double total_proba = 1;
     mutable bool total_pending = false;
     qd_dbuf objects, begin, size, mag, d_total;
+    // u64 [2] {n, nbytes} on the device, written by the steps of a planned
+    // run (the host fields are updated when the run ends)
+    qd_dbuf meta;
     // batched state: n_inst independent instances, each a contiguous run of
     // objects (inst: instance of each object; inst_begin: u64 [n_inst+1]
     // offsets, mirrored in h_inst_begin; inst_total: double [n_inst] total
@@ -145,9 +160,20 @@ inline int cuda_status(cudaError_t e) {
     } while (0)
 #define QD_CUDA(expr) QD_TRY(::qd::engine::cuda_status(expr))
 
+// Bumped by every device (re)allocation or release of a buffer: a captured
+// CUDA graph, which names buffers by address, stays valid while it is
+// unchanged.
+inline std::atomic<uint64_t> g_alloc_epoch{0};
+// Set while a planned run is captured into a graph: a buffer that would have
+// to grow makes ensure() fail with kAllocFrozen instead.
+inline thread_local bool g_alloc_frozen = false;
+constexpr int kAllocFrozen = -1001;
+
 inline int ensure(qd_dbuf &b, size_t bytes, bool headroom = true) {
     if (bytes == 0) bytes = 8;
     if (b.cap >= bytes) return QUIDS_OK;
+    if (g_alloc_frozen) return kAllocFrozen;
+    g_alloc_epoch.fetch_add(1);
     if (b.p) {
         cudaError_t e = cudaFree(b.p);
         b.p = nullptr;
@@ -169,14 +195,38 @@ inline int ensure(qd_dbuf &b, size_t bytes, bool headroom = true) {
     b.cap = want;
     return QUIDS_OK;
 }
+inline void release(qd_dbuf &b);
+// ensure() that keeps the buffer's contents when it grows (a state that is
+// still to be read)
+inline int ensure_keep(qd_dbuf &b, size_t bytes, cudaStream_t s) {
+    if (bytes == 0) bytes = 8;
+    if (b.cap >= bytes) return QUIDS_OK;
+    if (g_alloc_frozen) return kAllocFrozen;
+    qd_dbuf nb;
+    QD_TRY(ensure(nb, bytes));
+    if (b.p) {
+        cudaError_t e = cudaMemcpyAsync(nb.p, b.p, b.cap, cudaMemcpyDeviceToDevice, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            release(nb);
+            return cuda_status(e);
+        }
+        release(b);
+    }
+    b = nb;
+    return QUIDS_OK;
+}
 inline void release(qd_dbuf &b) {
-    if (b.p) cudaFree(b.p);
+    if (b.p) {
+        g_alloc_epoch.fetch_add(1);
+        cudaFree(b.p);
+    }
     b.p = nullptr;
     b.cap = 0;
 }
 inline void release_state(quids_gpu_state *st) {
-    for (qd_dbuf *b : {&st->objects, &st->begin, &st->size, &st->mag, &st->d_total, &st->inst, &st->inst_begin,
-                       &st->inst_total})
+    for (qd_dbuf *b : {&st->objects, &st->begin, &st->size, &st->mag, &st->d_total, &st->meta, &st->inst,
+                       &st->inst_begin, &st->inst_total})
         release(*b);
     st->n = st->nbytes = 0;
     st->n_inst = 0;
@@ -296,15 +346,20 @@ struct fill_set {
     uint64_t n[kMax];
     uint32_t v[kMax];  // the byte replicated
     int count;
+    // region r has (*dn[r]) * mul[r] + add[r] bytes when dn[r] is set (a size
+    // known only on the device; n[r] is then its bound)
+    const uint64_t *dn[kMax];
+    uint64_t mul[kMax], add[kMax];
 };
 static __global__ void __launch_bounds__(256) k_fill(fill_set f) {
     const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (uint64_t)gridDim.x * blockDim.x;
     for (int r = 0; r < f.count; ++r) {
         const uint32_t w = f.v[r] * 0x01010101u;
         const uint4 q = make_uint4(w, w, w, w);
-        const uint64_t n16 = f.n[r] / 16;
+        const uint64_t nb = f.dn[r] ? (*f.dn[r]) * f.mul[r] + f.add[r] : f.n[r];
+        const uint64_t n16 = nb / 16;
         for (uint64_t i = tid; i < n16; i += stride) ((uint4 *)f.p[r])[i] = q;
-        for (uint64_t i = n16 * 16 + tid; i < f.n[r]; i += stride) f.p[r][i] = (unsigned char)f.v[r];
+        for (uint64_t i = n16 * 16 + tid; i < nb; i += stride) f.p[r][i] = (unsigned char)f.v[r];
     }
 }
 inline int fill(quids_gpu_ctx *ctx, const fill_set &f) {
@@ -404,7 +459,8 @@ struct instance_rules {
 template <class RS>
 __global__ void __launch_bounds__(prim::kThreads)
     k_num_child(RS rs, const char *objects, const uint64_t *begin, const uint32_t *size, uint64_t n,
-                uint32_t *nchild, unsigned long long *d_maxsize, int *err) {
+                uint32_t *nchild, unsigned long long *d_maxsize, int *err, const uint64_t *d_n = nullptr) {
+    if (d_n) n = *d_n;  // the parent count on the device (n is then a bound)
     uint32_t mx = 0;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         const auto &rule = rs.get(i);
@@ -444,6 +500,8 @@ struct parents_view {
     const uint64_t *cbeg;  // [np+1]
     const uint64_t *pidx;  // kept parent -> parent index, or null (identity)
     uint64_t np;
+    const uint64_t *d_np = nullptr;  // if set, the parent count on the device (np is then a bound)
+    __device__ __forceinline__ uint64_t nparents() const { return d_np ? *d_np : np; }
 };
 
 struct region_count {
@@ -524,7 +582,7 @@ __global__ void __launch_bounds__(prim::kThreads)
                 }
                 p = plo + (uint64_t)lo;
             } else {
-                p = parent_of(pv.cbeg, pv.np, c);
+                p = parent_of(pv.cbeg, pv.nparents(), c);
             }
             uint64_t oid = pv.pidx ? pv.pidx[p] : p;
             uint32_t cid = (uint32_t)(c - pv.cbeg[p]);
@@ -637,7 +695,7 @@ __global__ void __launch_bounds__(prim::kThreads)
             }
             p = plo + (uint64_t)lo;
         } else {
-            p = parent_of(lbeg, pv.np, l);
+            p = parent_of(lbeg, pv.nparents(), l);
         }
         const uint64_t oid = pv.pidx ? pv.pidx[p] : p;
         const uint64_t c0 = pv.cbeg[p];
@@ -756,7 +814,9 @@ __global__ void __launch_bounds__(prim::kThreads)
 template <class Mod>
 __global__ void __launch_bounds__(prim::kThreads)
     k_modifier(Mod mod, char *objects, const uint64_t *begin, const uint32_t *size, double2 *mag, uint64_t n,
-               int *err) {
+               int *err, const uint64_t *d_n = nullptr, const uint64_t *stop = nullptr) {
+    if (stop && *stop) return;  // a planned run stopped at an earlier step
+    if (d_n) n = *d_n;
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         char *b = objects + begin[i];
         if (!object_fits(mod, size[i])) {

@@ -1,0 +1,359 @@
+// planned.cuh -- planned rule steps: the step of engine.cuh without its two
+// host waits, for runs whose sizes are known beforehand.
+//
+// A step sizes its buffers from the child count and from the survivors'
+// bytes, so simulate_rule waits for both on the host.  A run of ops that is
+// repeated (the same gate list from an input of the same size) has the sizes
+// of its earlier run: a *plan* holds, per rule step, bounds on its parents,
+// children, survivors and output bytes.  A planned step allocates to those
+// bounds and launches its kernels with grids that cover them; the kernels
+// read the true counts from device words, as they always do.  So nothing
+// waits on the host, the whole run is one stream of launches, and it can be
+// captured once as a CUDA graph and replayed.
+//
+// Guards on the device keep the result exact:
+//  * k_plan_begin: the step's parents fit the plan (and need no parent
+//    pre-truncation);
+//  * k_plan_sizes, after the child count: the children fit, the child size
+//    bound fits the symbolic pass chosen, and a step planned without
+//    truncation still needs none;
+//  * k_plan_end, after the layout: the output bytes fit.
+// A step that does not fit sets the status kReplan and the step index, and
+// from then on every step and modifier of the run does nothing: the failed
+// step's input state is left as it was (no kernel writes it), so the host
+// resumes the run there with the synchronous steps.  A real error (an unfit
+// object, a full table, ...) stops the run the same way and is returned.
+#pragma once
+#include <vector>
+
+#include "engine.cuh"
+
+namespace qd::planned {
+using namespace qd::engine;
+
+constexpr int kReplan = -1000;  // internal: a planned step's sizes exceeded its plan
+constexpr int kNotRun = -1002;  // internal: the plan's buffers could not be had; nothing was launched
+
+// bounds of one rule step of a planned run
+struct app_plan {
+    uint64_t n_cap;        // parents
+    uint64_t nc_cap;       // children
+    uint64_t ns_cap;       // survivors
+    uint64_t bytes_cap;    // output object bytes
+    uint64_t maxsize_lim;  // child size bound of the generic symbolic pass (256 or 4096)
+    bool may_truncate;     // the step takes the truncation path (select, then keep + layout)
+};
+
+// A plan: the op list and knobs it was made for, the two state handles, and
+// the bounds of each rule step; once a planned run of it has succeeded, the
+// run captured as a CUDA graph (valid while no buffer has been reallocated
+// and the input has the size it was captured with).
+struct run_plan {
+    std::vector<quids_gpu_op> ops;
+    quids_gpu_params prm{};
+    quids_gpu_state *a = nullptr, *b = nullptr;
+    std::vector<app_plan> apps;
+    uint64_t runs = 0;                 // planned runs that succeeded
+    cudaGraphExec_t exec = nullptr;
+    uint64_t epoch = 0;                // allocation epoch of the capture
+    uint64_t n0 = 0, bytes0 = 0;       // input size of the capture
+    uint64_t graph_launches = 0;       // kernels in the graph
+    ~run_plan() {
+        if (exec) cudaGraphExecDestroy(exec);
+    }
+};
+
+// what each planned step reports (words per step, written by k_plan_end
+// into mapped host memory)
+enum { R_N, R_NC, R_NU, R_NS, R_BYTES, R_MAXSIZE, R_M, R_DONE, R_WORDS };
+
+__device__ __forceinline__ bool stopped(const uint64_t *words) { return (uint32_t)words[W_STATUS] != 0; }
+__device__ __forceinline__ void stop_at(uint64_t *words, uint32_t app, int code) {
+    if (!stopped(words)) words[W_STATUS] = (uint64_t)(uint32_t)code;
+    if (words[W_FAILAPP] == ~0ull) words[W_FAILAPP] = app;
+}
+
+// Start of a planned run: no status, no failing step.
+static __global__ void k_plan_start(uint64_t *words) {
+    words[W_STATUS] = 0;
+    words[W_FAILAPP] = ~0ull;
+}
+
+// Start of planned step `app`: the step's words (the run's status and
+// failing step carried over), a sticky modifier status moved in, the parent
+// count from the input state's device words (or n_host for the run's
+// input), and nzero zeroed words of look-back chains.
+static __global__ void __launch_bounds__(256)
+    k_plan_begin(uint64_t *words, uint32_t app, uint64_t n_host, const uint64_t *in_meta, uint64_t n_cap,
+                 uint64_t maxn, int *modstatus, uint64_t *zero, uint64_t nzero) {
+    const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid == 0) {
+        uint64_t st = words[W_STATUS];
+        uint64_t fail = words[W_FAILAPP];
+        if (modstatus && *modstatus) {
+            if (!(uint32_t)st) st = (uint64_t)(uint32_t)*modstatus;
+            *modstatus = 0;
+        }
+        uint64_t n = in_meta ? in_meta[0] : n_host;
+        if (!(uint32_t)st && (n > n_cap || n > maxn)) st = (uint64_t)(uint32_t)kReplan;
+        if ((uint32_t)st && fail == ~0ull) fail = app;
+        if ((uint32_t)st) n = 0;
+        for (int w = 0; w < W_COUNT_WORDS; ++w) words[w] = 0;
+        words[W_N] = n;
+        words[W_NP] = n;
+        words[W_STATUS] = st;
+        words[W_FAILAPP] = fail;
+    }
+    for (uint64_t i = tid; i < nzero; i += (uint64_t)gridDim.x * blockDim.x) zero[i] = 0;
+}
+
+// After the child count: check the children against the plan, stop the
+// step if they do not fit (or an earlier kernel failed), and size the
+// collision table on the device: M = max(NC / load + 1, 1024) slots as the
+// synchronous step computes it, with the extra slot's sum cleared.
+static __global__ void k_plan_sizes(uint64_t *words, uint32_t app, uint64_t nc_cap, uint64_t maxsize_lim,
+                                    uint64_t nc_no_trunc, double load, unsigned long long *acc) {
+    uint64_t nc = words[W_NC];
+    if (!stopped(words) && nc > 0) {
+        const uint64_t ms = words[W_MAXSIZE];
+        if (ms > 4096)
+            stop_at(words, app, QUIDS_ERR_SIZE_BOUND);  // per-thread child buffer bound, as the synchronous step
+        else if (nc > nc_cap || ms > maxsize_lim || nc > nc_no_trunc)
+            stop_at(words, app, kReplan);
+    }
+    if (stopped(words)) {
+        stop_at(words, app, 0);
+        words[W_NC] = 0;
+        words[W_NP] = 0;
+        nc = 0;
+    }
+    uint64_t m = (uint64_t)((double)nc / load) + 1;
+    if (m < 1024) m = 1024;
+    words[W_M] = m;
+    for (int k = 0; k < 4; ++k) acc[4 * m + k] = 0;
+}
+
+// After the output layout: check the output bytes, publish the output
+// state's size on the device and the step's counts to the host; a stopped
+// step keeps no survivors (so the total and the populate do nothing) and
+// leaves the output state's words alone.
+static __global__ void k_plan_end(uint64_t *words, uint32_t app, uint64_t bytes_cap, bool truncating,
+                                  uint64_t *out_meta, volatile uint64_t *rec) {
+    if (!stopped(words) && words[W_OUTBYTES] > bytes_cap) stop_at(words, app, kReplan);
+    if (stopped(words)) {
+        stop_at(words, app, 0);
+        words[W_NS] = 0;
+        return;
+    }
+    out_meta[0] = words[W_NS];
+    out_meta[1] = words[W_OUTBYTES];
+    rec[R_N] = words[W_N];
+    rec[R_NC] = words[W_NC];
+    rec[R_NU] = truncating ? words[W_NU] : words[W_NS];
+    rec[R_NS] = words[W_NS];
+    rec[R_BYTES] = words[W_OUTBYTES];
+    rec[R_MAXSIZE] = words[W_MAXSIZE];
+    rec[R_M] = words[W_M];
+    rec[R_DONE] = 1;
+}
+
+// The run's end: its status, failing step and the two states' sizes.
+static __global__ void k_plan_finish(const uint64_t *words, const uint64_t *meta_a, const uint64_t *meta_b,
+                                     volatile uint64_t *out) {
+    out[0] = words[W_STATUS];
+    out[1] = words[W_FAILAPP];
+    out[2] = meta_a ? meta_a[0] : 0;
+    out[3] = meta_a ? meta_a[1] : 0;
+    out[4] = meta_b ? meta_b[0] : 0;
+    out[5] = meta_b ? meta_b[1] : 0;
+    __threadfence_system();
+}
+
+inline uint64_t sym_tiles_of(uint64_t nc) { return (nc + kTileChildren - 1) / kTileChildren; }
+
+// The buffers of a planned step, at the plan's bounds (nothing grows while a
+// run is captured).  keep: the output state's arrays keep their contents as
+// they grow (the run's input state, which later steps write into).
+inline int ensure_planned(quids_gpu_ctx *ctx, quids_gpu_state *out, const app_plan &ap, double load, bool keep) {
+    const uint64_t N = ap.n_cap, NC = ap.nc_cap, NS = ap.ns_cap;
+    const uint64_t M = std::max<uint64_t>((uint64_t)((double)NC / load) + 1, 1024);
+    const uint64_t tiles_nc = (NC + prim::kTile - 1) / prim::kTile;
+    QD_TRY(ensure(ctx->buf[B_NCHILD], (N ? N : 1) * sizeof(uint32_t)));
+    QD_TRY(ensure(ctx->buf[B_LOOKBACK], std::max(lookback_words(N), 4 * (tiles_nc + 2)) * sizeof(uint64_t)));
+    QD_TRY(ensure(ctx->buf[B_CBEGIN], (N + 1) * sizeof(uint64_t)));
+    QD_TRY(ensure(ctx->buf[B_LBEG], (N + 1) * sizeof(uint64_t)));
+    QD_TRY(ensure(ctx->buf[B_TILEPAR], (std::max(sym_tiles_of(NC), NC / kLeaderTile) + 2) * sizeof(uint64_t)));
+    QD_TRY(ensure(ctx->buf[B_HASH], NC * sizeof(uint64_t)));
+    QD_TRY(ensure(ctx->buf[B_CMAG], NC * sizeof(double2)));
+    QD_TRY(ensure(ctx->buf[B_CSIZE], NC * sizeof(uint32_t)));
+    QD_TRY(ensure(ctx->buf[B_SLOT], NC * sizeof(uint32_t)));
+    QD_TRY(ensure(ctx->buf[B_CPAR], NC * sizeof(uint32_t)));
+    QD_TRY(ensure(ctx->buf[B_NOTREP], NC));
+    QD_TRY(ensure(ctx->buf[B_HASJOIN], NC));
+    QD_TRY(ensure(ctx->buf[B_KEYS], (M + 1) * sizeof(prim::table_slot)));
+    QD_TRY(ensure(ctx->buf[B_ACC], 4 * (M + 1) * sizeof(uint64_t)));
+    QD_TRY(ensure(ctx->buf[B_SCHILD], NS * sizeof(uint64_t)));
+    if (ap.may_truncate) {
+        QD_TRY(ensure(ctx->buf[B_UCHILD], NC * sizeof(uint64_t)));
+        QD_TRY(ensure(ctx->buf[B_UMAG], NC * sizeof(double2)));
+        QD_TRY(ensure(ctx->buf[B_UNORM], NC * sizeof(uint64_t)));
+    }
+    QD_TRY(ensure(ctx->buf[B_MODSTATUS], sizeof(uint64_t)));
+    auto grow = [&](qd_dbuf &b, size_t bytes) { return keep ? ensure_keep(b, bytes, ctx->stream) : ensure(b, bytes); };
+    QD_TRY(grow(out->objects, ap.bytes_cap));
+    QD_TRY(grow(out->begin, (NS + 1) * sizeof(uint64_t)));
+    QD_TRY(grow(out->size, NS * sizeof(uint32_t)));
+    QD_TRY(grow(out->mag, NS * sizeof(double2)));
+    QD_TRY(grow(out->d_total, sizeof(double)));
+    QD_TRY(grow(out->meta, 2 * sizeof(uint64_t)));
+    return QUIDS_OK;
+}
+
+// One planned rule step from `in` into `out` (src/quids.hpp:448-543 as
+// simulate_rule runs it, with the plan's bounds in place of the host
+// waits).  in_meta: the input state's device size words (null for the run's
+// input, whose size n_host is known on the host).  rec: the step's report
+// words in mapped host memory.
+template <class Rule, class Post = no_post>
+int simulate_planned(quids_gpu_ctx *ctx, quids_gpu_state *in, const uint64_t *in_meta, uint64_t n_host,
+                     const Rule &rule_, quids_gpu_state *out, const quids_gpu_params &prm, const app_plan &ap,
+                     uint32_t app, uint64_t *rec, const Post &post = Post{}) {
+    const single_rule<Rule> rule{rule_};
+    const trunc_key tk{prm.simple_truncation == 0, prm.seed};
+    const uint64_t maxn = prm.max_num_object;
+    const double load = prm.table_load_factor > 0 && prm.table_load_factor < 0.95 ? prm.table_load_factor : 0.5;
+    const bool fast = (prm.flags & QUIDS_FLAG_NO_FAST_HASH) == 0;
+    QD_TRY(ensure_planned(ctx, out, ap, load, true));  // nothing grows here: the run ensured every step first
+    const uint64_t N = ap.n_cap, NC = ap.nc_cap, NSB = ap.ns_cap;
+    const uint64_t Mb = std::max<uint64_t>((uint64_t)((double)NC / load) + 1, 1024);
+    uint64_t *words = ctx->d_words;
+    int *err = (int *)(words + W_STATUS);
+    out->n_inst = 0;
+    out->h_inst_begin.clear();
+
+    // ---- stage 0: step words, num_child, child offsets (+ the symbolic tile map)
+    const uint64_t nzero0 = lookback_words(N);
+    k_plan_begin<<<(unsigned)std::min<uint64_t>((nzero0 + 255) / 256 + 1, (uint64_t)ctx->num_sms * 4), 256, 0,
+                   ctx->stream>>>(words, app, n_host, in_meta, N, maxn, bufp<int>(ctx, B_MODSTATUS),
+                                  bufp<uint64_t>(ctx, B_LOOKBACK), nzero0);
+    k_num_child<<<grid_for(ctx, N), prim::kThreads, 0, ctx->stream>>>(
+        rule, (const char *)in->objects.p, (const uint64_t *)in->begin.p, (const uint32_t *)in->size.p, N,
+        bufp<uint32_t>(ctx, B_NCHILD), (unsigned long long *)(words + W_MAXSIZE), err, words + W_N);
+    QD_TRY(launched(ctx, 2));
+    const uint64_t sym_tiles = sym_tiles_of(NC);
+    {
+        prim::lookback lb;
+        lookback_view(ctx, N, 1, lb);
+        scan_nchild f{bufp<uint32_t>(ctx, B_NCHILD), nullptr};
+        prim::k_scan_excl<<<lookback_grid(ctx, N), prim::kThreads, 0, ctx->stream>>>(
+            f, words + W_NP, bufp<uint64_t>(ctx, B_CBEGIN), words + W_NC, lb,
+            tile_parents_epilogue{bufp<uint64_t>(ctx, B_TILEPAR), sym_tiles + 2});
+    }
+    k_plan_sizes<<<1, 1, 0, ctx->stream>>>(words, app, ap.nc_cap, ap.maxsize_lim,
+                                           ap.may_truncate ? ~0ull : maxn, load, bufp<unsigned long long>(ctx, B_ACC));
+    QD_TRY(launched(ctx, 2));
+    parents_view pv{(const char *)in->objects.p, (const uint64_t *)in->begin.p, (const uint32_t *)in->size.p,
+                    (const double2 *)in->mag.p, bufp<uint64_t>(ctx, B_CBEGIN), nullptr, N, words + W_NP};
+
+    // ---- stage 1: symbolic iteration
+    bool grouped = false;
+    if constexpr (has_grouped<Rule>::value) grouped = fast;
+    if constexpr (has_grouped<Rule>::value) if (grouped) QD_TRY(launch_symbolic_grouped(ctx, rule, pv, NC));
+    if (!grouped) {
+        const region_count rc{Mb, 0u, nullptr};
+        if (ap.maxsize_lim <= 256) {
+            QD_TRY((launch_symbolic<single_rule<Rule>, 256>(ctx, rule, pv, NC, fast, rc)));
+        } else {
+            QD_TRY((launch_symbolic<single_rule<Rule>, 4096>(ctx, rule, pv, NC, fast, rc)));
+        }
+    }
+
+    // ---- stage 2: collision table, sized on the device
+    const uint64_t tiles_nc = (NC + prim::kTile - 1) / prim::kTile;
+    prim::table tb{bufp<prim::table_slot>(ctx, B_KEYS), bufp<unsigned long long>(ctx, B_ACC), Mb, 65536u,
+                   words + W_M};
+    {
+        fill_set f{};
+        f.p[0] = (unsigned char *)tb.slots, f.n[0] = (Mb + 1) * sizeof(prim::table_slot), f.v[0] = 0xff;
+        f.dn[0] = words + W_M, f.mul[0] = sizeof(prim::table_slot), f.add[0] = sizeof(prim::table_slot);
+        f.p[1] = bufp<unsigned char>(ctx, B_NOTREP), f.n[1] = NC, f.v[1] = 0;
+        f.dn[1] = words + W_NC, f.mul[1] = 1, f.add[1] = 0;
+        f.p[2] = bufp<unsigned char>(ctx, B_HASJOIN), f.n[2] = NC, f.v[2] = 0;
+        f.dn[2] = words + W_NC, f.mul[2] = 1, f.add[2] = 0;
+        f.p[3] = bufp<unsigned char>(ctx, B_LOOKBACK), f.n[3] = 4 * (tiles_nc + 2) * sizeof(uint64_t), f.v[3] = 0;
+        f.count = 4;
+        QD_TRY(fill(ctx, f));
+    }
+    uint8_t *not_rep = bufp<uint8_t>(ctx, B_NOTREP), *has_join = bufp<uint8_t>(ctx, B_HASJOIN);
+    const unsigned long long *d_maxabs = (const unsigned long long *)(words + W_MAXABS);
+    {
+        direct_src src{bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG)};
+        prim::k_table_claim<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(tb, src, words + W_NC,
+                                                                                   bufp<uint32_t>(ctx, B_SLOT), err);
+        prim::k_table_accumulate<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
+            tb, src, bufp<uint32_t>(ctx, B_SLOT), words + W_NC, d_maxabs, not_rep, has_join);
+        QD_TRY(launched(ctx, 2));
+    }
+
+    // ---- stages 3-4: groups above tolerance, truncation, output layout
+    group_view gv{bufp<uint32_t>(ctx, B_SLOT), not_rep, has_join, bufp<double2>(ctx, B_CMAG),
+                  bufp<unsigned long long>(ctx, B_ACC), words + W_NC, d_maxabs, prm.tolerance};
+    const uint32_t align = prm.align_byte_length;
+    unsigned long long *d_maxnorm = (unsigned long long *)(words + W_MAXNORM);
+    if (!ap.may_truncate) {
+        prim::lookback lbc, lbb;
+        lookback_view(ctx, NC, 0, lbc);
+        lookback_view(ctx, NC, 1, lbb);
+        groups_layout f{gv, bufp<uint32_t>(ctx, B_CSIZE), align, (double2 *)out->mag.p, (uint32_t *)out->size.p,
+                        (uint64_t *)out->begin.p, bufp<uint64_t>(ctx, B_SCHILD)};
+        prim::k_compact_layout<groups_layout, false><<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
+            f, words + W_NC, words + W_NS, words + W_OUTBYTES, (uint64_t *)out->begin.p, d_maxnorm, lbc, lbb, lbb);
+        QD_TRY(launched(ctx));
+    } else {
+        prim::lookback lb;
+        lookback_view(ctx, NC, 3, lb);
+        groups_collect f{gv, bufp<uint64_t>(ctx, B_UCHILD), bufp<double2>(ctx, B_UMAG), bufp<uint64_t>(ctx, B_UNORM)};
+        prim::k_compact<<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(f, words + W_NC, words + W_NU, lb);
+        QD_TRY(launched(ctx));
+        key_unorm k1{bufp<uint64_t>(ctx, B_UNORM), bufp<uint64_t>(ctx, B_UCHILD), tk};
+        QD_TRY(radix_select(ctx, words + W_NU, NC, maxn, k1));
+        prim::lookback lbc, lbb, lbt;
+        lookback_view(ctx, NC, 0, lbt);
+        lookback_view(ctx, NC, 1, lbc);
+        lookback_view(ctx, NC, 2, lbb);
+        keep_layout kl{k1, bufp<uint64_t>(ctx, B_UNORM), bufp<uint64_t>(ctx, B_UCHILD), bufp<double2>(ctx, B_UMAG),
+                       ctx->d_sel, bufp<uint32_t>(ctx, B_CSIZE), align, (double2 *)out->mag.p,
+                       (uint32_t *)out->size.p, (uint64_t *)out->begin.p, bufp<uint64_t>(ctx, B_SCHILD)};
+        prim::k_compact_layout<keep_layout, true><<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
+            kl, words + W_NU, words + W_NS, words + W_OUTBYTES, (uint64_t *)out->begin.p, d_maxnorm, lbc, lbb, lbt);
+        QD_TRY(launched(ctx));
+    }
+    k_plan_end<<<1, 1, 0, ctx->stream>>>(words, app, ap.bytes_cap, ap.may_truncate, (uint64_t *)out->meta.p, rec);
+    QD_TRY(launched(ctx));
+
+    // ---- stage 5: exact total probability, into the output state
+    prim::k_fix_total<<<grid_for(ctx, NSB, 4), prim::kThreads, 0, ctx->stream>>>(
+        (const double2 *)out->mag.p, words + W_NS, d_maxnorm, (unsigned long long *)(words + W_ACC),
+        (unsigned int *)(words + W_DONE), (double *)(words + W_TOTAL), (double *)(words + W_FACTOR),
+        (double *)out->d_total.p, words + W_STATUS);
+    QD_TRY(launched(ctx));
+
+    // ---- stage 6: finalize populate + normalisation (+ the fused modifiers)
+    QD_TRY((launch_populate<single_rule<Rule>, Post>(ctx, rule, pv, NSB, out, post)));
+    out->total_pending = true;
+    return QUIDS_OK;
+}
+
+// A modifier inside a planned run: the state's size from its device words
+// (or n_host for the run's input); nothing once the run has stopped.
+template <class Mod>
+int apply_modifier_planned(quids_gpu_ctx *ctx, quids_gpu_state *st, const uint64_t *meta, uint64_t n_host,
+                           uint64_t n_cap, const Mod &mod) {
+    QD_TRY(ensure(ctx->buf[B_MODSTATUS], sizeof(uint64_t)));
+    k_modifier<Mod><<<grid_for(ctx, n_cap), prim::kThreads, 0, ctx->stream>>>(
+        mod, (char *)st->objects.p, (const uint64_t *)st->begin.p, (const uint32_t *)st->size.p, (double2 *)st->mag.p,
+        n_host, bufp<int>(ctx, B_MODSTATUS), meta, ctx->d_words + W_STATUS);
+    return launched(ctx);
+}
+
+}  // namespace qd::planned

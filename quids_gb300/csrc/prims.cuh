@@ -460,6 +460,7 @@ struct table {
     unsigned long long *acc;
     uint64_t m;              // slots
     uint32_t max_probes;
+    const uint64_t *d_m = nullptr;  // if set, the slot count on the device (m is then a bound)
 };
 
 __device__ __forceinline__ uint64_t table_home(uint64_t h, uint64_t m) {
@@ -486,14 +487,15 @@ template <class Src>
 __global__ void __launch_bounds__(kThreads) k_table_claim(table t, Src src, const uint64_t *d_n, uint32_t *slot_out,
                                                            int *err) {
     const uint64_t n = *d_n;
+    const uint64_t m = t.d_m ? *t.d_m : t.m;
     for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t h = src.hash(k);
         uint64_t s;
         bool claimed = false;
         if (h == kEmptyKey) {
-            s = t.m;
+            s = m;
         } else {
-            s = table_home(h, t.m);
+            s = table_home(h, m);
             uint32_t probe = 0;
             while (true) {
                 const unsigned long long key = atomicCAS(&t.slots[s].key, kEmptyKey, h);
@@ -508,7 +510,7 @@ __global__ void __launch_bounds__(kThreads) k_table_claim(table t, Src src, cons
                     *(ulonglong4_32a *)&t.acc[4 * s] = z;
                     break;
                 }
-                if (++s == t.m) s = 0;
+                if (++s == m) s = 0;
                 if (++probe >= t.max_probes) {
                     set_error(err, QUIDS_ERR_TABLE_FULL);
                     s = ~0ull;
@@ -776,7 +778,8 @@ __global__ void __launch_bounds__(kThreads) k_compact_layout(P p, const uint64_t
 // sum: total = acc 2^-F, factor = sqrt(total).
 static __global__ void __launch_bounds__(kThreads)
     k_fix_total(const double2 *mag, const uint64_t *d_n, const unsigned long long *d_maxnorm,
-                unsigned long long *acc, unsigned int *done, double *d_total, double *d_factor) {
+                unsigned long long *acc, unsigned int *done, double *d_total, double *d_factor,
+                double *out_total = nullptr, const uint64_t *stop = nullptr) {
     __shared__ fix128 sm[kThreads / 32];
     __shared__ bool last;
     const uint64_t n = *d_n;
@@ -807,6 +810,8 @@ static __global__ void __launch_bounds__(kThreads)
         const double t = from_fix(tot, F);
         *d_total = t;
         *d_factor = __dsqrt_rn(t);
+        // the output state's total, unless a planned run stopped (its state is kept as it was)
+        if (out_total && !(stop && *stop)) *out_total = t;
     }
 }
 

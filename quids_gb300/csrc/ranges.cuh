@@ -41,7 +41,7 @@ __device__ __forceinline__ uint32_t range_of(uint64_t h, uint32_t k) {
 // staged in s_cb (count + 1 of them), else found in global memory
 __device__ __forceinline__ uint64_t tile_parent(const uint64_t *s_cb, int count, uint64_t plo,
                                                 const parents_view &pv, uint64_t c) {
-    if (count <= 0) return parent_of(pv.cbeg, pv.np, c);
+    if (count <= 0) return parent_of(pv.cbeg, pv.nparents(), c);
     int lo = 0, hi = count;  // s_cb[lo] <= c < s_cb[hi]
     while (hi - lo > 1) {
         const int mid = (lo + hi) >> 1;
