@@ -434,18 +434,18 @@ def ours_batched(args, rank, world):
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.int32, device=f"cuda:{dev}")
     packed = [W.pack([g], [1.0 + 0j], 8) for g, _, _ in wl["insts"]]
     ops = batch_ops(quids, wl)
-    spare = [quids.it_t(ctx)]
+    # the same two handles every step: the instances are uploaded into `src`
+    # before each step (outside the timed region); repeated steps are planned
+    # runs, replayed as a CUDA graph from the third on
+    src, spare = quids.it_t(ctx), quids.it_t(ctx)
 
-    def step(src):
-        fin, st = quids.run_batched(src, spare[0], ops, wl["max"])
-        if fin is spare[0]:
-            spare[0] = src
+    def step(a):
+        fin, st = quids.run_batched(a, spare, ops, wl["max"])
         return sum(x["num_object"] for x in st), sum(x["algorithmic_bytes"] for x in st), fin
 
     def fresh():
-        a = quids.it_t(ctx)
-        a.upload_batched(packed)
-        return a
+        src.upload_batched(packed)
+        return src
 
     for _ in range(args.warmup):
         step(fresh())
@@ -454,6 +454,7 @@ def ours_batched(args, rank, world):
         torch.distributed.barrier()
     torch.cuda.synchronize()
     launches0 = ctx.lib.quids_gpu_ctx_launch_count(ctx.h)
+    runs0 = ctx.run_counts()
     ms, children, abytes = [], 0, 0.0
     t_wall0 = time.perf_counter()
     with Clocks(dev) as clk:
@@ -474,10 +475,13 @@ def ours_batched(args, rank, world):
     ctx.synchronize()
     t_wall = time.perf_counter() - t_wall0
     launches = ctx.lib.quids_gpu_ctx_launch_count(ctx.h) - launches0
+    runs = {k: v - runs0[k] for k, v in ctx.run_counts().items()}
     barrier(world)
     value, total_ms = job_value(children, sum(ms), world, dev)
 
-    # the same step, instance by instance through the plain path
+    # the same step, instance by instance through the plain path (a fresh
+    # pair of states per instance, as the reference's loop over instances
+    # would: the synchronous steps)
     plain_ms = []
     for _ in range(max(1, min(args.steps, 3))):
         with torch.cuda.stream(stream):
@@ -528,7 +532,8 @@ def ours_batched(args, rank, world):
             "data": "synthetic (seeded generators; the reference publishes no dataset)",
             "config": dict(wl["config"], parallelism=f"replicas x{world}",
                            l2="flushed before every step (256 MiB write)",
-                           children_per_step=children // args.steps),
+                           children_per_step=children // args.steps,
+                           runs_timed=runs),
             "plain_instance_by_instance": {"value": plain_value, "unit": UNIT,
                                            "ms_per_step": statistics.mean(plain_ms),
                                            "batched_over_plain": value / plain_value},

@@ -29,7 +29,8 @@ constexpr uint32_t kMaxInstances = 65536;
 // partitions [0, G]: every entry is written exactly once.
 template <class A>
 __global__ void __launch_bounds__(prim::kThreads)
-    k_inst_bounds(A inst, const uint64_t *d_n, uint32_t G, uint64_t *begin) {
+    k_inst_bounds(A inst, const uint64_t *d_n, uint32_t G, uint64_t *begin, const uint64_t *stop = nullptr) {
+    if (stop && *stop) return;  // a planned run stopped: the output state is left alone
     const uint64_t n = *d_n;
     for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j <= n; j += (uint64_t)gridDim.x * blockDim.x) {
         const int64_t prev = j == 0 ? -1 : (int64_t)inst(j - 1);
@@ -364,7 +365,9 @@ static __global__ void __launch_bounds__(prim::kThreads)
 }
 
 static __global__ void k_binst_factors(const unsigned long long *tot, uint32_t G, const uint64_t *obegin,
-                                       const unsigned long long *maxn, double *total, double *factor) {
+                                       const unsigned long long *maxn, double *total, double *factor,
+                                       const uint64_t *stop = nullptr) {
+    if (stop && *stop) return;  // a planned run stopped: the output state is left alone
     for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < G; g += gridDim.x * blockDim.x) {
         const double t = from_fix(fix128{tot[2ull * g], tot[2ull * g + 1]}, inst_scale(maxn, obegin, g));
         total[g] = t;

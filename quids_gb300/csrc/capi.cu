@@ -146,33 +146,6 @@ bool plannable(const quids_gpu_params &prm, const quids_gpu_state *a) {
            prm.hash_ranges < 2 && a->n_inst == 0;
 }
 
-run_plan *find_plan(quids_gpu_ctx *ctx, const quids_gpu_state *a, const quids_gpu_state *b, const quids_gpu_op *ops,
-                    uint64_t n_ops, const quids_gpu_params &prm) {
-    for (run_plan *p : ctx->plans)
-        if (p->a == a && p->b == b && p->ops.size() == n_ops &&
-            (n_ops == 0 || std::memcmp(p->ops.data(), ops, n_ops * sizeof(quids_gpu_op)) == 0) &&
-            std::memcmp(&p->prm, &prm, sizeof(prm)) == 0)
-            return p;
-    return nullptr;
-}
-
-void drop_plan(quids_gpu_ctx *ctx, run_plan *p) {
-    for (size_t k = 0; k < ctx->plans.size(); ++k)
-        if (ctx->plans[k] == p) {
-            ctx->plans.erase(ctx->plans.begin() + (long)k);
-            delete p;
-            return;
-        }
-}
-
-void drop_plans_of(quids_gpu_ctx *ctx, const quids_gpu_state *st) {
-    for (size_t k = ctx->plans.size(); k-- > 0;)
-        if (ctx->plans[k]->a == st || ctx->plans[k]->b == st) {
-            delete ctx->plans[k];
-            ctx->plans.erase(ctx->plans.begin() + (long)k);
-        }
-}
-
 // The bounds of each rule step from a synchronous run's counts (1/16 and a
 // little more of headroom); false when a step cannot be planned (parent
 // pre-truncation, hash-range passes, 32-bit limits).
@@ -244,98 +217,15 @@ int run_planned(quids_gpu_ctx *ctx, run_plan &p, quids_gpu_state *a, quids_gpu_s
     const uint64_t R = p.apps.size();
     const double load = p.prm.table_load_factor > 0 && p.prm.table_load_factor < 0.95 ? p.prm.table_load_factor : 0.5;
     // every buffer at the plan's bounds before anything is launched
-    if (ensure_modstatus(ctx)) return planned::kNotRun;
     // (the input state *a keeps its contents; *b is written before it is read)
+    if (ensure_modstatus(ctx)) return planned::kNotRun;
     for (uint64_t r = 0; r < R; ++r)
         if (planned::ensure_planned(ctx, r % 2 ? a : b, p.apps[r], load, r % 2 == 1)) return planned::kNotRun;
-    const size_t words = R * planned::R_WORDS + 8;
-    if (ctx->h_plan_words < words) {
-        if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return QUIDS_ERR_CUDA;
-        if (ctx->h_plan) cudaFreeHost(ctx->h_plan);
-        ctx->h_plan = ctx->h_plan_dev = nullptr;
-        ctx->h_plan_words = 0;
-        const size_t want = words + words / 2;
-        if (cudaHostAlloc((void **)&ctx->h_plan, want * sizeof(uint64_t), cudaHostAllocMapped) != cudaSuccess ||
-            cudaHostGetDevicePointer((void **)&ctx->h_plan_dev, ctx->h_plan, 0) != cudaSuccess) {
-            cudaGetLastError();
-            if (ctx->h_plan) cudaFreeHost(ctx->h_plan);
-            ctx->h_plan = ctx->h_plan_dev = nullptr;
-            return planned::kNotRun;
-        }
-        ctx->h_plan_words = want;
-        g_alloc_epoch.fetch_add(1);  // graphs name the old words
-    }
-    const uint64_t epoch = g_alloc_epoch.load();
-    if (p.exec && !(p.epoch == epoch && p.n0 == a->n && p.bytes0 == a->nbytes)) {
-        cudaGraphExecDestroy(p.exec);
-        p.exec = nullptr;
-    }
-    bool launched_run = false;
-    if (p.exec) {
-        QD_CUDA(cudaGraphLaunch(p.exec, ctx->stream));
-        ctx->launches += p.graph_launches;
-        ++ctx->runs_graph;
-        launched_run = true;
-    } else if (p.runs >= 1) {  // capture the run once a planned run has succeeded
-        const uint64_t l0 = ctx->launches;
-        g_alloc_frozen = true;
-        cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
-        int rc = e == cudaSuccess ? enqueue_planned(ctx, p, a, b) : QUIDS_ERR_CUDA;
-        cudaGraph_t g = nullptr;
-        if (e == cudaSuccess) {
-            const cudaError_t e2 = cudaStreamEndCapture(ctx->stream, &g);
-            if (e2 != cudaSuccess && !rc) rc = QUIDS_ERR_CUDA;
-        }
-        g_alloc_frozen = false;
-        const uint64_t n_launch = ctx->launches - l0;
-        ctx->launches = l0;
-        if (!rc && g && cudaGraphInstantiate(&p.exec, g, 0) == cudaSuccess) {
-            p.epoch = epoch;
-            p.n0 = a->n;
-            p.bytes0 = a->nbytes;
-            p.graph_launches = n_launch;
-            QD_CUDA(cudaGraphLaunch(p.exec, ctx->stream));
-            ctx->launches += n_launch;
-            ++ctx->runs_graph;
-            launched_run = true;
-        } else {
-            p.exec = nullptr;
-        }
-        if (g) cudaGraphDestroy(g);
-        cudaGetLastError();  // a failed capture leaves nothing behind: run uncaptured
-    }
-    if (!launched_run) {
-        const int rc = enqueue_planned(ctx, p, a, b);
-        if (rc) {
-            cudaStreamSynchronize(ctx->stream);
-            return rc;
-        }
-    }
-    ++ctx->runs_planned;
-    QD_CUDA(cudaStreamSynchronize(ctx->stream));  // the run's one host wait
-    const volatile uint64_t *fin = ctx->h_plan + R * planned::R_WORDS;
+    const volatile uint64_t *fin = nullptr;
+    QD_TRY(planned::launch_planned(ctx, p, a, [&] { return enqueue_planned(ctx, p, a, b); }, &fin));
     const int status = (int)(uint32_t)fin[0];
     const uint64_t fa = status ? fin[1] : R;
-    // the counts of the steps done
-    uint64_t in_bytes = a->nbytes;
-    for (uint64_t r = 0; r < fa && r < R; ++r) {
-        const volatile uint64_t *rec = ctx->h_plan + r * planned::R_WORDS;
-        quids_gpu_step_stats s{};
-        s.num_parents = s.num_parents_kept = rec[planned::R_N];
-        s.num_object = rec[planned::R_NC];
-        s.num_object_after_interferences = rec[planned::R_NU];
-        s.num_object_out = rec[planned::R_NS];
-        s.out_bytes = rec[planned::R_BYTES];
-        s.max_child_size = rec[planned::R_MAXSIZE];
-        s.table_capacity = s.num_object ? rec[planned::R_M] : 0;
-        s.total_proba = std::numeric_limits<double>::quiet_NaN();
-        const double N = (double)s.num_parents, NS = (double)s.num_object_out;
-        const double sbar_p = N ? (double)in_bytes / N : 0, sbar_c = NS ? (double)s.out_bytes / NS : 0;
-        s.algorithmic_bytes = (double)in_bytes + 24.0 * N + 72.0 * (double)s.num_object +
-                              24.0 * (double)s.num_object_after_interferences + NS * (sbar_p + sbar_c + 24.0);
-        in_bytes = s.out_bytes;
-        st[r] = s;
-    }
+    planned::read_stats(ctx, R, fa, a->nbytes, false, st);
     auto set_state = [](quids_gpu_state *x, uint64_t n, uint64_t nbytes) {
         x->n = n;
         x->nbytes = nbytes;
@@ -504,7 +394,7 @@ int quids_gpu_state_destroy(quids_gpu_state *st) {
     }
     cudaSetDevice(st->ctx->device);
     cudaStreamSynchronize(st->ctx->stream);
-    drop_plans_of(st->ctx, st);
+    planned::drop_plans_of(st->ctx, st);
     st->ctx->states.erase(st);
     release_state(st);
     delete st;
@@ -631,7 +521,7 @@ int quids_gpu_run(quids_gpu_ctx *ctx, quids_gpu_state *a, quids_gpu_state *b, co
     std::vector<quids_gpu_step_stats> st(n_rules ? n_rules : 1);
     quids_gpu_state *cur = a, *other = b;
     uint64_t i0 = 0, r0 = 0;
-    run_plan *p = n_rules && plannable(prm, a) ? find_plan(ctx, a, b, ops, n_ops, prm) : nullptr;
+    run_plan *p = n_rules && plannable(prm, a) ? planned::find_plan(ctx, a, b, ops, n_ops, prm, 0, nullptr) : nullptr;
     bool replan = false;
     if (p) {
         uint64_t fa = 0;
@@ -642,7 +532,7 @@ int quids_gpu_run(quids_gpu_ctx *ctx, quids_gpu_state *a, quids_gpu_state *b, co
             return QUIDS_OK;
         }
         if (rc == planned::kNotRun) {  // the plan's bounds do not fit: synchronous from now on
-            drop_plan(ctx, p);
+            planned::drop_plan(ctx, p);
             p = nullptr;
         } else if (rc != planned::kReplan) {
             *final_index = fa % 2 ? 1 : 0;
@@ -680,10 +570,10 @@ int quids_gpu_run(quids_gpu_ctx *ctx, quids_gpu_state *a, quids_gpu_state *b, co
             p->a = a;
             p->b = b;
             ctx->plans.push_back(p);
-            if (ctx->plans.size() > kMaxPlans) drop_plan(ctx, ctx->plans.front());
+            if (ctx->plans.size() > kMaxPlans) planned::drop_plan(ctx, ctx->plans.front());
         }
         if (!make_plan(*p, st.data(), n_rules, prm)) {
-            drop_plan(ctx, p);
+            planned::drop_plan(ctx, p);
         } else if (replan) {
             p->runs = 0;  // the new bounds are tried uncaptured first
             if (p->exec) cudaGraphExecDestroy(p->exec);

@@ -24,6 +24,8 @@
 // resumes the run there with the synchronous steps.  A real error (an unfit
 // object, a full table, ...) stops the run the same way and is returned.
 #pragma once
+#include <cstring>
+#include <limits>
 #include <vector>
 
 #include "engine.cuh"
@@ -58,10 +60,51 @@ struct run_plan {
     uint64_t epoch = 0;                // allocation epoch of the capture
     uint64_t n0 = 0, bytes0 = 0;       // input size of the capture
     uint64_t graph_launches = 0;       // kernels in the graph
+    // batched runs: the instances, the per-step per-instance rule parameters
+    // (empty: every instance takes its op's), and every step's rules on the
+    // device (rule_off: byte offset of each step's)
+    uint32_t n_inst = 0;
+    std::vector<quids_gpu_rule_params> inst_params;
+    qd_dbuf rules;
+    std::vector<uint64_t> rule_off;
+    bool rules_ready = false;
     ~run_plan() {
         if (exec) cudaGraphExecDestroy(exec);
+        release(rules);
     }
 };
+
+inline run_plan *find_plan(quids_gpu_ctx *ctx, const quids_gpu_state *a, const quids_gpu_state *b,
+                           const quids_gpu_op *ops, uint64_t n_ops, const quids_gpu_params &prm, uint32_t n_inst,
+                           const quids_gpu_rule_params *inst_params) {
+    uint64_t n_rules = 0;
+    for (uint64_t i = 0; i < n_ops; ++i) n_rules += ops[i].is_rule ? 1 : 0;
+    const size_t n_ip = inst_params ? (size_t)n_rules * n_inst : 0;
+    for (run_plan *p : ctx->plans)
+        if (p->a == a && p->b == b && p->n_inst == n_inst && p->ops.size() == n_ops &&
+            (n_ops == 0 || std::memcmp(p->ops.data(), ops, n_ops * sizeof(quids_gpu_op)) == 0) &&
+            std::memcmp(&p->prm, &prm, sizeof(prm)) == 0 && p->inst_params.size() == n_ip &&
+            (n_ip == 0 || std::memcmp(p->inst_params.data(), inst_params, n_ip * sizeof(quids_gpu_rule_params)) == 0))
+            return p;
+    return nullptr;
+}
+
+inline void drop_plan(quids_gpu_ctx *ctx, run_plan *p) {
+    for (size_t k = 0; k < ctx->plans.size(); ++k)
+        if (ctx->plans[k] == p) {
+            ctx->plans.erase(ctx->plans.begin() + (long)k);
+            delete p;
+            return;
+        }
+}
+
+inline void drop_plans_of(quids_gpu_ctx *ctx, const quids_gpu_state *st) {
+    for (size_t k = ctx->plans.size(); k-- > 0;)
+        if (ctx->plans[k]->a == st || ctx->plans[k]->b == st) {
+            delete ctx->plans[k];
+            ctx->plans.erase(ctx->plans.begin() + (long)k);
+        }
+}
 
 // what each planned step reports (words per step, written by k_plan_end
 // into mapped host memory)
@@ -354,6 +397,108 @@ int apply_modifier_planned(quids_gpu_ctx *ctx, quids_gpu_state *st, const uint64
         mod, (char *)st->objects.p, (const uint64_t *)st->begin.p, (const uint32_t *)st->size.p, (double2 *)st->mag.p,
         n_host, bufp<int>(ctx, B_MODSTATUS), meta, ctx->d_words + W_STATUS);
     return launched(ctx);
+}
+
+// The launch of a planned run: the mapped host words its steps report into,
+// then a replay of its CUDA graph (same buffers, same input size), or its
+// capture once a planned run of it has succeeded, or its launches on the
+// stream; then the run's one host wait.  *fin: the words of k_plan_finish.
+template <class Enqueue>
+int launch_planned(quids_gpu_ctx *ctx, run_plan &p, const quids_gpu_state *a, Enqueue &&enqueue,
+                   const volatile uint64_t **fin) {
+    const uint64_t R = p.apps.size();
+    const size_t words = R * R_WORDS + 8;
+    if (ctx->h_plan_words < words) {
+        if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return QUIDS_ERR_CUDA;
+        if (ctx->h_plan) cudaFreeHost(ctx->h_plan);
+        ctx->h_plan = ctx->h_plan_dev = nullptr;
+        ctx->h_plan_words = 0;
+        const size_t want = words + words / 2;
+        if (cudaHostAlloc((void **)&ctx->h_plan, want * sizeof(uint64_t), cudaHostAllocMapped) != cudaSuccess ||
+            cudaHostGetDevicePointer((void **)&ctx->h_plan_dev, ctx->h_plan, 0) != cudaSuccess) {
+            cudaGetLastError();
+            if (ctx->h_plan) cudaFreeHost(ctx->h_plan);
+            ctx->h_plan = ctx->h_plan_dev = nullptr;
+            return kNotRun;
+        }
+        ctx->h_plan_words = want;
+        g_alloc_epoch.fetch_add(1);  // graphs name the old words
+    }
+    const uint64_t epoch = g_alloc_epoch.load();
+    if (p.exec && !(p.epoch == epoch && p.n0 == a->n && p.bytes0 == a->nbytes)) {
+        cudaGraphExecDestroy(p.exec);
+        p.exec = nullptr;
+    }
+    bool launched_run = false;
+    if (p.exec) {
+        QD_CUDA(cudaGraphLaunch(p.exec, ctx->stream));
+        ctx->launches += p.graph_launches;
+        ++ctx->runs_graph;
+        launched_run = true;
+    } else if (p.runs >= 1) {  // capture the run once a planned run has succeeded
+        const uint64_t l0 = ctx->launches;
+        g_alloc_frozen = true;
+        cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+        int rc = e == cudaSuccess ? enqueue() : QUIDS_ERR_CUDA;
+        cudaGraph_t g = nullptr;
+        if (e == cudaSuccess) {
+            const cudaError_t e2 = cudaStreamEndCapture(ctx->stream, &g);
+            if (e2 != cudaSuccess && !rc) rc = QUIDS_ERR_CUDA;
+        }
+        g_alloc_frozen = false;
+        const uint64_t n_launch = ctx->launches - l0;
+        ctx->launches = l0;
+        if (!rc && g && cudaGraphInstantiate(&p.exec, g, 0) == cudaSuccess) {
+            p.epoch = epoch;
+            p.n0 = a->n;
+            p.bytes0 = a->nbytes;
+            p.graph_launches = n_launch;
+            QD_CUDA(cudaGraphLaunch(p.exec, ctx->stream));
+            ctx->launches += n_launch;
+            ++ctx->runs_graph;
+            launched_run = true;
+        } else {
+            p.exec = nullptr;
+        }
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();  // a failed capture leaves nothing behind: run uncaptured
+    }
+    if (!launched_run) {
+        const int rc = enqueue();
+        if (rc) {
+            cudaStreamSynchronize(ctx->stream);
+            return rc;
+        }
+    }
+    ++ctx->runs_planned;
+    QD_CUDA(cudaStreamSynchronize(ctx->stream));  // the run's one host wait
+    *fin = ctx->h_plan + R * R_WORDS;
+    return QUIDS_OK;
+}
+
+// The counters of the first `done` rule steps of a planned run from its
+// report words (in_bytes: the run's input bytes).
+inline void read_stats(const quids_gpu_ctx *ctx, uint64_t R, uint64_t done, uint64_t in_bytes, bool batched,
+                       quids_gpu_step_stats *st) {
+    const double per_n = batched ? 28.0 : 24.0, per_c = batched ? 76.0 : 72.0;
+    for (uint64_t r = 0; r < done && r < R; ++r) {
+        const volatile uint64_t *rec = ctx->h_plan + r * R_WORDS;
+        quids_gpu_step_stats s{};
+        s.num_parents = s.num_parents_kept = rec[R_N];
+        s.num_object = rec[R_NC];
+        s.num_object_after_interferences = rec[R_NU];
+        s.num_object_out = rec[R_NS];
+        s.out_bytes = rec[R_BYTES];
+        s.max_child_size = rec[R_MAXSIZE];
+        s.table_capacity = s.num_object ? rec[R_M] : 0;
+        s.total_proba = std::numeric_limits<double>::quiet_NaN();
+        const double N = (double)s.num_parents, NS = (double)s.num_object_out;
+        const double sbar_p = N ? (double)in_bytes / N : 0, sbar_c = NS ? (double)s.out_bytes / NS : 0;
+        s.algorithmic_bytes = (double)in_bytes + per_n * N + per_c * (double)s.num_object +
+                              per_n * (double)s.num_object_after_interferences + NS * (sbar_p + sbar_c + per_n);
+        in_bytes = s.out_bytes;
+        st[r] = s;
+    }
 }
 
 }  // namespace qd::planned

@@ -174,3 +174,64 @@ def test_planned_error_matches_synchronous(ctx):
     want, _ = quids.run(x, y, ops, U64_MAX, capi.FLAG_NO_PLAN)
     for u, v in zip(fin.download(), want.download()):
         assert np.array_equal(u, v)
+
+
+# ------------------------------------------------------------ batched form
+def batch_case(n_inst, seed, lo=4, hi=8):
+    insts = W.qcgd_batch_instances(n_inst, seed, lo, hi)
+    packed = [W.pack([g], [1.0 + 0j], 8) for g, _, _ in insts]
+    ops = [quids.rules.step, quids.rule_from(True, W.RULE_QCGD_COIN, W.COIN_DEFAULT),
+           [quids.rule_from(True, W.RULE_QCGD_SPLIT_MERGE, sm) for _, sm, _ in insts],
+           [quids.rule_from(True, W.RULE_QCGD_ERASE_CREATE, ec) for _, _, ec in insts]]
+    return packed, ops * 2
+
+
+def batched_result(fin, stats):
+    ib, tot = fin.instances()
+    return fin.download(), ib, tot, [{k: s[k] for k in COUNTERS} for s in stats]
+
+
+def test_planned_batched_bit_identical(ctx):
+    """Two QCGD steps of 24 instances with per-instance angles, under a
+    per-instance cap: planned and replayed batched runs give the synchronous
+    batched steps' states, instance offsets and per-instance totals."""
+    packed, ops = batch_case(24, 5)
+    maxn = 200
+    x, y = quids.it_t(ctx), quids.it_t(ctx)
+    x.upload_batched(packed)
+    want = batched_result(*quids.run_batched(x, y, ops, maxn, capi.FLAG_NO_PLAN))
+    a, b = quids.it_t(ctx), quids.it_t(ctx)
+    c0 = ctx.run_counts()
+    for k in range(4):
+        a.upload_batched(packed)
+        got = batched_result(*quids.run_batched(a, b, ops, maxn))
+        for u, v in zip(got[0], want[0]):
+            assert np.array_equal(u, v), f"run {k}: state differs"
+        assert np.array_equal(got[1], want[1]), f"run {k}: instance offsets differ"
+        assert np.array_equal(got[2], want[2]), f"run {k}: instance totals differ"
+        assert got[3] == want[3], f"run {k}: counters differ"
+    d = counts_delta(ctx, c0)
+    assert d == {"sync": 1, "planned": 3, "graph": 2}, d
+
+
+def test_planned_batched_replan(ctx):
+    """A batched plan made on 4-node graphs, then run on 8-node graphs of the
+    same instance count: the bounds are exceeded, the run resumes
+    synchronously and equals the synchronous batched run."""
+    small, ops_s = batch_case(16, 6, 4, 4)
+    big, _ = batch_case(16, 6, 8, 8)
+    ops = ops_s
+    want = {}
+    for name, packed in (("small", small), ("big", big)):
+        x, y = quids.it_t(ctx), quids.it_t(ctx)
+        x.upload_batched(packed)
+        want[name] = batched_result(*quids.run_batched(x, y, ops, U64_MAX, capi.FLAG_NO_PLAN))
+    a, b = quids.it_t(ctx), quids.it_t(ctx)
+    for k, name in enumerate(["small", "small", "small", "big", "big", "big", "small"]):
+        a.upload_batched(small if name == "small" else big)
+        got = batched_result(*quids.run_batched(a, b, ops, U64_MAX))
+        w = want[name]
+        for u, v in zip(got[0], w[0]):
+            assert np.array_equal(u, v), f"run {k} ({name}): state differs"
+        assert np.array_equal(got[1], w[1]) and np.array_equal(got[2], w[2]), f"run {k} ({name})"
+        assert got[3] == w[3], f"run {k} ({name}): counters differ"
