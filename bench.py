@@ -290,7 +290,7 @@ def ours(args, rank, world):
     # planned runs, captured as a CUDA graph from the third on)
     for _ in range(args.warmup):
         src.upload(init_packed)
-        run_step_gpu(ctx, quids, wl, src, spare=spare)
+        run_step_gpu(ctx, quids, wl, src, spare=spare, flags=capi.FLAG_AUTOTUNE)
     ctx.synchronize()
 
     # timed: device-resident input, L2 flushed before each step (outside the events)
@@ -312,7 +312,7 @@ def ours(args, rank, world):
                 e0 = torch.cuda.Event(enable_timing=True)
                 e1 = torch.cuda.Event(enable_timing=True)
                 e0.record(stream)
-            c, _ = run_step_gpu(ctx, quids, wl, src, spare=spare)
+            c, _ = run_step_gpu(ctx, quids, wl, src, spare=spare, flags=capi.FLAG_AUTOTUNE)
             with torch.cuda.stream(stream):
                 e1.record(stream)
             e1.synchronize()
@@ -368,7 +368,7 @@ def ours(args, rank, world):
         e2e_children = 0
         for _ in range(args.steps):
             src.upload(h_in)
-            c, out = run_step_gpu(ctx, quids, wl, src, spare=spare)
+            c, out = run_step_gpu(ctx, quids, wl, src, spare=spare, flags=capi.FLAG_AUTOTUNE)
             e2e_children += c
             capi.check(ctx.lib.quids_gpu_state_download(out.h, h_out[0].data_ptr(), h_out[1].data_ptr(),
                                                         h_out[2].data_ptr(), h_out[3].data_ptr()), "download")
@@ -390,7 +390,7 @@ def ours(args, rank, world):
             "config": dict(wl["config"], parallelism=f"replicas x{world}",
                            l2="flushed before every step (256 MiB write)",
                            children_per_step=children // args.steps,
-                           runs_timed=runs),
+                           runs_timed=runs, autotuned=ctx.last_tuning()),
             "e2e": e2e,
             "gpu_launches": int(launches),
             "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak,
@@ -440,7 +440,7 @@ def ours_batched(args, rank, world):
     src, spare = quids.it_t(ctx), quids.it_t(ctx)
 
     def step(a):
-        fin, st = quids.run_batched(a, spare, ops, wl["max"])
+        fin, st = quids.run_batched(a, spare, ops, wl["max"], capi.FLAG_AUTOTUNE)
         return sum(x["num_object"] for x in st), sum(x["algorithmic_bytes"] for x in st), fin
 
     def fresh():
@@ -533,7 +533,7 @@ def ours_batched(args, rank, world):
             "config": dict(wl["config"], parallelism=f"replicas x{world}",
                            l2="flushed before every step (256 MiB write)",
                            children_per_step=children // args.steps,
-                           runs_timed=runs),
+                           runs_timed=runs, autotuned=ctx.last_tuning()),
             "plain_instance_by_instance": {"value": plain_value, "unit": UNIT,
                                            "ms_per_step": statistics.mean(plain_ms),
                                            "batched_over_plain": value / plain_value},

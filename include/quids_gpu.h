@@ -100,6 +100,10 @@ typedef struct quids_gpu_params {
 #define QUIDS_FLAG_NO_REGIONS 4u     /* fill the collision table in child order even when it exceeds L2 */
 #define QUIDS_FLAG_REGIONS 8u        /* fill the collision table region by region even when it is small */
 #define QUIDS_FLAG_NO_PLAN 16u       /* quids_gpu_run: always the synchronous steps (no planned run, no graph) */
+#define QUIDS_FLAG_AUTOTUNE 32u      /* quids_gpu_run / quids_gpu_run_batched: before a planned run is first captured
+                                        as a CUDA graph, time it under several launch configurations (collision-table
+                                        load factor, table-pass block size, blocks per SM) and keep the fastest;
+                                        every configuration gives the same result bits */
 
 /* Counters of one rule step (the reference's public counters plus timing). */
 typedef struct quids_gpu_step_stats {
@@ -128,6 +132,17 @@ typedef struct quids_gpu_step_stats {
                                                 stage 4 includes the merge and final selection) */
 } quids_gpu_step_stats;
 
+/* The outcome of the most recent autotuning (QUIDS_FLAG_AUTOTUNE) in a context. */
+typedef struct quids_gpu_tuning {
+    double table_load_factor;   /* chosen collision-table load factor */
+    uint32_t table_block;       /* chosen block size of the collision-table passes */
+    uint32_t blocks_per_sm;     /* chosen grid size of the grid-stride kernels, in blocks per SM */
+    float ms_default;           /* run time (CUDA events, best of 3) under the default configuration */
+    float ms_tuned;             /* run time under the chosen configuration */
+    uint32_t trials;            /* configurations timed */
+    uint32_t pad;
+} quids_gpu_tuning;
+
 typedef struct quids_gpu_ctx quids_gpu_ctx;
 typedef struct quids_gpu_state quids_gpu_state;
 
@@ -148,6 +163,8 @@ uint64_t quids_gpu_ctx_launch_count(quids_gpu_ctx *ctx);
  * waits per rule step), planned (one host wait per run), and of the planned
  * ones, replays of a captured CUDA graph.  Any pointer may be NULL. */
 int quids_gpu_ctx_run_counts(quids_gpu_ctx *ctx, uint64_t *sync_runs, uint64_t *planned_runs, uint64_t *graph_runs);
+/* the most recent autotuning of this context (all zero if none ran) */
+int quids_gpu_ctx_last_tuning(quids_gpu_ctx *ctx, quids_gpu_tuning *out);
 
 /* ----------------------------------------------------------------- states
  * A state is the device-resident `it_t`.  Handles are not copyable;

@@ -151,6 +151,16 @@ class Context:
         capi.check(self.lib.quids_gpu_ctx_run_counts(self.h, *[C.byref(x) for x in v]), "run_counts")
         return {"sync": int(v[0].value), "planned": int(v[1].value), "graph": int(v[2].value)}
 
+    def last_tuning(self) -> dict:
+        """The most recent autotuning of a planned run in this context
+        (run(..., flags=capi.FLAG_AUTOTUNE)): the chosen collision-table load
+        factor, table-pass block size and blocks per SM, the run time under
+        the default and the chosen configuration, and the configurations
+        timed."""
+        t = capi.Tuning()
+        capi.check(self.lib.quids_gpu_ctx_last_tuning(self.h, C.byref(t)), "last_tuning")
+        return {k: getattr(t, k) for k, _ in t._fields_ if k != "pad"}
+
 
 _default_ctx = None
 

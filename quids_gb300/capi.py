@@ -24,6 +24,7 @@ FLAG_STAGE_TIMING = 2
 FLAG_NO_REGIONS = 4
 FLAG_REGIONS = 8
 FLAG_NO_PLAN = 16
+FLAG_AUTOTUNE = 32
 
 
 class QuidsError(RuntimeError):
@@ -70,10 +71,15 @@ class StepStats(C.Structure):
         return d
 
 
+class Tuning(C.Structure):
+    _fields_ = [("table_load_factor", C.c_double), ("table_block", C.c_uint32), ("blocks_per_sm", C.c_uint32),
+                ("ms_default", C.c_float), ("ms_tuned", C.c_float), ("trials", C.c_uint32), ("pad", C.c_uint32)]
+
+
 EXPORTS = [
     "quids_gpu_ctx_create", "quids_gpu_ctx_destroy", "quids_gpu_ctx_stream", "quids_gpu_ctx_synchronize",
     "quids_gpu_ctx_scratch_bytes", "quids_gpu_ctx_trim", "quids_gpu_status_string", "quids_gpu_ctx_launch_count",
-    "quids_gpu_ctx_run_counts",
+    "quids_gpu_ctx_run_counts", "quids_gpu_ctx_last_tuning",
     "quids_gpu_state_create", "quids_gpu_state_destroy", "quids_gpu_state_upload", "quids_gpu_state_num_object",
     "quids_gpu_state_num_bytes", "quids_gpu_state_total_proba", "quids_gpu_state_download",
     "quids_gpu_state_device_arrays", "quids_gpu_simulate", "quids_gpu_apply_modifier",
@@ -117,6 +123,7 @@ def load(build_if_missing: bool = True):
     L.quids_gpu_ctx_launch_count.argtypes = [vp]
     L.quids_gpu_ctx_launch_count.restype = C.c_uint64
     L.quids_gpu_ctx_run_counts.argtypes = [vp, u64p, u64p, u64p]
+    L.quids_gpu_ctx_last_tuning.argtypes = [vp, C.POINTER(Tuning)]
     L.quids_gpu_state_create.argtypes = [vp, C.POINTER(vp)]
     L.quids_gpu_state_destroy.argtypes = [vp]
     L.quids_gpu_state_upload.argtypes = [vp, C.c_uint64, vp, vp, vp, vp, C.c_uint64]

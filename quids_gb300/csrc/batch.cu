@@ -170,17 +170,22 @@ int run_planned_batched(quids_gpu_ctx *ctx, run_plan &p, quids_gpu_state *a, qui
                         quids_gpu_step_stats *st, uint64_t *fail_app) {
     const uint64_t R = p.apps.size();
     const uint32_t G = p.n_inst;
-    const double load = p.prm.table_load_factor > 0 && p.prm.table_load_factor < 0.95 ? p.prm.table_load_factor : 0.5;
     if (!p.rules_ready && upload_rules(ctx, p)) return planned::kNotRun;
-    if (!ctx->buf[B_MODSTATUS].p) {
-        if (ensure(ctx->buf[B_MODSTATUS], sizeof(uint64_t))) return planned::kNotRun;
-        QD_CUDA(cudaMemsetAsync(ctx->buf[B_MODSTATUS].p, 0, sizeof(uint64_t), ctx->stream));
-    }
-    for (uint64_t r = 0; r < R; ++r)
-        if (planned::ensure_planned_batched(ctx, r % 2 ? a : b, p.apps[r], load, r % 2 == 1, G))
-            return planned::kNotRun;
+    auto ensure_all = [&]() -> int {
+        if (!ctx->buf[B_MODSTATUS].p) {
+            QD_TRY(ensure(ctx->buf[B_MODSTATUS], sizeof(uint64_t)));
+            QD_CUDA(cudaMemsetAsync(ctx->buf[B_MODSTATUS].p, 0, sizeof(uint64_t), ctx->stream));
+        }
+        const double load = planned::eff_load(ctx, p.prm);
+        for (uint64_t r = 0; r < R; ++r)
+            QD_TRY(planned::ensure_planned_batched(ctx, r % 2 ? a : b, p.apps[r], load, r % 2 == 1, G));
+        return QUIDS_OK;
+    };
     const volatile uint64_t *fin = nullptr;
-    QD_TRY(planned::launch_planned(ctx, p, a, [&] { return enqueue_planned_batched(ctx, p, a, b); }, &fin));
+    QD_TRY(planned::launch_planned(
+        ctx, p, a, ensure_all, [&] { return enqueue_planned_batched(ctx, p, a, b); },
+        [&] { return planned::backup_input(ctx, p, a, true); }, [&] { return planned::backup_input(ctx, p, a, false); },
+        &fin));
     const int status = (int)(uint32_t)fin[0];
     const uint64_t fa = status ? fin[1] : R;
     planned::read_stats(ctx, R, fa, a->nbytes, true, st);

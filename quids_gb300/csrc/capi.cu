@@ -215,14 +215,19 @@ int enqueue_planned(quids_gpu_ctx *ctx, run_plan &p, quids_gpu_state *a, quids_g
 int run_planned(quids_gpu_ctx *ctx, run_plan &p, quids_gpu_state *a, quids_gpu_state *b, quids_gpu_step_stats *st,
                 uint64_t *fail_app) {
     const uint64_t R = p.apps.size();
-    const double load = p.prm.table_load_factor > 0 && p.prm.table_load_factor < 0.95 ? p.prm.table_load_factor : 0.5;
     // every buffer at the plan's bounds before anything is launched
     // (the input state *a keeps its contents; *b is written before it is read)
-    if (ensure_modstatus(ctx)) return planned::kNotRun;
-    for (uint64_t r = 0; r < R; ++r)
-        if (planned::ensure_planned(ctx, r % 2 ? a : b, p.apps[r], load, r % 2 == 1)) return planned::kNotRun;
+    auto ensure_all = [&]() -> int {
+        QD_TRY(ensure_modstatus(ctx));
+        const double load = planned::eff_load(ctx, p.prm);
+        for (uint64_t r = 0; r < R; ++r) QD_TRY(planned::ensure_planned(ctx, r % 2 ? a : b, p.apps[r], load, r % 2));
+        return QUIDS_OK;
+    };
     const volatile uint64_t *fin = nullptr;
-    QD_TRY(planned::launch_planned(ctx, p, a, [&] { return enqueue_planned(ctx, p, a, b); }, &fin));
+    QD_TRY(planned::launch_planned(
+        ctx, p, a, ensure_all, [&] { return enqueue_planned(ctx, p, a, b); },
+        [&] { return planned::backup_input(ctx, p, a, true); }, [&] { return planned::backup_input(ctx, p, a, false); },
+        &fin));
     const int status = (int)(uint32_t)fin[0];
     const uint64_t fa = status ? fin[1] : R;
     planned::read_stats(ctx, R, fa, a->nbytes, false, st);
@@ -345,6 +350,12 @@ int quids_gpu_ctx_destroy(quids_gpu_ctx *ctx) {
 void *quids_gpu_ctx_stream(quids_gpu_ctx *ctx) { return ctx ? (void *)ctx->stream : nullptr; }
 
 uint64_t quids_gpu_ctx_launch_count(quids_gpu_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+int quids_gpu_ctx_last_tuning(quids_gpu_ctx *ctx, quids_gpu_tuning *out) {
+    if (!ctx || !out) return QUIDS_ERR_BAD_ARG;
+    *out = ctx->last_tuning;
+    return QUIDS_OK;
+}
 
 int quids_gpu_ctx_run_counts(quids_gpu_ctx *ctx, uint64_t *sync_runs, uint64_t *planned_runs, uint64_t *graph_runs) {
     if (!ctx) return QUIDS_ERR_BAD_ARG;

@@ -98,6 +98,16 @@ namespace qd::planned {
 struct run_plan;
 }
 
+// Launch knobs a planned run can be tuned over (none changes a result bit):
+// the collision table's load factor (0: the step's table_load_factor), the
+// block size of the table passes, and the blocks per SM of the grid-stride
+// kernels.
+struct qd_knobs {
+    double load = 0;
+    unsigned table_block = 256;
+    int per_sm = 8;
+};
+
 struct quids_gpu_ctx {
     int device = 0;
     int num_sms = 0;
@@ -121,6 +131,8 @@ struct quids_gpu_ctx {
     uint64_t *h_plan = nullptr, *h_plan_dev = nullptr;
     size_t h_plan_words = 0;
     uint64_t runs_sync = 0, runs_planned = 0, runs_graph = 0;
+    qd_knobs tune;                    // in effect while a planned run is launched or captured
+    quids_gpu_tuning last_tuning{};   // the most recent autotuning of a planned run
 };
 
 struct quids_gpu_state {
@@ -239,7 +251,8 @@ inline T *bufp(quids_gpu_ctx *ctx, qd_buf_id id) {
     return (T *)ctx->buf[id].p;
 }
 
-inline unsigned grid_for(quids_gpu_ctx *ctx, uint64_t n, int per_sm = 8) {
+inline unsigned grid_for(quids_gpu_ctx *ctx, uint64_t n, int per_sm = 0) {
+    if (per_sm <= 0) per_sm = ctx->tune.per_sm;
     uint64_t g = (n + prim::kThreads - 1) / prim::kThreads;
     uint64_t cap = (uint64_t)ctx->num_sms * per_sm;
     if (g > cap) g = cap;

@@ -68,9 +68,14 @@ struct run_plan {
     qd_dbuf rules;
     std::vector<uint64_t> rule_off;
     bool rules_ready = false;
+    // launch knobs of the run (QUIDS_FLAG_AUTOTUNE: chosen by timing before the first capture)
+    qd_knobs knobs;
+    bool tuned = false;
+    qd_dbuf backup[6];  // the run's input while it is autotuned
     ~run_plan() {
         if (exec) cudaGraphExecDestroy(exec);
         release(rules);
+        for (auto &b : backup) release(b);
     }
 };
 
@@ -214,6 +219,15 @@ static __global__ void k_plan_finish(const uint64_t *words, const uint64_t *meta
 
 inline uint64_t sym_tiles_of(uint64_t nc) { return (nc + kTileChildren - 1) / kTileChildren; }
 
+// the collision table's load factor of a step's knobs, and of a planned
+// step: the tuned one, else the step's
+inline double prm_load(const quids_gpu_params &prm) {
+    return prm.table_load_factor > 0 && prm.table_load_factor < 0.95 ? prm.table_load_factor : 0.5;
+}
+inline double eff_load(const quids_gpu_ctx *ctx, const quids_gpu_params &prm) {
+    return ctx->tune.load > 0 ? ctx->tune.load : prm_load(prm);
+}
+
 // The buffers of a planned step, at the plan's bounds (nothing grows while a
 // run is captured).  keep: the output state's arrays keep their contents as
 // they grow (the run's input state, which later steps write into).
@@ -264,7 +278,7 @@ int simulate_planned(quids_gpu_ctx *ctx, quids_gpu_state *in, const uint64_t *in
     const single_rule<Rule> rule{rule_};
     const trunc_key tk{prm.simple_truncation == 0, prm.seed};
     const uint64_t maxn = prm.max_num_object;
-    const double load = prm.table_load_factor > 0 && prm.table_load_factor < 0.95 ? prm.table_load_factor : 0.5;
+    const double load = eff_load(ctx, prm);
     const bool fast = (prm.flags & QUIDS_FLAG_NO_FAST_HASH) == 0;
     QD_TRY(ensure_planned(ctx, out, ap, load, true));  // nothing grows here: the run ensured every step first
     const uint64_t N = ap.n_cap, NC = ap.nc_cap, NSB = ap.ns_cap;
@@ -331,9 +345,9 @@ int simulate_planned(quids_gpu_ctx *ctx, quids_gpu_state *in, const uint64_t *in
     const unsigned long long *d_maxabs = (const unsigned long long *)(words + W_MAXABS);
     {
         direct_src src{bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG)};
-        prim::k_table_claim<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(tb, src, words + W_NC,
+        prim::k_table_claim<<<grid_for(ctx, NC), ctx->tune.table_block, 0, ctx->stream>>>(tb, src, words + W_NC,
                                                                                    bufp<uint32_t>(ctx, B_SLOT), err);
-        prim::k_table_accumulate<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
+        prim::k_table_accumulate<<<grid_for(ctx, NC), ctx->tune.table_block, 0, ctx->stream>>>(
             tb, src, bufp<uint32_t>(ctx, B_SLOT), words + W_NC, d_maxabs, not_rep, has_join);
         QD_TRY(launched(ctx, 2));
     }
@@ -399,15 +413,128 @@ int apply_modifier_planned(quids_gpu_ctx *ctx, quids_gpu_state *st, const uint64
     return launched(ctx);
 }
 
+// A planned run captured as a CUDA graph (the launch knobs are ctx->tune).
+template <class Enqueue>
+int capture_planned(quids_gpu_ctx *ctx, Enqueue &&enqueue, cudaGraphExec_t *exec, uint64_t *n_launch) {
+    const uint64_t l0 = ctx->launches;
+    *exec = nullptr;
+    g_alloc_frozen = true;
+    cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+    int rc = e == cudaSuccess ? enqueue() : QUIDS_ERR_CUDA;
+    cudaGraph_t g = nullptr;
+    if (e == cudaSuccess) {
+        const cudaError_t e2 = cudaStreamEndCapture(ctx->stream, &g);
+        if (e2 != cudaSuccess && !rc) rc = QUIDS_ERR_CUDA;
+    }
+    g_alloc_frozen = false;
+    *n_launch = ctx->launches - l0;
+    ctx->launches = l0;
+    if (!rc && g && cudaGraphInstantiate(exec, g, 0) != cudaSuccess) {
+        *exec = nullptr;
+        rc = QUIDS_ERR_CUDA;
+    }
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();  // a failed capture leaves nothing behind
+    return rc;
+}
+
+// Autotuning (QUIDS_FLAG_AUTOTUNE) of a plan, before its first capture: the
+// run is captured and timed (CUDA events on the stream, best of 3, the input
+// restored before each) under the default knobs, then one knob at a time
+// over its candidates (collision-table load factor, table-pass block size,
+// blocks per SM), keeping a value only when it is faster by more than 2 %.
+// A timed run that stops (beyond its bounds) does not count.
+template <class Ensure, class Enqueue, class Restore>
+int autotune_planned(quids_gpu_ctx *ctx, run_plan &p, Ensure &&ensure_all, Enqueue &&enqueue, Restore &&restore,
+                     const volatile uint64_t *fin) {
+    const float kInf = 3.0e38f;
+    uint32_t trials = 0;
+    auto trial = [&](const qd_knobs &k) -> float {
+        ctx->tune = k;
+        ++trials;
+        if (ensure_all()) return kInf;
+        cudaGraphExec_t ex = nullptr;
+        uint64_t nl = 0;
+        if (capture_planned(ctx, enqueue, &ex, &nl)) return kInf;
+        float best = kInf;
+        for (int rep = 0; rep < 3; ++rep) {
+            if (restore()) break;
+            cudaEventRecord(ctx->ev0, ctx->stream);
+            if (cudaGraphLaunch(ex, ctx->stream) != cudaSuccess) break;
+            cudaEventRecord(ctx->ev1, ctx->stream);
+            if (cudaEventSynchronize(ctx->ev1) != cudaSuccess) break;
+            float ms = kInf;
+            cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+            if ((uint32_t)fin[0] != 0) {  // the run stopped: not a measurement of this configuration
+                best = kInf;
+                break;
+            }
+            best = ms < best ? ms : best;
+        }
+        cudaGraphExecDestroy(ex);
+        cudaGetLastError();
+        return best;
+    };
+    qd_knobs best = p.knobs;
+    const double load0 = best.load > 0 ? best.load : prm_load(p.prm);
+    const float t0 = trial(best);
+    float t_best = t0;
+    const double loads[] = {0.3, 0.5, 0.7};
+    const unsigned blocks[] = {128, 256, 512};
+    const int sms[] = {4, 8, 16};
+    for (double v : loads) {
+        qd_knobs k = best;
+        k.load = v;
+        if ((best.load > 0 ? best.load : load0) == v) continue;
+        const float t = trial(k);
+        if (t < 0.98f * t_best) best = k, t_best = t;
+    }
+    for (unsigned v : blocks) {
+        if (v == best.table_block) continue;
+        qd_knobs k = best;
+        k.table_block = v;
+        const float t = trial(k);
+        if (t < 0.98f * t_best) best = k, t_best = t;
+    }
+    for (int v : sms) {
+        if (v == best.per_sm) continue;
+        qd_knobs k = best;
+        k.per_sm = v;
+        const float t = trial(k);
+        if (t < 0.98f * t_best) best = k, t_best = t;
+    }
+    p.knobs = best;
+    p.tuned = true;
+    ctx->tune = best;
+    quids_gpu_tuning &tu = ctx->last_tuning;
+    tu.table_load_factor = best.load > 0 ? best.load : load0;
+    tu.table_block = best.table_block;
+    tu.blocks_per_sm = (uint32_t)best.per_sm;
+    tu.ms_default = t0;
+    tu.ms_tuned = t_best;
+    tu.trials = trials;
+    QD_TRY(ensure_all());
+    return restore();
+}
+
 // The launch of a planned run: the mapped host words its steps report into,
 // then a replay of its CUDA graph (same buffers, same input size), or its
-// capture once a planned run of it has succeeded, or its launches on the
-// stream; then the run's one host wait.  *fin: the words of k_plan_finish.
-template <class Enqueue>
-int launch_planned(quids_gpu_ctx *ctx, run_plan &p, const quids_gpu_state *a, Enqueue &&enqueue,
-                   const volatile uint64_t **fin) {
+// capture once a planned run of it has succeeded (autotuned first with
+// QUIDS_FLAG_AUTOTUNE), or its launches on the stream; then the run's one
+// host wait.  *fin: the words of k_plan_finish.  ensure_all: every buffer at
+// the plan's bounds for the knobs in ctx->tune; backup / restore: a copy of
+// the run's input, for the autotuning's repeated runs.
+template <class Ensure, class Enqueue, class Backup, class Restore>
+int launch_planned(quids_gpu_ctx *ctx, run_plan &p, const quids_gpu_state *a, Ensure &&ensure_all,
+                   Enqueue &&enqueue, Backup &&backup, Restore &&restore, const volatile uint64_t **fin) {
     const uint64_t R = p.apps.size();
     const size_t words = R * R_WORDS + 8;
+    ctx->tune = p.knobs;
+    struct reset_knobs {
+        quids_gpu_ctx *c;
+        ~reset_knobs() { c->tune = qd_knobs{}; }
+    } reset{ctx};
+    if (ensure_all()) return kNotRun;
     if (ctx->h_plan_words < words) {
         if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return QUIDS_ERR_CUDA;
         if (ctx->h_plan) cudaFreeHost(ctx->h_plan);
@@ -424,10 +551,14 @@ int launch_planned(quids_gpu_ctx *ctx, run_plan &p, const quids_gpu_state *a, En
         ctx->h_plan_words = want;
         g_alloc_epoch.fetch_add(1);  // graphs name the old words
     }
-    const uint64_t epoch = g_alloc_epoch.load();
-    if (p.exec && !(p.epoch == epoch && p.n0 == a->n && p.bytes0 == a->nbytes)) {
+    *fin = ctx->h_plan + R * R_WORDS;
+    if (p.exec && !(p.epoch == g_alloc_epoch.load() && p.n0 == a->n && p.bytes0 == a->nbytes)) {
         cudaGraphExecDestroy(p.exec);
         p.exec = nullptr;
+    }
+    if (!p.exec && p.runs >= 1 && (p.prm.flags & QUIDS_FLAG_AUTOTUNE) && !p.tuned) {
+        QD_TRY(backup());
+        QD_TRY(autotune_planned(ctx, p, ensure_all, enqueue, restore, *fin));
     }
     bool launched_run = false;
     if (p.exec) {
@@ -436,19 +567,9 @@ int launch_planned(quids_gpu_ctx *ctx, run_plan &p, const quids_gpu_state *a, En
         ++ctx->runs_graph;
         launched_run = true;
     } else if (p.runs >= 1) {  // capture the run once a planned run has succeeded
-        const uint64_t l0 = ctx->launches;
-        g_alloc_frozen = true;
-        cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
-        int rc = e == cudaSuccess ? enqueue() : QUIDS_ERR_CUDA;
-        cudaGraph_t g = nullptr;
-        if (e == cudaSuccess) {
-            const cudaError_t e2 = cudaStreamEndCapture(ctx->stream, &g);
-            if (e2 != cudaSuccess && !rc) rc = QUIDS_ERR_CUDA;
-        }
-        g_alloc_frozen = false;
-        const uint64_t n_launch = ctx->launches - l0;
-        ctx->launches = l0;
-        if (!rc && g && cudaGraphInstantiate(&p.exec, g, 0) == cudaSuccess) {
+        uint64_t n_launch = 0;
+        const uint64_t epoch = g_alloc_epoch.load();
+        if (capture_planned(ctx, enqueue, &p.exec, &n_launch) == QUIDS_OK) {
             p.epoch = epoch;
             p.n0 = a->n;
             p.bytes0 = a->nbytes;
@@ -457,11 +578,7 @@ int launch_planned(quids_gpu_ctx *ctx, run_plan &p, const quids_gpu_state *a, En
             ctx->launches += n_launch;
             ++ctx->runs_graph;
             launched_run = true;
-        } else {
-            p.exec = nullptr;
         }
-        if (g) cudaGraphDestroy(g);
-        cudaGetLastError();  // a failed capture leaves nothing behind: run uncaptured
     }
     if (!launched_run) {
         const int rc = enqueue();
@@ -472,7 +589,24 @@ int launch_planned(quids_gpu_ctx *ctx, run_plan &p, const quids_gpu_state *a, En
     }
     ++ctx->runs_planned;
     QD_CUDA(cudaStreamSynchronize(ctx->stream));  // the run's one host wait
-    *fin = ctx->h_plan + R * R_WORDS;
+    return QUIDS_OK;
+}
+
+// A copy of the arrays of a run's input state in the plan (copy = true), or
+// the input restored from it, on the stream.  Batched states add the
+// instance ids and offsets.
+inline int backup_input(quids_gpu_ctx *ctx, run_plan &p, quids_gpu_state *a, bool copy) {
+    qd_dbuf *src[6] = {&a->objects, &a->begin, &a->size, &a->mag, &a->inst, &a->inst_begin};
+    const size_t bytes[6] = {a->nbytes, (a->n + 1) * sizeof(uint64_t), a->n * sizeof(uint32_t), a->n * sizeof(double2),
+                             a->n_inst ? a->n * sizeof(uint32_t) : 0,
+                             a->n_inst ? ((size_t)a->n_inst + 1) * sizeof(uint64_t) : 0};
+    for (int k = 0; k < 6; ++k) {
+        if (!bytes[k]) continue;
+        if (copy) QD_TRY(ensure(p.backup[k], bytes[k], false));
+        void *dst = copy ? p.backup[k].p : src[k]->p;
+        const void *from = copy ? src[k]->p : p.backup[k].p;
+        QD_CUDA(cudaMemcpyAsync(dst, from, bytes[k], cudaMemcpyDeviceToDevice, ctx->stream));
+    }
     return QUIDS_OK;
 }
 

@@ -53,7 +53,7 @@ int simulate_batched_planned(quids_gpu_ctx *ctx, quids_gpu_state *in, const uint
     using namespace qd::batch;
     const uint32_t G = in->n_inst;
     const uint64_t maxc = prm.max_num_object;
-    const double load = prm.table_load_factor > 0 && prm.table_load_factor < 0.95 ? prm.table_load_factor : 0.5;
+    const double load = eff_load(ctx, prm);
     const bool fast = (prm.flags & QUIDS_FLAG_NO_FAST_HASH) == 0;
     const trunc_key tk{prm.simple_truncation == 0, prm.seed};
     QD_TRY(ensure_planned_batched(ctx, out, ap, load, true, G));  // no-ops: the run ensured every step first
@@ -132,9 +132,9 @@ int simulate_batched_planned(quids_gpu_ctx *ctx, quids_gpu_state *in, const uint
     uint8_t *not_rep = bufp<uint8_t>(ctx, B_NOTREP), *has_join = bufp<uint8_t>(ctx, B_HASJOIN);
     const unsigned long long *d_maxabs = (const unsigned long long *)(words + W_MAXABS);
     direct_src src{bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG)};
-    prim::k_table_claim<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(tb, src, words + W_NC,
+    prim::k_table_claim<<<grid_for(ctx, NC), ctx->tune.table_block, 0, ctx->stream>>>(tb, src, words + W_NC,
                                                                                bufp<uint32_t>(ctx, B_SLOT), err);
-    prim::k_table_accumulate<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
+    prim::k_table_accumulate<<<grid_for(ctx, NC), ctx->tune.table_block, 0, ctx->stream>>>(
         tb, src, bufp<uint32_t>(ctx, B_SLOT), words + W_NC, d_maxabs, not_rep, has_join);
     QD_TRY(launched(ctx, 2));
 

@@ -17,6 +17,7 @@
 namespace qd::prim {
 
 constexpr int kThreads = 256;
+constexpr int kMaxTableThreads = 512;  // block size bound of the collision-table passes (a tuning knob)
 constexpr int kItems = 8;
 constexpr int kTile = kThreads * kItems;
 constexpr uint64_t kFlagAgg = 1ull << 62;
@@ -484,7 +485,7 @@ constexpr uint32_t kJoin = 0x80000000u;
 constexpr uint32_t kNoSlot = 0xffffffffu;
 
 template <class Src>
-__global__ void __launch_bounds__(kThreads) k_table_claim(table t, Src src, const uint64_t *d_n, uint32_t *slot_out,
+__global__ void __launch_bounds__(kMaxTableThreads) k_table_claim(table t, Src src, const uint64_t *d_n, uint32_t *slot_out,
                                                            int *err) {
     const uint64_t n = *d_n;
     const uint64_t m = t.d_m ? *t.d_m : t.m;
@@ -534,7 +535,7 @@ __global__ void __launch_bounds__(kThreads) k_table_claim(table t, Src src, cons
 // not_rep, and it is marked has_join exactly when its group has more than
 // one member.
 template <class Src>
-__global__ void __launch_bounds__(kThreads) k_table_accumulate(table t, Src src, uint32_t *slot_of,
+__global__ void __launch_bounds__(kMaxTableThreads) k_table_accumulate(table t, Src src, uint32_t *slot_of,
                                                                 const uint64_t *d_n,
                                                                 const unsigned long long *d_maxabs,
                                                                 uint8_t *not_rep, uint8_t *has_join,

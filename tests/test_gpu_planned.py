@@ -235,3 +235,49 @@ def test_planned_batched_replan(ctx):
             assert np.array_equal(u, v), f"run {k} ({name}): state differs"
         assert np.array_equal(got[1], w[1]) and np.array_equal(got[2], w[2]), f"run {k} ({name})"
         assert got[3] == w[3], f"run {k} ({name}): counters differ"
+
+
+# ------------------------------------------------------------ autotuning
+def check_tuning(t):
+    assert t["trials"] >= 7, t
+    assert t["table_load_factor"] in (0.3, 0.5, 0.7) and t["table_block"] in (128, 256, 512), t
+    assert t["blocks_per_sm"] in (4, 8, 16) and 0 < t["ms_tuned"] <= t["ms_default"], t
+
+
+@pytest.mark.parametrize("case", ["circuit", "layers"])
+def test_autotuned_runs_bit_identical(ctx, case):
+    """QUIDS_FLAG_AUTOTUNE times the planned run under several launch
+    configurations before its first capture; every configuration, and so the
+    chosen one, gives the synchronous steps' result bit for bit."""
+    if case == "circuit":
+        ops, init, maxn = ops_of(W.circuit_small(0)), W.qc_zero_state(12), U64_MAX
+    else:
+        gates = [g for layer in W.circuit_layers(5, n_qubits=16, n_layers=4, n_mods=16) for g in layer]
+        ops, init, maxn = ops_of(gates), W.qc_zero_state(16), 1 << 10
+    want = sync_result(ctx, init, ops, maxn)
+    a, b = quids.it_t(ctx), quids.it_t(ctx)
+    c0 = ctx.run_counts()
+    for k in range(4):
+        a.upload(init)
+        fin, stats = quids.run(a, b, ops, maxn, capi.FLAG_AUTOTUNE)
+        assert_same((fin.download(), fin.total_proba, [{c: s[c] for c in COUNTERS} for s in stats]), want,
+                    f"run {k}")
+    check_tuning(ctx.last_tuning())
+    assert counts_delta(ctx, c0) == {"sync": 1, "planned": 3, "graph": 2}
+
+
+def test_autotuned_batched_bit_identical(ctx):
+    packed, ops = batch_case(24, 7)
+    maxn = 150
+    x, y = quids.it_t(ctx), quids.it_t(ctx)
+    x.upload_batched(packed)
+    want = batched_result(*quids.run_batched(x, y, ops, maxn, capi.FLAG_NO_PLAN))
+    a, b = quids.it_t(ctx), quids.it_t(ctx)
+    for k in range(4):
+        a.upload_batched(packed)
+        got = batched_result(*quids.run_batched(a, b, ops, maxn, capi.FLAG_AUTOTUNE))
+        for u, v in zip(got[0], want[0]):
+            assert np.array_equal(u, v), f"run {k}: state differs"
+        assert np.array_equal(got[1], want[1]) and np.array_equal(got[2], want[2]), f"run {k}"
+        assert got[3] == want[3], f"run {k}: counters differ"
+    check_tuning(ctx.last_tuning())
