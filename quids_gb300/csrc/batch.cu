@@ -77,6 +77,7 @@ bool make_plan_batched(run_plan &p, const quids_gpu_step_stats *st, uint64_t n_r
         ap.ns_cap = all < (double)ap.nc_cap ? prm.max_num_object * (uint64_t)G : ap.nc_cap;
         ap.bytes_cap = pad(s.out_bytes) + 4096;
         ap.maxsize_lim = s.max_child_size <= 256 ? 256 : 4096;
+        ap.maxsize = s.max_child_size;
         p.apps.push_back(ap);
     }
     return true;

@@ -164,6 +164,7 @@ bool make_plan(run_plan &p, const quids_gpu_step_stats *st, uint64_t n_rules, co
         ap.ns_cap = ap.may_truncate ? std::min<uint64_t>(prm.max_num_object, ap.nc_cap) : ap.nc_cap;
         ap.bytes_cap = pad(s.out_bytes) + 4096;
         ap.maxsize_lim = s.max_child_size <= 256 ? 256 : 4096;
+        ap.maxsize = s.max_child_size;
         p.apps.push_back(ap);
     }
     return true;

@@ -773,32 +773,99 @@ struct pc_source {
     }
 };
 
+// Finalize (src/quids.hpp:958-967): each survivor's bytes by the rule's
+// populate_child_simple, padding zeroed, magnitude normalised (and the fused
+// modifiers applied).  Small objects (a few words) are written by their
+// thread directly: neighbouring threads write neighbouring bytes.  For large
+// objects (`staged`, the step's child size bound above kStageMin bytes) a
+// thread writing its own object would scatter small stores over many lines;
+// instead a block takes a chunk of kPopChunk output bytes at a time, the
+// survivors that start in it are populated into shared memory, and the block
+// writes the chunk's contiguous byte range out with coalesced 16-byte
+// stores.  A range too long for the staging buffer (objects near the
+// 4096-byte bound with a large alignment) is written directly.
+constexpr uint32_t kPopChunk = 32 * 1024;
+constexpr uint32_t kPopStage = kPopChunk + 4096 + 16 + 4096;
+constexpr uint64_t kStageMin = 64;
+
+template <class RS, class SS, class Post>
+__device__ __forceinline__ void populate_one(const RS &rs, const parents_view &pv, const SS &ss, uint64_t i,
+                                             const uint64_t *obegin, const uint32_t *osize, char *dst,
+                                             double2 *omag, const double *d_factor, double f0, const uint32_t *finst,
+                                             int *err, const Post &post) {
+    uint64_t p;
+    uint32_t cid;
+    ss.get(i, p, cid);
+    const uint64_t oid = pv.pidx ? pv.pidx[p] : p;
+    const char *pb = pv.objects + pv.begin[oid];
+    const char *pe = pb + pv.size[oid];
+    const uint64_t len = obegin[i + 1] - obegin[i];
+    const uint32_t sz = osize[i];
+    rule_populate_simple(rs.get(oid), pb, pe, dst, cid);
+    for (uint64_t q = sz; q < len; ++q) dst[q] = 0;
+    const double f = finst ? d_factor[finst[i]] : f0;  // batched: the survivor's instance factor
+    if (f != 1.0 || Post::active) {
+        const double2 m = omag[i];
+        mag_t mm{m.x, m.y};
+        if (f != 1.0) mm = mag_t{__ddiv_rn(mm.re, f), __ddiv_rn(mm.im, f)};
+        post(dst, dst + sz, mm, err);
+        omag[i] = make_double2(mm.re, mm.im);
+    }
+}
+
 template <class RS, class SS, class Post>
 __global__ void __launch_bounds__(prim::kThreads)
     k_populate(RS rs, parents_view pv, SS ss, const uint64_t *d_ns, const uint64_t *obegin, const uint32_t *osize,
-               char *objects, double2 *omag, const double *d_factor, const uint32_t *finst, int *err, Post post) {
+               char *objects, double2 *omag, const double *d_factor, const uint32_t *finst, int *err, Post post,
+               bool staged) {
+    __shared__ __align__(16) unsigned char s_out[kPopStage];
+    __shared__ uint64_t s_range[2];
     const uint64_t ns = *d_ns;
+    if (ns == 0) return;
     const double f0 = finst ? 1.0 : *d_factor;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ns; i += (uint64_t)gridDim.x * blockDim.x) {
-        uint64_t p;
-        uint32_t cid;
-        ss.get(i, p, cid);
-        const uint64_t oid = pv.pidx ? pv.pidx[p] : p;
-        const char *pb = pv.objects + pv.begin[oid];
-        const char *pe = pb + pv.size[oid];
-        const uint64_t ob = obegin[i], oe = obegin[i + 1];
-        const uint32_t sz = osize[i];
-        char *dst = objects + ob;
-        rule_populate_simple(rs.get(oid), pb, pe, dst, cid);
-        for (uint64_t q = ob + sz; q < oe; ++q) objects[q] = 0;
-        const double f = finst ? d_factor[finst[i]] : f0;  // batched: the survivor's instance factor
-        if (f != 1.0 || Post::active) {
-            const double2 m = omag[i];
-            mag_t mm{m.x, m.y};
-            if (f != 1.0) mm = mag_t{__ddiv_rn(mm.re, f), __ddiv_rn(mm.im, f)};
-            post(dst, dst + sz, mm, err);
-            omag[i] = make_double2(mm.re, mm.im);
+    if (!staged) {
+        for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ns; i += (uint64_t)gridDim.x * blockDim.x)
+            populate_one(rs, pv, ss, i, obegin, osize, objects + obegin[i], omag, d_factor, f0, finst, err, post);
+        return;
+    }
+    const uint64_t total = obegin[ns];
+    const uint64_t nchunks = (total + kPopChunk - 1) / kPopChunk;
+    for (uint64_t ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
+        if (threadIdx.x < 2) {  // the first survivor starting at or after the chunk's start / end
+            const uint64_t t = (ch + threadIdx.x) * (uint64_t)kPopChunk;
+            uint64_t lo = 0, hi = ns;
+            while (lo < hi) {
+                const uint64_t mid = (lo + hi) >> 1;
+                if (obegin[mid] < t) lo = mid + 1; else hi = mid;
+            }
+            s_range[threadIdx.x] = lo;
         }
+        __syncthreads();
+        const uint64_t i0 = s_range[0], i1 = s_range[1];
+        const uint64_t base = obegin[i0], end = obegin[i1];
+        const uint32_t shift = (uint32_t)(base & 15);
+        if (end - base + shift > kPopStage) {  // too long to stage: each object written in place
+            for (uint64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x)
+                populate_one(rs, pv, ss, i, obegin, osize, objects + obegin[i], omag, d_factor, f0, finst, err, post);
+            __syncthreads();
+            continue;
+        }
+        for (uint64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x)
+            populate_one(rs, pv, ss, i, obegin, osize, (char *)s_out + shift + (obegin[i] - base), omag, d_factor, f0,
+                         finst, err, post);
+        __syncthreads();
+        // s_out[shift + k] is objects[base + k]: both have the same address modulo 16
+        const uint64_t nbytes = end - base;
+        const uint64_t head = ((16 - shift) & 15) < nbytes ? ((16 - shift) & 15) : nbytes;
+        const uint64_t body = (nbytes - head) / 16;
+        char *g = objects + base;
+        if (threadIdx.x < head) g[threadIdx.x] = (char)s_out[shift + threadIdx.x];
+        const uint4 *sv = (const uint4 *)(s_out + shift + head);
+        uint4 *gv = (uint4 *)(g + head);
+        for (uint64_t k = threadIdx.x; k < body; k += blockDim.x) gv[k] = sv[k];
+        const uint64_t tail0 = head + body * 16;
+        for (uint64_t k = tail0 + threadIdx.x; k < nbytes; k += blockDim.x) g[k] = (char)s_out[shift + k];
+        __syncthreads();  // the next chunk reuses s_out
     }
 }
 
@@ -1128,12 +1195,13 @@ inline int launch_symbolic(quids_gpu_ctx *ctx, const RS &rule, const parents_vie
 
 template <class RS, class Post>
 inline int launch_populate(quids_gpu_ctx *ctx, const RS &rule, const parents_view &pv, uint64_t ns,
-                           quids_gpu_state *out, const Post &post) {
+                           quids_gpu_state *out, const Post &post, uint64_t max_child_size) {
     k_populate<RS, schild_source, Post><<<grid_for(ctx, ns), prim::kThreads, 0, ctx->stream>>>(
         rule, pv, schild_source{bufp<uint64_t>(ctx, B_SCHILD), bufp<uint32_t>(ctx, B_CPAR), pv.cbeg},
         ctx->d_words + W_NS, (const uint64_t *)out->begin.p,
         (const uint32_t *)out->size.p, (char *)out->objects.p, (double2 *)out->mag.p,
-        (const double *)(ctx->d_words + W_FACTOR), nullptr, (int *)(ctx->d_words + W_STATUS), post);
+        (const double *)(ctx->d_words + W_FACTOR), nullptr, (int *)(ctx->d_words + W_STATUS), post,
+        max_child_size > kStageMin);
     return launched(ctx);
 }
 
@@ -1581,7 +1649,7 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, qu
 
     // ---- stage 6: finalize populate (src/quids.hpp:958-967) + normalisation
     begin_stage(6);
-    QD_TRY((launch_populate<single_rule<Rule>, Post>(ctx, rule, pv, NS, out, post)));
+    QD_TRY((launch_populate<single_rule<Rule>, Post>(ctx, rule, pv, NS, out, post, maxsize)));
     end_stage(6);
     out->n = NS;
     out->nbytes = outbytes;

@@ -43,6 +43,7 @@ struct app_plan {
     uint64_t ns_cap;       // survivors
     uint64_t bytes_cap;    // output object bytes
     uint64_t maxsize_lim;  // child size bound of the generic symbolic pass (256 or 4096)
+    uint64_t maxsize;      // the recorded child size bound (the populate stages objects above kStageMin)
     bool may_truncate;     // the step takes the truncation path (select, then keep + layout)
 };
 
@@ -396,7 +397,7 @@ int simulate_planned(quids_gpu_ctx *ctx, quids_gpu_state *in, const uint64_t *in
     QD_TRY(launched(ctx));
 
     // ---- stage 6: finalize populate + normalisation (+ the fused modifiers)
-    QD_TRY((launch_populate<single_rule<Rule>, Post>(ctx, rule, pv, NSB, out, post)));
+    QD_TRY((launch_populate<single_rule<Rule>, Post>(ctx, rule, pv, NSB, out, post, ap.maxsize)));
     out->total_pending = true;
     return QUIDS_OK;
 }
