@@ -312,7 +312,9 @@ def ours(args, rank, world):
                 e0 = torch.cuda.Event(enable_timing=True)
                 e1 = torch.cuda.Event(enable_timing=True)
                 e0.record(stream)
+            torch.cuda.nvtx.range_push("timed_step")  # lets ncu --nvtx-include select the timed launches
             c, _ = run_step_gpu(ctx, quids, wl, src, spare=spare, flags=capi.FLAG_AUTOTUNE)
+            torch.cuda.nvtx.range_pop()
             with torch.cuda.stream(stream):
                 e1.record(stream)
             e1.synchronize()
@@ -465,7 +467,9 @@ def ours_batched(args, rank, world):
                 e0 = torch.cuda.Event(enable_timing=True)
                 e1 = torch.cuda.Event(enable_timing=True)
                 e0.record(stream)
+            torch.cuda.nvtx.range_push("timed_step")
             c, b, _ = step(src)
+            torch.cuda.nvtx.range_pop()
             with torch.cuda.stream(stream):
                 e1.record(stream)
             e1.synchronize()

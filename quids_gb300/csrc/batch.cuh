@@ -256,24 +256,35 @@ struct bkeep_layout {
         return s.active && kf.key(i) == s.prefix;
     }
     __device__ bool rank_needed() const { return true; }  // ranks are offset per instance
-    __device__ bool select(uint64_t i, uint64_t tie_rank) const {
+    struct item {
+        uint64_t c;
+        uint32_t g;
+        uint32_t size;
+    };
+    __device__ bool load(uint64_t i, uint64_t tie_rank, item &it) const {
         const uint32_t g = uinst[i];
         const prim::select_state &s = st[g];
-        if (!s.active) return true;
-        const uint64_t k = kf.key(i);
-        if (k > s.prefix) return true;
-        if (k < s.prefix) return false;
-        return tie_rank - tie_off[g] < s.k_rem;
+        bool keep = true;
+        if (s.active) {
+            const uint64_t k = kf.key(i);
+            keep = k > s.prefix || (k == s.prefix && tie_rank - tie_off[g] < s.k_rem);
+        }
+        if (keep) {
+            it.c = uchild[i];
+            it.g = g;
+            it.size = csize[it.c];
+        }
+        return keep;
     }
-    __device__ uint64_t bytes(uint64_t i) const { return padded_size(csize[uchild[i]], align); }
-    __device__ double norm(uint64_t) const { return 0.0; }  // instances are normalised separately
-    __device__ void emit(uint64_t i, uint64_t j, uint64_t off) const {
-        const uint64_t c = uchild[i];
+    __device__ uint64_t bytes(const item &it) const { return padded_size(it.size, align); }
+    __device__ double norm(const item &) const { return 0.0; }  // instances are normalised separately
+    __device__ void emit(uint64_t i, uint64_t j, uint64_t off, const item &it) const {
+        const uint64_t c = it.c;
         omag[j] = umag[i];
-        osize[j] = csize[c];
+        osize[j] = it.size;
         obegin[j] = off;
         schild[j] = c;
-        oinst[j] = uinst[i];
+        oinst[j] = it.g;
     }
 };
 

@@ -67,6 +67,7 @@ enum qd_buf_id {
     B_UBEGIN,      // u64 [G+1] instance offsets over the groups
     B_PBEGIN,      // u64 [G+1] instance offsets over the kept parents
     B_BFACTOR,     // double [G] per-instance sqrt(total)
+    B_SELCAND,     // u64 [NC/8 + 2^16] keys left in a truncation's selection after its first two digits
     B_COUNT
 };
 
@@ -91,6 +92,9 @@ enum qd_word {
     W_DONE_LAYOUT,       // blocks done with the layout compaction (u32)
     W_FAILAPP,           // planned run: the step at which it stopped (~0: none)
     W_M,                 // planned run: collision table slots of the step
+    W_SELN,              // truncation select: items of its later passes
+    W_SELUSE,            // truncation select: the later passes read the kept candidates
+    W_SELCNT,            // truncation select: candidates kept
     W_COUNT_WORDS = 24
 };
 
@@ -992,22 +996,20 @@ struct groups_layout {
     uint32_t *osize;
     uint64_t *obegin;
     uint64_t *schild;
+    struct item {
+        mag_t m;
+        uint32_t size;
+    };
     __device__ bool tie(uint64_t) const { return false; }
-    __device__ bool select(uint64_t c, uint64_t) const {
-        mag_t m;
-        return g.kept(c, m);
+    __device__ bool load(uint64_t c, uint64_t, item &it) const {
+        it.size = csize[c];
+        return g.kept(c, it.m);
     }
-    __device__ uint64_t bytes(uint64_t c) const { return padded_size(csize[c], align); }
-    __device__ double norm(uint64_t c) const {
-        mag_t m;
-        g.rep_mag(c, m);
-        return cnorm(m);
-    }
-    __device__ void emit(uint64_t c, uint64_t j, uint64_t off) const {
-        mag_t m;
-        g.rep_mag(c, m);
-        omag[j] = make_double2(m.re, m.im);
-        osize[j] = csize[c];
+    __device__ uint64_t bytes(const item &it) const { return padded_size(it.size, align); }
+    __device__ double norm(const item &it) const { return cnorm(it.m); }
+    __device__ void emit(uint64_t c, uint64_t j, uint64_t off, const item &it) const {
+        omag[j] = make_double2(it.m.re, it.m.im);
+        osize[j] = it.size;
         obegin[j] = off;
         schild[j] = c;
     }
@@ -1070,12 +1072,57 @@ struct key_parent_norm {
         return tk(cnorm(mag_t{m.x, m.y}), i);
     }
 };
-static __global__ void k_select_init(prim::select_state *st, const uint64_t *d_n, uint64_t k) {
+static __global__ void k_select_init(prim::select_state *st, const uint64_t *d_n, uint64_t k,
+                                     uint64_t *zero = nullptr) {
     prim::select_state s{};
     s.k_rem = k;
     s.active = k < *d_n ? 1u : 0u;
     st[0] = s;
+    if (zero) *zero = 0;
 }
+
+// After the first digits of a selection: the keys still matching its prefix
+// (st->n_equal of them), copied into cand in any order when they fit
+// (st->n_equal <= cap), so the later passes read only those.  Sets the later
+// passes' item count and whether they read cand.
+template <class K>
+__global__ void __launch_bounds__(prim::kThreads)
+    k_radix_filter(K kf, const uint64_t *d_n, const prim::select_state *st, uint64_t *cand, uint64_t cap,
+                   uint64_t *words) {
+    const uint64_t n = *d_n;
+    const bool use = st->active && st->n_equal <= cap;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        words[W_SELUSE] = use ? 1 : 0;
+        words[W_SELN] = use ? st->n_equal : n;
+    }
+    if (!use) return;
+    const uint64_t prefix = st->prefix, mask = st->mask;
+    const int lane = threadIdx.x & 31;
+    const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+    const uint64_t warp = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    for (uint64_t base = warp * 32; base < n; base += warps * 32) {
+        const uint64_t i = base + lane;
+        uint64_t k = 0;
+        bool m = false;
+        if (i < n) {
+            k = kf.key(i);
+            m = (k & mask) == prefix;
+        }
+        const unsigned ball = __ballot_sync(0xffffffffu, m);
+        if (!ball) continue;
+        unsigned long long pos = 0;
+        if (lane == 0) pos = atomicAdd((unsigned long long *)(words + W_SELCNT), (unsigned long long)__popc(ball));
+        pos = __shfl_sync(0xffffffffu, pos, 0);
+        if (m) cand[pos + __popc(ball & ((1u << lane) - 1))] = k;
+    }
+}
+template <class K>
+struct filtered_key {
+    K kf;
+    const uint64_t *cand;
+    const uint64_t *use;
+    __device__ __forceinline__ uint64_t key(uint64_t i) const { return *use ? cand[i] : kf.key(i); }
+};
 // the truncation's survivors (norm above the cutoff; among exact ties at the
 // cutoff, the lower child indices) into the output layout (src/quids.hpp:866-948)
 struct keep_layout {
@@ -1090,23 +1137,35 @@ struct keep_layout {
     uint32_t *osize;
     uint64_t *obegin;
     uint64_t *schild;
+    // a selected group: its child, size and norm (the size is read only for
+    // selected groups: most groups of a large truncation are not)
+    struct item {
+        uint64_t c;
+        uint64_t norm_bits;
+        uint32_t size;
+    };
     __device__ bool tie(uint64_t i) const { return st->active && kf.key(i) == st->prefix; }
     __device__ bool rank_needed() const { return st->active && st->n_equal > st->k_rem; }
-    __device__ bool select(uint64_t i, uint64_t tie_rank) const {
-        if (!st->active) return true;
-        uint64_t k = kf.key(i);
-        if (k > st->prefix) return true;
-        if (k < st->prefix) return false;
-        return tie_rank < st->k_rem;
+    __device__ bool load(uint64_t i, uint64_t tie_rank, item &it) const {
+        bool keep = true;
+        if (st->active) {
+            const uint64_t k = kf.key(i);
+            keep = k > st->prefix || (k == st->prefix && tie_rank < st->k_rem);
+        }
+        if (keep) {
+            it.c = uchild[i];
+            it.norm_bits = unorm[i];
+            it.size = csize[it.c];
+        }
+        return keep;
     }
-    __device__ uint64_t bytes(uint64_t i) const { return padded_size(csize[uchild[i]], align); }
-    __device__ double norm(uint64_t i) const { return __longlong_as_double((long long)unorm[i]); }
-    __device__ void emit(uint64_t i, uint64_t j, uint64_t off) const {
-        const uint64_t c = uchild[i];
+    __device__ uint64_t bytes(const item &it) const { return padded_size(it.size, align); }
+    __device__ double norm(const item &it) const { return __longlong_as_double((long long)it.norm_bits); }
+    __device__ void emit(uint64_t i, uint64_t j, uint64_t off, const item &it) const {
         omag[j] = umag[i];
-        osize[j] = csize[c];
+        osize[j] = it.size;
         obegin[j] = off;
-        schild[j] = c;
+        schild[j] = it.c;
     }
 };
 
@@ -1160,6 +1219,33 @@ inline int radix_select(quids_gpu_ctx *ctx, const uint64_t *d_n, uint64_t n_host
         prim::k_radix_pick<<<1, prim::kBins, 0, ctx->stream>>>(ctx->d_sel, ctx->d_hist, shift, true);
     }
     return launched(ctx, 1 + 2 * 64 / prim::kDigitBits);
+}
+
+// radix_select for a truncation over many items: after the first two digits
+// (16 bits: the sign, exponent and 4 mantissa bits of a norm), the keys that
+// still match are copied aside when they fit cand's cap_items, and the 6 later
+// passes read those instead of every item.  The result is radix_select's.
+inline uint64_t filter_cap(uint64_t n) { return n / 8 + 65536; }
+template <class K1>
+inline int radix_select_filtered(quids_gpu_ctx *ctx, const uint64_t *d_n, uint64_t n_host, uint64_t k, K1 k1,
+                                 uint64_t *cand, uint64_t cap_items) {
+    unsigned grid = grid_for(ctx, n_host);
+    uint64_t *words = ctx->d_words;
+    k_select_init<<<1, 1, 0, ctx->stream>>>(ctx->d_sel, d_n, k, words + W_SELCNT);
+    QD_CUDA(cudaMemsetAsync(ctx->d_hist, 0, prim::kBins * sizeof(unsigned long long), ctx->stream));
+    int shift = 64 - prim::kDigitBits;
+    for (int pass = 0; pass < 2; ++pass, shift -= prim::kDigitBits) {
+        prim::k_radix_hist<<<grid, prim::kThreads, 0, ctx->stream>>>(k1, d_n, ctx->d_sel, shift, ctx->d_hist);
+        prim::k_radix_pick<<<1, prim::kBins, 0, ctx->stream>>>(ctx->d_sel, ctx->d_hist, shift, true);
+    }
+    k_radix_filter<<<grid, prim::kThreads, 0, ctx->stream>>>(k1, d_n, ctx->d_sel, cand, cap_items, words);
+    const filtered_key<K1> kf{k1, cand, words + W_SELUSE};
+    for (; shift >= 0; shift -= prim::kDigitBits) {
+        prim::k_radix_hist<<<grid, prim::kThreads, 0, ctx->stream>>>(kf, words + W_SELN, ctx->d_sel, shift,
+                                                                    ctx->d_hist);
+        prim::k_radix_pick<<<1, prim::kBins, 0, ctx->stream>>>(ctx->d_sel, ctx->d_hist, shift, true);
+    }
+    return launched(ctx, 2 + 2 * 64 / prim::kDigitBits);
 }
 
 inline uint64_t next_pow2(uint64_t v) {
@@ -1613,7 +1699,9 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, qu
         end_stage(3);
         begin_stage(4);
         key_unorm k1{bufp<uint64_t>(ctx, B_UNORM), bufp<uint64_t>(ctx, B_UCHILD), tk};
-        QD_TRY(radix_select(ctx, ctx->d_words + W_NU, NC, maxc, k1));
+        QD_TRY(ensure(ctx->buf[B_SELCAND], filter_cap(NC) * sizeof(uint64_t)));
+        QD_TRY(radix_select_filtered(ctx, ctx->d_words + W_NU, NC, maxc, k1, bufp<uint64_t>(ctx, B_SELCAND),
+                                     filter_cap(NC)));
         prim::lookback lbc, lbb, lbt;
         lookback_view(ctx, NC, 0, lbt);
         lookback_view(ctx, NC, 1, lbc);

@@ -252,6 +252,7 @@ inline int ensure_planned(quids_gpu_ctx *ctx, quids_gpu_state *out, const app_pl
     QD_TRY(ensure(ctx->buf[B_ACC], 4 * (M + 1) * sizeof(uint64_t)));
     QD_TRY(ensure(ctx->buf[B_SCHILD], NS * sizeof(uint64_t)));
     if (ap.may_truncate) {
+        QD_TRY(ensure(ctx->buf[B_SELCAND], filter_cap(NC) * sizeof(uint64_t)));
         QD_TRY(ensure(ctx->buf[B_UCHILD], NC * sizeof(uint64_t)));
         QD_TRY(ensure(ctx->buf[B_UMAG], NC * sizeof(double2)));
         QD_TRY(ensure(ctx->buf[B_UNORM], NC * sizeof(uint64_t)));
@@ -374,7 +375,8 @@ int simulate_planned(quids_gpu_ctx *ctx, quids_gpu_state *in, const uint64_t *in
         prim::k_compact<<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(f, words + W_NC, words + W_NU, lb);
         QD_TRY(launched(ctx));
         key_unorm k1{bufp<uint64_t>(ctx, B_UNORM), bufp<uint64_t>(ctx, B_UCHILD), tk};
-        QD_TRY(radix_select(ctx, words + W_NU, NC, maxn, k1));
+        QD_TRY(radix_select_filtered(ctx, words + W_NU, NC, maxn, k1, bufp<uint64_t>(ctx, B_SELCAND),
+                                     filter_cap(NC)));
         prim::lookback lbc, lbb, lbt;
         lookback_view(ctx, NC, 0, lbt);
         lookback_view(ctx, NC, 1, lbc);

@@ -663,17 +663,19 @@ static __global__ void __launch_bounds__(kThreads)
 
 // --------------------------------------------- compaction + byte offsets
 // Order-preserving compaction that also lays out the selected items'
-// variable-size payloads: P::select(i, tie_rank) -> bool, P::bytes(i) ->
-// padded size, P::norm(i) -> double, P::emit(i, j, byte_offset).  With TIES,
-// P::tie(i) -> bool marks the items equal to a selection threshold and
-// tie_rank is the item's rank among them in item order (a third look-back
-// chain), so a selection can take the first ties; P::rank_needed() -> bool
-// (the same for every thread) skips the ranking when the selection keeps
-// every tie, and select then gets tie_rank 0.  The largest selected norm
-// goes to *d_maxnorm (as IEEE bits) when d_maxnorm is not null.  At the end:
-// *d_count, *d_bytes and begin_out[count] = total bytes.
+// variable-size payloads.  P::load(i, tie_rank, item&) -> bool selects item i
+// and keeps what the layout needs in a P::item (loaded once), P::bytes(item)
+// -> padded size (asked for selected items only), P::norm(item) -> double,
+// P::emit(i, j, byte_offset, item).  With TIES, P::tie(i) -> bool marks the
+// items equal to a selection threshold and tie_rank is the item's rank among
+// them in item order (a third look-back chain), so a selection can take the
+// first ties; P::rank_needed() -> bool (the same for every thread) skips the
+// ranking when the selection keeps every tie, and load then gets tie_rank 0.
+// The largest selected norm goes to *d_maxnorm (as IEEE bits) when d_maxnorm
+// is not null.  At the end: *d_count, *d_bytes and begin_out[count] = total
+// bytes.
 template <class P, bool TIES>
-__global__ void __launch_bounds__(kThreads) k_compact_layout(P p, const uint64_t *d_n, uint64_t *d_count,
+__global__ void __launch_bounds__(kThreads, 3) k_compact_layout(P p, const uint64_t *d_n, uint64_t *d_count,
                                                               uint64_t *d_bytes, uint64_t *begin_out,
                                                               unsigned long long *d_maxnorm, lookback lb_count,
                                                               lookback lb_bytes, lookback lb_ties,
@@ -722,13 +724,12 @@ __global__ void __launch_bounds__(kThreads) k_compact_layout(P p, const uint64_t
         // item past the end reads item n-1 and is dropped), so the loads of
         // all items are in flight together
         bool sel[kItems];
-        uint64_t ib[kItems];
+        typename P::item it[kItems];
 #pragma unroll
         for (int k = 0; k < kItems; ++k) {
             const uint64_t i = base + k;
             const uint64_t ic = i < n ? i : n - 1;
-            sel[k] = p.select(ic, rank) && i < n;
-            ib[k] = p.bytes(ic);
+            sel[k] = p.load(ic, rank, it[k]) && i < n;
             if (ties & (1u << k)) ++rank;
         }
 #pragma unroll
@@ -736,8 +737,8 @@ __global__ void __launch_bounds__(kThreads) k_compact_layout(P p, const uint64_t
             if (sel[k]) {
                 flags |= 1u << k;
                 ++cnt;
-                bytes += ib[k];
-                const unsigned long long b = (unsigned long long)__double_as_longlong(p.norm(base + k));
+                bytes += p.bytes(it[k]);
+                const unsigned long long b = (unsigned long long)__double_as_longlong(p.norm(it[k]));
                 mx = mx > b ? mx : b;
             }
         }
@@ -750,9 +751,8 @@ __global__ void __launch_bounds__(kThreads) k_compact_layout(P p, const uint64_t
 #pragma unroll
         for (int k = 0; k < kItems; ++k)
             if (flags & (1u << k)) {
-                uint64_t i = base + k;
-                p.emit(i, j++, off);
-                off += p.bytes(i);
+                p.emit(base + k, j++, off, it[k]);
+                off += p.bytes(it[k]);
             }
         if (tile == ntiles - 1 && threadIdx.x == kThreads - 1) {
             *d_count = pre_c + agg_c;

@@ -348,19 +348,28 @@ struct merged_layout {
     uint32_t *spar, *scid;
     __device__ bool tie(uint64_t i) const { return st->active && kf.key(i) == st->prefix; }
     __device__ bool rank_needed() const { return st->active && st->n_equal > st->k_rem; }
-    __device__ bool select(uint64_t i, uint64_t tie_rank) const {
-        if (!st->active) return true;
-        const uint64_t k = kf.key(i);
-        if (k > st->prefix) return true;
-        if (k < st->prefix) return false;
-        return tie_rank < st->k_rem;
+    struct item {
+        uint32_t q;
+        uint32_t size;
+    };
+    __device__ bool load(uint64_t i, uint64_t tie_rank, item &it) const {
+        bool keep = true;
+        if (st->active) {
+            const uint64_t k = kf.key(i);
+            keep = k > st->prefix || (k == st->prefix && tie_rank < st->k_rem);
+        }
+        if (keep) {
+            it.q = kf.perm[i];
+            it.size = kf.c.size[it.q];
+        }
+        return keep;
     }
-    __device__ uint64_t bytes(uint64_t i) const { return padded_size(kf.c.size[kf.perm[i]], align); }
-    __device__ double norm(uint64_t i) const { return __longlong_as_double((long long)kf.c.norm[kf.perm[i]]); }
-    __device__ void emit(uint64_t i, uint64_t j, uint64_t off) const {
-        const uint32_t q = kf.perm[i];
+    __device__ uint64_t bytes(const item &it) const { return padded_size(it.size, align); }
+    __device__ double norm(const item &it) const { return __longlong_as_double((long long)kf.c.norm[it.q]); }
+    __device__ void emit(uint64_t, uint64_t j, uint64_t off, const item &it) const {
+        const uint32_t q = it.q;
         omag[j] = kf.c.mag[q];
-        osize[j] = kf.c.size[q];
+        osize[j] = it.size;
         obegin[j] = off;
         spar[j] = kf.c.par[q];
         scid[j] = kf.c.cid[q];
