@@ -1015,25 +1015,6 @@ struct groups_layout {
     }
 };
 
-// truncation possible: keep the groups with their norms for the selection
-struct groups_collect {
-    group_view g;
-    uint64_t *uchild;
-    double2 *umag;
-    uint64_t *unorm;
-    __device__ bool select(uint64_t c) const {
-        mag_t m;
-        return g.kept(c, m);
-    }
-    __device__ void emit(uint64_t c, uint64_t j) const {
-        mag_t m;
-        g.rep_mag(c, m);
-        uchild[j] = c;
-        umag[j] = make_double2(m.re, m.im);
-        unorm[j] = (uint64_t)__double_as_longlong(cnorm(m));
-    }
-};
-
 // radix-select keys
 // Truncation keys, larger = kept first.  Simple truncation: the IEEE bits
 // of the norm (src/quids.hpp:884-889).  Probabilistic truncation
@@ -1123,13 +1104,36 @@ struct filtered_key {
     const uint64_t *use;
     __device__ __forceinline__ uint64_t key(uint64_t i) const { return *use ? cand[i] : kf.key(i); }
 };
-// the truncation's survivors (norm above the cutoff; among exact ties at the
-// cutoff, the lower child indices) into the output layout (src/quids.hpp:866-948)
-struct keep_layout {
-    key_unorm kf;
-    const uint64_t *unorm;
-    const uint64_t *uchild;
-    const double2 *umag;
+// The truncation path over the children themselves, with no list of groups:
+// k_group_keys gives each child the truncation key of its group if it
+// represents one kept after zero elimination (src/quids.hpp:819-823), else 0
+// (a kept group's key is never 0), and counts those groups (*d_nu).  The
+// selection then runs over the children's keys, and child_keep_layout lays
+// out the selected representatives in child order, recomputing the few
+// selected groups' magnitudes.
+static __global__ void __launch_bounds__(prim::kThreads)
+    k_group_keys(group_view g, trunc_key tk, const uint64_t *d_nc, uint64_t *key, unsigned long long *d_nu) {
+    const uint64_t n = *d_nc;
+    unsigned long long kept = 0;
+    for (uint64_t c = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (uint64_t)gridDim.x * blockDim.x) {
+        mag_t m;
+        uint64_t k = 0;
+        if (g.kept(c, m)) {
+            k = tk(cnorm(m), c);
+            ++kept;
+        }
+        key[c] = k;
+    }
+    for (int o = 16; o > 0; o >>= 1) kept += __shfl_xor_sync(0xffffffffu, kept, o);
+    if ((threadIdx.x & 31) == 0 && kept) atomicAdd(d_nu, kept);
+}
+struct key_direct {
+    const uint64_t *k;
+    __device__ __forceinline__ uint64_t key(uint64_t i) const { return k[i]; }
+};
+struct child_keep_layout {
+    group_view g;
+    const uint64_t *key;
     const prim::select_state *st;
     const uint32_t *csize;
     uint32_t align;
@@ -1137,35 +1141,29 @@ struct keep_layout {
     uint32_t *osize;
     uint64_t *obegin;
     uint64_t *schild;
-    // a selected group: its child, size and norm (the size is read only for
-    // selected groups: most groups of a large truncation are not)
     struct item {
-        uint64_t c;
-        uint64_t norm_bits;
+        mag_t m;
         uint32_t size;
     };
-    __device__ bool tie(uint64_t i) const { return st->active && kf.key(i) == st->prefix; }
+    __device__ bool tie(uint64_t c) const { return st->active && key[c] == st->prefix; }
     __device__ bool rank_needed() const { return st->active && st->n_equal > st->k_rem; }
-    __device__ bool load(uint64_t i, uint64_t tie_rank, item &it) const {
-        bool keep = true;
-        if (st->active) {
-            const uint64_t k = kf.key(i);
-            keep = k > st->prefix || (k == st->prefix && tie_rank < st->k_rem);
-        }
+    __device__ bool load(uint64_t c, uint64_t tie_rank, item &it) const {
+        const uint64_t k = key[c];
+        if (k == 0) return false;
+        const bool keep = !st->active || k > st->prefix || (k == st->prefix && tie_rank < st->k_rem);
         if (keep) {
-            it.c = uchild[i];
-            it.norm_bits = unorm[i];
-            it.size = csize[it.c];
+            g.rep_mag(c, it.m);
+            it.size = csize[c];
         }
         return keep;
     }
     __device__ uint64_t bytes(const item &it) const { return padded_size(it.size, align); }
-    __device__ double norm(const item &it) const { return __longlong_as_double((long long)it.norm_bits); }
-    __device__ void emit(uint64_t i, uint64_t j, uint64_t off, const item &it) const {
-        omag[j] = umag[i];
+    __device__ double norm(const item &it) const { return cnorm(it.m); }
+    __device__ void emit(uint64_t c, uint64_t j, uint64_t off, const item &it) const {
+        omag[j] = make_double2(it.m.re, it.m.im);
         osize[j] = it.size;
         obegin[j] = off;
-        schild[j] = it.c;
+        schild[j] = c;
     }
 };
 
@@ -1226,12 +1224,14 @@ inline int radix_select(quids_gpu_ctx *ctx, const uint64_t *d_n, uint64_t n_host
 // still match are copied aside when they fit cand's cap_items, and the 6 later
 // passes read those instead of every item.  The result is radix_select's.
 inline uint64_t filter_cap(uint64_t n) { return n / 8 + 65536; }
+// d_active: the count of items that can be selected (default *d_n; the
+// children's keys hold 0 for the children that represent no kept group).
 template <class K1>
 inline int radix_select_filtered(quids_gpu_ctx *ctx, const uint64_t *d_n, uint64_t n_host, uint64_t k, K1 k1,
-                                 uint64_t *cand, uint64_t cap_items) {
+                                 uint64_t *cand, uint64_t cap_items, const uint64_t *d_active = nullptr) {
     unsigned grid = grid_for(ctx, n_host);
     uint64_t *words = ctx->d_words;
-    k_select_init<<<1, 1, 0, ctx->stream>>>(ctx->d_sel, d_n, k, words + W_SELCNT);
+    k_select_init<<<1, 1, 0, ctx->stream>>>(ctx->d_sel, d_active ? d_active : d_n, k, words + W_SELCNT);
     QD_CUDA(cudaMemsetAsync(ctx->d_hist, 0, prim::kBins * sizeof(unsigned long long), ctx->stream));
     int shift = 64 - prim::kDigitBits;
     for (int pass = 0; pass < 2; ++pass, shift -= prim::kDigitBits) {
@@ -1585,11 +1585,7 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, qu
     QD_TRY(ensure(out->size, NSB * sizeof(uint32_t)));
     QD_TRY(ensure(out->mag, NSB * sizeof(double2)));
     QD_TRY(ensure(out->d_total, sizeof(double)));
-    if (may_truncate) {
-        QD_TRY(ensure(ctx->buf[B_UCHILD], NC * sizeof(uint64_t)));
-        QD_TRY(ensure(ctx->buf[B_UMAG], NC * sizeof(double2)));
-        QD_TRY(ensure(ctx->buf[B_UNORM], NC * sizeof(uint64_t)));
-    }
+    if (may_truncate) QD_TRY(ensure(ctx->buf[B_UNORM], NC * sizeof(uint64_t)));
     if (regions) {
         QD_TRY(ensure(ctx->buf[B_RHASH], NC * sizeof(uint64_t)));
         QD_TRY(ensure(ctx->buf[B_RIDX], NC * sizeof(uint32_t)));
@@ -1690,27 +1686,23 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, qu
         QD_TRY(launched(ctx));
         end_stage(3);
     } else {
-        prim::lookback lb;
-        lookback_view(ctx, NC, 3, lb);
-        groups_collect f{gv, bufp<uint64_t>(ctx, B_UCHILD), bufp<double2>(ctx, B_UMAG), bufp<uint64_t>(ctx, B_UNORM)};
-        prim::k_compact<<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(f, ctx->d_words + W_NC,
-                                                                                   ctx->d_words + W_NU, lb);
+        uint64_t *gkey = bufp<uint64_t>(ctx, B_UNORM);  // per child: its group's truncation key, or 0
+        k_group_keys<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
+            gv, tk, ctx->d_words + W_NC, gkey, (unsigned long long *)(ctx->d_words + W_NU));
         QD_TRY(launched(ctx));
         end_stage(3);
         begin_stage(4);
-        key_unorm k1{bufp<uint64_t>(ctx, B_UNORM), bufp<uint64_t>(ctx, B_UCHILD), tk};
         QD_TRY(ensure(ctx->buf[B_SELCAND], filter_cap(NC) * sizeof(uint64_t)));
-        QD_TRY(radix_select_filtered(ctx, ctx->d_words + W_NU, NC, maxc, k1, bufp<uint64_t>(ctx, B_SELCAND),
-                                     filter_cap(NC)));
+        QD_TRY(radix_select_filtered(ctx, ctx->d_words + W_NC, NC, maxc, key_direct{gkey},
+                                     bufp<uint64_t>(ctx, B_SELCAND), filter_cap(NC), ctx->d_words + W_NU));
         prim::lookback lbc, lbb, lbt;
         lookback_view(ctx, NC, 0, lbt);
         lookback_view(ctx, NC, 1, lbc);
         lookback_view(ctx, NC, 2, lbb);
-        keep_layout kl{k1, bufp<uint64_t>(ctx, B_UNORM), bufp<uint64_t>(ctx, B_UCHILD), bufp<double2>(ctx, B_UMAG),
-                       ctx->d_sel, bufp<uint32_t>(ctx, B_CSIZE), align, (double2 *)out->mag.p,
-                       (uint32_t *)out->size.p, (uint64_t *)out->begin.p, bufp<uint64_t>(ctx, B_SCHILD)};
-        prim::k_compact_layout<keep_layout, true><<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
-            kl, ctx->d_words + W_NU, ctx->d_words + W_NS, ctx->d_words + W_OUTBYTES, (uint64_t *)out->begin.p,
+        child_keep_layout kl{gv, gkey, ctx->d_sel, bufp<uint32_t>(ctx, B_CSIZE), align, (double2 *)out->mag.p,
+                             (uint32_t *)out->size.p, (uint64_t *)out->begin.p, bufp<uint64_t>(ctx, B_SCHILD)};
+        prim::k_compact_layout<child_keep_layout, true><<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
+            kl, ctx->d_words + W_NC, ctx->d_words + W_NS, ctx->d_words + W_OUTBYTES, (uint64_t *)out->begin.p,
             d_maxnorm, lbc, lbb, lbt, pb1);
         QD_TRY(launched(ctx));
         end_stage(4);

@@ -14,10 +14,11 @@
 // Guards on the device keep the result exact:
 //  * k_plan_begin: the step's parents fit the plan (and need no parent
 //    pre-truncation);
-//  * k_plan_sizes, after the child count: the children fit, the child size
-//    bound fits the symbolic pass chosen, and a step planned without
-//    truncation still needs none;
-//  * k_plan_end, after the layout: the output bytes fit.
+//  * plan_sizes, run by the last block of the child-offset scan: the
+//    children fit, the child size bound fits the symbolic pass chosen, and a
+//    step planned without truncation still needs none;
+//  * plan_end, run by the last block of the layout compaction: the output
+//    bytes fit.
 // A step that does not fit sets the status kReplan and the step index, and
 // from then on every step and modifier of the run does nothing: the failed
 // step's input state is left as it was (no kernel writes it), so the host
@@ -112,7 +113,7 @@ inline void drop_plans_of(quids_gpu_ctx *ctx, const quids_gpu_state *st) {
         }
 }
 
-// what each planned step reports (words per step, written by k_plan_end
+// what each planned step reports (words per step, written by plan_end
 // into mapped host memory)
 enum { R_N, R_NC, R_NU, R_NS, R_BYTES, R_MAXSIZE, R_M, R_DONE, R_WORDS };
 
@@ -160,8 +161,9 @@ static __global__ void __launch_bounds__(256)
 // step if they do not fit (or an earlier kernel failed), and size the
 // collision table on the device: M = max(NC / load + 1, 1024) slots as the
 // synchronous step computes it, with the extra slot's sum cleared.
-static __global__ void k_plan_sizes(uint64_t *words, uint32_t app, uint64_t nc_cap, uint64_t maxsize_lim,
-                                    uint64_t nc_no_trunc, double load, unsigned long long *acc) {
+// (run by the last block of the child-offset scan: plan_sizes_hook)
+__device__ __forceinline__ void plan_sizes(uint64_t *words, uint32_t app, uint64_t nc_cap, uint64_t maxsize_lim,
+                                           uint64_t nc_no_trunc, double load, unsigned long long *acc) {
     uint64_t nc = words[W_NC];
     if (!stopped(words) && nc > 0) {
         const uint64_t ms = words[W_MAXSIZE];
@@ -182,12 +184,23 @@ static __global__ void k_plan_sizes(uint64_t *words, uint32_t app, uint64_t nc_c
     for (int k = 0; k < 4; ++k) acc[4 * m + k] = 0;
 }
 
+struct plan_sizes_hook {
+    static constexpr bool active = true;
+    uint64_t *words;
+    uint32_t app;
+    uint64_t nc_cap, maxsize_lim, nc_no_trunc;
+    double load;
+    unsigned long long *acc;
+    __device__ void operator()() const { plan_sizes(words, app, nc_cap, maxsize_lim, nc_no_trunc, load, acc); }
+};
+
 // After the output layout: check the output bytes, publish the output
 // state's size on the device and the step's counts to the host; a stopped
 // step keeps no survivors (so the total and the populate do nothing) and
-// leaves the output state's words alone.
-static __global__ void k_plan_end(uint64_t *words, uint32_t app, uint64_t bytes_cap, bool truncating,
-                                  uint64_t *out_meta, volatile uint64_t *rec) {
+// leaves the output state's words alone.  (Run by the last block of the
+// layout compaction: plan_end_hook.)
+__device__ __forceinline__ void plan_end(uint64_t *words, uint32_t app, uint64_t bytes_cap, bool truncating,
+                                         uint64_t *out_meta, volatile uint64_t *rec) {
     if (!stopped(words) && words[W_OUTBYTES] > bytes_cap) stop_at(words, app, kReplan);
     if (stopped(words)) {
         stop_at(words, app, 0);
@@ -204,6 +217,22 @@ static __global__ void k_plan_end(uint64_t *words, uint32_t app, uint64_t bytes_
     rec[R_MAXSIZE] = words[W_MAXSIZE];
     rec[R_M] = words[W_M];
     rec[R_DONE] = 1;
+}
+struct plan_end_hook {
+    static constexpr bool active = true;
+    uint64_t *words;
+    uint32_t app;
+    uint64_t bytes_cap;
+    bool truncating;
+    uint64_t *out_meta;
+    uint64_t *rec;
+    __device__ void operator()() const { plan_end(words, app, bytes_cap, truncating, out_meta, rec); }
+};
+// the hooks' block counters (zeroed by k_plan_begin)
+inline prim::publish hook_counter(quids_gpu_ctx *ctx, qd_word done) {
+    prim::publish pb;
+    pb.done = (unsigned int *)(ctx->d_words + done);
+    return pb;
 }
 
 // The run's end: its status, failing step and the two states' sizes.
@@ -253,8 +282,6 @@ inline int ensure_planned(quids_gpu_ctx *ctx, quids_gpu_state *out, const app_pl
     QD_TRY(ensure(ctx->buf[B_SCHILD], NS * sizeof(uint64_t)));
     if (ap.may_truncate) {
         QD_TRY(ensure(ctx->buf[B_SELCAND], filter_cap(NC) * sizeof(uint64_t)));
-        QD_TRY(ensure(ctx->buf[B_UCHILD], NC * sizeof(uint64_t)));
-        QD_TRY(ensure(ctx->buf[B_UMAG], NC * sizeof(double2)));
         QD_TRY(ensure(ctx->buf[B_UNORM], NC * sizeof(uint64_t)));
     }
     QD_TRY(ensure(ctx->buf[B_MODSTATUS], sizeof(uint64_t)));
@@ -304,13 +331,14 @@ int simulate_planned(quids_gpu_ctx *ctx, quids_gpu_state *in, const uint64_t *in
         prim::lookback lb;
         lookback_view(ctx, N, 1, lb);
         scan_nchild f{bufp<uint32_t>(ctx, B_NCHILD), nullptr};
+        const plan_sizes_hook hook{words, app, ap.nc_cap, ap.maxsize_lim, ap.may_truncate ? ~0ull : maxn, load,
+                                   bufp<unsigned long long>(ctx, B_ACC)};
         prim::k_scan_excl<<<lookback_grid(ctx, N), prim::kThreads, 0, ctx->stream>>>(
             f, words + W_NP, bufp<uint64_t>(ctx, B_CBEGIN), words + W_NC, lb,
-            tile_parents_epilogue{bufp<uint64_t>(ctx, B_TILEPAR), sym_tiles + 2});
+            tile_parents_epilogue{bufp<uint64_t>(ctx, B_TILEPAR), sym_tiles + 2}, hook_counter(ctx, W_DONE_SCAN),
+            hook);
     }
-    k_plan_sizes<<<1, 1, 0, ctx->stream>>>(words, app, ap.nc_cap, ap.maxsize_lim,
-                                           ap.may_truncate ? ~0ull : maxn, load, bufp<unsigned long long>(ctx, B_ACC));
-    QD_TRY(launched(ctx, 2));
+    QD_TRY(launched(ctx));
     parents_view pv{(const char *)in->objects.p, (const uint64_t *)in->begin.p, (const uint32_t *)in->size.p,
                     (const double2 *)in->mag.p, bufp<uint64_t>(ctx, B_CBEGIN), nullptr, N, words + W_NP};
 
@@ -359,6 +387,7 @@ int simulate_planned(quids_gpu_ctx *ctx, quids_gpu_state *in, const uint64_t *in
                   bufp<unsigned long long>(ctx, B_ACC), words + W_NC, d_maxabs, prm.tolerance};
     const uint32_t align = prm.align_byte_length;
     unsigned long long *d_maxnorm = (unsigned long long *)(words + W_MAXNORM);
+    const plan_end_hook end_hook{words, app, ap.bytes_cap, ap.may_truncate, (uint64_t *)out->meta.p, rec};
     if (!ap.may_truncate) {
         prim::lookback lbc, lbb;
         lookback_view(ctx, NC, 0, lbc);
@@ -366,30 +395,27 @@ int simulate_planned(quids_gpu_ctx *ctx, quids_gpu_state *in, const uint64_t *in
         groups_layout f{gv, bufp<uint32_t>(ctx, B_CSIZE), align, (double2 *)out->mag.p, (uint32_t *)out->size.p,
                         (uint64_t *)out->begin.p, bufp<uint64_t>(ctx, B_SCHILD)};
         prim::k_compact_layout<groups_layout, false><<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
-            f, words + W_NC, words + W_NS, words + W_OUTBYTES, (uint64_t *)out->begin.p, d_maxnorm, lbc, lbb, lbb);
+            f, words + W_NC, words + W_NS, words + W_OUTBYTES, (uint64_t *)out->begin.p, d_maxnorm, lbc, lbb, lbb,
+            hook_counter(ctx, W_DONE_LAYOUT), end_hook);
         QD_TRY(launched(ctx));
     } else {
-        prim::lookback lb;
-        lookback_view(ctx, NC, 3, lb);
-        groups_collect f{gv, bufp<uint64_t>(ctx, B_UCHILD), bufp<double2>(ctx, B_UMAG), bufp<uint64_t>(ctx, B_UNORM)};
-        prim::k_compact<<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(f, words + W_NC, words + W_NU, lb);
+        uint64_t *gkey = bufp<uint64_t>(ctx, B_UNORM);  // per child: its group's truncation key, or 0
+        k_group_keys<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(gv, tk, words + W_NC, gkey,
+                                                                           (unsigned long long *)(words + W_NU));
         QD_TRY(launched(ctx));
-        key_unorm k1{bufp<uint64_t>(ctx, B_UNORM), bufp<uint64_t>(ctx, B_UCHILD), tk};
-        QD_TRY(radix_select_filtered(ctx, words + W_NU, NC, maxn, k1, bufp<uint64_t>(ctx, B_SELCAND),
-                                     filter_cap(NC)));
+        QD_TRY(radix_select_filtered(ctx, words + W_NC, NC, maxn, key_direct{gkey}, bufp<uint64_t>(ctx, B_SELCAND),
+                                     filter_cap(NC), words + W_NU));
         prim::lookback lbc, lbb, lbt;
         lookback_view(ctx, NC, 0, lbt);
         lookback_view(ctx, NC, 1, lbc);
         lookback_view(ctx, NC, 2, lbb);
-        keep_layout kl{k1, bufp<uint64_t>(ctx, B_UNORM), bufp<uint64_t>(ctx, B_UCHILD), bufp<double2>(ctx, B_UMAG),
-                       ctx->d_sel, bufp<uint32_t>(ctx, B_CSIZE), align, (double2 *)out->mag.p,
-                       (uint32_t *)out->size.p, (uint64_t *)out->begin.p, bufp<uint64_t>(ctx, B_SCHILD)};
-        prim::k_compact_layout<keep_layout, true><<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
-            kl, words + W_NU, words + W_NS, words + W_OUTBYTES, (uint64_t *)out->begin.p, d_maxnorm, lbc, lbb, lbt);
+        child_keep_layout kl{gv, gkey, ctx->d_sel, bufp<uint32_t>(ctx, B_CSIZE), align, (double2 *)out->mag.p,
+                             (uint32_t *)out->size.p, (uint64_t *)out->begin.p, bufp<uint64_t>(ctx, B_SCHILD)};
+        prim::k_compact_layout<child_keep_layout, true><<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
+            kl, words + W_NC, words + W_NS, words + W_OUTBYTES, (uint64_t *)out->begin.p, d_maxnorm, lbc, lbb, lbt,
+            hook_counter(ctx, W_DONE_LAYOUT), end_hook);
         QD_TRY(launched(ctx));
     }
-    k_plan_end<<<1, 1, 0, ctx->stream>>>(words, app, ap.bytes_cap, ap.may_truncate, (uint64_t *)out->meta.p, rec);
-    QD_TRY(launched(ctx));
 
     // ---- stage 5: exact total probability, into the output state
     prim::k_fix_total<<<grid_for(ctx, NSB, 4), prim::kThreads, 0, ctx->stream>>>(

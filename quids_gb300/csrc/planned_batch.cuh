@@ -36,6 +36,8 @@ inline int ensure_planned_batched(quids_gpu_ctx *ctx, quids_gpu_state *out, cons
     QD_TRY(ensure(ctx->buf[B_PBEGIN], (size_t)(G + 1) * sizeof(uint64_t)));
     QD_TRY(ensure(ctx->buf[B_BFACTOR], (size_t)G * sizeof(double)));
     QD_TRY(ensure(ctx->buf[B_UINST], ap.nc_cap * sizeof(uint32_t)));
+    QD_TRY(ensure(ctx->buf[B_UCHILD], ap.nc_cap * sizeof(uint64_t)));
+    QD_TRY(ensure(ctx->buf[B_UMAG], ap.nc_cap * sizeof(double2)));
     auto grow = [&](qd_dbuf &b, size_t bytes) { return keep ? ensure_keep(b, bytes, ctx->stream) : ensure(b, bytes); };
     QD_TRY(grow(out->inst, ap.ns_cap * sizeof(uint32_t)));
     QD_TRY(grow(out->inst_begin, (size_t)(G + 1) * sizeof(uint64_t)));
@@ -90,13 +92,14 @@ int simulate_batched_planned(quids_gpu_ctx *ctx, quids_gpu_state *in, const uint
         prim::lookback lb;
         lookback_view(ctx, N, 1, lb);
         scan_nchild f{bufp<uint32_t>(ctx, B_NCHILD), nullptr};
+        const plan_sizes_hook hook{words, app, ap.nc_cap, ap.maxsize_lim, ~0ull, load,
+                                   bufp<unsigned long long>(ctx, B_ACC)};
         prim::k_scan_excl<<<lookback_grid(ctx, N), prim::kThreads, 0, ctx->stream>>>(
             f, words + W_NP, bufp<uint64_t>(ctx, B_CBEGIN), words + W_NC, lb,
-            tile_parents_epilogue{bufp<uint64_t>(ctx, B_TILEPAR), sym_tiles + 2});
+            tile_parents_epilogue{bufp<uint64_t>(ctx, B_TILEPAR), sym_tiles + 2}, hook_counter(ctx, W_DONE_SCAN),
+            hook);
     }
-    k_plan_sizes<<<1, 1, 0, ctx->stream>>>(words, app, ap.nc_cap, ap.maxsize_lim, ~0ull, load,
-                                           bufp<unsigned long long>(ctx, B_ACC));
-    QD_TRY(launched(ctx, 2));
+    QD_TRY(launched(ctx));
     parents_view pv{(const char *)in->objects.p, (const uint64_t *)in->begin.p, (const uint32_t *)in->size.p,
                     (const double2 *)in->mag.p, bufp<uint64_t>(ctx, B_CBEGIN), nullptr, N, words + W_NP};
 
@@ -166,11 +169,10 @@ int simulate_batched_planned(quids_gpu_ctx *ctx, quids_gpu_state *in, const uint
                         (uint32_t *)out->size.p, (uint64_t *)out->begin.p, bufp<uint64_t>(ctx, B_SCHILD),
                         (uint32_t *)out->inst.p};
         prim::k_compact_layout<bkeep_layout, true><<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
-            kl, words + W_NU, words + W_NS, words + W_OUTBYTES, (uint64_t *)out->begin.p, nullptr, lbc, lbb, lbt);
+            kl, words + W_NU, words + W_NS, words + W_OUTBYTES, (uint64_t *)out->begin.p, nullptr, lbc, lbb, lbt,
+            hook_counter(ctx, W_DONE_LAYOUT), plan_end_hook{words, app, ap.bytes_cap, true, (uint64_t *)out->meta.p, rec});
         QD_TRY(launched(ctx));
     }
-    k_plan_end<<<1, 1, 0, ctx->stream>>>(words, app, ap.bytes_cap, true, (uint64_t *)out->meta.p, rec);
-    QD_TRY(launched(ctx));
 
     // ---- per-instance normalisation and finalize
     uint64_t *obegin = (uint64_t *)out->inst_begin.p;

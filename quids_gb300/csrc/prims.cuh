@@ -198,9 +198,18 @@ struct publish {
     uint64_t seq = 0;
     unsigned int *done = nullptr;
 };
-__device__ __forceinline__ void publish_at_exit(const publish &pb) {
+// A last-block hook L (L::active): one thread of the kernel's last block to
+// finish runs last() once every other block is done (before the words are
+// published), so a follow-up that needs the whole kernel's results costs no
+// launch.  It needs pb.done even when nothing is published.
+struct no_last {
+    static constexpr bool active = false;
+    __device__ void operator()() const {}
+};
+template <class L = no_last>
+__device__ __forceinline__ void publish_at_exit(const publish &pb, const L &hook = L{}) {
     __shared__ bool last;
-    if (!pb.host) return;
+    if (!pb.host && !L::active) return;
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
@@ -209,6 +218,14 @@ __device__ __forceinline__ void publish_at_exit(const publish &pb) {
     __syncthreads();
     if (last) {
         __threadfence();
+        if constexpr (L::active) {
+            if (threadIdx.x == 0) {
+                hook();
+                __threadfence();
+            }
+            __syncthreads();
+        }
+        if (!pb.host) return;
         for (uint32_t i = threadIdx.x; i < pb.count; i += blockDim.x)
             pb.host[i] = ((const volatile uint64_t *)pb.words)[i];
         __threadfence_system();
@@ -222,10 +239,10 @@ struct no_epilogue {
 };
 
 // E::operator()(i, out[i], f(i), n) runs once per item after its prefix is known.
-template <class F, class E = no_epilogue>
+template <class F, class E = no_epilogue, class L = no_last>
 __global__ void __launch_bounds__(kThreads) k_scan_excl(F f, const uint64_t *d_n, uint64_t *out,
                                                          uint64_t *d_total, lookback lb, E epi = E{},
-                                                         publish pb = publish{}) {
+                                                         publish pb = publish{}, L hook = L{}) {
     __shared__ uint64_t sm[kThreads / 32 + 1];
     __shared__ uint64_t bcast;
     __shared__ uint32_t sm_tile;
@@ -265,12 +282,13 @@ __global__ void __launch_bounds__(kThreads) k_scan_excl(F f, const uint64_t *d_n
             if (d_total) *d_total = prefix + agg;
         }
     }
-    publish_at_exit(pb);
+    publish_at_exit(pb, hook);
 }
 
 // ------------------------------------------------------------- compact
-// Stream compaction preserving order: P::select(i) -> bool, P::emit(i, j)
-// writes item i to output slot j.  *d_count = number selected.
+// Stream compaction preserving order: P::load(i, item&) -> bool selects item
+// i and keeps what its output needs in a P::item (loaded once), P::emit(i, j,
+// item) writes it to output slot j.  *d_count = number selected.
 template <class P>
 __global__ void __launch_bounds__(kThreads) k_compact(P p, const uint64_t *d_n, uint64_t *d_count,
                                                        lookback lb) {
@@ -289,10 +307,11 @@ __global__ void __launch_bounds__(kThreads) k_compact(P p, const uint64_t *d_n, 
         const uint64_t base = (uint64_t)tile * kTile + (uint64_t)threadIdx.x * kItems;
         uint32_t flags = 0;
         uint64_t cnt = 0;
+        typename P::item it[kItems];
 #pragma unroll
         for (int k = 0; k < kItems; ++k) {
             uint64_t i = base + k;
-            if (i < n && p.select(i)) {
+            if (i < n && p.load(i, it[k])) {
                 flags |= 1u << k;
                 ++cnt;
             }
@@ -303,7 +322,7 @@ __global__ void __launch_bounds__(kThreads) k_compact(P p, const uint64_t *d_n, 
         uint64_t j = prefix + texcl;
 #pragma unroll
         for (int k = 0; k < kItems; ++k)
-            if (flags & (1u << k)) p.emit(base + k, j++);
+            if (flags & (1u << k)) p.emit(base + k, j++, it[k]);
         if (tile == ntiles - 1 && threadIdx.x == kThreads - 1) *d_count = prefix + agg;
     }
 }
@@ -674,12 +693,12 @@ static __global__ void __launch_bounds__(kThreads)
 // The largest selected norm goes to *d_maxnorm (as IEEE bits) when d_maxnorm
 // is not null.  At the end: *d_count, *d_bytes and begin_out[count] = total
 // bytes.
-template <class P, bool TIES>
+template <class P, bool TIES, class L = no_last>
 __global__ void __launch_bounds__(kThreads, 3) k_compact_layout(P p, const uint64_t *d_n, uint64_t *d_count,
                                                               uint64_t *d_bytes, uint64_t *begin_out,
                                                               unsigned long long *d_maxnorm, lookback lb_count,
                                                               lookback lb_bytes, lookback lb_ties,
-                                                              publish pb = publish{}) {
+                                                              publish pb = publish{}, L hook = L{}) {
     __shared__ uint64_t sm[kThreads / 32 + 1];
     __shared__ uint64_t bcast;
     __shared__ uint32_t sm_tile;
@@ -691,7 +710,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_compact_layout(P p, const uint6
             *d_bytes = 0;
             begin_out[0] = 0;
         }
-        publish_at_exit(pb);
+        publish_at_exit(pb, hook);
         return;
     }
     __shared__ uint64_t bcast2[2];
@@ -767,7 +786,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_compact_layout(P p, const uint6
         }
         if ((threadIdx.x & 31) == 0 && mx) atomicMax(d_maxnorm, mx);
     }
-    publish_at_exit(pb);
+    publish_at_exit(pb, hook);
 }
 
 // --------------------------------------------------------- normalisation

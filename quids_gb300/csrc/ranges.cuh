@@ -238,13 +238,9 @@ struct range_collect {
     double2 *umag;
     uint64_t *unorm;
     uint32_t *usize, *upar, *ucid;
-    __device__ bool select(uint64_t c) const {
-        mag_t m;
-        return g.kept(c, m);
-    }
-    __device__ void emit(uint64_t c, uint64_t j) const {
-        mag_t m;
-        g.rep_mag(c, m);
+    using item = mag_t;
+    __device__ bool load(uint64_t c, item &m) const { return g.kept(c, m); }
+    __device__ void emit(uint64_t c, uint64_t j, const item &m) const {
         const uint32_t p = rpar[c], cid = rcid[c];
         uglob[j] = cbeg[p] + cid;
         umag[j] = make_double2(m.re, m.im);
