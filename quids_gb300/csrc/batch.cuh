@@ -273,14 +273,15 @@ struct bkeep_layout {
         return keep;
     }
     __device__ uint64_t bytes(const item &it) const { return padded_size(it.size, align); }
-    __device__ double norm(const item &) const { return 0.0; }  // instances are normalised separately
-    __device__ void emit(uint64_t i, uint64_t j, uint64_t off, const item &it) const {
+    // (returns 0: instances are normalised separately)
+    __device__ double emit(uint64_t i, uint64_t j, uint64_t off, const item &it) const {
         const uint64_t c = it.c;
         omag[j] = umag[i];
         osize[j] = it.size;
         obegin[j] = off;
         schild[j] = c;
         oinst[j] = it.g;
+        return 0.0;
     }
 };
 

@@ -1006,12 +1006,12 @@ struct groups_layout {
         return g.kept(c, it.m);
     }
     __device__ uint64_t bytes(const item &it) const { return padded_size(it.size, align); }
-    __device__ double norm(const item &it) const { return cnorm(it.m); }
-    __device__ void emit(uint64_t c, uint64_t j, uint64_t off, const item &it) const {
+    __device__ double emit(uint64_t c, uint64_t j, uint64_t off, const item &it) const {
         omag[j] = make_double2(it.m.re, it.m.im);
         osize[j] = it.size;
         obegin[j] = off;
         schild[j] = c;
+        return cnorm(it.m);
     }
 };
 
@@ -1141,8 +1141,9 @@ struct child_keep_layout {
     uint32_t *osize;
     uint64_t *obegin;
     uint64_t *schild;
+    // a selected group's size; its magnitude is recomputed when it is laid out
+    // (few groups are selected, and holding it for all would cost registers)
     struct item {
-        mag_t m;
         uint32_t size;
     };
     __device__ bool tie(uint64_t c) const { return st->active && key[c] == st->prefix; }
@@ -1151,21 +1152,21 @@ struct child_keep_layout {
         const uint64_t k = key[c];
         if (k == 0) return false;
         const bool keep = !st->active || k > st->prefix || (k == st->prefix && tie_rank < st->k_rem);
-        if (keep) {
-            g.rep_mag(c, it.m);
-            it.size = csize[c];
-        }
+        if (keep) it.size = csize[c];
         return keep;
     }
     __device__ uint64_t bytes(const item &it) const { return padded_size(it.size, align); }
-    __device__ double norm(const item &it) const { return cnorm(it.m); }
-    __device__ void emit(uint64_t c, uint64_t j, uint64_t off, const item &it) const {
-        omag[j] = make_double2(it.m.re, it.m.im);
+    __device__ double emit(uint64_t c, uint64_t j, uint64_t off, const item &it) const {
+        mag_t m;
+        g.rep_mag(c, m);
+        omag[j] = make_double2(m.re, m.im);
         osize[j] = it.size;
         obegin[j] = off;
         schild[j] = c;
+        return cnorm(m);
     }
 };
+constexpr int kKeepItems = 16;  // items per thread of the truncation's keep layout (a sparse selection)
 
 struct keep_parents {
     key_parent_norm kf;
@@ -1701,7 +1702,7 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, qu
         lookback_view(ctx, NC, 2, lbb);
         child_keep_layout kl{gv, gkey, ctx->d_sel, bufp<uint32_t>(ctx, B_CSIZE), align, (double2 *)out->mag.p,
                              (uint32_t *)out->size.p, (uint64_t *)out->begin.p, bufp<uint64_t>(ctx, B_SCHILD)};
-        prim::k_compact_layout<child_keep_layout, true><<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
+        prim::k_compact_layout<child_keep_layout, true, prim::no_last, kKeepItems><<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
             kl, ctx->d_words + W_NC, ctx->d_words + W_NS, ctx->d_words + W_OUTBYTES, (uint64_t *)out->begin.p,
             d_maxnorm, lbc, lbb, lbt, pb1);
         QD_TRY(launched(ctx));

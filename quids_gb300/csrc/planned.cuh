@@ -411,7 +411,7 @@ int simulate_planned(quids_gpu_ctx *ctx, quids_gpu_state *in, const uint64_t *in
         lookback_view(ctx, NC, 2, lbb);
         child_keep_layout kl{gv, gkey, ctx->d_sel, bufp<uint32_t>(ctx, B_CSIZE), align, (double2 *)out->mag.p,
                              (uint32_t *)out->size.p, (uint64_t *)out->begin.p, bufp<uint64_t>(ctx, B_SCHILD)};
-        prim::k_compact_layout<child_keep_layout, true><<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
+        prim::k_compact_layout<child_keep_layout, true, plan_end_hook, kKeepItems><<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
             kl, words + W_NC, words + W_NS, words + W_OUTBYTES, (uint64_t *)out->begin.p, d_maxnorm, lbc, lbb, lbt,
             hook_counter(ctx, W_DONE_LAYOUT), end_hook);
         QD_TRY(launched(ctx));

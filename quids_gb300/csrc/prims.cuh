@@ -693,7 +693,7 @@ static __global__ void __launch_bounds__(kThreads)
 // The largest selected norm goes to *d_maxnorm (as IEEE bits) when d_maxnorm
 // is not null.  At the end: *d_count, *d_bytes and begin_out[count] = total
 // bytes.
-template <class P, bool TIES, class L = no_last>
+template <class P, bool TIES, class L = no_last, int ITEMS = kItems>
 __global__ void __launch_bounds__(kThreads, 3) k_compact_layout(P p, const uint64_t *d_n, uint64_t *d_count,
                                                               uint64_t *d_bytes, uint64_t *begin_out,
                                                               unsigned long long *d_maxnorm, lookback lb_count,
@@ -703,7 +703,8 @@ __global__ void __launch_bounds__(kThreads, 3) k_compact_layout(P p, const uint6
     __shared__ uint64_t bcast;
     __shared__ uint32_t sm_tile;
     const uint64_t n = *d_n;
-    const uint64_t ntiles = (n + kTile - 1) / kTile;
+    constexpr uint64_t kT = (uint64_t)kThreads * ITEMS;
+    const uint64_t ntiles = (n + kT - 1) / kT;
     if (n == 0) {
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             *d_count = 0;
@@ -720,13 +721,13 @@ __global__ void __launch_bounds__(kThreads, 3) k_compact_layout(P p, const uint6
     while (true) {
         uint32_t tile = next_tile(lb_count, &sm_tile);
         if (tile >= ntiles) break;
-        const uint64_t base = (uint64_t)tile * kTile + (uint64_t)threadIdx.x * kItems;
+        const uint64_t base = (uint64_t)tile * kT + (uint64_t)threadIdx.x * ITEMS;
         uint64_t rank = 0;
         uint32_t ties = 0;
         if (ranked) {
             uint64_t tcnt = 0;
 #pragma unroll
-            for (int k = 0; k < kItems; ++k) {
+            for (int k = 0; k < ITEMS; ++k) {
                 uint64_t i = base + k;
                 if (i < n && p.tie(i)) {
                     ties |= 1u << k;
@@ -742,23 +743,21 @@ __global__ void __launch_bounds__(kThreads, 3) k_compact_layout(P p, const uint6
         // the selection of the thread's items, with every load unguarded (an
         // item past the end reads item n-1 and is dropped), so the loads of
         // all items are in flight together
-        bool sel[kItems];
-        typename P::item it[kItems];
+        bool sel[ITEMS];
+        typename P::item it[ITEMS];
 #pragma unroll
-        for (int k = 0; k < kItems; ++k) {
+        for (int k = 0; k < ITEMS; ++k) {
             const uint64_t i = base + k;
             const uint64_t ic = i < n ? i : n - 1;
             sel[k] = p.load(ic, rank, it[k]) && i < n;
             if (ties & (1u << k)) ++rank;
         }
 #pragma unroll
-        for (int k = 0; k < kItems; ++k) {
+        for (int k = 0; k < ITEMS; ++k) {
             if (sel[k]) {
                 flags |= 1u << k;
                 ++cnt;
                 bytes += p.bytes(it[k]);
-                const unsigned long long b = (unsigned long long)__double_as_longlong(p.norm(it[k]));
-                mx = mx > b ? mx : b;
             }
         }
         uint64_t agg_c, agg_b;
@@ -768,9 +767,11 @@ __global__ void __launch_bounds__(kThreads, 3) k_compact_layout(P p, const uint6
         tile_prefix2(lb_count, agg_c, lb_bytes, agg_b, tile, bcast2, pre_c, pre_b);
         uint64_t j = pre_c + excl_c, off = pre_b + excl_b;
 #pragma unroll
-        for (int k = 0; k < kItems; ++k)
+        for (int k = 0; k < ITEMS; ++k)
             if (flags & (1u << k)) {
-                p.emit(base + k, j++, off, it[k]);
+                const double nrm = p.emit(base + k, j++, off, it[k]);
+                const unsigned long long b = (unsigned long long)__double_as_longlong(nrm);
+                mx = mx > b ? mx : b;
                 off += p.bytes(it[k]);
             }
         if (tile == ntiles - 1 && threadIdx.x == kThreads - 1) {

@@ -361,14 +361,14 @@ struct merged_layout {
         return keep;
     }
     __device__ uint64_t bytes(const item &it) const { return padded_size(it.size, align); }
-    __device__ double norm(const item &it) const { return __longlong_as_double((long long)kf.c.norm[it.q]); }
-    __device__ void emit(uint64_t, uint64_t j, uint64_t off, const item &it) const {
+    __device__ double emit(uint64_t, uint64_t j, uint64_t off, const item &it) const {
         const uint32_t q = it.q;
         omag[j] = kf.c.mag[q];
         osize[j] = it.size;
         obegin[j] = off;
         spar[j] = kf.c.par[q];
         scid[j] = kf.c.cid[q];
+        return __longlong_as_double((long long)kf.c.norm[q]);
     }
 };
 
