@@ -55,6 +55,10 @@ METRIC = "child objects/s per simulate() step"
 UNIT = "children/s"
 MAX24 = 1 << 22
 L2_BYTES = 129 * 1024 * 1024
+# DRAM traffic (read + write) of the collision-table kernels over one timed
+# circuit24 step, from ncu (profiles/collision_table_circuit24_step.md); ncu
+# cannot run inside this process, so the capture's total is kept here
+TABLE_TRAFFIC_CIRCUIT24_STEP = 4381.8e6 + 2677.5e6
 
 
 # ------------------------------------------------------------------ workloads
@@ -350,6 +354,12 @@ def ours(args, rank, world):
     peak, peak_kind = peaks()
     achieved = stage_b[dom] / (stage_t[dom] / 1e3) / 1e9 if stage_t[dom] > 0 else 0.0
     step_bytes = sum(st["algorithmic_bytes"] for st in stats)
+    # per launch of the dominant stage (one per rule application)
+    n_apps = max(1, len(stats) // args.steps)
+    alg_per_launch = stage_b[dom] / args.steps / n_apps
+    traffic = None
+    if wl["name"] == "circuit24" and names[dom] == "collision_table":
+        traffic = TABLE_TRAFFIC_CIRCUIT24_STEP / n_apps
 
     # e2e through the public API with host buffers (pinned), copies inside the timed region
     e2e = None
@@ -397,7 +407,9 @@ def ours(args, rank, world):
             "gpu_launches": int(launches),
             "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-                         "traffic": None,
+                         "traffic": traffic, "algorithmic_bytes_per_launch": alg_per_launch,
+                         "traffic_source": "ncu capture, profiles/collision_table_circuit24_step.md"
+                         if traffic else None,
                          "stage_ms_per_step": [t / args.steps for t in stage_t],
                          "step_algorithmic_GBps": step_bytes / (total_ms / 1e3) / 1e9},
             "cpu_baseline": cpu,

@@ -68,6 +68,8 @@ enum qd_buf_id {
     B_PBEGIN,      // u64 [G+1] instance offsets over the kept parents
     B_BFACTOR,     // double [G] per-instance sqrt(total)
     B_SELCAND,     // u64 [NC/8 + 2^16] keys left in a truncation's selection after its first two digits
+    B_KEEPCAND,    // u32 [NC] children selected or tied at a truncation's cutoff, in child order
+    B_TILECNT,     // u32 [NC / kCandTile + 1] their count per tile of children, then u64 tile offsets
     B_COUNT
 };
 
@@ -95,7 +97,9 @@ enum qd_word {
     W_SELN,              // truncation select: items of its later passes
     W_SELUSE,            // truncation select: the later passes read the kept candidates
     W_SELCNT,            // truncation select: candidates kept
-    W_COUNT_WORDS = 24
+    W_NTILES,            // keep layout: tiles of the candidate filter
+    W_NCAND,             // keep layout: children selected or tied at the cutoff
+    W_COUNT_WORDS = 32
 };
 
 namespace qd::planned {
@@ -1168,6 +1172,93 @@ struct child_keep_layout {
 };
 constexpr int kKeepItems = 16;  // items per thread of the truncation's keep layout (a sparse selection)
 
+// A truncation keeps few of many children.  Rather than one look-back
+// compaction over every child, the children the selection can keep (a key
+// above the cutoff, or tied with it) are listed first, in child order, by
+// a filter without inter-block waits: per-tile counts, a scan of the counts,
+// then each tile writes its candidates at its offset.  The keep layout then
+// runs over that short list.
+constexpr int kCandItems = 16;
+constexpr uint64_t kCandTile = (uint64_t)prim::kThreads * kCandItems;
+struct keep_candidate {
+    const uint64_t *key;
+    const prim::select_state *st;
+    __device__ __forceinline__ bool operator()(uint64_t c) const {
+        const uint64_t k = key[c];
+        return k != 0 && (!st->active || k >= st->prefix);
+    }
+};
+// per tile of kCandTile children: how many are candidates (any order of reads)
+template <class Pred>
+__global__ void __launch_bounds__(prim::kThreads)
+    k_tile_counts(Pred pred, const uint64_t *d_n, uint32_t *cnt, uint64_t *d_ntiles) {
+    __shared__ uint32_t s_w[prim::kThreads / 32];
+    const uint64_t n = *d_n;
+    const uint64_t ntiles = (n + kCandTile - 1) / kCandTile;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *d_ntiles = ntiles;
+    for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        uint32_t c = 0;
+#pragma unroll
+        for (int k = 0; k < kCandItems; ++k) {
+            const uint64_t i = t * kCandTile + (uint64_t)k * prim::kThreads + threadIdx.x;
+            c += (i < n && pred(i)) ? 1u : 0u;
+        }
+        for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+        if ((threadIdx.x & 31) == 0) s_w[threadIdx.x >> 5] = c;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t sum = 0;
+            for (int w = 0; w < prim::kThreads / 32; ++w) sum += s_w[w];
+            cnt[t] = sum;
+        }
+        __syncthreads();
+    }
+}
+struct scan_u32 {
+    const uint32_t *v;
+    __device__ uint64_t operator()(uint64_t i) const { return v[i]; }
+};
+// each tile writes its candidates, in child order, at its offset
+template <class Pred>
+__global__ void __launch_bounds__(prim::kThreads)
+    k_tile_write(Pred pred, const uint64_t *d_n, const uint64_t *tile_off, uint32_t *cand) {
+    __shared__ uint64_t sm[prim::kThreads / 32 + 1];
+    const uint64_t n = *d_n;
+    const uint64_t ntiles = (n + kCandTile - 1) / kCandTile;
+    for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const uint64_t base = t * kCandTile + (uint64_t)threadIdx.x * kCandItems;  // a run per thread: child order
+        uint32_t flags = 0;
+        uint64_t c = 0;
+#pragma unroll
+        for (int k = 0; k < kCandItems; ++k) {
+            const uint64_t i = base + k;
+            if (i < n && pred(i)) {
+                flags |= 1u << k;
+                ++c;
+            }
+        }
+        uint64_t agg;
+        uint64_t j = tile_off[t] + prim::block_excl_scan(c, sm, agg);
+#pragma unroll
+        for (int k = 0; k < kCandItems; ++k)
+            if (flags & (1u << k)) cand[j++] = (uint32_t)(base + k);
+    }
+}
+// child_keep_layout over the candidate list
+struct cand_keep_layout {
+    child_keep_layout kl;
+    const uint32_t *cand;
+    using item = child_keep_layout::item;
+    __device__ bool tie(uint64_t i) const { return kl.tie(cand[i]); }
+    __device__ bool rank_needed() const { return kl.rank_needed(); }
+    __device__ bool load(uint64_t i, uint64_t tie_rank, item &it) const { return kl.load(cand[i], tie_rank, it); }
+    __device__ uint64_t bytes(const item &it) const { return kl.bytes(it); }
+    __device__ double emit(uint64_t i, uint64_t j, uint64_t off, const item &it) const {
+        return kl.emit(cand[i], j, off, it);
+    }
+};
+
+
 struct keep_parents {
     key_parent_norm kf;
     const prim::select_state *st;
@@ -1324,6 +1415,29 @@ inline unsigned lookback_grid(quids_gpu_ctx *ctx, uint64_t n) {
     uint64_t tiles = (n + prim::kTile - 1) / prim::kTile;
     uint64_t cap = (uint64_t)ctx->num_sms * 4;
     return (unsigned)(tiles < 1 ? 1 : (tiles < cap ? tiles : cap));
+}
+
+inline uint64_t cand_tiles(uint64_t n) { return (n + kCandTile - 1) / kCandTile + 1; }
+// The candidate list of a truncation over NC children (bounds: nc_cap) into
+// B_KEEPCAND, its length in W_NCAND; uses look-back chain 3 (zeroed with the
+// table).
+inline int list_keep_candidates(quids_gpu_ctx *ctx, const keep_candidate &pred, uint64_t nc_cap) {
+    uint64_t *words = ctx->d_words;
+    const uint64_t tiles = cand_tiles(nc_cap);
+    uint32_t *cnt = bufp<uint32_t>(ctx, B_TILECNT);
+    uint64_t *off = (uint64_t *)(cnt + (tiles + 1) / 2 * 2);
+    const unsigned g = (unsigned)std::min<uint64_t>(tiles, (uint64_t)ctx->num_sms * 8);
+    k_tile_counts<<<g, prim::kThreads, 0, ctx->stream>>>(pred, words + W_NC, cnt, words + W_NTILES);
+    prim::lookback lb;
+    lookback_view(ctx, nc_cap, 3, lb);
+    prim::k_scan_excl<<<lookback_grid(ctx, tiles), prim::kThreads, 0, ctx->stream>>>(
+        scan_u32{cnt}, words + W_NTILES, off, words + W_NCAND, lb);
+    k_tile_write<<<g, prim::kThreads, 0, ctx->stream>>>(pred, words + W_NC, off, bufp<uint32_t>(ctx, B_KEEPCAND));
+    return launched(ctx, 3);
+}
+inline size_t tilecnt_bytes(uint64_t nc_cap) {
+    const uint64_t tiles = cand_tiles(nc_cap);
+    return ((tiles + 1) / 2 * 2) * sizeof(uint32_t) + (tiles + 1) * sizeof(uint64_t);
 }
 
 // leader offsets and their tile map (one scan), then the grouped pass
@@ -1586,7 +1700,11 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, qu
     QD_TRY(ensure(out->size, NSB * sizeof(uint32_t)));
     QD_TRY(ensure(out->mag, NSB * sizeof(double2)));
     QD_TRY(ensure(out->d_total, sizeof(double)));
-    if (may_truncate) QD_TRY(ensure(ctx->buf[B_UNORM], NC * sizeof(uint64_t)));
+    if (may_truncate) {
+        QD_TRY(ensure(ctx->buf[B_UNORM], NC * sizeof(uint64_t)));
+        QD_TRY(ensure(ctx->buf[B_KEEPCAND], NC * sizeof(uint32_t)));
+        QD_TRY(ensure(ctx->buf[B_TILECNT], tilecnt_bytes(NC)));
+    }
     if (regions) {
         QD_TRY(ensure(ctx->buf[B_RHASH], NC * sizeof(uint64_t)));
         QD_TRY(ensure(ctx->buf[B_RIDX], NC * sizeof(uint32_t)));
@@ -1700,10 +1818,12 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, qu
         lookback_view(ctx, NC, 0, lbt);
         lookback_view(ctx, NC, 1, lbc);
         lookback_view(ctx, NC, 2, lbb);
-        child_keep_layout kl{gv, gkey, ctx->d_sel, bufp<uint32_t>(ctx, B_CSIZE), align, (double2 *)out->mag.p,
-                             (uint32_t *)out->size.p, (uint64_t *)out->begin.p, bufp<uint64_t>(ctx, B_SCHILD)};
-        prim::k_compact_layout<child_keep_layout, true, prim::no_last, kKeepItems><<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
-            kl, ctx->d_words + W_NC, ctx->d_words + W_NS, ctx->d_words + W_OUTBYTES, (uint64_t *)out->begin.p,
+        QD_TRY(list_keep_candidates(ctx, keep_candidate{gkey, ctx->d_sel}, NC));
+        const cand_keep_layout kl{{gv, gkey, ctx->d_sel, bufp<uint32_t>(ctx, B_CSIZE), align, (double2 *)out->mag.p,
+                                   (uint32_t *)out->size.p, (uint64_t *)out->begin.p, bufp<uint64_t>(ctx, B_SCHILD)},
+                                  bufp<uint32_t>(ctx, B_KEEPCAND)};
+        prim::k_compact_layout<cand_keep_layout, true><<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
+            kl, ctx->d_words + W_NCAND, ctx->d_words + W_NS, ctx->d_words + W_OUTBYTES, (uint64_t *)out->begin.p,
             d_maxnorm, lbc, lbb, lbt, pb1);
         QD_TRY(launched(ctx));
         end_stage(4);

@@ -283,6 +283,8 @@ inline int ensure_planned(quids_gpu_ctx *ctx, quids_gpu_state *out, const app_pl
     if (ap.may_truncate) {
         QD_TRY(ensure(ctx->buf[B_SELCAND], filter_cap(NC) * sizeof(uint64_t)));
         QD_TRY(ensure(ctx->buf[B_UNORM], NC * sizeof(uint64_t)));
+        QD_TRY(ensure(ctx->buf[B_KEEPCAND], NC * sizeof(uint32_t)));
+        QD_TRY(ensure(ctx->buf[B_TILECNT], tilecnt_bytes(NC)));
     }
     QD_TRY(ensure(ctx->buf[B_MODSTATUS], sizeof(uint64_t)));
     auto grow = [&](qd_dbuf &b, size_t bytes) { return keep ? ensure_keep(b, bytes, ctx->stream) : ensure(b, bytes); };
@@ -409,10 +411,12 @@ int simulate_planned(quids_gpu_ctx *ctx, quids_gpu_state *in, const uint64_t *in
         lookback_view(ctx, NC, 0, lbt);
         lookback_view(ctx, NC, 1, lbc);
         lookback_view(ctx, NC, 2, lbb);
-        child_keep_layout kl{gv, gkey, ctx->d_sel, bufp<uint32_t>(ctx, B_CSIZE), align, (double2 *)out->mag.p,
-                             (uint32_t *)out->size.p, (uint64_t *)out->begin.p, bufp<uint64_t>(ctx, B_SCHILD)};
-        prim::k_compact_layout<child_keep_layout, true, plan_end_hook, kKeepItems><<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
-            kl, words + W_NC, words + W_NS, words + W_OUTBYTES, (uint64_t *)out->begin.p, d_maxnorm, lbc, lbb, lbt,
+        QD_TRY(list_keep_candidates(ctx, keep_candidate{gkey, ctx->d_sel}, NC));
+        const cand_keep_layout kl{{gv, gkey, ctx->d_sel, bufp<uint32_t>(ctx, B_CSIZE), align, (double2 *)out->mag.p,
+                                   (uint32_t *)out->size.p, (uint64_t *)out->begin.p, bufp<uint64_t>(ctx, B_SCHILD)},
+                                  bufp<uint32_t>(ctx, B_KEEPCAND)};
+        prim::k_compact_layout<cand_keep_layout, true, plan_end_hook><<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
+            kl, words + W_NCAND, words + W_NS, words + W_OUTBYTES, (uint64_t *)out->begin.p, d_maxnorm, lbc, lbb, lbt,
             hook_counter(ctx, W_DONE_LAYOUT), end_hook);
         QD_TRY(launched(ctx));
     }

@@ -75,47 +75,72 @@ struct lookback {
     int *err;
 };
 
+// Warp-level decoupled look-back of tile `tile` (> 0): publishes its
+// aggregate, sums its predecessors' values back to the nearest inclusive one,
+// publishes its own inclusive value and returns its exclusive prefix (in every
+// lane).  Each round looks at 32 * kLookWindow predecessors, every lane
+// loading kLookWindow status words at once (measured on GB300: a window of
+// 128 tiles was slower than 32, the nearest inclusive value being usually
+// close).  Waits are bounded (kSpinLimit polls): a wait that runs out records
+// QUIDS_ERR_TIMEOUT and counts the tile as an inclusive zero.
+constexpr int kLookWindow = 1;
+static __device__ uint64_t warp_lookback(const lookback &lb, uint32_t tile, uint64_t aggregate) {
+    const int lane = threadIdx.x & 31;
+    if (lane == 0) st_volatile_u64(&lb.status[tile], kFlagAgg | (aggregate & kValMask));
+    int64_t base = (int64_t)tile - 1;
+    uint64_t prefix = 0;
+    bool failed = false;
+    while (true) {
+        uint64_t s[kLookWindow];
+#pragma unroll
+        for (int r = 0; r < kLookWindow; ++r) {
+            const int64_t j = base - lane - 32 * r;
+            s[r] = j >= 0 ? ld_volatile_u64(&lb.status[j]) : kFlagInc;  // before tile 0: an inclusive 0
+        }
+#pragma unroll
+        for (int r = 0; r < kLookWindow; ++r) {
+            const int64_t j = base - lane - 32 * r;
+            uint32_t it = 0;
+            while ((s[r] >> 62) == 0 && ++it < kSpinLimit) {
+                __nanosleep(64);
+                s[r] = ld_volatile_u64(&lb.status[j]);
+            }
+            if ((s[r] >> 62) == 0) {
+                failed = true;
+                s[r] = kFlagInc;
+            }
+        }
+        bool done = false;  // uniform over the warp
+#pragma unroll
+        for (int r = 0; r < kLookWindow; ++r) {
+            if (!done) {
+                const unsigned inc = __ballot_sync(0xffffffffu, (s[r] >> 62) == 2);
+                uint64_t v = s[r] & kValMask;
+                if (inc) {
+                    if (lane > __ffs(inc) - 1) v = 0;  // beyond the nearest inclusive value
+                    done = true;
+                }
+                prefix += warp_sum(v);
+            }
+        }
+        if (done) break;
+        base -= 32 * kLookWindow;
+    }
+    if (__any_sync(0xffffffffu, failed) && lane == 0) set_error(lb.err, QUIDS_ERR_TIMEOUT);
+    if (lane == 0) st_volatile_u64(&lb.status[tile], kFlagInc | ((prefix + aggregate) & kValMask));
+    return prefix;
+}
+
 // Exclusive prefix of tile `tile` given its aggregate; all threads call it.
 static __device__ uint64_t tile_prefix(const lookback &lb, uint32_t tile, uint64_t aggregate, uint64_t *bcast) {
     if (threadIdx.x < 32) {
-        const int lane = threadIdx.x;
         uint64_t prefix = 0;
         if (tile == 0) {
-            if (lane == 0) st_volatile_u64(&lb.status[0], kFlagInc | (aggregate & kValMask));
+            if (threadIdx.x == 0) st_volatile_u64(&lb.status[0], kFlagInc | (aggregate & kValMask));
         } else {
-            if (lane == 0) st_volatile_u64(&lb.status[tile], kFlagAgg | (aggregate & kValMask));
-            int64_t base = (int64_t)tile - 1;
-            bool failed = false;
-            while (true) {
-                int64_t j = base - lane;
-                uint64_t s = kFlagInc;  // tiles before 0 contribute an inclusive 0
-                if (j >= 0) {
-                    uint32_t it = 0;
-                    s = ld_volatile_u64(&lb.status[j]);
-                    while ((s >> 62) == 0 && ++it < kSpinLimit) {
-                        __nanosleep(64);
-                        s = ld_volatile_u64(&lb.status[j]);
-                    }
-                    if ((s >> 62) == 0) {
-                        failed = true;
-                        s = kFlagInc;
-                    }
-                }
-                unsigned inc = __ballot_sync(0xffffffffu, (s >> 62) == 2);
-                uint64_t v = s & kValMask;
-                if (inc) {
-                    int first = __ffs(inc) - 1;
-                    if (lane > first) v = 0;
-                    prefix += warp_sum(v);
-                    break;
-                }
-                prefix += warp_sum(v);
-                base -= 32;
-            }
-            if (__any_sync(0xffffffffu, failed) && lane == 0) set_error(lb.err, QUIDS_ERR_TIMEOUT);
-            if (lane == 0) st_volatile_u64(&lb.status[tile], kFlagInc | ((prefix + aggregate) & kValMask));
+            prefix = warp_lookback(lb, tile, aggregate);
         }
-        if (lane == 0) *bcast = prefix;
+        if (threadIdx.x == 0) *bcast = prefix;
     }
     __syncthreads();
     uint64_t p = *bcast;
@@ -136,37 +161,7 @@ static __device__ void tile_prefix2(const lookback &la, uint64_t agg_a, const lo
         if (tile == 0) {
             if (lane == 0) st_volatile_u64(&lb.status[0], kFlagInc | (aggregate & kValMask));
         } else {
-            if (lane == 0) st_volatile_u64(&lb.status[tile], kFlagAgg | (aggregate & kValMask));
-            int64_t base = (int64_t)tile - 1;
-            bool failed = false;
-            while (true) {
-                int64_t j = base - lane;
-                uint64_t s = kFlagInc;
-                if (j >= 0) {
-                    uint32_t it = 0;
-                    s = ld_volatile_u64(&lb.status[j]);
-                    while ((s >> 62) == 0 && ++it < kSpinLimit) {
-                        __nanosleep(64);
-                        s = ld_volatile_u64(&lb.status[j]);
-                    }
-                    if ((s >> 62) == 0) {
-                        failed = true;
-                        s = kFlagInc;
-                    }
-                }
-                unsigned inc = __ballot_sync(0xffffffffu, (s >> 62) == 2);
-                uint64_t v = s & kValMask;
-                if (inc) {
-                    int first = __ffs(inc) - 1;
-                    if (lane > first) v = 0;
-                    prefix += warp_sum(v);
-                    break;
-                }
-                prefix += warp_sum(v);
-                base -= 32;
-            }
-            if (__any_sync(0xffffffffu, failed) && lane == 0) set_error(lb.err, QUIDS_ERR_TIMEOUT);
-            if (lane == 0) st_volatile_u64(&lb.status[tile], kFlagInc | ((prefix + aggregate) & kValMask));
+            prefix = warp_lookback(lb, tile, aggregate);
         }
         if (lane == 0) bcast2[warp] = prefix;
     }
