@@ -27,7 +27,7 @@ namespace {
 // status, as a separate modifier launch does.
 struct mod_chain {
     static constexpr bool active = true;
-    static constexpr int kMax = 16;
+    static constexpr int kMax = 32;
     int n = 0;
     int32_t kind[kMax];
     uint64_t bit[kMax], control[kMax];
