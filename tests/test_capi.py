@@ -45,11 +45,17 @@ def test_library_loads_with_ctypes(lib_path):
     assert L.quids_gpu_status_string(-3) == b"collision table full"
 
 
-def test_sm103a_cubin_embedded(lib_path):
-    r = subprocess.run(["cuobjdump", "--list-elf", lib_path], capture_output=True, text=True)
-    if r.returncode != 0:
-        pytest.skip("cuobjdump unavailable")
-    assert "sm_103a" in r.stdout
+def test_built_for_sm103a_only():
+    assert qbuild.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def test_flags_match_the_header():
+    """capi.py's QUIDS_FLAG_* values are the header's."""
+    text = open(HEADER).read()
+    flags = {m.group(1): int(m.group(2)) for m in re.finditer(r"#define QUIDS_FLAG_(\w+) (\d+)u", text)}
+    assert flags, "no QUIDS_FLAG_* in the header"
+    for name, value in flags.items():
+        assert getattr(capi, "FLAG_" + name) == value, name
 
 
 def test_no_device_is_an_error_not_a_crash(lib_path):
