@@ -436,8 +436,10 @@ struct split_merge {
         int n, cn;
         uint32_t cid;  // child id with the wrap bits consumed
     };
+    // the wrap decisions alone (their factors first, as the reference applies
+    // them); cn counts the nodes before the middle sites' splits and merges
     template <class M>
-    QD_HD plan make_plan(const char *p, uint32_t cid, M *mag) const {
+    QD_HD plan wrap_plan(const char *p, uint32_t cid, M *mag) const {
         plan pl;
         int n = pl.n = num_nodes(p);
         bool fs, lm;
@@ -456,8 +458,19 @@ struct split_merge {
             }
             cid >>= 1;
         }
-        int cn = n + fs - lm;
-        uint32_t bits = cid;
+        pl.fs = fs;
+        pl.lm = lm;
+        pl.cn = n + fs - lm;
+        pl.cid = cid;
+        return pl;
+    }
+    template <class M>
+    QD_HD plan make_plan(const char *p, uint32_t cid, M *mag) const {
+        plan pl = wrap_plan(p, cid, mag);
+        const int n = pl.n;
+        const bool fs = pl.fs, lm = pl.lm;
+        int cn = pl.cn;
+        uint32_t bits = pl.cid;
         for (int i = fs + lm; i < n - lm; ++i) {
             bool s, m;
             get_operations(p, n, i, s, m);
@@ -470,17 +483,18 @@ struct split_merge {
             }
             bits >>= 1;
         }
-        pl.fs = fs;
-        pl.lm = lm;
         pl.cn = cn;
-        pl.cid = cid;
         return pl;
     }
 
-    // second pass (:702-845)
-    template <class Sink>
-    QD_HD static void walk(const char *p, const plan &pl, Sink &sink) {
-        const int n = pl.n, cn = pl.cn;
+    // second pass (:702-845).  With mag, the middle sites' factors are applied
+    // on the way, in the order make_plan applies them (a site's node comes
+    // before the next site's; a taken merge's second node is never a site), so
+    // wrap_plan + walk(mag) is make_plan + walk in one pass over the nodes.
+    template <class Sink, class M = mag_t>
+    QD_HD void walk(const char *p, const plan &pl, Sink &sink, M *mag = nullptr) const {
+        const int n = pl.n;
+        int cn = pl.n + pl.fs - pl.lm;  // the child's nodes, counted as the sites are taken
         const bool fs = pl.fs, lm = pl.lm;
         uint32_t cid = pl.cid;
         const char *pn = names(p, n);
@@ -507,7 +521,9 @@ struct split_merge {
             bool taken = false;
             if (s || m) {
                 taken = cid & 1;
+                mulf(mag, f, taken ? (s ? F_D : F_DC) : (s ? F_DN : F_NDNC));
                 if (taken) {
+                    cn += (int)s - (int)m;
                     int b = name_begin(p, n, i), e = name_begin(p, n, i + 1);
                     if (s) {
                         sink.emit(i + off, true, false, OP_LEFT, b, e, 0, 0);
@@ -544,7 +560,9 @@ struct split_merge {
         const char *pn;
         uint64_t lh, rh, nh;
         int len;
+        int cn = 0;  // nodes emitted
         QD_HD void emit(int k, bool l, bool r, int op, int b1, int e1, int b2, int e2) {
+            ++cn;
             if (l) hash_combine(lh, (uint64_t)k);
             if (r) hash_combine(rh, (uint64_t)k);
             int ln;
@@ -574,9 +592,10 @@ struct split_merge {
     QD_HD uint64_t hasher(const char *b, const char *) const { return hash_graph(b); }
     QD_HD uint64_t hash_child(const char *pb, const char *, uint32_t child_id, uint32_t &size,
                               mag_t &mag) const {
-        plan pl = make_plan(pb, child_id, &mag);
+        plan pl = wrap_plan(pb, child_id, &mag);
         hash_sink s{names(pb, pl.n), 0, 0, 0, 0};
-        walk(pb, pl, s);
+        walk(pb, pl, s, &mag);
+        pl.cn = s.cn;
         hash_combine(s.nh, s.lh);
         hash_combine(s.nh, s.rh);
         size = 4 + 4 * (uint32_t)pl.cn + 16 * (uint32_t)s.len;

@@ -178,3 +178,31 @@ def test_grouped_expansion_is_hash_child_bit_for_bit(shim, kind, h):
                 assert (mm[0], mm[1]) == (ms[2 * j], ms[2 * j + 1]), (trial, e, j)
                 checked += 1
     assert checked > 500
+
+
+@pytest.mark.parametrize("params", [(math.pi / 4, 0.0, -math.pi / 2), (0.7, 2.1, 4.4)])
+def test_split_merge_hash_child_is_populate_then_hash(shim, params):
+    """split_merge's hash_child (one pass: wrap decisions, then the walk with
+    the site factors applied on the way) gives, for every child of many
+    graphs, the hash_graph of populate_child's bytes, its size and its
+    magnitude, bit for bit."""
+    rng = W.Rng(2024)
+    graphs = [W.random_graph(n, rng) for n in range(1, 15) for _ in range(6)]
+    for g in graphs[:30]:  # graphs with split and merged names
+        for cid in range(3):
+            graphs.append(_child(shim, 4, params, g, cid, 1.0 + 0j, 4 * len(g))[0])
+    keep, pp = _dp(params)
+    checked = 0
+    for g in graphs:
+        a, b = C.c_uint32(), C.c_uint32()
+        shim.shim_num_child(4, pp, _buf(g), len(g), C.byref(a), C.byref(b))
+        for cid in range(min(a.value, 64)):
+            child, cm = _child(shim, 4, params, g, cid, 0.28 + 0.96j, b.value)
+            sz = C.c_uint32()
+            mm = (C.c_double * 2)(0.28, 0.96)
+            h = shim.shim_hash_child(4, pp, _buf(g), len(g), cid, C.byref(sz), mm)
+            assert h == shim.shim_hash_graph(_buf(child))
+            assert sz.value == len(child)
+            assert complex(mm[0], mm[1]) == cm
+            checked += 1
+    assert checked > 500
