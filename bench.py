@@ -28,6 +28,13 @@ simulate_backward of the expected node count (checkpoints every 5 QCGD
 steps); the value counts the forward's children per second of the whole
 forward + backward, and the plain forward is timed beside it.
 
+Every bench step runs from the same two state handles, the input uploaded
+before the step: the first warm-up step is the synchronous steps, the next
+are planned runs (sizes from the first, no host waits), autotuned and
+captured as a CUDA graph that the timed steps replay (quids_gpu_run with
+QUIDS_FLAG_AUTOTUNE; config.runs_timed counts how the timed steps ran).  The
+stage timing pass runs the synchronous steps with CUDA events per stage.
+
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--config NAME]
 
 --impl reference times the CPU restatement of the reference algorithm
