@@ -104,7 +104,10 @@ int upload_rules(quids_gpu_ctx *ctx, run_plan &p) {
         ++r;
     }
     QD_TRY(ensure(p.rules, bytes.size(), false));
-    QD_CUDA(cudaMemcpy(p.rules.p, bytes.data(), bytes.size(), cudaMemcpyHostToDevice));
+    // on the context's stream: a plain cudaMemcpy from pageable memory may return before its DMA
+    // lands, and the legacy stream does not order the non-blocking stream's kernels after it
+    QD_CUDA(cudaMemcpyAsync(p.rules.p, bytes.data(), bytes.size(), cudaMemcpyHostToDevice, ctx->stream));
+    QD_CUDA(cudaStreamSynchronize(ctx->stream));
     p.rules_ready = true;
     return QUIDS_OK;
 }
@@ -155,7 +158,7 @@ int enqueue_planned_batched(quids_gpu_ctx *ctx, run_plan &p, quids_gpu_state *a,
 }
 
 // the host mirror of a batched state written on the device
-int set_batched_state(quids_gpu_ctx *ctx, quids_gpu_state *x, uint64_t n, uint64_t nbytes, uint32_t G) {
+int set_batched_state(quids_gpu_state *x, uint64_t n, uint64_t nbytes, uint32_t G) {
     x->n = n;
     x->nbytes = nbytes;
     x->n_inst = G;
@@ -192,13 +195,13 @@ int run_planned_batched(quids_gpu_ctx *ctx, run_plan &p, quids_gpu_state *a, qui
     planned::read_stats(ctx, R, fa, a->nbytes, true, st);
     const uint64_t na = fin[2], ba = fin[3], nb = fin[4], bb = fin[5];
     if (!status) {
-        if (R >= 1) QD_TRY(set_batched_state(ctx, b, nb, bb, G));
-        if (R >= 2) QD_TRY(set_batched_state(ctx, a, na, ba, G));
+        if (R >= 1) QD_TRY(set_batched_state(b, nb, bb, G));
+        if (R >= 2) QD_TRY(set_batched_state(a, na, ba, G));
         ++p.runs;
         return QUIDS_OK;
     }
     quids_gpu_state *in = fa % 2 ? b : a, *out = fa % 2 ? a : b;
-    if (fa >= 1) QD_TRY(set_batched_state(ctx, in, fa % 2 ? nb : na, fa % 2 ? bb : ba, G));
+    if (fa >= 1) QD_TRY(set_batched_state(in, fa % 2 ? nb : na, fa % 2 ? bb : ba, G));
     out->n = out->nbytes = 0;
     *fail_app = fa;
     return status;
