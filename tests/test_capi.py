@@ -65,3 +65,17 @@ def test_no_device_is_an_error_not_a_crash(lib_path):
     L = capi.load()
     h = C.c_void_p()
     assert L.quids_gpu_ctx_create(0, C.byref(h)) == -8
+
+
+def test_null_handles_are_bad_arg_not_a_crash(lib_path):
+    """Every status-returning entry point, called with null handles and
+    pointers and zero sizes, returns QUIDS_ERR_BAD_ARG before any CUDA call
+    (so here, with no GPU, not QUIDS_ERR_NO_DEVICE)."""
+    text = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    status_fns = sorted(set(re.findall(r"^int (quids_gpu_\w+)\s*\(", text, flags=re.M)))
+    assert len(status_fns) > 30
+    raw = C.CDLL(lib_path)  # a separate handle: no argtypes, every argument NULL / 0
+    for name in status_fns:
+        f = getattr(raw, name)
+        f.restype = C.c_int
+        assert f(*([None] * 20)) == -1, name
