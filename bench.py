@@ -670,11 +670,22 @@ def ours_adjoint(args, rank, world):
         }), flush=True)
 
 
-def cpu_baseline_batched(wl, packed):
-    """The oracle port on all host cores, instance after instance."""
+def cpu_oracle():
+    """The CPU implementation timed as the baseline: the reference compiled
+    from its own headers (oracle/_ref) where it was built on this host, else
+    the oracle port (the reference algorithm restated, built anywhere).
+    Returns (oracle, kind) with kind "reference" or "port"."""
     from oracle.oracle import Oracle
+    try:
+        return Oracle("ref", autobuild=False), "reference"
+    except OSError:  # not built here, or built for another architecture
+        return Oracle("port"), "port"
+
+
+def cpu_baseline_batched(wl, packed):
+    """The CPU oracle on all host cores, instance after instance."""
     from quids_gb300 import workloads as W
-    o = Oracle("port")
+    o, kind = cpu_oracle()
     cores = os.cpu_count() or 1
     o.set_threads(cores)
     o.set_globals(wl["tolerance"], True, wl["align"])
@@ -683,21 +694,20 @@ def cpu_baseline_batched(wl, packed):
     for (g, sm, ec), p in zip(wl["insts"], packed):
         s = o.new_state(p)
         o.modifier(s, W.MOD_QCGD_STEP, ())
-        for kind, prm in ((W.RULE_QCGD_COIN, W.COIN_DEFAULT), (W.RULE_QCGD_SPLIT_MERGE, sm),
-                          (W.RULE_QCGD_ERASE_CREATE, ec)):
+        for rule_kind, prm in ((W.RULE_QCGD_COIN, W.COIN_DEFAULT), (W.RULE_QCGD_SPLIT_MERGE, sm),
+                               (W.RULE_QCGD_ERASE_CREATE, ec)):
             t = o.new_state()
-            ch += o.simulate(s, kind, prm, t, wl["max"])[0]
+            ch += o.simulate(s, rule_kind, prm, t, wl["max"])[0]
             s = t
     dt = time.perf_counter() - t0
-    return {"value": ch / dt, "unit": UNIT, "cores": cores, "kind": "port",
+    return {"value": ch / dt, "unit": UNIT, "cores": cores, "kind": kind,
             "sample": f"the first step of all {len(packed)} instances, one after another ({ch} children, "
                       f"{dt:.2f} s)"}
 
 
 def cpu_baseline(wl, init_packed, samples=1, warm=True):
-    """The oracle port (the reference algorithm restated, OpenMP) on all host cores."""
-    from oracle.oracle import Oracle
-    o = Oracle("port")
+    """The CPU oracle (cpu_oracle) on all host cores."""
+    o, kind = cpu_oracle()
     cores = os.cpu_count() or 1
     o.set_threads(cores)
     o.set_globals(wl["tolerance"], True, wl["align"])
@@ -720,7 +730,7 @@ def cpu_baseline(wl, init_packed, samples=1, warm=True):
     ch = sum(one() for _ in range(samples))
     dt = time.perf_counter() - t0
     part = (f"the first {wl['cpu_sample_objects']} objects of " if wl.get("cpu_sample_objects") else "")
-    return {"value": ch / dt, "unit": UNIT, "cores": cores, "kind": "port",
+    return {"value": ch / dt, "unit": UNIT, "cores": cores, "kind": kind,
             "sample": f"{samples} step(s) of {part}the {wl['name']} workload ({ch} children, {dt:.2f} s)"}
 
 
@@ -744,8 +754,7 @@ def reference(args, rank, world):
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         }), flush=True)
         return
-    from oracle.oracle import Oracle
-    o = Oracle("port")
+    o, kind = cpu_oracle()
     cores = os.cpu_count() or 1
     o.set_threads(cores)
     o.set_globals(wl["tolerance"], True, wl["align"])
@@ -778,7 +787,7 @@ def reference(args, rank, world):
         "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": dict(wl["config"], parallelism="host cores"),
-        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": kind,
                          "sample": f"{args.steps} step(s) of "
                                    + (f"the first {wl['cpu_sample_objects']} objects of "
                                       if wl.get("cpu_sample_objects") else "")
