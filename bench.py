@@ -37,8 +37,10 @@ stage timing pass runs the synchronous steps with CUDA events per stage.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--config NAME]
 
---impl reference times the CPU restatement of the reference algorithm
-(oracle/quids_port.cpp, OpenMP + libstdc++ parallel mode) on all host cores.
+--impl reference times the reference's CPU algorithm on all host cores: the
+reference compiled from its own headers (oracle/_ref) where it was built on
+this host, else its restatement (oracle/quids_port.cpp, OpenMP + libstdc++
+parallel mode).
 Under torchrun each rank runs an independent replica (the step does not
 shard across GPUs); rank 0 prints one JSON line.
 """
