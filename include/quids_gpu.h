@@ -39,7 +39,7 @@ extern "C" {
 #define QUIDS_ERR_TIMEOUT (-6)              /* a bounded device wait gave up */
 #define QUIDS_ERR_CUDA (-7)                 /* a CUDA runtime call failed */
 #define QUIDS_ERR_NO_DEVICE (-8)            /* no CUDA device */
-#define QUIDS_ERR_UNSUPPORTED (-9)          /* valid request this build does not implement */
+#define QUIDS_ERR_UNSUPPORTED (-9)          /* valid request this library does not implement */
 #define QUIDS_ERR_NOALLOC_LIMIT (-10)       /* beyond the static scratch of quids_gpu_rule_children_noalloc */
 
 /* ------------------------------------------------------- rules/modifiers */

@@ -9,7 +9,7 @@
 //   populate_child_simple(...)             (bytes only)
 //   hasher(object_begin, object_end)       (default: std::hash<string_view>)
 //   hash_child(parent_begin, parent_end, child_id, size, mag) -> hash
-// The last one is this build's fast path: the child's hash, size and
+// The last one is this library's fast path: the child's hash, size and
 // magnitude without materialising its bytes; it must equal
 // hasher(populate_child(...)).
 #pragma once
