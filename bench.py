@@ -64,9 +64,11 @@ METRIC = "child objects/s per simulate() step"
 UNIT = "children/s"
 MAX24 = 1 << 22
 L2_BYTES = 129 * 1024 * 1024
-# DRAM traffic (read + write) of the collision-table kernels over one timed
-# circuit24 step, from ncu (profiles/collision_table_circuit24_step.md); ncu
-# cannot run inside this process, so the capture's total is kept here
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of k_fill,
+# k_table_claim and k_table_accumulate over one timed circuit24 step (the
+# graph replay of 72 rule applications), from one ncu capture of this
+# script; ncu cannot run inside this process, so the capture's total is kept
+# here
 TABLE_TRAFFIC_CIRCUIT24_STEP = 4381.8e6 + 2677.5e6
 
 
@@ -417,7 +419,7 @@ def ours(args, rank, world):
             "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
                          "traffic": traffic, "algorithmic_bytes_per_launch": alg_per_launch,
-                         "traffic_source": "ncu capture, profiles/collision_table_circuit24_step.md"
+                         "traffic_source": "ncu capture of k_fill + k_table_claim + k_table_accumulate over one circuit24 step"
                          if traffic else None,
                          "stage_ms_per_step": [t / args.steps for t in stage_t],
                          "step_algorithmic_GBps": step_bytes / (total_ms / 1e3) / 1e9},
