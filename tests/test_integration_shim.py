@@ -45,3 +45,21 @@ def test_cpp_shim_compiles_links_and_rejects_a_null_context(tmp_path):
                     f"-Wl,-rpath,{cuda_lib}"], check=True)
     out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()
     assert out == ["-1", "0"]
+
+
+def test_python_example_names_exist_and_no_device_is_an_error():
+    """The guide's Python example uses names the package has; without a GPU
+    it stops at the context with the library's no-device status."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    import quids_gb300 as quids
+    from quids_gb300 import capi
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    blocks = re.findall(r"```python\n(.*?)```", text, flags=re.S)
+    assert len(blocks) == 1
+    with pytest.raises(capi.QuidsError, match="no CUDA device"):
+        exec(blocks[0], {})
+    for name in ("Context", "it_t", "sy_it_t", "simulate"):
+        assert hasattr(quids, name), name
+    assert hasattr(quids.it_t, "append")
