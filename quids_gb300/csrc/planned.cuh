@@ -1,5 +1,7 @@
 // planned.cuh -- planned rule steps: the step of engine.cuh without its two
-// host waits, for runs whose sizes are known beforehand.
+// host waits, for runs whose sizes are known beforehand (the reference's
+// examples loop over simulate calls, examples/quantum_computer_test.cpp:26-49,
+// each step sizing its buffers as it goes, src/quids.hpp:448-543).
 //
 // A step sizes its buffers from the child count and from the survivors'
 // bytes, so simulate_rule waits for both on the host.  A run of ops that is

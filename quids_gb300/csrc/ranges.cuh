@@ -20,6 +20,11 @@
 // the step's child count), a group's representative is its lowest child
 // index, the truncation keys and their ties (lower child index first) are
 // the same, and the survivors come out in child order.
+//
+// The reference's counterpart is its MPI engine, which gives each node the
+// children of one hash range (src/quids_mpi.hpp:624-865, owner by the hash's
+// top bits :665-669) and merges collisions on the owner; here one GPU runs
+// the ranges one after another and recomputes the children for each.
 #pragma once
 #include "engine.cuh"
 
