@@ -80,6 +80,15 @@ int shim_expand_group(int kind, int h, const double *p, const uint8_t *o, uint32
     return -1;
 }
 uint64_t shim_murmur(const uint8_t *b, uint64_t len) { return murmur64a((const char *)b, len); }
+// a collision group's sum as the table forms it: from_fix of the 128-bit sum
+// of to_fix(x_i, F), F = fix_scale(maxabs, n_scale)
+double shim_fix_sum(const double *x, uint64_t n, double maxabs, uint64_t n_scale, int *F_out) {
+    const int F = fix_scale(maxabs, n_scale);
+    fix128 s{0, 0};
+    for (uint64_t i = 0; i < n; ++i) s = fix_add(s, to_fix(x[i], F));
+    if (F_out) *F_out = F;
+    return from_fix(s, F);
+}
 uint64_t shim_hash_graph(const uint8_t *b) { return qcgd::hash_graph((const char *)b); }
 int shim_modifier(int kind, const double *p, uint8_t *o, uint32_t sz, double *mag) {
     mag_t m{mag[0], mag[1]};
