@@ -55,3 +55,35 @@ def test_job_value_single_rank():
     import bench
     value, total_ms = bench.job_value(500, 5.0, 1)
     assert (value, total_ms) == (pytest.approx(1e5), 5.0)
+
+
+def _reference_arm(rank, world):
+    import json
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, RANK=str(rank), WORLD_SIZE=str(world), LOCAL_RANK=str(rank))
+    r = subprocess.run([sys.executable, os.path.join(root, "bench.py"), "--impl", "reference", "--gpus", str(world),
+                        "--steps", "1", "--warmup", "0"], capture_output=True, text=True, timeout=600, env=env,
+                       cwd=root)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    return [json.loads(ln) for ln in lines]
+
+
+def test_reference_arm_prints_the_contract_line_on_rank_0_only():
+    """bench.py --impl reference times the CPU implementation of the rule
+    step on the host cores: rank 0 prints one JSON line with the bench's
+    metric, a cpu_baseline and an e2e of zero copies; other ranks print
+    nothing and exit 0."""
+    (line,) = _reference_arm(0, 2)
+    assert line["impl"] == "reference"
+    assert line["metric"] == "child objects/s per simulate() step" and line["unit"] == "children/s"
+    assert line["value"] > 0 and line["higher_is_better"] is True
+    assert (line["n_gpus"], line["steps"], line["warmup"]) == (2, 1, 0)
+    cb = line["cpu_baseline"]
+    assert cb["kind"] in ("reference", "port") and cb["cores"] >= 1 and cb["value"] == line["value"]
+    assert line["e2e"] == {"value": line["value"], "unit": "children/s", "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}
+    assert "workload" in line["config"]
+    assert _reference_arm(1, 2) == []
