@@ -91,7 +91,20 @@ typedef struct quids_gpu_params {
     uint64_t seed;               /* probabilistic truncation: generator seed (same seed and input,
                                     same result) */
     uint64_t memory_budget;      /* automatic truncation: bytes a step may use (0: from the device) */
+    uint32_t max_probes;         /* collision-table probe limit (0: 65536); a child whose probe sequence
+                                    reaches it stops the step with QUIDS_ERR_TABLE_FULL */
+    uint32_t debug_flags;        /* QUIDS_DEBUG_*: failure injection for tests of the error paths; 0 */
+    uint64_t max_alloc_bytes;    /* 0: no limit; else a device allocation of more bytes than this, by
+                                    the step's scratch or its output, fails with QUIDS_ERR_OOM before
+                                    cudaMalloc is called (a cap on what one call may grow to) */
 } quids_gpu_params;
+
+/* quids_gpu_params.debug_flags.  Each makes a bounded device wait run out on
+ * purpose: the wait gives up after its poll limit (well under a second),
+ * records QUIDS_ERR_TIMEOUT, and the call returns that status with the
+ * context still usable.  Nothing faults, traps or hangs. */
+#define QUIDS_DEBUG_STALL_LOOKBACK 1u  /* tile 1 of the child-offset scan never publishes its prefix, so
+                                          the look-back of tile 2 waits for it until its poll limit */
 
 /* quids_gpu_params.flags */
 #define QUIDS_FLAG_NO_FAST_HASH 1u   /* hash children through populate_child + hasher, not hash_child */

@@ -33,6 +33,9 @@ truncation_seed: int = 0          # generator seed of probabilistic truncation
 memory_budget: int = 0            # automatic truncation (max_num_object = 0): bytes per step, 0 = device
 table_load_factor: float = 0.5    # collision table maximum load
 hash_ranges: int = 0              # 0: one pass while the children fit; k >= 2: k hash-range passes
+max_probes: int = 0               # collision-table probe limit (0: the library's default)
+max_alloc_bytes: int = 0          # largest device allocation a call may make (0: no limit)
+debug_flags: int = 0              # capi.DEBUG_*: failure injection for tests of the error paths
 
 
 class rules:
@@ -349,7 +352,8 @@ class it_t:
 def _params(max_num_object, flags=0):
     return capi.Params(float(tolerance), int(max_num_object) & U64_MAX, int(bool(simple_truncation)),
                        int(align_byte_length), float(table_load_factor), int(hash_ranges), int(flags),
-                       int(truncation_seed) & U64_MAX, int(memory_budget))
+                       int(truncation_seed) & U64_MAX, int(memory_budget), int(max_probes), int(debug_flags),
+                       int(max_alloc_bytes))
 
 
 def simulate(iteration: it_t, rule, next_iteration: it_t | None = None, symbolic_iteration: sy_it_t | None = None,

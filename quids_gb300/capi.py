@@ -19,12 +19,15 @@ STATUS = {
     -6: "bounded device wait expired", -7: "CUDA runtime error", -8: "no CUDA device",
     -9: "unsupported request", -10: "beyond the static scratch of the no-allocation entry point",
 }
+ERR_BAD_ARG, ERR_OOM, ERR_TABLE_FULL, ERR_CHILD_COUNT_OVERFLOW, ERR_SIZE_BOUND, ERR_TIMEOUT = -1, -2, -3, -4, -5, -6
+ERR_CUDA, ERR_NO_DEVICE, ERR_UNSUPPORTED, ERR_NOALLOC_LIMIT = -7, -8, -9, -10
 FLAG_NO_FAST_HASH = 1
 FLAG_STAGE_TIMING = 2
 FLAG_NO_REGIONS = 4
 FLAG_REGIONS = 8
 FLAG_NO_PLAN = 16
 FLAG_AUTOTUNE = 32
+DEBUG_STALL_LOOKBACK = 1
 
 
 class QuidsError(RuntimeError):
@@ -42,7 +45,8 @@ class Params(C.Structure):
     _fields_ = [("tolerance", C.c_double), ("max_num_object", C.c_uint64), ("simple_truncation", C.c_int32),
                 ("align_byte_length", C.c_uint32), ("table_load_factor", C.c_double),
                 ("hash_ranges", C.c_uint32), ("flags", C.c_uint32), ("seed", C.c_uint64),
-                ("memory_budget", C.c_uint64)]
+                ("memory_budget", C.c_uint64), ("max_probes", C.c_uint32), ("debug_flags", C.c_uint32),
+                ("max_alloc_bytes", C.c_uint64)]
 
 
 class Op(C.Structure):

@@ -161,6 +161,7 @@ int quids_gpu_forward(quids_gpu_ctx *ctx, quids_gpu_tape *t, quids_gpu_state *in
     for (uint64_t i = 0; i < n_ops; ++i)
         if (!ops[i].is_rule && !backward_modifier(ops[i].kind)) return QUIDS_ERR_UNSUPPORTED;
     QD_CUDA(cudaSetDevice(ctx->device));
+    const alloc_limit_scope alloc_limit(params->max_alloc_bytes);
     clear_tape(t);
     t->ops.assign(ops, ops + n_ops);
     t->prm = *params;
@@ -299,6 +300,7 @@ int quids_gpu_simulate_backward(quids_gpu_ctx *ctx, quids_gpu_tape *t, const dou
     if (!ctx || !t || t->ctx != ctx || !t->ready || !grad_angles || (!loss_adjoint && t->final->n))
         return QUIDS_ERR_BAD_ARG;
     QD_CUDA(cudaSetDevice(ctx->device));
+    const alloc_limit_scope alloc_limit(t->prm.max_alloc_bytes);  // the forward's limit
     const uint64_t n = t->final->n;
     QD_TRY(ensure(t->a0, (n ? n : 1) * sizeof(double2)));
     if (n)
@@ -311,6 +313,7 @@ int quids_gpu_simulate_backward_observable(quids_gpu_ctx *ctx, quids_gpu_tape *t
                                            double *grad_angles) {
     if (!ctx || !t || t->ctx != ctx || !t->ready || !grad_angles) return QUIDS_ERR_BAD_ARG;
     QD_CUDA(cudaSetDevice(ctx->device));
+    const alloc_limit_scope alloc_limit(t->prm.max_alloc_bytes);  // the forward's limit
     const uint64_t n = t->final->n;
     QD_TRY(ensure(t->a0, (n ? n : 1) * sizeof(double2)));
     QD_TRY(ensure(t->grads, (t->ops.size() * 3 + 3) * sizeof(double)));

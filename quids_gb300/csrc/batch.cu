@@ -289,6 +289,7 @@ int quids_gpu_simulate_batched(quids_gpu_ctx *ctx, quids_gpu_state *iteration, i
     if (!ctx || !iteration || !rules || !params) return QUIDS_ERR_BAD_ARG;
     if (iteration->n_inst == 0) return QUIDS_ERR_BAD_ARG;
     const quids_gpu_params prm = *params;
+    const alloc_limit_scope alloc_limit(prm.max_alloc_bytes);
     switch (rule_kind) {
     case QUIDS_RULE_HADAMARD:
         return simulate_batched_with(ctx, iteration, rules, next_iteration, prm, inst_stats, stats,
@@ -318,6 +319,7 @@ int quids_gpu_run_batched(quids_gpu_ctx *ctx, quids_gpu_state *a, quids_gpu_stat
     QD_CUDA(cudaSetDevice(ctx->device));
     const uint32_t G = a->n_inst;
     const quids_gpu_params prm = *params;
+    const alloc_limit_scope alloc_limit(prm.max_alloc_bytes);
     uint64_t n_rules = 0;
     for (uint64_t i = 0; i < n_ops; ++i) n_rules += ops[i].is_rule ? 1 : 0;
     std::vector<quids_gpu_step_stats> st(n_rules ? n_rules : 1);

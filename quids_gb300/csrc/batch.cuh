@@ -584,7 +584,7 @@ int simulate_batched(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule *rules_
     }
 
     // ---- collision elimination (src/quids.hpp:785-809)
-    prim::table tb{bufp<prim::table_slot>(ctx, B_KEYS), bufp<unsigned long long>(ctx, B_ACC), M, 65536u};
+    prim::table tb{bufp<prim::table_slot>(ctx, B_KEYS), bufp<unsigned long long>(ctx, B_ACC), M, probe_limit(prm)};
     QD_CUDA(cudaMemsetAsync(tb.slots, 0xff, (M + 1) * sizeof(prim::table_slot), ctx->stream));
     QD_CUDA(cudaMemsetAsync(tb.acc + 4 * M, 0, 4 * sizeof(uint64_t), ctx->stream));
     QD_CUDA(cudaMemsetAsync(ctx->buf[B_NOTREP].p, 0, NC, ctx->stream));

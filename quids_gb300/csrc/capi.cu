@@ -503,6 +503,7 @@ int quids_gpu_simulate(quids_gpu_ctx *ctx, quids_gpu_state *iteration, int rule_
                        const quids_gpu_params *params, quids_gpu_step_stats *stats) {
     if (!params) return QUIDS_ERR_BAD_ARG;
     quids_gpu_params prm = *params;
+    const alloc_limit_scope alloc_limit(prm.max_alloc_bytes);
     return dispatch_rule(rule_kind, rule, [&](auto r) {
         return ranges::simulate_step(ctx, iteration, r, next_iteration, prm, stats);
     });
@@ -528,6 +529,7 @@ int quids_gpu_run(quids_gpu_ctx *ctx, quids_gpu_state *a, quids_gpu_state *b, co
     if (a->ctx != ctx || b->ctx != ctx) return QUIDS_ERR_BAD_ARG;
     QD_CUDA(cudaSetDevice(ctx->device));
     const quids_gpu_params prm = *params;
+    const alloc_limit_scope alloc_limit(prm.max_alloc_bytes);
     uint64_t n_rules = 0;
     for (uint64_t i = 0; i < n_ops; ++i) n_rules += ops[i].is_rule ? 1 : 0;
     std::vector<quids_gpu_step_stats> st(n_rules ? n_rules : 1);

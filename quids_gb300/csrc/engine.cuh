@@ -188,11 +188,22 @@ inline std::atomic<uint64_t> g_alloc_epoch{0};
 // to grow makes ensure() fail with kAllocFrozen instead.
 inline thread_local bool g_alloc_frozen = false;
 constexpr int kAllocFrozen = -1001;
+// The largest device allocation the current call may make
+// (quids_gpu_params::max_alloc_bytes; 0: no limit), set for the duration of
+// a call by alloc_limit_scope.
+inline thread_local size_t g_alloc_limit = 0;
+struct alloc_limit_scope {
+    size_t saved;
+    explicit alloc_limit_scope(uint64_t limit) : saved(g_alloc_limit) { g_alloc_limit = (size_t)limit; }
+    ~alloc_limit_scope() { g_alloc_limit = saved; }
+};
 
 inline int ensure(qd_dbuf &b, size_t bytes, bool headroom = true) {
     if (bytes == 0) bytes = 8;
     if (b.cap >= bytes) return QUIDS_OK;
     if (g_alloc_frozen) return kAllocFrozen;
+    if (g_alloc_limit && bytes > g_alloc_limit) return QUIDS_ERR_OOM;
+    if (g_alloc_limit && bytes + bytes / 4 > g_alloc_limit) headroom = false;
     g_alloc_epoch.fetch_add(1);
     if (b.p) {
         cudaError_t e = cudaFree(b.p);
@@ -258,6 +269,9 @@ template <class T>
 inline T *bufp(quids_gpu_ctx *ctx, qd_buf_id id) {
     return (T *)ctx->buf[id].p;
 }
+
+// collision-table probe limit of a step (quids_gpu_params::max_probes)
+inline uint32_t probe_limit(const quids_gpu_params &prm) { return prm.max_probes ? prm.max_probes : 65536u; }
 
 inline unsigned grid_for(quids_gpu_ctx *ctx, uint64_t n, int per_sm = 0) {
     if (per_sm <= 0) per_sm = ctx->tune.per_sm;
@@ -421,6 +435,14 @@ template <class R>
 struct has_populate_simple<R, std::void_t<decltype(std::declval<const R &>().populate_child_simple(
                                   (const char *)0, (const char *)0, (char *)0, 0u))>> : std::true_type {};
 
+// rules that can tell when a parent's child count overflows the u32 of
+// get_num_child (child_count_overflows(pb, pe) -> bool)
+template <class R, class = void>
+struct has_count_check : std::false_type {};
+template <class R>
+struct has_count_check<R, std::void_t<decltype(std::declval<const R &>().child_count_overflows(
+                              (const char *)0, (const char *)0))>> : std::true_type {};
+
 template <class R, class = void>
 struct has_fits : std::false_type {};
 template <class R>
@@ -493,6 +515,12 @@ __global__ void __launch_bounds__(prim::kThreads)
         }
         uint32_t nc, mcs;
         rule.get_num_child(pb, pb + size[i], nc, mcs);
+        if constexpr (has_count_check<std::decay_t<decltype(rule)>>::value) {
+            if (rule.child_count_overflows(pb, pb + size[i])) {
+                nc = 0;
+                prim::set_error(err, QUIDS_ERR_CHILD_COUNT_OVERFLOW);
+            }
+        }
         nchild[i] = nc;
         mx = mx > mcs ? mx : mcs;
     }
@@ -575,11 +603,15 @@ template <class RS, int MAXC, bool FAST>
 __global__ void __launch_bounds__(prim::kThreads)
     k_symbolic(RS rs, parents_view pv, const uint64_t *tile_first, const uint64_t *d_nc, uint64_t *hash,
                double2 *cmag, uint32_t *csize, uint32_t *cpar, unsigned long long *d_maxabs, int *err,
-               region_count rc) {
+               region_count rc, const uint64_t *d_bound) {
     __shared__ uint64_t s_cb[kStagedParents + 1];
     extern __shared__ unsigned int s_rhist[];  // [rc.r]
     for (uint32_t i = threadIdx.x; i < rc.r; i += blockDim.x) s_rhist[i] = 0;
     const uint64_t nc = *d_nc;
+    // the step's child size bound: the largest max_child_size its parents
+    // declared (get_num_child), which sized the per-thread child buffer; a
+    // rule reporting a larger child breaks its contract
+    const uint64_t bound = *d_bound;
     const uint64_t ntiles = (nc + kTileChildren - 1) / kTileChildren;
     double mx = 0;
     for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
@@ -616,12 +648,13 @@ __global__ void __launch_bounds__(prim::kThreads)
             const auto &rule = rs.get(oid);
             if constexpr (FAST) {
                 h = rule.hash_child(pb, pe, cid, sz, m);
+                if (sz > bound) prim::set_error(err, QUIDS_ERR_SIZE_BOUND);
             } else {
                 uint64_t buf[MAXC / 8];
                 rule.populate_child(pb, pe, (char *)buf, cid, sz, m);
-                if (sz > MAXC) {
+                if (sz > bound || sz > MAXC) {
                     prim::set_error(err, QUIDS_ERR_SIZE_BOUND);
-                    sz = MAXC;
+                    if (sz > MAXC) sz = MAXC;
                 }
                 h = rule_hash(rule, (const char *)buf, (const char *)buf + sz);
             }
@@ -1356,18 +1389,19 @@ inline int launch_symbolic(quids_gpu_ctx *ctx, const RS &rule, const parents_vie
     uint64_t *d_nc = ctx->d_words + W_NC;
     unsigned long long *d_maxabs = (unsigned long long *)(ctx->d_words + W_MAXABS);
     int *err = (int *)(ctx->d_words + W_STATUS);
+    const uint64_t *d_bound = ctx->d_words + W_MAXSIZE;
     const size_t smem = rc.r * sizeof(unsigned int);
     if constexpr (has_hash_child<Rule>::value) {
         if (fast) {
             k_symbolic<RS, 8, true><<<grid, prim::kThreads, smem, ctx->stream>>>(
                 rule, pv, bufp<uint64_t>(ctx, B_TILEPAR), d_nc, bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG),
-                bufp<uint32_t>(ctx, B_CSIZE), bufp<uint32_t>(ctx, B_CPAR), d_maxabs, err, rc);
+                bufp<uint32_t>(ctx, B_CSIZE), bufp<uint32_t>(ctx, B_CPAR), d_maxabs, err, rc, d_bound);
             return launched(ctx);
         }
     }
     k_symbolic<RS, MAXC, false><<<grid, prim::kThreads, smem, ctx->stream>>>(
         rule, pv, bufp<uint64_t>(ctx, B_TILEPAR), d_nc, bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG),
-        bufp<uint32_t>(ctx, B_CSIZE), bufp<uint32_t>(ctx, B_CPAR), d_maxabs, err, rc);
+        bufp<uint32_t>(ctx, B_CSIZE), bufp<uint32_t>(ctx, B_CPAR), d_maxabs, err, rc, d_bound);
     return launched(ctx);
 }
 
@@ -1573,6 +1607,7 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, qu
     {
         prim::lookback lb;
         lookback_view(ctx, N, 1, lb);
+        if (prm.debug_flags & QUIDS_DEBUG_STALL_LOOKBACK) lb.stall_tile = 1;
         scan_nchild f{bufp<uint32_t>(ctx, B_NCHILD), pidx};
         prim::k_scan_excl<<<lookback_grid(ctx, NP), prim::kThreads, 0, ctx->stream>>>(
             f, ctx->d_words + W_NP, bufp<uint64_t>(ctx, B_CBEGIN), ctx->d_words + W_NC, lb,
@@ -1742,7 +1777,7 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, qu
 
     // ---- stage 2: collision table (src/quids.hpp:726-809)
     begin_stage(2);
-    prim::table tb{bufp<prim::table_slot>(ctx, B_KEYS), bufp<unsigned long long>(ctx, B_ACC), M, 65536u};
+    prim::table tb{bufp<prim::table_slot>(ctx, B_KEYS), bufp<unsigned long long>(ctx, B_ACC), M, probe_limit(prm)};
     {  // table slots free, the extra slot's sum, the group marks, the look-back chains of stages 3-4
         fill_set f{};
         f.p[0] = (unsigned char *)tb.slots, f.n[0] = (M + 1) * sizeof(prim::table_slot), f.v[0] = 0xff;

@@ -361,7 +361,7 @@ int simulate_planned(quids_gpu_ctx *ctx, quids_gpu_state *in, const uint64_t *in
 
     // ---- stage 2: collision table, sized on the device
     const uint64_t tiles_nc = (NC + prim::kTile - 1) / prim::kTile;
-    prim::table tb{bufp<prim::table_slot>(ctx, B_KEYS), bufp<unsigned long long>(ctx, B_ACC), Mb, 65536u,
+    prim::table tb{bufp<prim::table_slot>(ctx, B_KEYS), bufp<unsigned long long>(ctx, B_ACC), Mb, probe_limit(prm),
                    words + W_M};
     {
         fill_set f{};

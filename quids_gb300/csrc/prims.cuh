@@ -73,6 +73,9 @@ struct lookback {
     uint64_t *status;   // one word per tile, zeroed before the launch
     uint32_t *counter;  // tile ticket, zeroed before the launch
     int *err;
+    // failure injection (QUIDS_DEBUG_STALL_LOOKBACK): this tile never
+    // publishes, so the next tile's bounded wait runs out (~0: none)
+    uint32_t stall_tile = 0xffffffffu;
 };
 
 // Warp-level decoupled look-back of tile `tile` (> 0): publishes its
@@ -86,6 +89,7 @@ struct lookback {
 constexpr int kLookWindow = 1;
 static __device__ uint64_t warp_lookback(const lookback &lb, uint32_t tile, uint64_t aggregate) {
     const int lane = threadIdx.x & 31;
+    if (tile == lb.stall_tile) return 0;  // injected failure: publishes nothing
     if (lane == 0) st_volatile_u64(&lb.status[tile], kFlagAgg | (aggregate & kValMask));
     int64_t base = (int64_t)tile - 1;
     uint64_t prefix = 0;

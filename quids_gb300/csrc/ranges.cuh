@@ -632,7 +632,7 @@ int simulate_ranges(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, 
         }
         const uint64_t Mk = std::max<uint64_t>((uint64_t)((double)nk / load) + 1, 1024);
         Mmax = std::max(Mmax, Mk);
-        const prim::table tb{bufp<prim::table_slot>(ctx, B_KEYS), bufp<unsigned long long>(ctx, B_ACC), Mk, 65536u};
+        const prim::table tb{bufp<prim::table_slot>(ctx, B_KEYS), bufp<unsigned long long>(ctx, B_ACC), Mk, probe_limit(prm)};
         const uint64_t words = (nk + prim::kTile - 1) / prim::kTile + 2;
         clk.begin(2);
         {
@@ -824,7 +824,11 @@ int simulate_step(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule, qui
                   const quids_gpu_params &prm, quids_gpu_step_stats *stats, const Post &post = Post{}) {
     const int rc = simulate_rule(ctx, in, rule, out, prm, stats, post);
     if (rc != kNeedRanges) return rc;
-    return simulate_ranges(ctx, in, rule, out, prm, stats, post);
+    // the range passes recompute the children with the rule's hash_child
+    if constexpr (has_hash_child<Rule>::value)
+        return simulate_ranges(ctx, in, rule, out, prm, stats, post);
+    else
+        return QUIDS_ERR_UNSUPPORTED;
 }
 
 }  // namespace qd::ranges

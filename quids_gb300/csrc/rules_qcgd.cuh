@@ -256,6 +256,16 @@ struct flip_rule {
             if (site(L(pb, i), R(pb, n, i))) nc *= 2;
         num_child = nc;
     }
+    // 2^sites does not fit the u32 child count (32 sites or more): the
+    // reference's uint wraps to 0 and loses the parent's children
+    // (src/rules/qcgd.hpp:480-485, :555-560); this library reports
+    // QUIDS_ERR_CHILD_COUNT_OVERFLOW instead
+    QD_HD bool child_count_overflows(const char *pb, const char *) const {
+        const int n = num_nodes(pb);
+        int sites = 0;
+        for (int i = 0; i < n; ++i) sites += site(L(pb, i), R(pb, n, i)) ? 1 : 0;
+        return sites >= 32;
+    }
     template <class M>
     QD_HD void apply(const char *pb, int n, uint32_t cid, M *mag, char *cb, uint64_t *lh, uint64_t *rh) const {
         for (int i = 0; i < n; ++i) {
@@ -428,6 +438,20 @@ struct split_merge {
             if (s || m) nc *= 2;
         }
         num_child = nc;
+    }
+    // the child count 2^(sites + wrap site) does not fit u32 (the reference's
+    // uint wraps, src/rules/qcgd.hpp:623-642)
+    QD_HD bool child_count_overflows(const char *pb, const char *) const {
+        const int n = num_nodes(pb);
+        bool fs, lm;
+        wrap_sites(pb, n, fs, lm);
+        int bits = (fs || lm) ? 1 : 0;
+        for (int i = fs; i < n - lm; ++i) {
+            bool s, m;
+            get_operations(pb, n, i, s, m);
+            bits += (s || m) ? 1 : 0;
+        }
+        return bits >= 32;
     }
 
     // first pass (:647-700): wrap decisions, child node count, magnitude

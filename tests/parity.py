@@ -118,9 +118,10 @@ def assert_fixed_state_parity(got, exp, truncated=False, what=""):
 def assert_hashed_state_parity(ctx, got_it, exp_packed, hash_rule, qcgd=True, truncated=False, what="",
                                sample=2000):
     """Large-state parity through hashes: both states are hashed on the GPU
-    with the rule's hasher (pinned to the reference's by the golden vectors),
-    compared as (hash -> magnitude) maps with the tie band, and a random
-    sample of objects is compared byte for byte."""
+    with the rule's hasher (pinned to the reference's by the golden vectors)
+    and compared as (hash -> magnitude) maps with the tie band; then, paired
+    by hash, every object's bytes are compared on the host (QCGD padding
+    masked), and a random sample once more object by object."""
     import quids_gb300 as quids
     exp_it = quids.it_t(ctx, exp_packed)
     gh = quids.state_hash(got_it, hash_rule)
@@ -145,6 +146,9 @@ def assert_hashed_state_parity(ctx, got_it, exp_packed, hash_rule, qcgd=True, tr
     tol = REL * np.maximum(np.maximum(np.abs(gm), np.abs(em)), FLOOR)
     bad = np.abs(gm - em) > tol
     assert not bad.any(), f"{what}: {int(bad.sum())} magnitudes differ"
+    # every object's bytes (padding masked), in hash order on both sides
+    assert_all_bytes_equal(got, exp_packed, gsel, esel, qcgd, what)
+    # and a random sample object by object, through the scalar mask
     rng = np.random.default_rng(0)
     pick = rng.choice(len(gsel), size=min(sample, len(gsel)), replace=False) if len(gsel) else []
     gobj, gbeg, gsz = got[0], got[1], got[2]
@@ -159,3 +163,44 @@ def assert_hashed_state_parity(ctx, got_it, exp_packed, hash_rule, qcgd=True, tr
             assert (np.frombuffer(x, np.uint8)[mk] == np.frombuffer(y, np.uint8)[mk]).all(), f"{what}: bytes differ"
         else:
             assert x == y, f"{what}: bytes differ"
+
+
+def assert_all_bytes_equal(got, exp, gsel, esel, qcgd: bool, what: str = "", chunk_bytes: int = 1 << 27):
+    """Object gsel[k] of `got` has the bytes of object esel[k] of `exp`, for
+    every k: sizes equal, and every byte equal except, for QCGD graphs, the 4
+    padding bytes of each 16-byte name sub-node (never initialised by the
+    reference, src/rules/qcgd.hpp:35-61; the layout is that of
+    graph_padding_mask).  Vectorised on the host in chunks of about
+    chunk_bytes bytes, so states of 2^24 objects compare in full."""
+    gobj, eobj = np.asarray(got[0]), np.asarray(exp[0])
+    gbeg, ebeg = np.asarray(got[1], np.int64), np.asarray(exp[1], np.int64)
+    gsel, esel = np.asarray(gsel, np.int64), np.asarray(esel, np.int64)
+    gsz = np.asarray(got[2], np.int64)[gsel]
+    esz = np.asarray(exp[2], np.int64)[esel]
+    assert len(gsel) == len(esel), f"{what}: {len(gsel)} objects paired with {len(esel)}"
+    bad = np.nonzero(gsz != esz)[0]
+    assert not len(bad), f"{what}: {len(bad)} object sizes differ"
+    ends = np.cumsum(gsz)
+    lo = 0
+    while lo < len(gsel):
+        start_bytes = int(ends[lo - 1]) if lo else 0
+        hi = int(np.searchsorted(ends, start_bytes + chunk_bytes, side="right"))
+        hi = max(hi, lo + 1)
+        sz = gsz[lo:hi]
+        tot = int(sz.sum())
+        rel = np.arange(tot, dtype=np.int64) - np.repeat(np.cumsum(sz) - sz, sz)
+        gb = gobj[np.repeat(gbeg[gsel[lo:hi]], sz) + rel]
+        eb = eobj[np.repeat(ebeg[esel[lo:hi]], sz) + rel]
+        diff = gb != eb
+        if qcgd:
+            e0 = ebeg[esel[lo:hi]]
+            n = eobj[e0].astype(np.int64) | (eobj[e0 + 1].astype(np.int64) << 8)
+            q = rel - np.repeat(4 + 4 * n, sz)
+            r = q & 15
+            pad = (q >= 0) & (r >= 4) & (r < 8) & (q - r + 8 <= np.repeat(sz, sz) - np.repeat(4 + 4 * n, sz))
+            diff &= ~pad
+        if diff.any():
+            first = int(np.searchsorted(np.cumsum(sz), int(np.argmax(diff)), side="right")) + lo
+            raise AssertionError(f"{what}: bytes differ (first at paired object {first}, "
+                                 f"{int(diff.sum())} bytes in this chunk)")
+        lo = hi

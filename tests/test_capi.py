@@ -79,3 +79,18 @@ def test_null_handles_are_bad_arg_not_a_crash(lib_path):
         f = getattr(raw, name)
         f.restype = C.c_int
         assert f(*([None] * 20)) == -1, name
+
+
+def test_params_struct_layout_matches_the_header(tmp_path):
+    """ctypes' mirror of quids_gpu_params and quids_gpu_step_stats has the C
+    layout (size and the offsets of the last fields)."""
+    src = tmp_path / "layout.c"
+    src.write_text('#include <stddef.h>\n#include <stdio.h>\n#include "quids_gpu.h"\nint main(void) {\n'
+                   '  printf("%zu %zu %zu %zu %zu\\n", sizeof(quids_gpu_params), offsetof(quids_gpu_params, max_probes),'
+                   ' offsetof(quids_gpu_params, max_alloc_bytes), sizeof(quids_gpu_step_stats),'
+                   ' offsetof(quids_gpu_step_stats, hash_ranges));\n  return 0;\n}\n')
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    assert got == [C.sizeof(capi.Params), capi.Params.max_probes.offset, capi.Params.max_alloc_bytes.offset,
+                   C.sizeof(capi.StepStats), capi.StepStats.hash_ranges.offset]

@@ -363,7 +363,7 @@ def test_probabilistic_truncation(ctx):
         quids.truncation_seed = 0
 
 
-def test_automatic_truncation(ctx):
+def test_automatic_truncation(ctx, port):
     """max_num_object = 0: as many top-norm parents as the memory budget
     allows (src/quids.hpp:459-485), then as many survivors as fit."""
     rng = W.Rng(17)
@@ -385,11 +385,30 @@ def test_automatic_truncation(ctx):
     kept = sy.stats["num_parents_kept"]
     assert 1900 <= kept <= 2000 and sy.num_object == 2 * kept
     assert sy.num_object * per_child <= budget
-    assert b.num_object <= sy.num_object_after_interferences and abs(b.total_proba - 1) < 1e-12 or b.total_proba < 1
-    # the kept parents are the ones of largest norm
-    norms = np.sort(np.abs(mags) ** 2)[::-1]
-    _, bm = W.unpack(b.download())
-    assert b.download()[0].size > 0
+    assert 0 < b.num_object <= sy.num_object_after_interferences
+    # The kept parents are the `kept` of largest norm (ties: lower index;
+    # the random norms here have none), in their input order
+    # (src/quids.hpp:613-642): the oracle's step on exactly those parents
+    # has the GPU's child and group counts ...
+    norms = np.abs(mags) ** 2
+    top = np.sort(np.argsort(-norms, kind="stable")[:kept])
+    sub = W.pack([objs[i] for i in top], mags[top], 8)
+    port.set_globals(1e-18, True, 8)
+    a, c = port.new_state(sub), port.new_state()
+    nc, nu = port.simulate(a, 1, (5,), c, U64_MAX)
+    assert (sy.num_object, sy.num_object_after_interferences) == (nc, nu)
+    # ... and the survivors, cut to what the budget left for them
+    # (src/quids.hpp:510-536), are the oracle's groups of largest norm,
+    # renormalised (a tie band at the cutoff)
+    e_objs, e_mags = W.unpack(c.store())
+    assert b.num_object < len(e_objs), "the survivor budget binds in this case"
+    pick = np.sort(np.argsort(-np.abs(e_mags) ** 2, kind="stable")[:b.num_object])
+    kept_mags = e_mags[pick]
+    exp = W.pack([e_objs[i] for i in pick], kept_mags / np.linalg.norm(kept_mags), 8)
+    assert_state_parity(b.download(), exp, False, truncated=True, what="memory-driven truncation")
+    # total_proba is the survivors' norm before normalising; the oracle's
+    # magnitudes are normalised over all its groups
+    assert b.total_proba == pytest.approx(float(np.sum(np.abs(kept_mags) ** 2)) * c.total_proba, rel=1e-12)
 
 
 def test_observables(ctx):
