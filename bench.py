@@ -1,16 +1,22 @@
 """Benchmark of the QuIDS rule step on GB300: child objects/s per simulate() step.
 
-Workload (default "circuit24"): the plain quantum_computer rule at scale --
-24 qubits at one byte each, all |0>, 6 seeded layers (Hadamard rule on a
-random half of the qubits, then 24 random CNOT/Z modifiers), max_num_object
-2^22, simple truncation, tolerance 1e-18, align 8.  One bench step is the
-whole circuit from |0...0> (72 rule applications, 144 modifiers); the metric
-is the sum of symbolic children over the step's rule applications divided by
-the step time.
+Workload (default "qcgd12"): the 2^24-object QCGD step -- one step of the
+QCGD rule sequence (step, coin(pi/4), split_merge(pi/4, 0, -pi/2),
+erase_create(pi/3, pi/5, 0)) on a 12-node cycle graph (Bernoulli(0.5) bits,
+seed 1), from the 149,760-object state after the first step, max_num_object
+2^24, simple truncation, tolerance 1e-18, align 8: 7.3e8 children, 2^24
+survivors.  The metric is the sum of symbolic children over the step's rule
+applications divided by the step time.  The line also carries the batched
+form against the plain path run instance by instance ("batched_vs_plain",
+the batch256 workload) and the adjoint's forward + backward against the
+plain forward ("adjoint_vs_forward", the adjoint10 workload), measured after
+the main line on the same GPU (--no-extras leaves them out).
 
-"qcgd12": one step of the QCGD rule sequence (step, coin, split_merge,
-erase_create) on a 12-node cycle graph, starting from the state after the
-first step (the reference needs ~60 s on 8 cores for it).
+"circuit24": the plain quantum_computer rule at scale -- 24 qubits at one
+byte each, all |0>, 6 seeded layers (Hadamard rule on a random half of the
+qubits, then 24 random CNOT/Z modifiers), max_num_object 2^22.  One bench
+step is the whole circuit from |0...0> (72 rule applications, 144
+modifiers).
 
 "batch256": the batched form -- 256 independent QCGD instances (cycle
 graphs of U[4,16] nodes, Bernoulli(0.5) bits, per-instance split_merge and
@@ -64,12 +70,11 @@ METRIC = "child objects/s per simulate() step"
 UNIT = "children/s"
 MAX24 = 1 << 22
 L2_BYTES = 129 * 1024 * 1024
-# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of k_fill,
-# k_table_claim and k_table_accumulate over one timed circuit24 step (the
-# graph replay of 72 rule applications), from one ncu capture of this
-# script; ncu cannot run inside this process, so the capture's total is kept
-# here
-TABLE_TRAFFIC_CIRCUIT24_STEP = 4381.8e6 + 2677.5e6
+# DRAM traffic of the dominant stage is not measured in this process (ncu
+# cannot run inside it): a recorded ncu figure per workload, with the
+# profile it comes from.  dram__bytes_read.sum + dram__bytes_write.sum over
+# the stage's kernels, per rule application of the timed step.
+RECORDED_TRAFFIC = {}
 
 
 # ------------------------------------------------------------------ workloads
@@ -84,8 +89,11 @@ def workload(name):
                                        "tolerance": 1e-18, "align_byte_length": 8}}
     if name in ("qcgd12", "qcgd10"):
         nodes, seed, cap = (12, 1, 1 << 24) if name == "qcgd12" else (10, 3, 1 << 22)
+        # the reference arm's bounded sample: the first quarter of the
+        # 149,760 objects of the input (about 3 s per step on 16 cores)
+        ref_sample = 37440 if name == "qcgd12" else None
         return {"name": name, "init": None, "nodes": nodes, "seed": seed, "gates": W.qcgd_step_rules(), "max": cap,
-                "tolerance": 1e-18, "align": 8,
+                "tolerance": 1e-18, "align": 8, "ref_sample_objects": ref_sample,
                 "config": {"workload": f"QCGD step 1 (step, coin(pi/4), split_merge(pi/4,0,-pi/2), "
                                        f"erase_create(pi/3,pi/5,0)) of a {nodes}-node cycle graph, from the "
                                        f"state after step 0, max_num_object 2^{cap.bit_length() - 1}",
@@ -368,9 +376,8 @@ def ours(args, rank, world):
     # per launch of the dominant stage (one per rule application)
     n_apps = max(1, len(stats) // args.steps)
     alg_per_launch = stage_b[dom] / args.steps / n_apps
-    traffic = None
-    if wl["name"] == "circuit24" and names[dom] == "collision_table":
-        traffic = TABLE_TRAFFIC_CIRCUIT24_STEP / n_apps
+    rec = RECORDED_TRAFFIC.get((wl["name"], names[dom]))
+    traffic = rec["bytes_per_launch"] if rec else None
 
     # e2e through the public API with host buffers (pinned), copies inside the timed region
     e2e = None
@@ -403,6 +410,11 @@ def ours(args, rank, world):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(wl, cpu_sample(wl, init_packed), samples=1, warm=wl["name"] == "circuit24")
+        # the same work?  Both start from the same input; a truncation with
+        # exact ties can send the two along different states afterwards
+        cpu["gpu_children_per_step"] = children // args.steps
+        cpu["same_trajectory"] = (cpu["children_per_step"] == children // args.steps
+                                  and not wl.get("cpu_sample_objects"))
 
     if rank == 0:
         line = {
@@ -418,16 +430,52 @@ def ours(args, rank, world):
             "gpu_launches": int(launches),
             "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                         "achieved_source": "stage-timing pass: the timed steps run again synchronously with "
+                                            "CUDA events around each stage on the library's stream; "
+                                            "algorithmic bytes of the stage / its event time",
                          "traffic": traffic, "algorithmic_bytes_per_launch": alg_per_launch,
-                         "traffic_source": "ncu capture of k_fill + k_table_claim + k_table_accumulate over one circuit24 step"
-                         if traffic else None,
+                         "traffic_source": (f"recorded, not measured in this run: {rec['source']}" if rec
+                                            else "not measured in this run"),
                          "stage_ms_per_step": [t / args.steps for t in stage_t],
-                         "step_algorithmic_GBps": step_bytes / (total_ms / 1e3) / 1e9},
+                         "stage_share_of_timed_step": [t / args.steps / (total_ms / args.steps) for t in stage_t],
+                         "step_algorithmic_GBps": step_bytes / (total_ms / 1e3) / 1e9,
+                         "step_frac": step_bytes / (total_ms / 1e3) / 1e9 / peak},
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
             "wall_s_timed": t_wall,
         }
+    ctx.close()
+    del flush
+    if rank == 0 and world == 1 and args.extras:
+        line.update(extra_ratios(args, rank, world))
+    if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def extra_ratios(args, rank, world):
+    """The benchmark spec's two ratios on the same GPU, beside the default line:
+    the batched form against the plain path instance by instance (batch256),
+    and the adjoint's forward + backward against the plain forward
+    (adjoint10).  Fewer steps than the main line (each is a full workload)."""
+    import torch
+    out = {}
+    torch.cuda.empty_cache()
+    b = ours_batched(argparse.Namespace(**dict(vars(args), config="batch256", steps=min(args.steps, 5),
+                                               warmup=max(3, min(args.warmup, 3)))), rank, world, emit=False)
+    pl = b["plain_instance_by_instance"]
+    out["batched_vs_plain"] = {
+        "workload": b["config"]["workload"], "unit": UNIT, "batched": b["value"], "batched_ms_per_step": b["ms_per_step"],
+        "plain_instance_by_instance": pl["value"], "plain_ms_per_step": pl["ms_per_step"],
+        "ratio": b["value"] / pl["value"], "steps": b["steps"], "clocks": b["clocks"]}
+    torch.cuda.empty_cache()
+    a = ours_adjoint(argparse.Namespace(**dict(vars(args), config="adjoint10", steps=1, warmup=1)), rank, world,
+                     emit=False)
+    out["adjoint_vs_forward"] = {
+        "workload": a["config"]["workload"], "forward_plus_backward_ms": a["ms_per_step"],
+        "plain_forward_ms": a["adjoint"]["plain_forward_ms"],
+        "ratio": a["adjoint"]["forward_plus_backward_over_forward"], "loss": a["adjoint"]["loss"],
+        "grad": a["adjoint"]["grad"], "steps": a["steps"], "clocks": a["clocks"]}
+    return out
 
 
 def batch_ops(quids, wl):
@@ -444,8 +492,10 @@ def instance_ops(quids, sm, ec):
             quids.rule_from(True, W.RULE_QCGD_SPLIT_MERGE, sm), quids.rule_from(True, W.RULE_QCGD_ERASE_CREATE, ec)]
 
 
-def ours_batched(args, rank, world):
-    """The batched form: one QCGD step of 256 instances per bench step."""
+def ours_batched(args, rank, world, emit=True):
+    """The batched form: one QCGD step of 256 instances per bench step.
+    emit=False: no end-to-end or CPU legs, the line is returned, not printed
+    (the batched-vs-plain ratio of the default line)."""
     import torch
     import quids_gb300 as quids
     from quids_gb300 import capi, workloads as W
@@ -530,7 +580,7 @@ def ours_batched(args, rank, world):
     # probability out (the full final state is 7.9 GB), copies inside the
     # timed region
     e2e = None
-    if rank == 0 or world > 1:
+    if emit and (rank == 0 or world > 1):
         ctx.synchronize()
         t0 = time.perf_counter()
         e2e_children, h2d, d2h = 0, 0, 0
@@ -549,8 +599,9 @@ def ours_batched(args, rank, world):
     peak, peak_kind = peaks()
     achieved = abytes / (total_ms / 1e3) / 1e9
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    if emit and rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline_batched(wl, packed)
+    ctx.close()
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -573,11 +624,15 @@ def ours_batched(args, rank, world):
             "clocks": clk.summary(),
             "wall_s_timed": t_wall,
         }
-        print(json.dumps(line), flush=True)
+        if emit:
+            print(json.dumps(line), flush=True)
+        return line
 
 
-def ours_adjoint(args, rank, world):
-    """The adjoint: taped forward + simulate_backward per bench step."""
+def ours_adjoint(args, rank, world, emit=True):
+    """The adjoint: taped forward + simulate_backward per bench step.
+    emit=False: no end-to-end leg, the line is returned, not printed (the
+    adjoint-vs-forward ratio of the default line)."""
     import torch
     import quids_gb300 as quids
     from quids_gb300 import workloads as W
@@ -643,15 +698,17 @@ def ours_adjoint(args, rank, world):
     h_in = tuple(pin(a) for a in (objects, begin, size, mag))
     t0 = time.perf_counter()
     e2e_children = 0
-    for _ in range(args.steps):
+    for _ in range(args.steps if emit else 0):
         final, st = tape.forward(quids.it_t(ctx, h_in), ops, wl["max"], wl["every"])
         tape.backward_observable(quids.OBS_QCGD_NUM_NODES)
         e2e_children += sum(x["num_object"] for x in st)
     t_e2e = time.perf_counter() - t0
     peak, peak_kind = peaks()
     achieved = abytes / (total_ms / 1e3) / 1e9
+    del tape
+    ctx.close()
     if rank == 0:
-        print(json.dumps({
+        line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -663,7 +720,7 @@ def ours_adjoint(args, rank, world):
                         "forward_plus_backward_over_forward": (total_ms / args.steps) / fwd_ms},
             "e2e": {"value": e2e_children / t_e2e, "unit": UNIT,
                     "h2d_bytes_per_step": int(sum(a.nbytes for a in h_in)), "d2h_bytes_per_step": 6 * 8 + 8,
-                    "ms_per_step": 1e3 * t_e2e / args.steps},
+                    "ms_per_step": 1e3 * t_e2e / args.steps} if emit else None,
             "gpu_launches": int(launches),
             "roofline": {"bound": "hbm", "kernel": "whole forward (all kernels; backward not counted)",
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
@@ -671,7 +728,10 @@ def ours_adjoint(args, rank, world):
             "cpu_baseline": None,
             "clocks": clk.summary(),
             "wall_s_timed": t_wall,
-        }), flush=True)
+        }
+        if emit:
+            print(json.dumps(line), flush=True)
+        return line
 
 
 def cpu_oracle():
@@ -734,8 +794,9 @@ def cpu_baseline(wl, init_packed, samples=1, warm=True):
     ch = sum(one() for _ in range(samples))
     dt = time.perf_counter() - t0
     part = (f"the first {wl['cpu_sample_objects']} objects of " if wl.get("cpu_sample_objects") else "")
-    return {"value": ch / dt, "unit": UNIT, "cores": cores, "kind": kind,
-            "sample": f"{samples} step(s) of {part}the {wl['name']} workload ({ch} children, {dt:.2f} s)"}
+    return {"value": ch / dt, "unit": UNIT, "cores": cores, "kind": kind, "children_per_step": ch // samples,
+            "sample": f"{samples} step(s) of {part}the {wl['name']} workload from the GPU arm's input "
+                      f"({ch} children, {dt:.2f} s)"}
 
 
 def reference(args, rank, world):
@@ -766,6 +827,8 @@ def reference(args, rank, world):
         from quids_gb300 import workloads as W
         wl["gates"] = W.qcgd_adjoint_ops(wl["angles"], 2)[0]
         wl["config"] = dict(wl["config"], sample="reference forward only, first 2 of the 20 steps")
+    if wl.get("ref_sample_objects"):  # a bounded sample of each step (children/s is per child)
+        wl["cpu_sample_objects"] = wl["ref_sample_objects"]
     init_packed = wl["init"] if wl["init"] is not None else qcgd_initial_cpu(wl, o)
 
     def one():
@@ -806,10 +869,14 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="circuit24", choices=["circuit24", "qcgd12", "qcgd10", "qcgd12s2", "batch256",
-                                                                 "adjoint10"])
+    ap.add_argument("--config", default="qcgd12", choices=["circuit24", "qcgd12", "qcgd10", "qcgd12s2", "batch256",
+                                                              "adjoint10"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", dest="extras", action="store_false",
+                    help="qcgd12 line without the batched-vs-plain and adjoint-vs-forward ratios")
     args = ap.parse_args()
+    if args.config != "qcgd12":
+        args.extras = False
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if world > 1 and args.impl == "ours":
