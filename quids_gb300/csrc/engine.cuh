@@ -273,6 +273,31 @@ inline T *bufp(quids_gpu_ctx *ctx, qd_buf_id id) {
 // collision-table probe limit of a step (quids_gpu_params::max_probes)
 inline uint32_t probe_limit(const quids_gpu_params &prm) { return prm.max_probes ? prm.max_probes : 65536u; }
 
+// Blocks of `kernel` (at `threads` per block, `smem` dynamic shared bytes)
+// one SM holds at once: a grid of that many per SM is one full wave.
+// Queried once per kernel (and shared-memory size) and device.
+template <class K>
+inline int resident_per_sm(K kernel, int threads, size_t smem = 0) {
+    static thread_local const void *cached_fn = nullptr;  // kernels of one signature share K
+    static thread_local int cached_dev = -1;
+    static thread_local size_t cached_smem = 0;
+    static thread_local int cached = 0;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if ((const void *)kernel != cached_fn || dev != cached_dev || smem != cached_smem || cached <= 0) {
+        cached_fn = (const void *)kernel;
+        int n = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, smem) != cudaSuccess || n <= 0) {
+            cudaGetLastError();
+            n = 8;
+        }
+        cached_dev = dev;
+        cached_smem = smem;
+        cached = n;
+    }
+    return cached;
+}
+
 inline unsigned grid_for(quids_gpu_ctx *ctx, uint64_t n, int per_sm = 0) {
     if (per_sm <= 0) per_sm = ctx->tune.per_sm;
     uint64_t g = (n + prim::kThreads - 1) / prim::kThreads;
@@ -1385,20 +1410,26 @@ inline int launch_symbolic(quids_gpu_ctx *ctx, const RS &rule, const parents_vie
                            region_count rc) {
     using Rule = typename RS::rule_type;
     uint64_t tiles = (nc + kTileChildren - 1) / kTileChildren;
-    unsigned grid = (unsigned)(tiles < (uint64_t)ctx->num_sms * 8 ? tiles : (uint64_t)ctx->num_sms * 8);
     uint64_t *d_nc = ctx->d_words + W_NC;
     unsigned long long *d_maxabs = (unsigned long long *)(ctx->d_words + W_MAXABS);
     int *err = (int *)(ctx->d_words + W_STATUS);
     const uint64_t *d_bound = ctx->d_words + W_MAXSIZE;
     const size_t smem = rc.r * sizeof(unsigned int);
+    // one full wave of resident blocks (each strides over tiles)
+    auto wave = [&](auto kernel) {
+        const uint64_t w = (uint64_t)ctx->num_sms * resident_per_sm(kernel, prim::kThreads, smem);
+        return (unsigned)(tiles < w ? (tiles ? tiles : 1) : w);
+    };
     if constexpr (has_hash_child<Rule>::value) {
         if (fast) {
+            const unsigned grid = wave(k_symbolic<RS, 8, true>);
             k_symbolic<RS, 8, true><<<grid, prim::kThreads, smem, ctx->stream>>>(
                 rule, pv, bufp<uint64_t>(ctx, B_TILEPAR), d_nc, bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG),
                 bufp<uint32_t>(ctx, B_CSIZE), bufp<uint32_t>(ctx, B_CPAR), d_maxabs, err, rc, d_bound);
             return launched(ctx);
         }
     }
+    const unsigned grid = wave(k_symbolic<RS, MAXC, false>);
     k_symbolic<RS, MAXC, false><<<grid, prim::kThreads, smem, ctx->stream>>>(
         rule, pv, bufp<uint64_t>(ctx, B_TILEPAR), d_nc, bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG),
         bufp<uint32_t>(ctx, B_CSIZE), bufp<uint32_t>(ctx, B_CPAR), d_maxabs, err, rc, d_bound);
@@ -1488,7 +1519,8 @@ inline int launch_symbolic_grouped(quids_gpu_ctx *ctx, const RS &rs, const paren
         f, ctx->d_words + W_NP, bufp<uint64_t>(ctx, B_LBEG), ctx->d_words + W_TMP, lb,
         leader_tile_epilogue{bufp<uint64_t>(ctx, B_TILEPAR), ltiles_cap});
     const uint64_t est_tiles = (nc >> kGroupBits) / kLeaderTile + 1;
-    const unsigned g = (unsigned)std::min<uint64_t>(est_tiles, (uint64_t)ctx->num_sms * 8);
+    const unsigned g = (unsigned)std::min<uint64_t>(
+        est_tiles, (uint64_t)ctx->num_sms * resident_per_sm(k_symbolic_grouped<RS, child_records>, prim::kThreads));
     const child_records rec{bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG), bufp<uint32_t>(ctx, B_CSIZE),
                             bufp<uint32_t>(ctx, B_CPAR)};
     k_symbolic_grouped<RS, child_records><<<g, prim::kThreads, 0, ctx->stream>>>(
@@ -1758,7 +1790,7 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, qu
     // ---- stage 1: symbolic iteration (src/quids.hpp:647-721)
     begin_stage(1);
     bool grouped = false;
-    if constexpr (has_grouped<Rule>::value) grouped = fast && !regions;
+    if constexpr (has_grouped<Rule>::value) grouped = fast;
     if constexpr (has_grouped<Rule>::value) if (grouped) QD_TRY(launch_symbolic_grouped(ctx, rule, pv, NC));
     if (!grouped) {
         if (sym_tiles + 1 > tile_map_cap || bufp<uint64_t>(ctx, B_TILEPAR) != tile_map) {
@@ -1766,6 +1798,8 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, qu
                 bufp<uint64_t>(ctx, B_CBEGIN), NP, sym_tiles, bufp<uint64_t>(ctx, B_TILEPAR));
             QD_TRY(launched(ctx));
         }
+        // the region histogram comes with the symbolic records (the grouped
+        // pass leaves it to k_region_hist)
         region_count rc{M, regions ? R : 0u, regions ? bufp<unsigned int>(ctx, B_RHIST) : nullptr};
         if (maxsize <= 256) {
             QD_TRY((launch_symbolic<single_rule<Rule>, 256>(ctx, rule, pv, NC, fast, rc)));
@@ -1798,6 +1832,11 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, qu
             tb, src, bufp<uint32_t>(ctx, B_SLOT), ctx->d_words + W_NC, d_maxabs, not_rep, has_join);
         QD_TRY(launched(ctx, 2));
     } else {
+        if (grouped) {
+            prim::k_region_hist<<<grid_for(ctx, NC), prim::kThreads, R * sizeof(unsigned int), ctx->stream>>>(
+                bufp<uint64_t>(ctx, B_HASH), ctx->d_words + W_NC, M, R, bufp<unsigned int>(ctx, B_RHIST));
+            QD_TRY(launched(ctx));
+        }
         prim::k_region_offsets<<<1, 1024, 0, ctx->stream>>>(bufp<unsigned int>(ctx, B_RHIST), R,
                                                            bufp<uint64_t>(ctx, B_ROFF),
                                                            bufp<unsigned long long>(ctx, B_RCUR));

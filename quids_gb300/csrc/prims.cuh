@@ -596,6 +596,21 @@ __device__ __forceinline__ uint32_t table_region(uint64_t h, uint64_t m, uint32_
 constexpr uint32_t kMaxRegions = 2048;
 __host__ __device__ constexpr size_t region_scatter_smem(uint32_t r) { return 4 * ((r + 1) & ~1u) + 8 * (size_t)r; }
 
+// hist[r] += children of table region r (shared-memory counts per block,
+// one global add per block and region)
+static __global__ void __launch_bounds__(kThreads)
+    k_region_hist(const uint64_t *hash, const uint64_t *d_n, uint64_t m, uint32_t r, unsigned int *hist) {
+    extern __shared__ unsigned int s_hist[];  // [r]
+    for (uint32_t i = threadIdx.x; i < r; i += blockDim.x) s_hist[i] = 0;
+    __syncthreads();
+    const uint64_t n = *d_n;
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x)
+        atomicAdd(&s_hist[table_region(hash[k], m, r)], 1u);
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < r; i += blockDim.x)
+        if (s_hist[i]) atomicAdd(&hist[i], s_hist[i]);
+}
+
 // roff[r] = exclusive prefix of hist (one block), cursor zeroed
 static __global__ void __launch_bounds__(1024) k_region_offsets(const unsigned int *hist, uint32_t r,
                                                                  uint64_t *roff, unsigned long long *cursor) {

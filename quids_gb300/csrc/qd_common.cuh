@@ -15,8 +15,6 @@
 #define QD_D inline
 #endif
 
-#include "softfp64.cuh"
-
 namespace qd {
 
 // ------------------------------------------------------------------ mag_t
@@ -28,42 +26,23 @@ struct mag_t {
     double re, im;
 };
 
-// On the device, QD_FP64_MODE picks where the products and sums run: 0 the
-// FP64 pipe (__dmul_rn, __dadd_rn), 1 products on the integer pipes
-// (softfp64.cuh) and sums on the FP64 pipe, 2 both on the integer pipes.
-// Every mode gives the same bits.
-#ifndef QD_FP64_MODE
-#define QD_FP64_MODE 1
-#endif
 QD_HD double dmul(double a, double b) {
 #ifdef __CUDA_ARCH__
-#if QD_FP64_MODE >= 1
-    return softfp::mul(a, b);
-#else
     return __dmul_rn(a, b);
-#endif
 #else
     return a * b;
 #endif
 }
 QD_HD double dadd(double a, double b) {
 #ifdef __CUDA_ARCH__
-#if QD_FP64_MODE >= 2
-    return softfp::add(a, b);
-#else
     return __dadd_rn(a, b);
-#endif
 #else
     return a + b;
 #endif
 }
 QD_HD double dsub(double a, double b) {
 #ifdef __CUDA_ARCH__
-#if QD_FP64_MODE >= 2
-    return softfp::sub(a, b);
-#else
     return __dsub_rn(a, b);
-#endif
 #else
     return a - b;
 #endif

@@ -542,29 +542,43 @@ struct split_merge {
         for (int i = fs + lm; i < n - lm; ++i) {
             bool s, m;
             get_operations(p, n, i, s, m);
-            bool taken = false;
             if (s || m) {
-                taken = cid & 1;
-                mulf(mag, f, taken ? (s ? F_D : F_DC) : (s ? F_DN : F_NDNC));
-                if (taken) {
-                    cn += (int)s - (int)m;
-                    int b = name_begin(p, n, i), e = name_begin(p, n, i + 1);
-                    if (s) {
-                        sink.emit(i + off, true, false, OP_LEFT, b, e, 0, 0);
-                        sink.emit(i + off + 1, false, true, OP_RIGHT, b, e, 0, 0);
-                    } else {
-                        sink.emit(i + off, true, true, OP_MERGE, b, e, e, name_begin(p, n, i + 2));
-                    }
-                    off += (int)s - (int)m;
-                    i += m;
-                }
+                i = walk_site(p, n, i, s, m, cid & 1, sink, mag, off, cn);
                 cid >>= 1;
+            } else {
+                sink.emit(i + off, L(p, i), R(p, n, i), OP_COPY, name_begin(p, n, i), name_begin(p, n, i + 1), 0,
+                          0);
             }
-            if (!taken)
-                sink.emit(i + off, L(p, i), R(p, n, i), OP_COPY, name_begin(p, n, i),
-                          name_begin(p, n, i + 1), 0, 0);
         }
         if (overflow) sink.emit(cn - 1, true, false, OP_LEFT, 0, name_begin(p, n, 1), 0, 0);
+    }
+    // the first pass's handling of the wrap split of node 0 (:702-735):
+    // true when its left half overflows to the end of the child
+    QD_HD static bool first_split_overflows(const char *p, int n) {
+        const char *pn = names(p, n);
+        return node_rot(pn, 0) >= 0 && node_hmlz(pn, 1) > 0;
+    }
+    // one middle site, split (s) or merge (m) of node i, taken or not: its
+    // factor, its nodes; returns the last node it consumed (a taken merge
+    // consumes node i + 1, which is never a site)
+    template <class Sink, class M>
+    QD_HD int walk_site(const char *p, int n, int i, bool s, bool m, bool taken, Sink &sink, M *mag, int &off,
+                        int &cn) const {
+        mulf(mag, f, taken ? (s ? F_D : F_DC) : (s ? F_DN : F_NDNC));
+        if (!taken) {
+            sink.emit(i + off, L(p, i), R(p, n, i), OP_COPY, name_begin(p, n, i), name_begin(p, n, i + 1), 0, 0);
+            return i;
+        }
+        cn += (int)s - (int)m;
+        const int b = name_begin(p, n, i), e = name_begin(p, n, i + 1);
+        if (s) {
+            sink.emit(i + off, true, false, OP_LEFT, b, e, 0, 0);
+            sink.emit(i + off + 1, false, true, OP_RIGHT, b, e, 0, 0);
+        } else {
+            sink.emit(i + off, true, true, OP_MERGE, b, e, e, name_begin(p, n, i + 2));
+        }
+        off += (int)s - (int)m;
+        return i + (int)m;
     }
 
     struct byte_sink {
@@ -624,6 +638,115 @@ struct split_merge {
         hash_combine(s.nh, s.rh);
         size = 4 + 4 * (uint32_t)pl.cn + 16 * (uint32_t)s.len;
         return s.nh;
+    }
+
+    // The grouped symbolic pass (as flip_rule's): the 2^H children e +
+    // j 2^(s-H) share their child id's low s-H bits, so they share the wrap
+    // decisions and the walk up to the first of the last H middle sites (the
+    // bits are consumed in node order).  That prefix is walked once, and
+    // the last H sites as a binary tree with the j bits reversed; each level
+    // keeps the walk's state (magnitude, hash sink, index offset, node
+    // count).  Bit for bit what hash_child gives each child.  A group whose
+    // top H bits are not all middle sites (a wrap bit among them) is
+    // computed child by child.  emit(j, hash, magnitude, size).
+    static constexpr bool grouped_children = true;
+    struct tree_state {
+        mag_t m;
+        hash_sink s;
+        int off, cn;
+    };
+    template <int H, class Emit>
+    QD_HD void expand_group(const char *pb, const char *pe, uint32_t e, int s, mag_t pm, Emit &&emit) const {
+        mag_t m0 = pm;
+        plan pl = wrap_plan(pb, e, &m0);
+        const int n = pl.n;
+        bool fs0, lm0;
+        wrap_sites(pb, n, fs0, lm0);
+        // bit 0 decides a possible wrap site (taken or not, it shapes the
+        // walk), so it must be one of e's bits; it is consumed as a wrap bit
+        // when the first split is taken or a last merge is possible, and is
+        // node 0's middle-site bit when the first split is not taken
+        const int wrap_bits = (int)pl.fs + (int)lm0;
+        if (s - H < ((fs0 || lm0) ? 1 : 0)) {
+            for (uint32_t j = 0; j < (1u << H); ++j) {
+                mag_t m = pm;
+                uint32_t sz = 0;
+                const uint64_t h = hash_child(pb, pe, e + (j << (s - H)), sz, m);
+                emit(j, h, m, sz);
+            }
+            return;
+        }
+        // the prefix: wrap nodes and middle sites before the last H (as walk)
+        const char *pn = names(pb, n);
+        tree_state w{m0, hash_sink{pn, 0, 0, 0, 0}, 0, n + (int)pl.fs - (int)pl.lm};
+        const bool fs = pl.fs, lm = pl.lm;
+        bool overflow = false;
+        if (fs) {
+            overflow = first_split_overflows(pb, n);
+            const int e0 = name_begin(pb, n, 1);
+            if (!overflow) {
+                w.s.emit(0, true, false, OP_LEFT, 0, e0, 0, 0);
+                w.s.emit(1, false, true, OP_RIGHT, 0, e0, 0, 0);
+            } else {
+                w.s.emit(0, false, true, OP_RIGHT, 0, e0, 0, 0);
+            }
+        }
+        if (lm)
+            w.s.emit(0, true, true, OP_MERGE, name_begin(pb, n, n - 1), name_begin(pb, n, n), 0,
+                     name_begin(pb, n, 1));
+        w.off = (int)fs - (int)overflow;
+        const int prefix_sites = s - H - wrap_bits;
+        uint32_t bits = pl.cid;
+        int i = fs + lm, k = 0;
+        for (; i < n - lm; ++i) {
+            bool sp, mg;
+            get_operations(pb, n, i, sp, mg);
+            if (sp || mg) {
+                if (k == prefix_sites) break;
+                i = walk_site(pb, n, i, sp, mg, bits & 1, w.s, &w.m, w.off, w.cn);
+                bits >>= 1;
+                ++k;
+            } else {
+                w.s.emit(i + w.off, L(pb, i), R(pb, n, i), OP_COPY, name_begin(pb, n, i), name_begin(pb, n, i + 1),
+                         0, 0);
+            }
+        }
+        int q[H + 1];  // node index of each of the last H sites, then the end of the middle nodes
+        {
+            int x = i, c = 0;
+            for (; x < n - lm && c < H; ++x) {
+                bool sp, mg;
+                get_operations(pb, n, x, sp, mg);
+                if (sp || mg) q[c++] = x;
+            }
+            q[H] = n - lm;
+        }
+        tree_state P[H + 1];  // P[lv]: the state before site lv (P[H]: the child's)
+        P[0] = w;
+#pragma unroll
+        for (int t = 0; t < (1 << H); ++t) {
+            int j = 0;
+#pragma unroll
+            for (int b = 0; b < H; ++b) j |= ((t >> b) & 1) << (H - 1 - b);
+            const int k0 = t == 0 ? 0 : H - 1 - ctz_small(t);
+#pragma unroll
+            for (int lv = 0; lv < H; ++lv) {
+                if (lv < k0) continue;
+                tree_state x = P[lv];
+                bool sp, mg;
+                get_operations(pb, n, q[lv], sp, mg);
+                const int last = walk_site(pb, n, q[lv], sp, mg, (j >> lv) & 1, x.s, &x.m, x.off, x.cn);
+                for (int y = last + 1; y < q[lv + 1]; ++y)
+                    x.s.emit(y + x.off, L(pb, y), R(pb, n, y), OP_COPY, name_begin(pb, n, y),
+                             name_begin(pb, n, y + 1), 0, 0);
+                P[lv + 1] = x;
+            }
+            hash_sink hs = P[H].s;
+            if (overflow) hs.emit(P[H].cn - 1, true, false, OP_LEFT, 0, name_begin(pb, n, 1), 0, 0);
+            hash_combine(hs.nh, hs.lh);
+            hash_combine(hs.nh, hs.rh);
+            emit((uint32_t)j, hs.nh, P[H].m, 4 + 4 * (uint32_t)hs.cn + 16 * (uint32_t)hs.len);
+        }
     }
 };
 

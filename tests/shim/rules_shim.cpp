@@ -55,7 +55,7 @@ uint64_t shim_hash_child(int kind, const double *p, const uint8_t *o, uint32_t s
     });
     return h;
 }
-// the grouped expansion of the flip rules (kind 2, 3) with H = h (2 or 3)
+// the grouped expansion of the QCGD rules (kind 2, 3, 4) with H = h (2 or 3)
 // for the children whose ids share the low s-h bits e: writes 2^h hashes and
 // 2^(h+1) doubles (child e + j 2^(s-h) at slot j); returns s, or -1
 int shim_expand_group(int kind, int h, const double *p, const uint8_t *o, uint32_t sz, uint32_t e,
@@ -77,6 +77,7 @@ int shim_expand_group(int kind, int h, const double *p, const uint8_t *o, uint32
     };
     if (kind == 2) return run(qcgd::erase_create{factors(p)});
     if (kind == 3) return run(qcgd::coin{factors(p)});
+    if (kind == 4) return run(qcgd::split_merge{factors(p)});
     return -1;
 }
 uint64_t shim_murmur(const uint8_t *b, uint64_t len) { return murmur64a((const char *)b, len); }

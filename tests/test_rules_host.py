@@ -180,6 +180,46 @@ def test_grouped_expansion_is_hash_child_bit_for_bit(shim, kind, h):
     assert checked > 500
 
 
+@pytest.mark.parametrize("h", [2, 3])
+@pytest.mark.parametrize("params", [(math.pi / 4, 0.0, -math.pi / 2), (0.7, 2.1, 4.4)])
+def test_split_merge_grouped_expansion_is_hash_child_bit_for_bit(shim, params, h):
+    """split_merge's grouped expansion (siblings share the wrap decisions and
+    the walk up to the last H middle sites, which form a tree) gives every
+    child's hash, size and magnitude as hash_child does, on graphs whose
+    names were split and merged, with and without the wrap sites."""
+    rng = W.Rng(77)
+    graphs = [W.random_graph(n, rng) for n in range(1, 21) for _ in range(12)]
+    for g in graphs[:120]:
+        for cid in range(4):
+            graphs.append(_child(shim, 4, params, g, cid, 1.0 + 0j, 4 * len(g))[0])
+    keep, pp = _dp(params)
+    checked, grouped = 0, 0
+    for trial, g in enumerate(graphs):
+        a, b = C.c_uint32(), C.c_uint32()
+        shim.shim_num_child(4, pp, _buf(g), len(g), C.byref(a), C.byref(b))
+        nc = a.value
+        if nc < (1 << h):
+            continue
+        s = nc.bit_length() - 1
+        pm = np.array([0.3 + 0.001 * trial, -0.2], np.float64)
+        pmp = pm.ctypes.data_as(C.POINTER(C.c_double))
+        for e in range(0, 1 << (s - h), max(1, (1 << (s - h)) // 7)):
+            hs = np.zeros(1 << h, np.uint64)
+            ms = np.zeros(2 << h, np.float64)
+            assert shim.shim_expand_group(4, h, pp, _buf(g), len(g), e, pmp, hs.ctypes.data, ms.ctypes.data) == s
+            for j in range(1 << h):
+                cid = e + (j << (s - h))
+                mm = (C.c_double * 2)(pm[0], pm[1])
+                sz = C.c_uint32()
+                hv = shim.shim_hash_child(4, pp, _buf(g), len(g), cid, C.byref(sz), mm)
+                assert hv == int(hs[j]), (trial, e, j)
+                assert (mm[0], mm[1]) == (ms[2 * j], ms[2 * j + 1]), (trial, e, j)
+                checked += 1
+            grouped += 1
+    print(f"{checked} children in {grouped} groups")
+    assert checked > 3000 and grouped > 700
+
+
 @pytest.mark.parametrize("params", [(math.pi / 4, 0.0, -math.pi / 2), (0.7, 2.1, 4.4)])
 def test_split_merge_hash_child_is_populate_then_hash(shim, params):
     """split_merge's hash_child (one pass: wrap decisions, then the walk with
