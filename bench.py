@@ -601,6 +601,7 @@ def ours_batched(args, rank, world, emit=True):
     cpu = None
     if emit and rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline_batched(wl, packed)
+    tuning = ctx.last_tuning()
     ctx.close()
     if rank == 0:
         line = {
@@ -611,7 +612,7 @@ def ours_batched(args, rank, world, emit=True):
             "config": dict(wl["config"], parallelism=f"replicas x{world}",
                            l2="flushed before every step (256 MiB write)",
                            children_per_step=children // args.steps,
-                           runs_timed=runs, autotuned=ctx.last_tuning()),
+                           runs_timed=runs, autotuned=tuning),
             "plain_instance_by_instance": {"value": plain_value, "unit": UNIT,
                                            "ms_per_step": statistics.mean(plain_ms),
                                            "batched_over_plain": value / plain_value},
