@@ -23,8 +23,8 @@ ERR_BAD_ARG, ERR_OOM, ERR_TABLE_FULL, ERR_CHILD_COUNT_OVERFLOW, ERR_SIZE_BOUND, 
 ERR_CUDA, ERR_NO_DEVICE, ERR_UNSUPPORTED, ERR_NOALLOC_LIMIT = -7, -8, -9, -10
 FLAG_NO_FAST_HASH = 1
 FLAG_STAGE_TIMING = 2
-FLAG_NO_REGIONS = 4
-FLAG_REGIONS = 8
+FLAG_TABLE = 4
+FLAG_PARTITION = 8
 FLAG_NO_PLAN = 16
 FLAG_AUTOTUNE = 32
 DEBUG_STALL_LOOKBACK = 1

@@ -89,6 +89,7 @@ int forward_rule(quids_gpu_tape *t, const quids_gpu_op &op, quids_gpu_state *cur
                  quids_gpu_step_stats *stats) {
     QD_TRY(new_state(t->ctx, out));
     quids_gpu_params prm = t->prm;
+    prm.flags |= QUIDS_FLAG_TABLE;  // the step records read the table's slots
     prm.hash_ranges = 0;  // the step records are those of one pass
     const int rc = host::dispatch_rule(op.kind, &op.params, [&](auto r) {
         return simulate_rule(t->ctx, cur, r, *out, prm, stats);

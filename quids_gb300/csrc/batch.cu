@@ -50,7 +50,7 @@ constexpr size_t kMaxPlans = 8;
 
 bool plannable_batched(const quids_gpu_params &prm) {
     return prm.max_num_object != 0 &&
-           !(prm.flags & (QUIDS_FLAG_STAGE_TIMING | QUIDS_FLAG_REGIONS | QUIDS_FLAG_NO_PLAN));
+           !(prm.flags & (QUIDS_FLAG_STAGE_TIMING | QUIDS_FLAG_NO_PLAN));
 }
 
 // the rule parameters of rule step r of instance g

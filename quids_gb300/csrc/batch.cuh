@@ -575,11 +575,10 @@ int simulate_batched(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule *rules_
         k_tile_parents<<<grid_for(ctx, NP), prim::kThreads, 0, ctx->stream>>>(
             bufp<uint64_t>(ctx, B_CBEGIN), NP, sym_tiles, bufp<uint64_t>(ctx, B_TILEPAR));
         QD_TRY(launched(ctx));
-        const region_count rc{M, 0u, nullptr};
         if (maxsize <= 256) {
-            QD_TRY((launch_symbolic<instance_rules<Rule>, 256>(ctx, rs, pv, NC, fast, rc)));
+            QD_TRY((launch_symbolic<instance_rules<Rule>, 256>(ctx, rs, pv, NC, fast)));
         } else {
-            QD_TRY((launch_symbolic<instance_rules<Rule>, 4096>(ctx, rs, pv, NC, fast, rc)));
+            QD_TRY((launch_symbolic<instance_rules<Rule>, 4096>(ctx, rs, pv, NC, fast)));
         }
     }
 

@@ -142,7 +142,7 @@ constexpr size_t kMaxPlans = 8;
 
 bool plannable(const quids_gpu_params &prm, const quids_gpu_state *a) {
     return prm.max_num_object != 0 &&
-           !(prm.flags & (QUIDS_FLAG_STAGE_TIMING | QUIDS_FLAG_REGIONS | QUIDS_FLAG_NO_PLAN)) &&
+           !(prm.flags & (QUIDS_FLAG_STAGE_TIMING | QUIDS_FLAG_NO_PLAN)) &&
            prm.hash_ranges < 2 && a->n_inst == 0;
 }
 

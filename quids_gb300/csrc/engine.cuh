@@ -44,15 +44,15 @@ enum qd_buf_id {
     B_SCHILD,      // u64 [NS] representative child of each survivor
     B_LOOKBACK,    // u64 [3 (tiles + 2)] look-back chains
     B_TILENORM,    // double [blocks] per-block partial sums of an observable
-    B_RHASH,       // u64 [NC] child hashes in table-region order
-    B_RIDX,        // u32 [NC] child indices in table-region order
-    B_RMAG,        // double2 [NC] child magnitudes in table-region order
-    B_RSLOT,       // u32 [NC] table slot of each region-ordered child
+    B_RHASH,       // u64 [NC] child hashes in bucket order (partitioned collisions)
+    B_RIDX,        // u32 [NC] child indices in bucket order
+    B_RMAG,        // double2 [NC] child magnitudes in bucket order
+    B_RSLOT,       // u32 [NC] representative of each group (partitioned collisions)
     B_NOTREP,      // u8 [NC] child is not its group's representative
     B_HASJOIN,     // u8 [NC] child's group has more than one member (for the representative)
-    B_RHIST,       // u32 [R] children per table region
-    B_ROFF,        // u64 [R+1] region offsets
-    B_RCUR,        // u64 [R] region write cursors
+    B_RHIST,       // u32 [2 NB] children per bucket, bucket write cursors
+    B_ROFF,        // u64 [NB+1] bucket offsets
+    B_RCUR,        // (unused)
     B_TILEPAR,     // u64 [tiles+1] first parent of each tile of children
     B_CPAR,        // u32 [NC] kept-parent index of each child
     B_MODSTATUS,   // int: sticky error of modifier launches (reported by the next step)
@@ -70,6 +70,9 @@ enum qd_buf_id {
     B_SELCAND,     // u64 [NC/8 + 2^16] keys left in a truncation's selection after its first two digits
     B_KEEPCAND,    // u32 [NC] children selected or tied at a truncation's cutoff, in child order
     B_TILECNT,     // u32 [NC / kCandTile + 1] their count per tile of children, then u64 tile offsets
+    // partitioned collision stage (collide.cuh)
+    B_BITMAP,      // u32 [2 (NC/32 + 1)] survivors and cutoff ties, one bit per child
+    B_BITPREFIX,   // u64 [2 (NC/32 + 1)] their popcount prefixes
     B_COUNT
 };
 
@@ -99,6 +102,8 @@ enum qd_word {
     W_SELCNT,            // truncation select: candidates kept
     W_NTILES,            // keep layout: tiles of the candidate filter
     W_NCAND,             // keep layout: children selected or tied at the cutoff
+    W_PCSNB,             // partitioned collisions: buckets
+    W_PCSNW,             // partitioned collisions: bitmap words
     W_COUNT_WORDS = 32
 };
 
@@ -272,6 +277,17 @@ inline T *bufp(quids_gpu_ctx *ctx, qd_buf_id id) {
 
 // collision-table probe limit of a step (quids_gpu_params::max_probes)
 inline uint32_t probe_limit(const quids_gpu_params &prm) { return prm.max_probes ? prm.max_probes : 65536u; }
+
+// A one-pass step groups its children by partition (collide.cuh) when its
+// open-addressing table (16-byte slots at load 1/2) would hold 512 MB or
+// more, several times what L2 holds; QUIDS_FLAG_TABLE / QUIDS_FLAG_PARTITION
+// force either.
+constexpr double kPartitionMinTableBytes = 512.0 * 1024 * 1024;
+inline bool use_partition(const quids_gpu_params &prm, uint64_t nc) {
+    if (prm.flags & QUIDS_FLAG_TABLE) return false;
+    if (prm.flags & QUIDS_FLAG_PARTITION) return true;
+    return 32.0 * (double)nc >= kPartitionMinTableBytes;
+}
 
 // Blocks of `kernel` (at `threads` per block, `smem` dynamic shared bytes)
 // one SM holds at once: a grid of that many per SM is one full wave.
@@ -578,11 +594,6 @@ struct parents_view {
     __device__ __forceinline__ uint64_t nparents() const { return d_np ? *d_np : np; }
 };
 
-struct region_count {
-    uint64_t m;           // table slots
-    uint32_t r;           // regions (0: no region histogram)
-    unsigned int *hist;   // [r]
-};
 
 // The children of one tile of kTileChildren come from a contiguous run of
 // parents, [tile_first[t], tile_first[t+1]]; their offsets are staged in
@@ -628,10 +639,8 @@ template <class RS, int MAXC, bool FAST>
 __global__ void __launch_bounds__(prim::kThreads)
     k_symbolic(RS rs, parents_view pv, const uint64_t *tile_first, const uint64_t *d_nc, uint64_t *hash,
                double2 *cmag, uint32_t *csize, uint32_t *cpar, unsigned long long *d_maxabs, int *err,
-               region_count rc, const uint64_t *d_bound) {
+               const uint64_t *d_bound) {
     __shared__ uint64_t s_cb[kStagedParents + 1];
-    extern __shared__ unsigned int s_rhist[];  // [rc.r]
-    for (uint32_t i = threadIdx.x; i < rc.r; i += blockDim.x) s_rhist[i] = 0;
     const uint64_t nc = *d_nc;
     // the step's child size bound: the largest max_child_size its parents
     // declared (get_num_child), which sized the per-thread child buffer; a
@@ -688,14 +697,10 @@ __global__ void __launch_bounds__(prim::kThreads)
             cmag[c] = make_double2(m.re, m.im);
             csize[c] = sz;
             cpar[c] = (uint32_t)p;
-            if (rc.r) atomicAdd(&s_rhist[prim::table_region(h, rc.m, rc.r)], 1u);
             double a = fabs(m.re) > fabs(m.im) ? fabs(m.re) : fabs(m.im);
             mx = mx > a ? mx : a;
         }
     }
-    __syncthreads();
-    for (uint32_t i = threadIdx.x; i < rc.r; i += blockDim.x)
-        if (s_rhist[i]) atomicAdd(&rc.hist[i], s_rhist[i]);
     unsigned long long bits = (unsigned long long)__double_as_longlong(mx);
     for (int o = 16; o > 0; o >>= 1) {
         unsigned long long y = __shfl_xor_sync(0xffffffffu, bits, o);
@@ -1039,15 +1044,6 @@ struct direct_src {
     __device__ __forceinline__ uint64_t child(uint64_t k) const { return k; }
     __device__ __forceinline__ double2 mag(uint64_t k) const { return mag_[k]; }
 };
-// ... or in table-region order
-struct region_src {
-    const uint64_t *rhash;
-    const uint32_t *ridx;
-    const double2 *rmag;
-    __device__ __forceinline__ uint64_t hash(uint64_t k) const { return rhash[k]; }
-    __device__ __forceinline__ uint64_t child(uint64_t k) const { return ridx[k]; }
-    __device__ __forceinline__ double2 mag(uint64_t k) const { return rmag[k]; }
-};
 
 // no truncation possible: survivors straight into the output layout
 struct groups_layout {
@@ -1347,14 +1343,6 @@ __global__ void __launch_bounds__(prim::kThreads)
     if ((threadIdx.x & 31) == 0 && acc) atomicAdd(out, acc);
 }
 
-// region path: slot of each child back in child order
-static __global__ void __launch_bounds__(prim::kThreads)
-    k_unpermute_slots(const uint32_t *rslot, const uint32_t *ridx, const uint64_t *d_n, uint32_t *slot_of) {
-    const uint64_t n = *d_n;
-    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x)
-        slot_of[ridx[k]] = rslot[k];
-}
-
 // ------------------------------------------------------------ radix select
 // Runs the 8 passes of a top-k threshold selection on the stream.
 template <class K1>
@@ -1406,15 +1394,14 @@ inline uint64_t next_pow2(uint64_t v) {
 
 // ------------------------------------------------------------- the step
 template <class RS, int MAXC>
-inline int launch_symbolic(quids_gpu_ctx *ctx, const RS &rule, const parents_view &pv, uint64_t nc, bool fast,
-                           region_count rc) {
+inline int launch_symbolic(quids_gpu_ctx *ctx, const RS &rule, const parents_view &pv, uint64_t nc, bool fast) {
     using Rule = typename RS::rule_type;
     uint64_t tiles = (nc + kTileChildren - 1) / kTileChildren;
     uint64_t *d_nc = ctx->d_words + W_NC;
     unsigned long long *d_maxabs = (unsigned long long *)(ctx->d_words + W_MAXABS);
     int *err = (int *)(ctx->d_words + W_STATUS);
     const uint64_t *d_bound = ctx->d_words + W_MAXSIZE;
-    const size_t smem = rc.r * sizeof(unsigned int);
+    const size_t smem = 0;
     // one full wave of resident blocks (each strides over tiles)
     auto wave = [&](auto kernel) {
         const uint64_t w = (uint64_t)ctx->num_sms * resident_per_sm(kernel, prim::kThreads, smem);
@@ -1425,14 +1412,14 @@ inline int launch_symbolic(quids_gpu_ctx *ctx, const RS &rule, const parents_vie
             const unsigned grid = wave(k_symbolic<RS, 8, true>);
             k_symbolic<RS, 8, true><<<grid, prim::kThreads, smem, ctx->stream>>>(
                 rule, pv, bufp<uint64_t>(ctx, B_TILEPAR), d_nc, bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG),
-                bufp<uint32_t>(ctx, B_CSIZE), bufp<uint32_t>(ctx, B_CPAR), d_maxabs, err, rc, d_bound);
+                bufp<uint32_t>(ctx, B_CSIZE), bufp<uint32_t>(ctx, B_CPAR), d_maxabs, err, d_bound);
             return launched(ctx);
         }
     }
     const unsigned grid = wave(k_symbolic<RS, MAXC, false>);
     k_symbolic<RS, MAXC, false><<<grid, prim::kThreads, smem, ctx->stream>>>(
         rule, pv, bufp<uint64_t>(ctx, B_TILEPAR), d_nc, bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG),
-        bufp<uint32_t>(ctx, B_CSIZE), bufp<uint32_t>(ctx, B_CPAR), d_maxabs, err, rc, d_bound);
+        bufp<uint32_t>(ctx, B_CSIZE), bufp<uint32_t>(ctx, B_CPAR), d_maxabs, err, d_bound);
     return launched(ctx);
 }
 
@@ -1529,6 +1516,8 @@ inline int launch_symbolic_grouped(quids_gpu_ctx *ctx, const RS &rs, const paren
     return launched(ctx, 2);
 }
 
+
+#include "collide.cuh"
 
 // simulate_rule's answer for a step beyond one pass (2^32 children, or
 // records and table beyond the device memory) or with hash-range passes
@@ -1738,49 +1727,36 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, qu
     }
     const uint64_t NSB = may_truncate ? maxc : NC;  // bound on the survivors
 
+    // collisions: the partitioned stage (collide.cuh) for steps whose table
+    // would be far larger than L2, else the open-addressing table
+    const bool pcs = use_partition(prm, NC);
     uint64_t M = (uint64_t)((double)NC / load) + 1;
     if (M < 1024) M = 1024;
-    if (M >= 0x7ffffff0ull) return QUIDS_ERR_OOM;  // slot indices are 31-bit (the top bit marks joiners)
-    s.table_capacity = M;
-    // tables larger than a share of L2 are filled region by region
-    const double table_bytes = 44.0 * (double)M;
-    uint32_t R = (uint32_t)(table_bytes / (32.0 * 1024 * 1024)) + 1;
-    if (R < 4) R = 1;
-    if (R > prim::kMaxRegions) R = prim::kMaxRegions;
-    // region order pays for its scatter only where the table traffic is latency
-    // bound; measured on GB300 it breaks even, so it is opt-in
-    if (!(prm.flags & QUIDS_FLAG_REGIONS)) R = 1;
-    else if (R < 4) R = 4;
-    const bool regions = R > 1;
+    if (!pcs && M >= 0x7ffffff0ull) return QUIDS_ERR_OOM;  // slot indices are 31-bit (the top bit marks joiners)
+    s.table_capacity = pcs ? 0 : M;
     const uint64_t tiles_nc = (NC + prim::kTile - 1) / prim::kTile;
     QD_TRY(ensure(ctx->buf[B_HASH], NC * sizeof(uint64_t)));
     QD_TRY(ensure(ctx->buf[B_CMAG], NC * sizeof(double2)));
     QD_TRY(ensure(ctx->buf[B_CSIZE], NC * sizeof(uint32_t)));
-    QD_TRY(ensure(ctx->buf[B_SLOT], NC * sizeof(uint32_t)));
-    QD_TRY(ensure(ctx->buf[B_NOTREP], NC));
-    QD_TRY(ensure(ctx->buf[B_HASJOIN], NC));
-    QD_TRY(ensure(ctx->buf[B_KEYS], (M + 1) * sizeof(prim::table_slot)));
-    QD_TRY(ensure(ctx->buf[B_ACC], 4 * (M + 1) * sizeof(uint64_t)));
     QD_TRY(ensure(ctx->buf[B_SCHILD], NSB * sizeof(uint64_t)));
     QD_TRY(ensure(ctx->buf[B_LOOKBACK], 4 * (tiles_nc + 2) * sizeof(uint64_t)));
     QD_TRY(ensure(out->begin, (NSB + 1) * sizeof(uint64_t)));
     QD_TRY(ensure(out->size, NSB * sizeof(uint32_t)));
     QD_TRY(ensure(out->mag, NSB * sizeof(double2)));
     QD_TRY(ensure(out->d_total, sizeof(double)));
-    if (may_truncate) {
-        QD_TRY(ensure(ctx->buf[B_UNORM], NC * sizeof(uint64_t)));
-        QD_TRY(ensure(ctx->buf[B_KEEPCAND], NC * sizeof(uint32_t)));
-        QD_TRY(ensure(ctx->buf[B_TILECNT], tilecnt_bytes(NC)));
-    }
-    if (regions) {
-        QD_TRY(ensure(ctx->buf[B_RHASH], NC * sizeof(uint64_t)));
-        QD_TRY(ensure(ctx->buf[B_RIDX], NC * sizeof(uint32_t)));
-        QD_TRY(ensure(ctx->buf[B_RMAG], NC * sizeof(double2)));
-        QD_TRY(ensure(ctx->buf[B_RSLOT], NC * sizeof(uint32_t)));
-        QD_TRY(ensure(ctx->buf[B_RHIST], R * sizeof(unsigned int)));
-        QD_TRY(ensure(ctx->buf[B_ROFF], (R + 1) * sizeof(uint64_t)));
-        QD_TRY(ensure(ctx->buf[B_RCUR], R * sizeof(uint64_t)));
-        QD_CUDA(cudaMemsetAsync(ctx->buf[B_RHIST].p, 0, R * sizeof(unsigned int), ctx->stream));
+    if (pcs) {
+        QD_TRY(pcs_ensure(ctx, NC, may_truncate));
+    } else {
+        QD_TRY(ensure(ctx->buf[B_SLOT], NC * sizeof(uint32_t)));
+        QD_TRY(ensure(ctx->buf[B_NOTREP], NC));
+        QD_TRY(ensure(ctx->buf[B_HASJOIN], NC));
+        QD_TRY(ensure(ctx->buf[B_KEYS], (M + 1) * sizeof(prim::table_slot)));
+        QD_TRY(ensure(ctx->buf[B_ACC], 4 * (M + 1) * sizeof(uint64_t)));
+        if (may_truncate) {
+            QD_TRY(ensure(ctx->buf[B_UNORM], NC * sizeof(uint64_t)));
+            QD_TRY(ensure(ctx->buf[B_KEEPCAND], NC * sizeof(uint32_t)));
+            QD_TRY(ensure(ctx->buf[B_TILECNT], tilecnt_bytes(NC)));
+        }
     }
 
     const uint64_t sym_tiles = (NC + kTileChildren - 1) / kTileChildren;
@@ -1798,114 +1774,94 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, qu
                 bufp<uint64_t>(ctx, B_CBEGIN), NP, sym_tiles, bufp<uint64_t>(ctx, B_TILEPAR));
             QD_TRY(launched(ctx));
         }
-        // the region histogram comes with the symbolic records (the grouped
-        // pass leaves it to k_region_hist)
-        region_count rc{M, regions ? R : 0u, regions ? bufp<unsigned int>(ctx, B_RHIST) : nullptr};
         if (maxsize <= 256) {
-            QD_TRY((launch_symbolic<single_rule<Rule>, 256>(ctx, rule, pv, NC, fast, rc)));
+            QD_TRY((launch_symbolic<single_rule<Rule>, 256>(ctx, rule, pv, NC, fast)));
         } else {
-            QD_TRY((launch_symbolic<single_rule<Rule>, 4096>(ctx, rule, pv, NC, fast, rc)));
+            QD_TRY((launch_symbolic<single_rule<Rule>, 4096>(ctx, rule, pv, NC, fast)));
         }
     }
     end_stage(1);
 
-    // ---- stage 2: collision table (src/quids.hpp:726-809)
-    begin_stage(2);
-    prim::table tb{bufp<prim::table_slot>(ctx, B_KEYS), bufp<unsigned long long>(ctx, B_ACC), M, probe_limit(prm)};
-    {  // table slots free, the extra slot's sum, the group marks, the look-back chains of stages 3-4
-        fill_set f{};
-        f.p[0] = (unsigned char *)tb.slots, f.n[0] = (M + 1) * sizeof(prim::table_slot), f.v[0] = 0xff;
-        f.p[1] = (unsigned char *)(tb.acc + 4 * M), f.n[1] = 4 * sizeof(uint64_t), f.v[1] = 0;
-        f.p[2] = bufp<unsigned char>(ctx, B_NOTREP), f.n[2] = NC, f.v[2] = 0;
-        f.p[3] = bufp<unsigned char>(ctx, B_HASJOIN), f.n[3] = NC, f.v[3] = 0;
-        f.p[4] = bufp<unsigned char>(ctx, B_LOOKBACK), f.n[4] = 4 * (tiles_nc + 2) * sizeof(uint64_t), f.v[4] = 0;
-        f.count = 5;
-        QD_TRY(fill(ctx, f));
-    }
-    uint8_t *not_rep = bufp<uint8_t>(ctx, B_NOTREP), *has_join = bufp<uint8_t>(ctx, B_HASJOIN);
-    const unsigned long long *d_maxabs = (const unsigned long long *)(ctx->d_words + W_MAXABS);
-    if (!regions) {
-        direct_src src{bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG)};
-        prim::k_table_claim<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
-            tb, src, ctx->d_words + W_NC, bufp<uint32_t>(ctx, B_SLOT), err);
-        prim::k_table_accumulate<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
-            tb, src, bufp<uint32_t>(ctx, B_SLOT), ctx->d_words + W_NC, d_maxabs, not_rep, has_join);
-        QD_TRY(launched(ctx, 2));
-    } else {
-        if (grouped) {
-            prim::k_region_hist<<<grid_for(ctx, NC), prim::kThreads, R * sizeof(unsigned int), ctx->stream>>>(
-                bufp<uint64_t>(ctx, B_HASH), ctx->d_words + W_NC, M, R, bufp<unsigned int>(ctx, B_RHIST));
-            QD_TRY(launched(ctx));
-        }
-        prim::k_region_offsets<<<1, 1024, 0, ctx->stream>>>(bufp<unsigned int>(ctx, B_RHIST), R,
-                                                           bufp<uint64_t>(ctx, B_ROFF),
-                                                           bufp<unsigned long long>(ctx, B_RCUR));
-        const uint64_t tiles = tiles_nc;
-        unsigned g = (unsigned)(tiles < (uint64_t)ctx->num_sms * 8 ? tiles : (uint64_t)ctx->num_sms * 8);
-        prim::k_region_scatter<<<g, prim::kThreads, prim::region_scatter_smem(R), ctx->stream>>>(
-            bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG), ctx->d_words + W_NC, M, R,
-            bufp<uint64_t>(ctx, B_ROFF), bufp<unsigned long long>(ctx, B_RCUR), bufp<uint64_t>(ctx, B_RHASH),
-            bufp<uint32_t>(ctx, B_RIDX), bufp<double2>(ctx, B_RMAG), err);
-        region_src src{bufp<uint64_t>(ctx, B_RHASH), bufp<uint32_t>(ctx, B_RIDX), bufp<double2>(ctx, B_RMAG)};
-        prim::k_table_claim<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
-            tb, src, ctx->d_words + W_NC, bufp<uint32_t>(ctx, B_RSLOT), err);
-        prim::k_table_accumulate<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
-            tb, src, bufp<uint32_t>(ctx, B_RSLOT), ctx->d_words + W_NC, d_maxabs, not_rep, has_join);
-        k_unpermute_slots<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
-            bufp<uint32_t>(ctx, B_RSLOT), bufp<uint32_t>(ctx, B_RIDX), ctx->d_words + W_NC,
-            bufp<uint32_t>(ctx, B_SLOT));
-        QD_TRY(launched(ctx, 5));
-    }
-    end_stage(2);
-
-    // ---- stage 3 (+4): representatives above tolerance (src/quids.hpp:819-823),
-    // truncation (src/quids.hpp:866-900, ties by lower child index) and the
-    // output layout (src/quids.hpp:927-948), with the largest survivor norm
-    group_view gv{bufp<uint32_t>(ctx, B_SLOT), not_rep, has_join, bufp<double2>(ctx, B_CMAG),
-                  bufp<unsigned long long>(ctx, B_ACC), ctx->d_words + W_NC, d_maxabs, prm.tolerance};
     const uint32_t align = prm.align_byte_length;
-    unsigned long long *d_maxnorm = (unsigned long long *)(ctx->d_words + W_MAXNORM);
     const prim::publish pb1 = publish_words(ctx, W_DONE_LAYOUT);
-    begin_stage(3);
-    if (!may_truncate) {
-        prim::lookback lbc, lbb;
-        lookback_view(ctx, NC, 0, lbc);
-        lookback_view(ctx, NC, 1, lbb);
-        groups_layout f{gv, bufp<uint32_t>(ctx, B_CSIZE), align, (double2 *)out->mag.p, (uint32_t *)out->size.p,
-                        (uint64_t *)out->begin.p, bufp<uint64_t>(ctx, B_SCHILD)};
-        prim::k_compact_layout<groups_layout, false><<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
-            f, ctx->d_words + W_NC, ctx->d_words + W_NS, ctx->d_words + W_OUTBYTES, (uint64_t *)out->begin.p,
-            d_maxnorm, lbc, lbb, lbb, pb1);
-        QD_TRY(launched(ctx));
-        end_stage(3);
+    unsigned long long *d_maxnorm = (unsigned long long *)(ctx->d_words + W_MAXNORM);
+    if (pcs) {
+        // ---- stages 2-4 by partition (src/quids.hpp:726-948): groups, truncation, layout
+        begin_stage(2);
+        QD_TRY(pcs_stage(ctx, NC, may_truncate, maxc, tk, prm.tolerance, align, out, pb1));
+        end_stage(2);
     } else {
-        uint64_t *gkey = bufp<uint64_t>(ctx, B_UNORM);  // per child: its group's truncation key, or 0
-        k_group_keys<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
-            gv, tk, ctx->d_words + W_NC, gkey, (unsigned long long *)(ctx->d_words + W_NU));
-        QD_TRY(launched(ctx));
-        end_stage(3);
-        begin_stage(4);
-        QD_TRY(ensure(ctx->buf[B_SELCAND], filter_cap(NC) * sizeof(uint64_t)));
-        QD_TRY(radix_select_filtered(ctx, ctx->d_words + W_NC, NC, maxc, key_direct{gkey},
-                                     bufp<uint64_t>(ctx, B_SELCAND), filter_cap(NC), ctx->d_words + W_NU));
-        prim::lookback lbc, lbb, lbt;
-        lookback_view(ctx, NC, 0, lbt);
-        lookback_view(ctx, NC, 1, lbc);
-        lookback_view(ctx, NC, 2, lbb);
-        QD_TRY(list_keep_candidates(ctx, keep_candidate{gkey, ctx->d_sel}, NC));
-        const cand_keep_layout kl{{gv, gkey, ctx->d_sel, bufp<uint32_t>(ctx, B_CSIZE), align, (double2 *)out->mag.p,
-                                   (uint32_t *)out->size.p, (uint64_t *)out->begin.p, bufp<uint64_t>(ctx, B_SCHILD)},
-                                  bufp<uint32_t>(ctx, B_KEEPCAND)};
-        prim::k_compact_layout<cand_keep_layout, true><<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
-            kl, ctx->d_words + W_NCAND, ctx->d_words + W_NS, ctx->d_words + W_OUTBYTES, (uint64_t *)out->begin.p,
-            d_maxnorm, lbc, lbb, lbt, pb1);
-        QD_TRY(launched(ctx));
-        end_stage(4);
-    }
+        // ---- stage 2: collision table (src/quids.hpp:726-809)
+        begin_stage(2);
+        prim::table tb{bufp<prim::table_slot>(ctx, B_KEYS), bufp<unsigned long long>(ctx, B_ACC), M, probe_limit(prm)};
+        {  // table slots free, the extra slot's sum, the group marks, the look-back chains of stages 3-4
+            fill_set f{};
+            f.p[0] = (unsigned char *)tb.slots, f.n[0] = (M + 1) * sizeof(prim::table_slot), f.v[0] = 0xff;
+            f.p[1] = (unsigned char *)(tb.acc + 4 * M), f.n[1] = 4 * sizeof(uint64_t), f.v[1] = 0;
+            f.p[2] = bufp<unsigned char>(ctx, B_NOTREP), f.n[2] = NC, f.v[2] = 0;
+            f.p[3] = bufp<unsigned char>(ctx, B_HASJOIN), f.n[3] = NC, f.v[3] = 0;
+            f.p[4] = bufp<unsigned char>(ctx, B_LOOKBACK), f.n[4] = 4 * (tiles_nc + 2) * sizeof(uint64_t), f.v[4] = 0;
+            f.count = 5;
+            QD_TRY(fill(ctx, f));
+        }
+        uint8_t *not_rep = bufp<uint8_t>(ctx, B_NOTREP), *has_join = bufp<uint8_t>(ctx, B_HASJOIN);
+        const unsigned long long *d_maxabs = (const unsigned long long *)(ctx->d_words + W_MAXABS);
+        {
+            direct_src src{bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG)};
+            prim::k_table_claim<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
+                tb, src, ctx->d_words + W_NC, bufp<uint32_t>(ctx, B_SLOT), err);
+            prim::k_table_accumulate<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
+                tb, src, bufp<uint32_t>(ctx, B_SLOT), ctx->d_words + W_NC, d_maxabs, not_rep, has_join);
+            QD_TRY(launched(ctx, 2));
+        }
+        end_stage(2);
+
+        // ---- stage 3 (+4): representatives above tolerance (src/quids.hpp:819-823),
+        // truncation (src/quids.hpp:866-900, ties by lower child index) and the
+        // output layout (src/quids.hpp:927-948), with the largest survivor norm
+        group_view gv{bufp<uint32_t>(ctx, B_SLOT), not_rep, has_join, bufp<double2>(ctx, B_CMAG),
+                      bufp<unsigned long long>(ctx, B_ACC), ctx->d_words + W_NC, d_maxabs, prm.tolerance};
+        begin_stage(3);
+        if (!may_truncate) {
+            prim::lookback lbc, lbb;
+            lookback_view(ctx, NC, 0, lbc);
+            lookback_view(ctx, NC, 1, lbb);
+            groups_layout f{gv, bufp<uint32_t>(ctx, B_CSIZE), align, (double2 *)out->mag.p, (uint32_t *)out->size.p,
+                            (uint64_t *)out->begin.p, bufp<uint64_t>(ctx, B_SCHILD)};
+            prim::k_compact_layout<groups_layout, false><<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
+                f, ctx->d_words + W_NC, ctx->d_words + W_NS, ctx->d_words + W_OUTBYTES, (uint64_t *)out->begin.p,
+                d_maxnorm, lbc, lbb, lbb, pb1);
+            QD_TRY(launched(ctx));
+            end_stage(3);
+        } else {
+            uint64_t *gkey = bufp<uint64_t>(ctx, B_UNORM);  // per child: its group's truncation key, or 0
+            k_group_keys<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
+                gv, tk, ctx->d_words + W_NC, gkey, (unsigned long long *)(ctx->d_words + W_NU));
+            QD_TRY(launched(ctx));
+            end_stage(3);
+            begin_stage(4);
+            QD_TRY(ensure(ctx->buf[B_SELCAND], filter_cap(NC) * sizeof(uint64_t)));
+            QD_TRY(radix_select_filtered(ctx, ctx->d_words + W_NC, NC, maxc, key_direct{gkey},
+                                         bufp<uint64_t>(ctx, B_SELCAND), filter_cap(NC), ctx->d_words + W_NU));
+            prim::lookback lbc, lbb, lbt;
+            lookback_view(ctx, NC, 0, lbt);
+            lookback_view(ctx, NC, 1, lbc);
+            lookback_view(ctx, NC, 2, lbb);
+            QD_TRY(list_keep_candidates(ctx, keep_candidate{gkey, ctx->d_sel}, NC));
+            const cand_keep_layout kl{{gv, gkey, ctx->d_sel, bufp<uint32_t>(ctx, B_CSIZE), align, (double2 *)out->mag.p,
+                                       (uint32_t *)out->size.p, (uint64_t *)out->begin.p, bufp<uint64_t>(ctx, B_SCHILD)},
+                                      bufp<uint32_t>(ctx, B_KEEPCAND)};
+            prim::k_compact_layout<cand_keep_layout, true><<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
+                kl, ctx->d_words + W_NCAND, ctx->d_words + W_NS, ctx->d_words + W_OUTBYTES, (uint64_t *)out->begin.p,
+                d_maxnorm, lbc, lbb, lbt, pb1);
+            QD_TRY(launched(ctx));
+            end_stage(4);
+        }
+}
     st = wait_words(ctx, pb1.seq);  // host wait 2: survivors and their bytes
     if (st) return st;
     const uint64_t NS = ctx->h_words[W_NS];
-    const uint64_t NU = may_truncate ? ctx->h_words[W_NU] : NS;
+    const uint64_t NU = (pcs || may_truncate) ? ctx->h_words[W_NU] : NS;
     const uint64_t outbytes = ctx->h_words[W_OUTBYTES];
     s.num_object_after_interferences = NU;
     if (NS == 0) return finish(true);

@@ -108,11 +108,10 @@ int simulate_batched_planned(quids_gpu_ctx *ctx, quids_gpu_state *in, const uint
     if constexpr (has_grouped<Rule>::value) grouped = fast;
     if constexpr (has_grouped<Rule>::value) if (grouped) QD_TRY(launch_symbolic_grouped(ctx, rs, pv, NC));
     if (!grouped) {
-        const region_count rc{Mb, 0u, nullptr};
         if (ap.maxsize_lim <= 256) {
-            QD_TRY((launch_symbolic<instance_rules<Rule>, 256>(ctx, rs, pv, NC, fast, rc)));
+            QD_TRY((launch_symbolic<instance_rules<Rule>, 256>(ctx, rs, pv, NC, fast)));
         } else {
-            QD_TRY((launch_symbolic<instance_rules<Rule>, 4096>(ctx, rs, pv, NC, fast, rc)));
+            QD_TRY((launch_symbolic<instance_rules<Rule>, 4096>(ctx, rs, pv, NC, fast)));
         }
     }
 

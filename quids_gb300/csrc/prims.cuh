@@ -551,7 +551,8 @@ __global__ void __launch_bounds__(kMaxTableThreads) k_table_claim(table t, Src s
 // atomicMin compares two members: the larger is marked not_rep, the smaller
 // has_join; at the end the representative is the one member never marked
 // not_rep, and it is marked has_join exactly when its group has more than
-// one member.
+// one member.  With not_rep = has_join = null nothing is marked (the region
+// path reads the marks from the final slots instead).
 template <class Src>
 __global__ void __launch_bounds__(kMaxTableThreads) k_table_accumulate(table t, Src src, uint32_t *slot_of,
                                                                 const uint64_t *d_n,
@@ -567,7 +568,7 @@ __global__ void __launch_bounds__(kMaxTableThreads) k_table_accumulate(table t, 
         slot_of[k] = s;
         const uint32_t c = (uint32_t)src.child(k);
         const uint32_t old = atomicMin(&t.slots[s].rep, c);
-        if (old != 0xffffffffu) {  // slot M starts without a member
+        if (not_rep && old != 0xffffffffu) {  // slot M starts without a member
             not_rep[old > c ? old : c] = 1;
             has_join[old < c ? old : c] = 1;
         }
@@ -581,116 +582,6 @@ __global__ void __launch_bounds__(kMaxTableThreads) k_table_accumulate(table t, 
         }
         fix_atomic_add(&t.acc[4ull * s + 0], re);
         fix_atomic_add(&t.acc[4ull * s + 2], im);
-    }
-}
-
-// ------------------------------------------------------ table regions
-// For tables larger than L2 the children are first grouped by table region
-// (a contiguous range of home slots), so the insert pass works on one region
-// of the table at a time.  region(h) = home(h) * R / M.
-__device__ __forceinline__ uint32_t table_region(uint64_t h, uint64_t m, uint32_t r) {
-    if (h == kEmptyKey) return 0;
-    return (uint32_t)((table_home(h, m) * (uint64_t)r) / m);
-}
-
-constexpr uint32_t kMaxRegions = 2048;
-__host__ __device__ constexpr size_t region_scatter_smem(uint32_t r) { return 4 * ((r + 1) & ~1u) + 8 * (size_t)r; }
-
-// hist[r] += children of table region r (shared-memory counts per block,
-// one global add per block and region)
-static __global__ void __launch_bounds__(kThreads)
-    k_region_hist(const uint64_t *hash, const uint64_t *d_n, uint64_t m, uint32_t r, unsigned int *hist) {
-    extern __shared__ unsigned int s_hist[];  // [r]
-    for (uint32_t i = threadIdx.x; i < r; i += blockDim.x) s_hist[i] = 0;
-    __syncthreads();
-    const uint64_t n = *d_n;
-    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (uint64_t)gridDim.x * blockDim.x)
-        atomicAdd(&s_hist[table_region(hash[k], m, r)], 1u);
-    __syncthreads();
-    for (uint32_t i = threadIdx.x; i < r; i += blockDim.x)
-        if (s_hist[i]) atomicAdd(&hist[i], s_hist[i]);
-}
-
-// roff[r] = exclusive prefix of hist (one block), cursor zeroed
-static __global__ void __launch_bounds__(1024) k_region_offsets(const unsigned int *hist, uint32_t r,
-                                                                 uint64_t *roff, unsigned long long *cursor) {
-    __shared__ uint64_t sm[1024];
-    const uint32_t per = (r + 1023) / 1024;
-    uint64_t sum = 0;
-    for (uint32_t k = 0; k < per; ++k) {
-        uint32_t i = threadIdx.x * per + k;
-        if (i < r) sum += hist[i];
-    }
-    sm[threadIdx.x] = sum;
-    __syncthreads();
-    for (int o = 1; o < 1024; o <<= 1) {  // inclusive scan (Hillis-Steele)
-        uint64_t v = threadIdx.x >= (unsigned)o ? sm[threadIdx.x - o] : 0;
-        __syncthreads();
-        sm[threadIdx.x] += v;
-        __syncthreads();
-    }
-    uint64_t run = threadIdx.x ? sm[threadIdx.x - 1] : 0;
-    for (uint32_t k = 0; k < per; ++k) {
-        uint32_t i = threadIdx.x * per + k;
-        if (i < r) {
-            roff[i] = run;
-            cursor[i] = 0;
-            run += hist[i];
-        }
-    }
-    if (threadIdx.x == 1023) roff[r] = sm[1023];
-}
-
-// Scatters the child records into region order: a block reserves, per
-// region, one range for all its items, then each item takes its rank
-// (warp-aggregated shared atomics).  The order inside a region is
-// unspecified; the insert pass does not depend on it.
-static __global__ void __launch_bounds__(kThreads)
-    k_region_scatter(const uint64_t *hash, const double2 *mag, const uint64_t *d_n, uint64_t m, uint32_t r,
-                     const uint64_t *roff, unsigned long long *cursor, uint64_t *rhash, uint32_t *ridx,
-                     double2 *rmag, int *err) {
-    extern __shared__ unsigned int s_region[];  // counts [r], then 8-byte aligned reserved bases [r]
-    unsigned int *s_cnt = s_region;
-    unsigned long long *s_base = (unsigned long long *)(s_region + ((r + 1) & ~1u));
-    const uint64_t n = *d_n;
-    const int lane = threadIdx.x & 31;
-    const uint64_t ntiles = (n + kTile - 1) / kTile;
-    for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        for (uint32_t i = threadIdx.x; i < r; i += blockDim.x) s_cnt[i] = 0;
-        __syncthreads();
-        const uint64_t base = tile * kTile;
-        uint32_t reg[kItems], rank[kItems];
-#pragma unroll
-        for (int k = 0; k < kItems; ++k) {
-            const uint64_t i = base + threadIdx.x + (uint64_t)k * kThreads;
-            unsigned g = 0xffffffffu;
-            if (i < n) g = table_region(hash[i], m, r);
-            const unsigned same = __match_any_sync(0xffffffffu, g);
-            const int leader = __ffs(same) - 1;
-            unsigned first = 0;
-            if (g != 0xffffffffu && lane == leader) first = atomicAdd(&s_cnt[g], (unsigned)__popc(same));
-            first = __shfl_sync(0xffffffffu, first, leader);
-            reg[k] = g;
-            rank[k] = first + (unsigned)__popc(same & ((1u << lane) - 1));
-        }
-        __syncthreads();
-        for (uint32_t i = threadIdx.x; i < r; i += blockDim.x)
-            if (s_cnt[i]) s_base[i] = roff[i] + atomicAdd(&cursor[i], (unsigned long long)s_cnt[i]);
-        __syncthreads();
-#pragma unroll
-        for (int k = 0; k < kItems; ++k) {
-            const uint64_t i = base + threadIdx.x + (uint64_t)k * kThreads;
-            if (i >= n) break;
-            const uint64_t pos = s_base[reg[k]] + rank[k];
-            if (pos >= roff[reg[k] + 1]) {  // counts disagree with the histogram
-                set_error(err, QUIDS_ERR_CUDA);
-                continue;
-            }
-            rhash[pos] = hash[i];
-            ridx[pos] = (uint32_t)i;
-            rmag[pos] = mag[i];
-        }
-        __syncthreads();
     }
 }
 

@@ -42,7 +42,7 @@ def test_golden_steps(ctx):
     for k, case in enumerate(man["steps"]):
         quids.tolerance, quids.align_byte_length = case["tolerance"], case["align"]
         maxn = int(case["max"])
-        for flags in (0, capi.FLAG_NO_FAST_HASH):
+        for flags in (0, capi.FLAG_NO_FAST_HASH, capi.FLAG_PARTITION):
             b, sy = gpu_step(ctx, packed(z, f"step{k}_in"), case["kind"], case["params"], maxn, flags)
             what = f"{case['name']} flags={flags}"
             assert sy.num_object == case["num_object"], what
@@ -250,8 +250,8 @@ def test_run_gate_list_equals_per_call(ctx):
 
 def test_large_steps(ctx, port):
     """The 8.4M-child Hadamard applications of the 24-qubit circuit against the
-    oracle from identical inputs, with truncation to 2^22; each also with the
-    collision table filled region by region."""
+    oracle from identical inputs, with truncation to 2^22 (exact ties at the
+    cutoff); each with the collision table and with the partitioned stage."""
     from tests.parity import assert_fixed_state_parity
     port.set_globals(1e-18, True, 8)
     gates = [g for layer in W.circuit_layers(0) for g in layer]
@@ -273,11 +273,14 @@ def test_large_steps(ctx, port):
             assert (sy.num_object, sy.num_object_after_interferences) == (nc, nu)
             assert_fixed_state_parity(nxt.download(), b.store(), truncated=nu > (1 << 22), what=f"H{g.params}")
             assert nxt.total_proba == pytest.approx(b.total_proba, rel=1e-12)
-            # the same step with the table filled in region order gives the same state
-            ra, rb, rsy = quids.it_t(ctx, inp), quids.it_t(ctx), quids.sy_it_t()
-            quids.simulate(ra, r, rb, rsy, 1 << 22, flags=capi.FLAG_REGIONS)
-            for u, v in zip(rb.download(), nxt.download()):
-                assert np.array_equal(u, v)
+            # the collision table and the partitioned stage give the same state, bit for bit
+            for fl in (capi.FLAG_TABLE, capi.FLAG_PARTITION):
+                ra, rb, rsy = quids.it_t(ctx, inp), quids.it_t(ctx), quids.sy_it_t()
+                quids.simulate(ra, r, rb, rsy, 1 << 22, flags=fl)
+                assert (rsy.num_object, rsy.num_object_after_interferences) == (nc, nu)
+                for u, v in zip(rb.download(), nxt.download()):
+                    assert np.array_equal(u, v)
+                assert rb.total_proba == nxt.total_proba
             checked += 1
             if checked == 3:
                 break
@@ -437,3 +440,37 @@ def test_observables(ctx):
     q = quids.it_t(ctx, W.pack([bytes([1, 0, 1]), bytes([0, 1, 1])], [0.6, 0.8j], 8))
     assert quids.average_value(q, quids.OBS_QC_BIT, bit=0) == pytest.approx(0.36)
     assert quids.average_value(q, quids.OBS_QC_BIT, bit=2) == pytest.approx(1.0)
+
+
+@pytest.mark.parametrize("simple", [True, False])
+@pytest.mark.parametrize("maxn", [U64_MAX, 3000, 700])
+def test_partitioned_collisions_equal_table(ctx, simple, maxn):
+    """The partitioned collision stage (per-block shared-memory tables, a
+    child-indexed bitmap for the order) and the open-addressing table give
+    the same steps bit for bit: QCGD trajectories with and without
+    truncation, simple and probabilistic, plus a Hadamard layer with massive
+    exact ties at the cutoff."""
+    quids.simple_truncation = simple
+    quids.truncation_seed = 11
+    try:
+        ops = [quids.rule_from(g.kind == "rule", g.code, g.params) for g in W.qcgd_step_rules() * 2]
+        runs = []
+        for fl in (capi.FLAG_TABLE | capi.FLAG_NO_PLAN, capi.FLAG_PARTITION | capi.FLAG_NO_PLAN):
+            fin, st = quids.run(quids.it_t(ctx, W.qcgd_single_state(9, seed=4)), quids.it_t(ctx), ops, maxn, fl)
+            runs.append((fin.download(), [(x["num_object"], x["num_object_after_interferences"],
+                                           x["num_object_out"]) for x in st], fin.total_proba))
+        assert runs[0][1] == runs[1][1]
+        for u, v in zip(runs[0][0], runs[1][0]):
+            assert np.array_equal(u, v)
+        assert runs[0][2] == runs[1][2]
+        gates = [g for layer in W.circuit_layers(0)[:3] for g in layer]
+        hops = [quids.rule_from(g.kind == "rule", g.code, g.params) for g in gates]
+        outs = []
+        for fl in (capi.FLAG_TABLE | capi.FLAG_NO_PLAN, capi.FLAG_PARTITION | capi.FLAG_NO_PLAN):
+            fin, _ = quids.run(quids.it_t(ctx, W.qc_zero_state(24)), quids.it_t(ctx), hops, maxn, fl)
+            outs.append(fin.download())
+        for u, v in zip(*outs):
+            assert np.array_equal(u, v)
+    finally:
+        quids.simple_truncation = True
+        quids.truncation_seed = 0
