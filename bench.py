@@ -263,24 +263,28 @@ def stage_bytes(st):
     sbar_p = sp / NP if NP else 0
     sbar_c = st["out_bytes"] / NS if NS else 0
     M = st["table_capacity"]
-    if st.get("_regions"):   # scatter (24 in, 28 out), insert (28 in, 4 out); mark (8 in, 17 out per rep); flags + gathers
-        s2 = 8.0 * M + 84.0 * NC
-        s3 = 9.0 * NC + 17.0 * NU
-    else:         # insert (24 in, 4 out); per child slot + rep, per rep its sum
-        s2 = 8.0 * M + 28.0 * NC
-        s3 = 8.0 * NC + 32.0 * NU
     out_layout = 56.0 * NS  # gathered magnitude and size, written magnitude, size, offset, child index
     trunc = NU > NS
-    return {
+    base = {
         0: 12.0 * st["num_parents"] + 8.0 * NP + sp,                   # num_child: sizes/begins/bytes, offsets
         1: sp + 36.0 * NP + 28.0 * NC,                                  # symbolic: parents in, 28 B/child out
-        2: s2,
-        3: s3 + (40.0 * NU if trunc else out_layout),
-        4: (8.0 * NU + 40.0 * NU + out_layout) if trunc else 0.0,       # select (first pass), keep + layout
         5: 16.0 * NS,                                                   # exact total: survivor magnitudes
         6: NS * (sbar_p + sbar_c + 48.0),                               # populate + normalise magnitudes
         7: 0.0,
     }
+    if M == 0 and NC:
+        # partitioned stage (stages 2-4 in one): each child's hash and
+        # magnitude read once, each group's record (key, representative,
+        # magnitude) written and read once, the survivors laid out
+        base.update({2: 24.0 * NC + 56.0 * NU + out_layout, 3: 0.0, 4: 0.0})
+        return base
+    # collision table: insert (24 in, 4 out); per child slot + rep, per rep its sum
+    base.update({
+        2: 8.0 * M + 28.0 * NC,
+        3: 8.0 * NC + 32.0 * NU + (40.0 * NU if trunc else out_layout),
+        4: (8.0 * NU + 40.0 * NU + out_layout) if trunc else 0.0,       # select (first pass), keep + layout
+    })
+    return base
 
 
 def ours(args, rank, world):
@@ -368,7 +372,7 @@ def ours(args, rank, world):
             stage_t[k] += st["stage_ms"][k]
             stage_b[k] += sb[k]
     dom = max(range(8), key=lambda k: stage_t[k])
-    names = ["num_child+offsets", "symbolic", "collision_table", "group_compaction+layout",
+    names = ["num_child+offsets", "symbolic", "collisions", "group_compaction+layout",
              "truncation+layout", "total_proba", "finalize_populate+normalize", "unused"]
     peak, peak_kind = peaks()
     achieved = stage_b[dom] / (stage_t[dom] / 1e3) / 1e9 if stage_t[dom] > 0 else 0.0

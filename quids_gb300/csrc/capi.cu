@@ -161,6 +161,7 @@ bool make_plan(run_plan &p, const quids_gpu_step_stats *st, uint64_t n_rules, co
         ap.nc_cap = pad(s.num_object);
         if (ap.nc_cap >= 0xffffffffull || (double)ap.nc_cap / load + 2 >= (double)0x7ffffff0ull) return false;
         ap.may_truncate = s.num_object > prm.max_num_object;
+        ap.partition = use_partition(prm, ap.nc_cap);
         ap.ns_cap = ap.may_truncate ? std::min<uint64_t>(prm.max_num_object, ap.nc_cap) : ap.nc_cap;
         ap.bytes_cap = pad(s.out_bytes) + 4096;
         ap.maxsize_lim = s.max_child_size <= 256 ? 256 : 4096;

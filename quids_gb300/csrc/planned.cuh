@@ -48,6 +48,7 @@ struct app_plan {
     uint64_t maxsize_lim;  // child size bound of the generic symbolic pass (256 or 4096)
     uint64_t maxsize;      // the recorded child size bound (the populate stages objects above kStageMin)
     bool may_truncate;     // the step takes the truncation path (select, then keep + layout)
+    bool partition = false;  // collisions by partition (collide.cuh), else the table
 };
 
 // A plan: the op list and knobs it was made for, the two state handles, and
@@ -180,6 +181,7 @@ __device__ __forceinline__ void plan_sizes(uint64_t *words, uint32_t app, uint64
         words[W_NP] = 0;
         nc = 0;
     }
+    if (!acc) return;  // collisions by partition: no table
     uint64_t m = (uint64_t)((double)nc / load) + 1;
     if (m < 1024) m = 1024;
     words[W_M] = m;
@@ -275,18 +277,24 @@ inline int ensure_planned(quids_gpu_ctx *ctx, quids_gpu_state *out, const app_pl
     QD_TRY(ensure(ctx->buf[B_HASH], NC * sizeof(uint64_t)));
     QD_TRY(ensure(ctx->buf[B_CMAG], NC * sizeof(double2)));
     QD_TRY(ensure(ctx->buf[B_CSIZE], NC * sizeof(uint32_t)));
-    QD_TRY(ensure(ctx->buf[B_SLOT], NC * sizeof(uint32_t)));
     QD_TRY(ensure(ctx->buf[B_CPAR], NC * sizeof(uint32_t)));
-    QD_TRY(ensure(ctx->buf[B_NOTREP], NC));
-    QD_TRY(ensure(ctx->buf[B_HASJOIN], NC));
-    QD_TRY(ensure(ctx->buf[B_KEYS], (M + 1) * sizeof(prim::table_slot)));
-    QD_TRY(ensure(ctx->buf[B_ACC], 4 * (M + 1) * sizeof(uint64_t)));
     QD_TRY(ensure(ctx->buf[B_SCHILD], NS * sizeof(uint64_t)));
-    if (ap.may_truncate) {
-        QD_TRY(ensure(ctx->buf[B_SELCAND], filter_cap(NC) * sizeof(uint64_t)));
-        QD_TRY(ensure(ctx->buf[B_UNORM], NC * sizeof(uint64_t)));
-        QD_TRY(ensure(ctx->buf[B_KEEPCAND], NC * sizeof(uint32_t)));
-        QD_TRY(ensure(ctx->buf[B_TILECNT], tilecnt_bytes(NC)));
+    if (ap.may_truncate) QD_TRY(ensure(ctx->buf[B_SELCAND], filter_cap(NC) * sizeof(uint64_t)));
+    if (ap.partition) {
+        QD_TRY(pcs_ensure(ctx, NC, ap.may_truncate));
+        QD_CUDA(cudaFuncSetAttribute(k_pcs_group, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)pcs_smem_bytes()));
+    } else {
+        QD_TRY(ensure(ctx->buf[B_SLOT], NC * sizeof(uint32_t)));
+        QD_TRY(ensure(ctx->buf[B_NOTREP], NC));
+        QD_TRY(ensure(ctx->buf[B_HASJOIN], NC));
+        QD_TRY(ensure(ctx->buf[B_KEYS], (M + 1) * sizeof(prim::table_slot)));
+        QD_TRY(ensure(ctx->buf[B_ACC], 4 * (M + 1) * sizeof(uint64_t)));
+        if (ap.may_truncate) {
+            QD_TRY(ensure(ctx->buf[B_UNORM], NC * sizeof(uint64_t)));
+            QD_TRY(ensure(ctx->buf[B_KEEPCAND], NC * sizeof(uint32_t)));
+            QD_TRY(ensure(ctx->buf[B_TILECNT], tilecnt_bytes(NC)));
+        }
     }
     QD_TRY(ensure(ctx->buf[B_MODSTATUS], sizeof(uint64_t)));
     auto grow = [&](qd_dbuf &b, size_t bytes) { return keep ? ensure_keep(b, bytes, ctx->stream) : ensure(b, bytes); };
@@ -336,7 +344,7 @@ int simulate_planned(quids_gpu_ctx *ctx, quids_gpu_state *in, const uint64_t *in
         lookback_view(ctx, N, 1, lb);
         scan_nchild f{bufp<uint32_t>(ctx, B_NCHILD), nullptr};
         const plan_sizes_hook hook{words, app, ap.nc_cap, ap.maxsize_lim, ap.may_truncate ? ~0ull : maxn, load,
-                                   bufp<unsigned long long>(ctx, B_ACC)};
+                                   ap.partition ? nullptr : bufp<unsigned long long>(ctx, B_ACC)};
         prim::k_scan_excl<<<lookback_grid(ctx, N), prim::kThreads, 0, ctx->stream>>>(
             f, words + W_NP, bufp<uint64_t>(ctx, B_CBEGIN), words + W_NC, lb,
             tile_parents_epilogue{bufp<uint64_t>(ctx, B_TILEPAR), sym_tiles + 2}, hook_counter(ctx, W_DONE_SCAN),
@@ -358,68 +366,74 @@ int simulate_planned(quids_gpu_ctx *ctx, quids_gpu_state *in, const uint64_t *in
         }
     }
 
-    // ---- stage 2: collision table, sized on the device
-    const uint64_t tiles_nc = (NC + prim::kTile - 1) / prim::kTile;
-    prim::table tb{bufp<prim::table_slot>(ctx, B_KEYS), bufp<unsigned long long>(ctx, B_ACC), Mb, probe_limit(prm),
-                   words + W_M};
-    {
-        fill_set f{};
-        f.p[0] = (unsigned char *)tb.slots, f.n[0] = (Mb + 1) * sizeof(prim::table_slot), f.v[0] = 0xff;
-        f.dn[0] = words + W_M, f.mul[0] = sizeof(prim::table_slot), f.add[0] = sizeof(prim::table_slot);
-        f.p[1] = bufp<unsigned char>(ctx, B_NOTREP), f.n[1] = NC, f.v[1] = 0;
-        f.dn[1] = words + W_NC, f.mul[1] = 1, f.add[1] = 0;
-        f.p[2] = bufp<unsigned char>(ctx, B_HASJOIN), f.n[2] = NC, f.v[2] = 0;
-        f.dn[2] = words + W_NC, f.mul[2] = 1, f.add[2] = 0;
-        f.p[3] = bufp<unsigned char>(ctx, B_LOOKBACK), f.n[3] = 4 * (tiles_nc + 2) * sizeof(uint64_t), f.v[3] = 0;
-        f.count = 4;
-        QD_TRY(fill(ctx, f));
-    }
-    uint8_t *not_rep = bufp<uint8_t>(ctx, B_NOTREP), *has_join = bufp<uint8_t>(ctx, B_HASJOIN);
-    const unsigned long long *d_maxabs = (const unsigned long long *)(words + W_MAXABS);
-    {
-        direct_src src{bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG)};
-        prim::k_table_claim<<<grid_for(ctx, NC), ctx->tune.table_block, 0, ctx->stream>>>(tb, src, words + W_NC,
-                                                                                   bufp<uint32_t>(ctx, B_SLOT), err);
-        prim::k_table_accumulate<<<grid_for(ctx, NC), ctx->tune.table_block, 0, ctx->stream>>>(
-            tb, src, bufp<uint32_t>(ctx, B_SLOT), words + W_NC, d_maxabs, not_rep, has_join);
-        QD_TRY(launched(ctx, 2));
-    }
-
-    // ---- stages 3-4: groups above tolerance, truncation, output layout
-    group_view gv{bufp<uint32_t>(ctx, B_SLOT), not_rep, has_join, bufp<double2>(ctx, B_CMAG),
-                  bufp<unsigned long long>(ctx, B_ACC), words + W_NC, d_maxabs, prm.tolerance};
     const uint32_t align = prm.align_byte_length;
     unsigned long long *d_maxnorm = (unsigned long long *)(words + W_MAXNORM);
     const plan_end_hook end_hook{words, app, ap.bytes_cap, ap.may_truncate, (uint64_t *)out->meta.p, rec};
-    if (!ap.may_truncate) {
-        prim::lookback lbc, lbb;
-        lookback_view(ctx, NC, 0, lbc);
-        lookback_view(ctx, NC, 1, lbb);
-        groups_layout f{gv, bufp<uint32_t>(ctx, B_CSIZE), align, (double2 *)out->mag.p, (uint32_t *)out->size.p,
-                        (uint64_t *)out->begin.p, bufp<uint64_t>(ctx, B_SCHILD)};
-        prim::k_compact_layout<groups_layout, false><<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
-            f, words + W_NC, words + W_NS, words + W_OUTBYTES, (uint64_t *)out->begin.p, d_maxnorm, lbc, lbb, lbb,
-            hook_counter(ctx, W_DONE_LAYOUT), end_hook);
-        QD_TRY(launched(ctx));
+    if (ap.partition) {
+        // ---- stages 2-4 by partition, counts on the device
+        QD_TRY(pcs_stage(ctx, NC, ap.may_truncate, maxn, tk, prm.tolerance, align, out,
+                         hook_counter(ctx, W_DONE_LAYOUT), end_hook));
     } else {
-        uint64_t *gkey = bufp<uint64_t>(ctx, B_UNORM);  // per child: its group's truncation key, or 0
-        k_group_keys<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(gv, tk, words + W_NC, gkey,
-                                                                           (unsigned long long *)(words + W_NU));
-        QD_TRY(launched(ctx));
-        QD_TRY(radix_select_filtered(ctx, words + W_NC, NC, maxn, key_direct{gkey}, bufp<uint64_t>(ctx, B_SELCAND),
-                                     filter_cap(NC), words + W_NU));
-        prim::lookback lbc, lbb, lbt;
-        lookback_view(ctx, NC, 0, lbt);
-        lookback_view(ctx, NC, 1, lbc);
-        lookback_view(ctx, NC, 2, lbb);
-        QD_TRY(list_keep_candidates(ctx, keep_candidate{gkey, ctx->d_sel}, NC));
-        const cand_keep_layout kl{{gv, gkey, ctx->d_sel, bufp<uint32_t>(ctx, B_CSIZE), align, (double2 *)out->mag.p,
-                                   (uint32_t *)out->size.p, (uint64_t *)out->begin.p, bufp<uint64_t>(ctx, B_SCHILD)},
-                                  bufp<uint32_t>(ctx, B_KEEPCAND)};
-        prim::k_compact_layout<cand_keep_layout, true, plan_end_hook><<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
-            kl, words + W_NCAND, words + W_NS, words + W_OUTBYTES, (uint64_t *)out->begin.p, d_maxnorm, lbc, lbb, lbt,
-            hook_counter(ctx, W_DONE_LAYOUT), end_hook);
-        QD_TRY(launched(ctx));
+        // ---- stage 2: collision table, sized on the device
+        const uint64_t tiles_nc = (NC + prim::kTile - 1) / prim::kTile;
+        prim::table tb{bufp<prim::table_slot>(ctx, B_KEYS), bufp<unsigned long long>(ctx, B_ACC), Mb, probe_limit(prm),
+                       words + W_M};
+        {
+            fill_set f{};
+            f.p[0] = (unsigned char *)tb.slots, f.n[0] = (Mb + 1) * sizeof(prim::table_slot), f.v[0] = 0xff;
+            f.dn[0] = words + W_M, f.mul[0] = sizeof(prim::table_slot), f.add[0] = sizeof(prim::table_slot);
+            f.p[1] = bufp<unsigned char>(ctx, B_NOTREP), f.n[1] = NC, f.v[1] = 0;
+            f.dn[1] = words + W_NC, f.mul[1] = 1, f.add[1] = 0;
+            f.p[2] = bufp<unsigned char>(ctx, B_HASJOIN), f.n[2] = NC, f.v[2] = 0;
+            f.dn[2] = words + W_NC, f.mul[2] = 1, f.add[2] = 0;
+            f.p[3] = bufp<unsigned char>(ctx, B_LOOKBACK), f.n[3] = 4 * (tiles_nc + 2) * sizeof(uint64_t), f.v[3] = 0;
+            f.count = 4;
+            QD_TRY(fill(ctx, f));
+        }
+        uint8_t *not_rep = bufp<uint8_t>(ctx, B_NOTREP), *has_join = bufp<uint8_t>(ctx, B_HASJOIN);
+        const unsigned long long *d_maxabs = (const unsigned long long *)(words + W_MAXABS);
+        {
+            direct_src src{bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG)};
+            prim::k_table_claim<<<grid_for(ctx, NC), ctx->tune.table_block, 0, ctx->stream>>>(tb, src, words + W_NC,
+                                                                                       bufp<uint32_t>(ctx, B_SLOT), err);
+            prim::k_table_accumulate<<<grid_for(ctx, NC), ctx->tune.table_block, 0, ctx->stream>>>(
+                tb, src, bufp<uint32_t>(ctx, B_SLOT), words + W_NC, d_maxabs, not_rep, has_join);
+            QD_TRY(launched(ctx, 2));
+        }
+
+        // ---- stages 3-4: groups above tolerance, truncation, output layout
+        group_view gv{bufp<uint32_t>(ctx, B_SLOT), not_rep, has_join, bufp<double2>(ctx, B_CMAG),
+                      bufp<unsigned long long>(ctx, B_ACC), words + W_NC, d_maxabs, prm.tolerance};
+        if (!ap.may_truncate) {
+            prim::lookback lbc, lbb;
+            lookback_view(ctx, NC, 0, lbc);
+            lookback_view(ctx, NC, 1, lbb);
+            groups_layout f{gv, bufp<uint32_t>(ctx, B_CSIZE), align, (double2 *)out->mag.p, (uint32_t *)out->size.p,
+                            (uint64_t *)out->begin.p, bufp<uint64_t>(ctx, B_SCHILD)};
+            prim::k_compact_layout<groups_layout, false><<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
+                f, words + W_NC, words + W_NS, words + W_OUTBYTES, (uint64_t *)out->begin.p, d_maxnorm, lbc, lbb, lbb,
+                hook_counter(ctx, W_DONE_LAYOUT), end_hook);
+            QD_TRY(launched(ctx));
+        } else {
+            uint64_t *gkey = bufp<uint64_t>(ctx, B_UNORM);  // per child: its group's truncation key, or 0
+            k_group_keys<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(gv, tk, words + W_NC, gkey,
+                                                                               (unsigned long long *)(words + W_NU));
+            QD_TRY(launched(ctx));
+            QD_TRY(radix_select_filtered(ctx, words + W_NC, NC, maxn, key_direct{gkey}, bufp<uint64_t>(ctx, B_SELCAND),
+                                         filter_cap(NC), words + W_NU));
+            prim::lookback lbc, lbb, lbt;
+            lookback_view(ctx, NC, 0, lbt);
+            lookback_view(ctx, NC, 1, lbc);
+            lookback_view(ctx, NC, 2, lbb);
+            QD_TRY(list_keep_candidates(ctx, keep_candidate{gkey, ctx->d_sel}, NC));
+            const cand_keep_layout kl{{gv, gkey, ctx->d_sel, bufp<uint32_t>(ctx, B_CSIZE), align, (double2 *)out->mag.p,
+                                       (uint32_t *)out->size.p, (uint64_t *)out->begin.p, bufp<uint64_t>(ctx, B_SCHILD)},
+                                      bufp<uint32_t>(ctx, B_KEEPCAND)};
+            prim::k_compact_layout<cand_keep_layout, true, plan_end_hook><<<lookback_grid(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
+                kl, words + W_NCAND, words + W_NS, words + W_OUTBYTES, (uint64_t *)out->begin.p, d_maxnorm, lbc, lbb, lbt,
+                hook_counter(ctx, W_DONE_LAYOUT), end_hook);
+            QD_TRY(launched(ctx));
+        }
     }
 
     // ---- stage 5: exact total probability, into the output state
