@@ -474,3 +474,23 @@ def test_partitioned_collisions_equal_table(ctx, simple, maxn):
     finally:
         quids.simple_truncation = True
         quids.truncation_seed = 0
+
+
+def test_partitioned_collisions_in_planned_runs(ctx):
+    """Repeated runs with the partitioned stage: synchronous, planned (sizes
+    on the device) and replayed as a CUDA graph, all equal to the table's
+    synchronous steps bit for bit."""
+    ops = [quids.rule_from(g.kind == "rule", g.code, g.params) for g in W.qcgd_step_rules() * 2]
+    init = W.qcgd_single_state(9, seed=4)
+    ref, ref_st = quids.run(quids.it_t(ctx, init), quids.it_t(ctx), ops, 2000, capi.FLAG_TABLE | capi.FLAG_NO_PLAN)
+    ref = ref.download()
+    a, b = quids.it_t(ctx), quids.it_t(ctx)
+    counts0 = ctx.run_counts()
+    for _ in range(4):
+        a.upload(init)
+        fin, st = quids.run(a, b, ops, 2000, capi.FLAG_PARTITION)
+        assert [x["num_object_out"] for x in st] == [x["num_object_out"] for x in ref_st]
+        for u, v in zip(fin.download(), ref):
+            assert np.array_equal(u, v)
+    counts = {k: v - counts0[k] for k, v in ctx.run_counts().items()}
+    assert counts["planned"] >= 2 and counts["graph"] >= 1, counts
