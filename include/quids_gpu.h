@@ -110,12 +110,10 @@ typedef struct quids_gpu_params {
 #define QUIDS_FLAG_NO_FAST_HASH 1u   /* hash children through populate_child + hasher, not hash_child */
 #define QUIDS_FLAG_STAGE_TIMING 2u   /* record per-stage CUDA events and synchronise at the end of the
                                         step, so stats carries timings and total_proba */
-#define QUIDS_FLAG_TABLE 4u          /* group colliding children in the open-addressing table in device memory even
-                                        where the partitioned stage would run (the batched form and the adjoint's
-                                        forward always use the table) */
-#define QUIDS_FLAG_PARTITION 8u      /* group colliding children by partition into per-block shared-memory tables
-                                        even for a small step (by default only steps whose table would hold 512 MB
-                                        or more); both give the same result bits */
+#define QUIDS_FLAG_TABLE 4u          /* group colliding children in the open-addressing table in device memory
+                                        (the default; the batched form and the adjoint's forward always use it) */
+#define QUIDS_FLAG_PARTITION 8u      /* one-pass steps group colliding children by partition into per-block
+                                        shared-memory tables instead (collide.cuh); the same result bits */
 #define QUIDS_FLAG_NO_PLAN 16u       /* quids_gpu_run: always the synchronous steps (no planned run, no graph) */
 #define QUIDS_FLAG_AUTOTUNE 32u      /* quids_gpu_run / quids_gpu_run_batched: before a planned run is first captured
                                         as a CUDA graph, time it under several launch configurations (collision-table

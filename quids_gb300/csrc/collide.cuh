@@ -516,7 +516,8 @@ inline int pcs_stage(quids_gpu_ctx *ctx, uint64_t nc_bound, bool truncating, uin
         bufp<double2>(ctx, B_CMAG), err);
     QD_TRY(launched(ctx, 3));
     const size_t smem = pcs_smem_bytes();
-    QD_CUDA(cudaFuncSetAttribute(k_pcs_group, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (!g_alloc_frozen)  // (a planned run sets it before its capture)
+        QD_CUDA(cudaFuncSetAttribute(k_pcs_group, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_pcs_group<<<(unsigned)std::min<uint64_t>(b.nb, gblocks), kPcsThreads, smem, ctx->stream>>>(
         bufp<uint64_t>(ctx, B_HASH), b.fidx, bufp<double2>(ctx, B_CMAG), b.boff, (uint32_t)b.nb, words + W_NC,
         (const unsigned long long *)(words + W_MAXABS), tolerance, tk, b.scratch, b.groups,

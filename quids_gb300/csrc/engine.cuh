@@ -278,15 +278,10 @@ inline T *bufp(quids_gpu_ctx *ctx, qd_buf_id id) {
 // collision-table probe limit of a step (quids_gpu_params::max_probes)
 inline uint32_t probe_limit(const quids_gpu_params &prm) { return prm.max_probes ? prm.max_probes : 65536u; }
 
-// A one-pass step groups its children by partition (collide.cuh) when its
-// open-addressing table (16-byte slots at load 1/2) would hold 512 MB or
-// more, several times what L2 holds; QUIDS_FLAG_TABLE / QUIDS_FLAG_PARTITION
-// force either.
-constexpr double kPartitionMinTableBytes = 512.0 * 1024 * 1024;
-inline bool use_partition(const quids_gpu_params &prm, uint64_t nc) {
-    if (prm.flags & QUIDS_FLAG_TABLE) return false;
-    if (prm.flags & QUIDS_FLAG_PARTITION) return true;
-    return 32.0 * (double)nc >= kPartitionMinTableBytes;
+// A one-pass step groups its children by partition (collide.cuh) when
+// QUIDS_FLAG_PARTITION asks for it, else in the open-addressing table.
+inline bool use_partition(const quids_gpu_params &prm, uint64_t) {
+    return (prm.flags & QUIDS_FLAG_PARTITION) && !(prm.flags & QUIDS_FLAG_TABLE);
 }
 
 // Blocks of `kernel` (at `threads` per block, `smem` dynamic shared bytes)
