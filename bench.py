@@ -299,6 +299,7 @@ def ours(args, rank, world):
     ctx = quids.Context(dev)
     stream = torch.cuda.ExternalStream(ctx.stream, device=f"cuda:{dev}")
     flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.int32, device=f"cuda:{dev}")
+    xflags = capi.FLAG_PARTITION if args.collisions == "partition" else 0
 
     init_packed = wl["init"]
     if init_packed is None:  # QCGD: the state after step 0, computed on the GPU
@@ -317,7 +318,7 @@ def ours(args, rank, world):
     # planned runs, captured as a CUDA graph from the third on)
     for _ in range(args.warmup):
         src.upload(init_packed)
-        run_step_gpu(ctx, quids, wl, src, spare=spare, flags=capi.FLAG_AUTOTUNE)
+        run_step_gpu(ctx, quids, wl, src, spare=spare, flags=capi.FLAG_AUTOTUNE | xflags)
     ctx.synchronize()
 
     # timed: device-resident input, L2 flushed before each step (outside the events)
@@ -340,7 +341,7 @@ def ours(args, rank, world):
                 e1 = torch.cuda.Event(enable_timing=True)
                 e0.record(stream)
             torch.cuda.nvtx.range_push("timed_step")  # lets ncu --nvtx-include select the timed launches
-            c, _ = run_step_gpu(ctx, quids, wl, src, spare=spare, flags=capi.FLAG_AUTOTUNE)
+            c, _ = run_step_gpu(ctx, quids, wl, src, spare=spare, flags=capi.FLAG_AUTOTUNE | xflags)
             torch.cuda.nvtx.range_pop()
             with torch.cuda.stream(stream):
                 e1.record(stream)
@@ -359,7 +360,7 @@ def ours(args, rank, world):
         src.upload(init_packed)
         with torch.cuda.stream(stream):
             flush.fill_(1)
-        run_step_gpu(ctx, quids, wl, src, stats, flags=capi.FLAG_STAGE_TIMING, spare=spare)
+        run_step_gpu(ctx, quids, wl, src, stats, flags=capi.FLAG_STAGE_TIMING | xflags, spare=spare)
     ctx.synchronize()
     value, total_ms = job_value(children, sum(ms), world, dev)
 
@@ -402,7 +403,7 @@ def ours(args, rank, world):
         e2e_children = 0
         for _ in range(args.steps):
             src.upload(h_in)
-            c, out = run_step_gpu(ctx, quids, wl, src, spare=spare, flags=capi.FLAG_AUTOTUNE)
+            c, out = run_step_gpu(ctx, quids, wl, src, spare=spare, flags=capi.FLAG_AUTOTUNE | xflags)
             e2e_children += c
             capi.check(ctx.lib.quids_gpu_state_download(out.h, h_out[0].data_ptr(), h_out[1].data_ptr(),
                                                         h_out[2].data_ptr(), h_out[3].data_ptr()), "download")
@@ -428,7 +429,7 @@ def ours(args, rank, world):
             "data": "synthetic (seeded generators; the reference publishes no dataset)",
             "config": dict(wl["config"], parallelism=f"replicas x{world}",
                            l2="flushed before every step (256 MiB write)",
-                           children_per_step=children // args.steps,
+                           children_per_step=children // args.steps, collisions=args.collisions,
                            runs_timed=runs, autotuned=ctx.last_tuning()),
             "e2e": e2e,
             "gpu_launches": int(launches),
@@ -877,6 +878,9 @@ def main():
     ap.add_argument("--config", default="qcgd12", choices=["circuit24", "qcgd12", "qcgd10", "qcgd12s2", "batch256",
                                                               "adjoint10"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--collisions", default="table", choices=["table", "partition"],
+                    help="collision elimination of the plain steps: the open-addressing table (default) or the "
+                         "partitioned stage (QUIDS_FLAG_PARTITION)")
     ap.add_argument("--no-extras", dest="extras", action="store_false",
                     help="qcgd12 line without the batched-vs-plain and adjoint-vs-forward ratios")
     args = ap.parse_args()
