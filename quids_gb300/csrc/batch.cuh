@@ -660,11 +660,11 @@ int simulate_batched(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule *rules_
     k_binst_factors<<<(G + 255) / 256, 256, 0, ctx->stream>>>(tot, G, obegin, maxn, (double *)out->inst_total.p,
                                                              bufp<double>(ctx, B_BFACTOR));
     QD_TRY(launched(ctx, 4));
-    k_populate<instance_rules<Rule>, schild_source, no_post><<<grid_for(ctx, NS), prim::kThreads, 0, ctx->stream>>>(
-        rs, pv, schild_source{bufp<uint64_t>(ctx, B_SCHILD), bufp<uint32_t>(ctx, B_CPAR), pv.cbeg}, ctx->d_words + W_NS,
+    QD_TRY(launch_populate_kernel(
+        ctx, NS, maxsize > kStageMin, rs, pv,
+        schild_source{bufp<uint64_t>(ctx, B_SCHILD), bufp<uint32_t>(ctx, B_CPAR), pv.cbeg}, ctx->d_words + W_NS,
         (const uint64_t *)out->begin.p, (const uint32_t *)out->size.p, (char *)out->objects.p, (double2 *)out->mag.p,
-        bufp<double>(ctx, B_BFACTOR), (const uint32_t *)out->inst.p, err, no_post{}, maxsize > kStageMin);
-    QD_TRY(launched(ctx));
+        bufp<double>(ctx, B_BFACTOR), (const uint32_t *)out->inst.p, err, no_post{}));
     if (inst_stats) {
         k_binst_stats<<<(G + 255) / 256, 256, 0, ctx->stream>>>(bufp<uint64_t>(ctx, B_CBEGIN), pbegin, ubegin,
                                                               (const uint64_t *)out->inst_begin.p, G, d_inst_stats);

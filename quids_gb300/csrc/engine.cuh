@@ -841,18 +841,19 @@ struct pc_source {
 
 // Finalize (src/quids.hpp:958-967): each survivor's bytes by the rule's
 // populate_child_simple, padding zeroed, magnitude normalised (and the fused
-// modifiers applied).  Small objects (a few words) are written by their
-// thread directly: neighbouring threads write neighbouring bytes.  For large
-// objects (`staged`, the step's child size bound above kStageMin bytes) a
-// thread writing its own object would scatter small stores over many lines;
-// instead a block takes a chunk of kPopChunk output bytes at a time, the
-// survivors that start in it are populated into shared memory, and the block
-// writes the chunk's contiguous byte range out with coalesced 16-byte
-// stores.  A range too long for the staging buffer (objects near the
-// 4096-byte bound with a large alignment) is written directly.
-constexpr uint32_t kPopChunk = 32 * 1024;
-constexpr uint32_t kPopStage = kPopChunk + 4096 + 16 + 4096;
+// modifiers applied), one survivor per thread.  Small objects (a few words)
+// are written by their thread directly: neighbouring threads write
+// neighbouring bytes.  For large objects (the step's child size bound above
+// kStageMin bytes) a thread writing its own object would scatter small
+// stores over many lines; instead each warp walks its 32 consecutive
+// survivors in batches that fit its own kPopWarpStage bytes of shared memory
+// (up to 32, one per lane), populates a batch there and writes its
+// contiguous byte range out with coalesced 16-byte stores.  The warps of a
+// block never wait on one another (a block-wide chunk made every warp wait
+// for the block's longest object).
 constexpr uint64_t kStageMin = 64;
+constexpr int kPopWarps = 4;                   // warps per block of the staged form
+constexpr uint32_t kPopWarpStage = 12 * 1024;  // bytes per warp: 4 x 12 KB, the static shared memory limit
 
 template <class RS, class SS, class Post>
 __device__ __forceinline__ void populate_one(const RS &rs, const parents_view &pv, const SS &ss, uint64_t i,
@@ -882,57 +883,81 @@ __device__ __forceinline__ void populate_one(const RS &rs, const parents_view &p
 template <class RS, class SS, class Post>
 __global__ void __launch_bounds__(prim::kThreads)
     k_populate(RS rs, parents_view pv, SS ss, const uint64_t *d_ns, const uint64_t *obegin, const uint32_t *osize,
-               char *objects, double2 *omag, const double *d_factor, const uint32_t *finst, int *err, Post post,
-               bool staged) {
-    __shared__ __align__(16) unsigned char s_out[kPopStage];
-    __shared__ uint64_t s_range[2];
+               char *objects, double2 *omag, const double *d_factor, const uint32_t *finst, int *err, Post post) {
     const uint64_t ns = *d_ns;
     if (ns == 0) return;
     const double f0 = finst ? 1.0 : *d_factor;
-    if (!staged) {
-        for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ns; i += (uint64_t)gridDim.x * blockDim.x)
-            populate_one(rs, pv, ss, i, obegin, osize, objects + obegin[i], omag, d_factor, f0, finst, err, post);
-        return;
-    }
-    const uint64_t total = obegin[ns];
-    const uint64_t nchunks = (total + kPopChunk - 1) / kPopChunk;
-    for (uint64_t ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
-        if (threadIdx.x < 2) {  // the first survivor starting at or after the chunk's start / end
-            const uint64_t t = (ch + threadIdx.x) * (uint64_t)kPopChunk;
-            uint64_t lo = 0, hi = ns;
-            while (lo < hi) {
-                const uint64_t mid = (lo + hi) >> 1;
-                if (obegin[mid] < t) lo = mid + 1; else hi = mid;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ns; i += (uint64_t)gridDim.x * blockDim.x)
+        populate_one(rs, pv, ss, i, obegin, osize, objects + obegin[i], omag, d_factor, f0, finst, err, post);
+}
+
+template <class RS, class SS, class Post>
+__global__ void __launch_bounds__(kPopWarps * 32)
+    k_populate_staged(RS rs, parents_view pv, SS ss, const uint64_t *d_ns, const uint64_t *obegin,
+                      const uint32_t *osize, char *objects, double2 *omag, const double *d_factor,
+                      const uint32_t *finst, int *err, Post post) {
+    __shared__ __align__(16) unsigned char s_stage[kPopWarps][kPopWarpStage];
+    const uint64_t ns = *d_ns;
+    if (ns == 0) return;
+    const double f0 = finst ? 1.0 : *d_factor;
+    const unsigned lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    unsigned char *st = s_stage[w];
+    const uint64_t ngroups = (ns + 31) / 32;
+    for (uint64_t g = (uint64_t)blockIdx.x * kPopWarps + w; g < ngroups; g += (uint64_t)gridDim.x * kPopWarps) {
+        const uint64_t i1 = (g + 1) * 32 < ns ? (g + 1) * 32 : ns;
+        for (uint64_t cur = g * 32; cur < i1;) {
+            // a batch: the longest run of survivors from cur whose bytes fit
+            // the warp's buffer (obegin is nondecreasing: `fits` holds for a
+            // prefix of the lanes)
+            const uint64_t base = obegin[cur];
+            const uint32_t shift = (uint32_t)(base & 15);
+            const uint64_t e = cur + lane + 1;
+            const bool fits = e <= i1 && obegin[e] - base + shift <= kPopWarpStage;
+            const uint32_t k = (uint32_t)__popc(__ballot_sync(0xffffffffu, fits));
+            if (k == 0) {  // one object longer than the buffer: written in place
+                if (lane == 0)
+                    populate_one(rs, pv, ss, cur, obegin, osize, objects + base, omag, d_factor, f0, finst, err, post);
+                ++cur;
+                continue;
             }
-            s_range[threadIdx.x] = lo;
+            if (lane < k)
+                populate_one(rs, pv, ss, cur + lane, obegin, osize, (char *)st + shift + (obegin[cur + lane] - base),
+                             omag, d_factor, f0, finst, err, post);
+            __syncwarp();
+            // st[shift + q] is objects[base + q]: both have the same address modulo 16
+            const uint32_t nbytes = (uint32_t)(obegin[cur + k] - base);
+            const uint32_t head = ((16 - shift) & 15) < nbytes ? ((16 - shift) & 15) : nbytes;
+            const uint32_t body = (nbytes - head) / 16;
+            char *gp = objects + base;
+            if (lane < head) gp[lane] = (char)st[shift + lane];
+            const uint4 *sv = (const uint4 *)(st + shift + head);
+            uint4 *gv = (uint4 *)(gp + head);
+            for (uint32_t q = lane; q < body; q += 32) gv[q] = sv[q];
+            for (uint32_t q = head + body * 16 + lane; q < nbytes; q += 32) gp[q] = (char)st[shift + q];
+            __syncwarp();  // the warp's next batch reuses st
+            cur += k;
         }
-        __syncthreads();
-        const uint64_t i0 = s_range[0], i1 = s_range[1];
-        const uint64_t base = obegin[i0], end = obegin[i1];
-        const uint32_t shift = (uint32_t)(base & 15);
-        if (end - base + shift > kPopStage) {  // too long to stage: each object written in place
-            for (uint64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x)
-                populate_one(rs, pv, ss, i, obegin, osize, objects + obegin[i], omag, d_factor, f0, finst, err, post);
-            __syncthreads();
-            continue;
-        }
-        for (uint64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x)
-            populate_one(rs, pv, ss, i, obegin, osize, (char *)s_out + shift + (obegin[i] - base), omag, d_factor, f0,
-                         finst, err, post);
-        __syncthreads();
-        // s_out[shift + k] is objects[base + k]: both have the same address modulo 16
-        const uint64_t nbytes = end - base;
-        const uint64_t head = ((16 - shift) & 15) < nbytes ? ((16 - shift) & 15) : nbytes;
-        const uint64_t body = (nbytes - head) / 16;
-        char *g = objects + base;
-        if (threadIdx.x < head) g[threadIdx.x] = (char)s_out[shift + threadIdx.x];
-        const uint4 *sv = (const uint4 *)(s_out + shift + head);
-        uint4 *gv = (uint4 *)(g + head);
-        for (uint64_t k = threadIdx.x; k < body; k += blockDim.x) gv[k] = sv[k];
-        const uint64_t tail0 = head + body * 16;
-        for (uint64_t k = tail0 + threadIdx.x; k < nbytes; k += blockDim.x) g[k] = (char)s_out[shift + k];
-        __syncthreads();  // the next chunk reuses s_out
     }
+}
+
+// one populate launch over n (a bound of *d_ns) survivors, staged or direct
+template <class RS, class SS, class Post>
+inline int launch_populate_kernel(quids_gpu_ctx *ctx, uint64_t n, bool staged, const RS &rs, const parents_view &pv,
+                                  const SS &ss, const uint64_t *d_ns, const uint64_t *obegin, const uint32_t *osize,
+                                  char *objects, double2 *omag, const double *d_factor, const uint32_t *finst,
+                                  int *err, const Post &post) {
+    if (staged) {
+        auto kernel = k_populate_staged<RS, SS, Post>;
+        const uint64_t blocks = ((n + 31) / 32 + kPopWarps - 1) / kPopWarps;
+        const uint64_t cap = (uint64_t)ctx->num_sms * resident_per_sm(kernel, kPopWarps * 32);
+        const unsigned grid = (unsigned)(blocks < cap ? (blocks ? blocks : 1) : cap);
+        kernel<<<grid, kPopWarps * 32, 0, ctx->stream>>>(rs, pv, ss, d_ns, obegin, osize, objects, omag, d_factor,
+                                                         finst, err, post);
+    } else {
+        k_populate<RS, SS, Post><<<grid_for(ctx, n), prim::kThreads, 0, ctx->stream>>>(
+            rs, pv, ss, d_ns, obegin, osize, objects, omag, d_factor, finst, err, post);
+    }
+    return launched(ctx);
 }
 
 // every child of every parent, bytes at a fixed stride (rule-level access)
@@ -1421,13 +1446,12 @@ inline int launch_symbolic(quids_gpu_ctx *ctx, const RS &rule, const parents_vie
 template <class RS, class Post>
 inline int launch_populate(quids_gpu_ctx *ctx, const RS &rule, const parents_view &pv, uint64_t ns,
                            quids_gpu_state *out, const Post &post, uint64_t max_child_size) {
-    k_populate<RS, schild_source, Post><<<grid_for(ctx, ns), prim::kThreads, 0, ctx->stream>>>(
-        rule, pv, schild_source{bufp<uint64_t>(ctx, B_SCHILD), bufp<uint32_t>(ctx, B_CPAR), pv.cbeg},
-        ctx->d_words + W_NS, (const uint64_t *)out->begin.p,
-        (const uint32_t *)out->size.p, (char *)out->objects.p, (double2 *)out->mag.p,
-        (const double *)(ctx->d_words + W_FACTOR), nullptr, (int *)(ctx->d_words + W_STATUS), post,
-        max_child_size > kStageMin);
-    return launched(ctx);
+    return launch_populate_kernel(ctx, ns, max_child_size > kStageMin, rule, pv,
+                                  schild_source{bufp<uint64_t>(ctx, B_SCHILD), bufp<uint32_t>(ctx, B_CPAR), pv.cbeg},
+                                  ctx->d_words + W_NS, (const uint64_t *)out->begin.p, (const uint32_t *)out->size.p,
+                                  (char *)out->objects.p, (double2 *)out->mag.p,
+                                  (const double *)(ctx->d_words + W_FACTOR), nullptr,
+                                  (int *)(ctx->d_words + W_STATUS), post);
 }
 
 inline int ensure_state(quids_gpu_state *st, uint64_t n, uint64_t nbytes) {

@@ -187,11 +187,11 @@ int simulate_batched_planned(quids_gpu_ctx *ctx, quids_gpu_state *in, const uint
     k_binst_factors<<<(G + 255) / 256, 256, 0, ctx->stream>>>(tot, G, obegin, maxn, (double *)out->inst_total.p,
                                                              bufp<double>(ctx, B_BFACTOR), stop);
     QD_TRY(launched(ctx, 4));
-    k_populate<instance_rules<Rule>, schild_source, no_post><<<grid_for(ctx, NSB), prim::kThreads, 0, ctx->stream>>>(
-        rs, pv, schild_source{bufp<uint64_t>(ctx, B_SCHILD), bufp<uint32_t>(ctx, B_CPAR), pv.cbeg}, words + W_NS,
+    QD_TRY(launch_populate_kernel(
+        ctx, NSB, ap.maxsize > kStageMin, rs, pv,
+        schild_source{bufp<uint64_t>(ctx, B_SCHILD), bufp<uint32_t>(ctx, B_CPAR), pv.cbeg}, words + W_NS,
         (const uint64_t *)out->begin.p, (const uint32_t *)out->size.p, (char *)out->objects.p, (double2 *)out->mag.p,
-        bufp<double>(ctx, B_BFACTOR), (const uint32_t *)out->inst.p, err, no_post{}, ap.maxsize > kStageMin);
-    QD_TRY(launched(ctx));
+        bufp<double>(ctx, B_BFACTOR), (const uint32_t *)out->inst.p, err, no_post{}));
     out->total_pending = false;
     out->total_proba = std::numeric_limits<double>::quiet_NaN();  // per instance: inst_total
     return QUIDS_OK;

@@ -780,11 +780,11 @@ int simulate_ranges(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, 
                                 ctx->stream));
         clk.end(5);
         clk.begin(6);
-        k_populate<single_rule<Rule>, pc_source, Post><<<grid_for(ctx, NS), prim::kThreads, 0, ctx->stream>>>(
-            rs, pv, pc_source{(const uint32_t *)rb.spar.p, (const uint32_t *)rb.scid.p}, ctx->d_words + W_NS,
-            (const uint64_t *)out->begin.p, (const uint32_t *)out->size.p, (char *)out->objects.p,
-            (double2 *)out->mag.p, (const double *)(ctx->d_words + W_FACTOR), nullptr, err, post, maxsize > kStageMin);
-        QD_TRY(launched(ctx));
+        QD_TRY(launch_populate_kernel(
+            ctx, NS, maxsize > kStageMin, rs, pv, pc_source{(const uint32_t *)rb.spar.p, (const uint32_t *)rb.scid.p},
+            ctx->d_words + W_NS, (const uint64_t *)out->begin.p, (const uint32_t *)out->size.p,
+            (char *)out->objects.p, (double2 *)out->mag.p, (const double *)(ctx->d_words + W_FACTOR), nullptr, err,
+            post));
         clk.end(6);
         out->n = NS;
         out->nbytes = outbytes;
