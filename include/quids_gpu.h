@@ -291,9 +291,10 @@ int quids_gpu_rule_children(quids_gpu_ctx *ctx, quids_gpu_state *iteration, int 
  * QUIDS_NOALLOC_SCRATCH_BYTES (about 3 MiB) that every GPU loading this
  * library holds until the process exits; a state of more than
  * QUIDS_NOALLOC_MAX_PARENTS objects is rejected with QUIDS_ERR_NOALLOC_LIMIT.
- * The first call on a device looks up the array's device address (with that
- * device current): make that first call before any stream capture.  Calls
- * share the array, so calls whose GPU work overlaps race on it.
+ * The stream must belong to the current device (QUIDS_ERR_BAD_ARG
+ * otherwise).  Every call synchronises its stream, so a call can never be
+ * part of a stream capture.  Calls share the array, so calls whose GPU work
+ * overlaps race on it.
  * Call with d_child_bytes = NULL to get *num_children and *stride; then with
  * capacity >= *num_children and buffers of capacity * stride bytes, capacity
  * u64 hashes, capacity u32 sizes and 2 * capacity doubles.  Synchronises the

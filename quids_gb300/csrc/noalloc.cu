@@ -5,15 +5,17 @@
 // offset scan with its look-back tiles, a few counters) lives in one
 // file-scope static device array.  Every GPU that loads this library holds
 // that array until the process exits.  Host code cannot use the array's name
-// as a device address (it names a host-side stand-in), so the first call on
-// each device looks the address up with cudaGetSymbolAddress while that
-// device is current, and caches it.  All calls on a device share the array:
-// the parts that must start at zero are cleared at every call, and calls whose
-// work overlaps on the GPU (e.g. issued on two streams at once) race on it.
+// as a device address (it names a host-side stand-in), so every call looks
+// the address up with cudaGetSymbolAddress on the current device, which must
+// be the device of the caller's stream (a call synchronises its stream, so it
+// is never part of a stream capture, and an address looked up per call stays
+// valid across a cudaDeviceReset that reloads the module).  All calls on a
+// device share the array: the parts that must start at zero are cleared at
+// every call, and calls whose work overlaps on the GPU (e.g. issued on two
+// streams at once) race on it.
 #include <cmath>
 #include <complex>
 #include <cstdint>
-#include <mutex>
 
 #include "engine.cuh"
 #include "rules_qc.cuh"
@@ -38,30 +40,29 @@ static_assert(kScratchBytes == QUIDS_NOALLOC_SCRATCH_BYTES, "header constant out
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_mutex;
-unsigned char *g_scratch_addr[kMaxDevices] = {};
-
-// device address of the static scratch on the current device (looked up once
-// per device, with that device current)
-int scratch_on_current_device(unsigned char **out, int *device) {
+// device address of the static scratch on the current device, which must be
+// the device of `stream` (the null, legacy and per-thread default streams
+// are the current device's)
+int scratch_on_current_device(cudaStream_t stream, unsigned char **out, int *device) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) {
         cudaGetLastError();
         return QUIDS_ERR_NO_DEVICE;
     }
-    if (dev < 0 || dev >= kMaxDevices) return QUIDS_ERR_BAD_ARG;
-    std::lock_guard<std::mutex> lock(g_mutex);
-    if (!g_scratch_addr[dev]) {
-        void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p) {
+    if (stream && stream != cudaStreamLegacy && stream != cudaStreamPerThread) {
+        int sdev = -1;
+        if (cudaStreamGetDevice(stream, &sdev) != cudaSuccess) {
             cudaGetLastError();
-            return QUIDS_ERR_CUDA;
+            return QUIDS_ERR_BAD_ARG;
         }
-        g_scratch_addr[dev] = (unsigned char *)p;
+        if (sdev != dev) return QUIDS_ERR_BAD_ARG;
     }
-    *out = g_scratch_addr[dev];
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
+        cudaGetLastError();
+        return QUIDS_ERR_CUDA;
+    }
+    *out = (unsigned char *)p;
     *device = dev;
     return QUIDS_OK;
 }
@@ -104,7 +105,7 @@ extern "C" int quids_gpu_rule_children_noalloc(void *stream, uint64_t num_object
     if (rule_kind < QUIDS_RULE_HADAMARD || rule_kind > QUIDS_RULE_QCGD_SPLIT_MERGE) return QUIDS_ERR_BAD_ARG;
     unsigned char *base = nullptr;
     int dev = 0;
-    QD_TRY(scratch_on_current_device(&base, &dev));
+    QD_TRY(scratch_on_current_device((cudaStream_t)stream, &base, &dev));
     if (num_object == 0) {
         *num_children = 0;
         *stride = 8;
