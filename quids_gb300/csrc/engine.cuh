@@ -747,22 +747,91 @@ struct child_records {
     }
 };
 
+// The parents of a tile are contiguous in the state's byte array (without a
+// parent index map), so a tile whose parents' bytes fit kParentStage is
+// staged in shared memory first: the 16-byte aligned body in one bulk copy
+// (cp.async.bulk, completing on an mbarrier), the last few bytes by plain
+// loads; the walks then read their parents there.  The wait is bounded: one
+// that runs out records QUIDS_ERR_TIMEOUT, waits (bounded again) for the
+// copy, and the block stops.
+constexpr uint32_t kParentStage = 36 * 1024;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    for (uint32_t it = 0; it < prim::kSpinLimit; ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
 template <class RS, class Out>
 __global__ void __launch_bounds__(prim::kThreads)
     k_symbolic_grouped(RS rs, parents_view pv, const uint64_t *lbeg, const uint64_t *tile_first, const uint64_t *d_nl,
-                       Out emit_child, unsigned long long *d_maxabs) {
+                       Out emit_child, unsigned long long *d_maxabs, int *err) {
     using Rule = typename RS::rule_type;
     constexpr int H = kGroupBits;
     __shared__ uint64_t s_lb[kStagedLeaderParents + 1];
+    __shared__ __align__(128) unsigned char s_par[kParentStage];
+    __shared__ __align__(8) uint64_t s_bar;
+    __shared__ int s_stop;
     const uint64_t nl = *d_nl;
     const uint64_t ntiles = (nl + kLeaderTile - 1) / kLeaderTile;
+    const uint32_t bar = smem_u32(&s_bar);
+    const bool can_stage = !pv.pidx && ((uintptr_t)pv.objects & 15) == 0;
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        s_stop = 0;
+    }
+    uint32_t parity = 0;
     unsigned long long mx = 0;  // IEEE bits of the largest |component| (ordered like the values)
     for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const uint64_t plo = tile_first[t], phi = tile_first[t + 1];
         const int count = phi - plo + 1 <= (uint64_t)kStagedLeaderParents ? (int)(phi - plo + 1) : -1;
-        __syncthreads();  // the previous tile is done with s_lb
+        __syncthreads();  // the previous tile is done with s_lb and s_par
         for (int k = threadIdx.x; k <= count; k += blockDim.x) s_lb[k] = lbeg[plo + k];
+        // the tile's parent bytes [lo, hi), staged from a0 = lo rounded down to 16
+        uint64_t a0 = 0, hi = 0;
+        bool staged = false;
+        if (can_stage) {
+            const uint64_t lo = pv.begin[plo];
+            hi = pv.begin[phi] + pv.size[phi];
+            a0 = lo & ~15ull;
+            staged = hi > lo && hi - a0 <= kParentStage;
+        }
+        if (staged) {
+            const uint64_t a1 = hi & ~15ull;  // the bulk copy's end; [a1, hi) by plain loads
+            if (threadIdx.x == 0 && a1 > a0) {
+                const uint32_t bytes = (uint32_t)(a1 - a0);
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                             : "memory");
+                asm volatile(
+                    "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                        smem_u32(s_par)),
+                    "l"(pv.objects + a0), "r"(bytes), "r"(bar)
+                    : "memory");
+            }
+            if (threadIdx.x < hi - a1) s_par[a1 - a0 + threadIdx.x] = (unsigned char)pv.objects[a1 + threadIdx.x];
+            if (a1 > a0) {
+                if (!mbar_wait(bar, parity)) {
+                    if (threadIdx.x == 0) {
+                        prim::set_error(err, QUIDS_ERR_TIMEOUT);
+                        s_stop = 1;
+                    }
+                    mbar_wait(bar, parity);
+                }
+                parity ^= 1;
+            }
+        }
         __syncthreads();
+        if (s_stop) break;
         const uint64_t l = t * kLeaderTile + threadIdx.x;
         if (l >= nl) continue;
         uint64_t p;
@@ -781,8 +850,12 @@ __global__ void __launch_bounds__(prim::kThreads)
         const uint64_t nch = pv.cbeg[p + 1] - c0;
         const int s = __ffsll((long long)nch) - 1;
         const uint32_t e = (uint32_t)(l - lbeg[p]);
-        const char *pb = pv.objects + pv.begin[oid];
-        const char *pe = pb + pv.size[oid];
+        const uint64_t ob = pv.begin[oid];
+        const uint32_t osz = pv.size[oid];
+        // (a state may place its objects in any order: only a parent inside
+        // the staged range reads there)
+        const char *pb = staged && ob >= a0 && ob + osz <= hi ? (const char *)s_par + (ob - a0) : pv.objects + ob;
+        const char *pe = pb + osz;
         const double2 pm = pv.mag[oid];
         const Rule &rule = rs.get(oid);
         auto out = [&](uint64_t c, uint64_t h, const mag_t &m, uint32_t sz) {
@@ -1531,7 +1604,7 @@ inline int launch_symbolic_grouped(quids_gpu_ctx *ctx, const RS &rs, const paren
                             bufp<uint32_t>(ctx, B_CPAR)};
     k_symbolic_grouped<RS, child_records><<<g, prim::kThreads, 0, ctx->stream>>>(
         rs, pv, bufp<uint64_t>(ctx, B_LBEG), bufp<uint64_t>(ctx, B_TILEPAR), ctx->d_words + W_TMP, rec,
-        (unsigned long long *)(ctx->d_words + W_MAXABS));
+        (unsigned long long *)(ctx->d_words + W_MAXABS), (int *)(ctx->d_words + W_STATUS));
     return launched(ctx, 2);
 }
 

@@ -582,7 +582,8 @@ int simulate_ranges(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, 
         const unsigned g = (unsigned)std::min<uint64_t>(est_tiles, (uint64_t)ctx->num_sms * 8);
         k_symbolic_grouped<single_rule<Rule>, range_ids><<<g, prim::kThreads, 0, ctx->stream>>>(
             rs, pv, bufp<uint64_t>(ctx, B_LBEG), (const uint64_t *)rb.ltile.p, ctx->d_words + W_NU,
-            range_ids{(uint8_t *)rb.rid.p, K}, (unsigned long long *)(ctx->d_words + W_MAXABS));
+            range_ids{(uint8_t *)rb.rid.p, K}, (unsigned long long *)(ctx->d_words + W_MAXABS),
+            (int *)(ctx->d_words + W_STATUS));
         QD_TRY(launched(ctx, 2));
         clk.end(1);
         ids_known = true;
