@@ -74,7 +74,21 @@ L2_BYTES = 129 * 1024 * 1024
 # cannot run inside it): a recorded ncu figure per workload, with the
 # profile it comes from.  dram__bytes_read.sum + dram__bytes_write.sum over
 # the stage's kernels, per rule application of the timed step.
-RECORDED_TRAFFIC = {}
+#
+# qcgd12's collision table is too large to capture under ncu's replay (the
+# step holds about 60 GB on the device), so its figure is the capture of the
+# qcgd10 erase_create table (6.06e7 children, about 3.1e6 joiners: the
+# k_table_claim launch moved 8.745 GB = 144.3 B per child, the
+# k_table_accumulate launch 0.961 GB = 310 B per joiner, k_fill 16 B per
+# slot; that table, like qcgd12's, is far larger than L2) scaled kernel by
+# kernel to the units of the three qcgd12 applications (7.26e8 children,
+# 1.63e8 joiners, 1.45e9 slots): 178.5 GB per step, 59.5 GB per application.
+RECORDED_TRAFFIC = {
+    ("qcgd12", "collisions", "table"): {
+        "bytes_per_launch": 59.5e9,
+        "source": "profiles/collision_table_qcgd10.md (ncu capture of the qcgd10 erase_create table kernels, "
+                  "scaled per kernel to qcgd12's children, joiners and slots)"},
+}
 
 
 # ------------------------------------------------------------------ workloads
@@ -381,7 +395,7 @@ def ours(args, rank, world):
     # per launch of the dominant stage (one per rule application)
     n_apps = max(1, len(stats) // args.steps)
     alg_per_launch = stage_b[dom] / args.steps / n_apps
-    rec = RECORDED_TRAFFIC.get((wl["name"], names[dom]))
+    rec = RECORDED_TRAFFIC.get((wl["name"], names[dom], args.collisions))
     traffic = rec["bytes_per_launch"] if rec else None
 
     # e2e through the public API with host buffers (pinned), copies inside the timed region
