@@ -1819,8 +1819,8 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, qu
     }
     const uint64_t NSB = may_truncate ? maxc : NC;  // bound on the survivors
 
-    // collisions: the partitioned stage (collide.cuh) for steps whose table
-    // would be far larger than L2, else the open-addressing table
+    // collisions: the open-addressing table, or the partitioned stage
+    // (collide.cuh) when QUIDS_FLAG_PARTITION asks for it
     const bool pcs = use_partition(prm, NC);
     uint64_t M = (uint64_t)((double)NC / load) + 1;
     if (M < 1024) M = 1024;
