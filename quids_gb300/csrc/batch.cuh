@@ -563,11 +563,19 @@ int simulate_batched(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule *rules_
     QD_TRY(ensure(out->inst_total, (size_t)G * sizeof(double)));
     QD_TRY(ensure(out->d_total, sizeof(double)));
 
+    // the collision table, cleared before the symbolic pass (whose grouped
+    // form claims the slots)
+    prim::table tb{bufp<prim::table_slot>(ctx, B_KEYS), bufp<unsigned long long>(ctx, B_ACC), M, probe_limit(prm)};
+    QD_CUDA(cudaMemsetAsync(tb.slots, 0xff, (M + 1) * sizeof(prim::table_slot), ctx->stream));
+    QD_CUDA(cudaMemsetAsync(tb.acc + 4 * M, 0, 4 * sizeof(uint64_t), ctx->stream));
+    QD_CUDA(cudaMemsetAsync(ctx->buf[B_NOTREP].p, 0, NC, ctx->stream));
+    QD_CUDA(cudaMemsetAsync(ctx->buf[B_HASJOIN].p, 0, NC, ctx->stream));
+
     // ---- symbolic iteration (src/quids.hpp:705-719), instance-tagged hashes
     bool grouped = false;
     if constexpr (has_grouped<Rule>::value) {
         if (fast) {
-            QD_TRY(launch_symbolic_grouped(ctx, rs, pv, NC));
+            QD_TRY(launch_symbolic_grouped(ctx, rs, pv, NC, table_claim{tb, bufp<uint32_t>(ctx, B_SLOT), err}));
             grouped = true;
         }
     }
@@ -583,19 +591,17 @@ int simulate_batched(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule *rules_
     }
 
     // ---- collision elimination (src/quids.hpp:785-809)
-    prim::table tb{bufp<prim::table_slot>(ctx, B_KEYS), bufp<unsigned long long>(ctx, B_ACC), M, probe_limit(prm)};
-    QD_CUDA(cudaMemsetAsync(tb.slots, 0xff, (M + 1) * sizeof(prim::table_slot), ctx->stream));
-    QD_CUDA(cudaMemsetAsync(tb.acc + 4 * M, 0, 4 * sizeof(uint64_t), ctx->stream));
-    QD_CUDA(cudaMemsetAsync(ctx->buf[B_NOTREP].p, 0, NC, ctx->stream));
-    QD_CUDA(cudaMemsetAsync(ctx->buf[B_HASJOIN].p, 0, NC, ctx->stream));
     uint8_t *not_rep = bufp<uint8_t>(ctx, B_NOTREP), *has_join = bufp<uint8_t>(ctx, B_HASJOIN);
     const unsigned long long *d_maxabs = (const unsigned long long *)(ctx->d_words + W_MAXABS);
     direct_src src{bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG)};
-    prim::k_table_claim<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(tb, src, ctx->d_words + W_NC,
-                                                                              bufp<uint32_t>(ctx, B_SLOT), err);
+    if (!grouped) {
+        prim::k_table_claim<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(tb, src, ctx->d_words + W_NC,
+                                                                                  bufp<uint32_t>(ctx, B_SLOT), err);
+        QD_TRY(launched(ctx));
+    }
     prim::k_table_accumulate<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
         tb, src, bufp<uint32_t>(ctx, B_SLOT), ctx->d_words + W_NC, d_maxabs, not_rep, has_join);
-    QD_TRY(launched(ctx, 2));
+    QD_TRY(launched(ctx));
 
     // ---- zero elimination (src/quids.hpp:819-823), groups with their instance
     group_view gv{bufp<uint32_t>(ctx, B_SLOT), not_rep, has_join, bufp<double2>(ctx, B_CMAG),

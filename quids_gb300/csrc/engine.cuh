@@ -451,6 +451,16 @@ template <class R, class = void>
 struct has_grouped : std::false_type {};
 template <class R>
 struct has_grouped<R, std::void_t<decltype(R::grouped_children)>> : std::bool_constant<R::grouped_children> {};
+// blocks per SM the grouped pass with a fused table claim is compiled for
+// (the register cap of __launch_bounds__): claimed_pass_blocks in the rule,
+// else 1 (no cap).  The flip rules' walk keeps its FP64 pipe busy only with
+// three resident blocks; split_merge's larger walk is slower when capped.
+// The batched pass (per-instance rules, more live state) is not capped.
+template <class R, class = void>
+struct claimed_pass_blocks : std::integral_constant<int, 1> {};
+template <class R>
+struct claimed_pass_blocks<R, std::void_t<decltype(R::claimed_pass_blocks)>>
+    : std::integral_constant<int, R::claimed_pass_blocks> {};
 
 template <class R, class = void>
 struct has_hash_child : std::false_type {};
@@ -519,6 +529,7 @@ QD_HD void rule_populate_simple(const R &r, const char *pb, const char *pe, char
 template <class Rule>
 struct single_rule {
     using rule_type = Rule;
+    static constexpr bool single = true;
     Rule r;
     __device__ __forceinline__ const Rule &get(uint64_t) const { return r; }
     __device__ __forceinline__ uint64_t tag(uint64_t h, uint64_t) const { return h; }
@@ -526,6 +537,7 @@ struct single_rule {
 template <class Rule>
 struct instance_rules {
     using rule_type = Rule;
+    static constexpr bool single = false;
     const Rule *rules;    // [instances]
     const uint32_t *inst; // instance of each parent
     __device__ __forceinline__ Rule get(uint64_t parent) const { return rules[inst[parent]]; }
@@ -747,6 +759,64 @@ struct child_records {
     }
 };
 
+// The grouped pass can also claim its children's collision-table slots
+// (the work of prim::k_table_claim, same table, same outcome per child): a
+// child's first compare-and-swap is issued as soon as its hash is known, and
+// its result is used after the leader's expansion (claimed, joined, or probe
+// on), so the atomics, bound by L2 misses, overlap the walk's FP64 work
+// instead of running as a pass of their own.  The table is cleared before
+// the pass.
+struct no_claim {
+    static constexpr bool active = false;
+    __device__ __forceinline__ uint64_t slots() const { return 0; }
+    __device__ __forceinline__ unsigned long long first(uint64_t, uint64_t) const { return 0; }
+    __device__ __forceinline__ void finish(uint64_t, uint64_t, unsigned long long, uint64_t) const {}
+};
+struct table_claim {
+    static constexpr bool active = true;
+    prim::table t;
+    uint32_t *slot_out;
+    int *err;
+    __device__ __forceinline__ uint64_t slots() const { return t.d_m ? *t.d_m : t.m; }
+    // the first probe of child c (hash h, home slot s): the old key
+    __device__ __forceinline__ unsigned long long first(uint64_t h, uint64_t m) const {
+        if (h == prim::kEmptyKey) return 0;
+        return atomicCAS(&t.slots[prim::table_home(h, m)].key, prim::kEmptyKey, h);
+    }
+    // the rest of k_table_claim's protocol for child c, given the first probe's key
+    __device__ __forceinline__ void finish(uint64_t c, uint64_t h, unsigned long long key, uint64_t m) const {
+        uint64_t sl;
+        bool claimed = false;
+        if (h == prim::kEmptyKey) {
+            sl = m;
+        } else {
+            sl = prim::table_home(h, m);
+            uint32_t probe = 0;
+            while (true) {
+                if (key == prim::kEmptyKey) {
+                    *(uint2 *)&t.slots[sl].rep = make_uint2((uint32_t)c, (uint32_t)c);
+                    claimed = true;
+                    break;
+                }
+                if (key == h) {
+                    ulonglong4_32a z;
+                    z.x = z.y = z.z = z.w = 0;
+                    *(ulonglong4_32a *)&t.acc[4 * sl] = z;
+                    break;
+                }
+                if (++sl == m) sl = 0;
+                if (++probe >= t.max_probes) {
+                    prim::set_error(err, QUIDS_ERR_TABLE_FULL);
+                    sl = ~0ull;
+                    break;
+                }
+                key = atomicCAS(&t.slots[sl].key, prim::kEmptyKey, h);
+            }
+        }
+        slot_out[c] = sl == ~0ull ? prim::kNoSlot : (claimed ? (uint32_t)sl : (uint32_t)sl | prim::kJoin);
+    }
+};
+
 // The parents of a tile are contiguous in the state's byte array (without a
 // parent index map), so a tile whose parents' bytes fit kParentStage is
 // staged in shared memory first: the 16-byte aligned body in one bulk copy
@@ -770,10 +840,11 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
     return false;
 }
 
-template <class RS, class Out>
-__global__ void __launch_bounds__(prim::kThreads)
+template <class RS, class Out, class Claim = no_claim>
+__global__ void __launch_bounds__(prim::kThreads,
+                                  Claim::active && RS::single ? claimed_pass_blocks<typename RS::rule_type>::value : 1)
     k_symbolic_grouped(RS rs, parents_view pv, const uint64_t *lbeg, const uint64_t *tile_first, const uint64_t *d_nl,
-                       Out emit_child, unsigned long long *d_maxabs, int *err) {
+                       Out emit_child, unsigned long long *d_maxabs, int *err, Claim claim = Claim{}) {
     using Rule = typename RS::rule_type;
     constexpr int H = kGroupBits;
     __shared__ uint64_t s_lb[kStagedLeaderParents + 1];
@@ -858,25 +929,53 @@ __global__ void __launch_bounds__(prim::kThreads)
         const char *pe = pb + osz;
         const double2 pm = pv.mag[oid];
         const Rule &rule = rs.get(oid);
-        auto out = [&](uint64_t c, uint64_t h, const mag_t &m, uint32_t sz) {
-            emit_child(c, rs.tag(h, oid), m, sz, p);
+        // with a claim: child k of this leader's (k = j, or the child id
+        // when the parent has fewer than 2^H children), its tagged hash and
+        // its first probe's key
+        constexpr int K = 1 << H;
+        static_assert(K == 4, "the claim keeps four children per leader");
+        uint64_t kh0 = 0, kh1 = 0, kh2 = 0, kh3 = 0;
+        unsigned long long kk0 = 0, kk1 = 0, kk2 = 0, kk3 = 0;
+        const uint64_t m_slots = Claim::active ? claim.slots() : 0;
+        auto out = [&](int k, uint64_t c, uint64_t h, const mag_t &m, uint32_t sz) {
+            const uint64_t ht = rs.tag(h, oid);
+            emit_child(c, ht, m, sz, p);
+            if constexpr (Claim::active) {
+                const unsigned long long key = claim.first(ht, m_slots);
+                switch (k) {
+                case 0: kh0 = ht, kk0 = key; break;
+                case 1: kh1 = ht, kk1 = key; break;
+                case 2: kh2 = ht, kk2 = key; break;
+                default: kh3 = ht, kk3 = key; break;
+                }
+            }
             const unsigned long long a = (unsigned long long)__double_as_longlong(m.re) & 0x7fffffffffffffffull;
             const unsigned long long b = (unsigned long long)__double_as_longlong(m.im) & 0x7fffffffffffffffull;
             const unsigned long long ab = a > b ? a : b;
             mx = mx > ab ? mx : ab;
         };
+        int nk;
         if (s >= H) {
             rule.template expand_group<H>(pb, pe, e, s, mag_t{pm.x, pm.y},
                                           [&](uint32_t j, uint64_t h, const mag_t &m, uint32_t sz) {
-                                              out(c0 + e + ((uint64_t)j << (s - H)), h, m, sz);
+                                              out((int)j, c0 + e + ((uint64_t)j << (s - H)), h, m, sz);
                                           });
+            nk = K;
         } else {
             for (uint32_t cid = 0; cid < (uint32_t)nch; ++cid) {
                 mag_t m{pm.x, pm.y};
                 uint32_t sz = 0;
                 const uint64_t h = rule.hash_child(pb, pe, cid, sz, m);
-                out(c0 + cid, h, m, sz);
+                out((int)cid, c0 + cid, h, m, sz);
             }
+            nk = (int)nch;
+        }
+        if constexpr (Claim::active) {
+            auto cidx = [&](int k) { return s >= H ? c0 + e + ((uint64_t)k << (s - H)) : c0 + (uint64_t)k; };
+            if (nk > 0) claim.finish(cidx(0), kh0, kk0, m_slots);
+            if (nk > 1) claim.finish(cidx(1), kh1, kk1, m_slots);
+            if (nk > 2) claim.finish(cidx(2), kh2, kk2, m_slots);
+            if (nk > 3) claim.finish(cidx(3), kh3, kk3, m_slots);
         }
     }
     for (int o = 16; o > 0; o >>= 1) {
@@ -1584,9 +1683,15 @@ inline size_t tilecnt_bytes(uint64_t nc_cap) {
     return ((tiles + 1) / 2 * 2) * sizeof(uint32_t) + (tiles + 1) * sizeof(uint64_t);
 }
 
-// leader offsets and their tile map (one scan), then the grouped pass
-template <class RS>
-inline int launch_symbolic_grouped(quids_gpu_ctx *ctx, const RS &rs, const parents_view &pv, uint64_t nc) {
+// leader offsets and their tile map (one scan), `pre` (after the scan,
+// whose look-back chain it may clear: the table fill of a fused claim), then
+// the grouped pass
+struct no_pre {
+    int operator()() const { return QUIDS_OK; }
+};
+template <class RS, class Claim = no_claim, class Pre = no_pre>
+inline int launch_symbolic_grouped(quids_gpu_ctx *ctx, const RS &rs, const parents_view &pv, uint64_t nc,
+                                   Claim claim = Claim{}, Pre pre = Pre{}) {
     const uint64_t np = pv.np;
     const uint64_t ltiles_cap = nc / kLeaderTile + 2;  // leaders <= children
     QD_TRY(ensure(ctx->buf[B_LBEG], (np + 1) * sizeof(uint64_t)));
@@ -1597,15 +1702,18 @@ inline int launch_symbolic_grouped(quids_gpu_ctx *ctx, const RS &rs, const paren
     prim::k_scan_excl<<<lookback_grid(ctx, np), prim::kThreads, 0, ctx->stream>>>(
         f, ctx->d_words + W_NP, bufp<uint64_t>(ctx, B_LBEG), ctx->d_words + W_TMP, lb,
         leader_tile_epilogue{bufp<uint64_t>(ctx, B_TILEPAR), ltiles_cap});
+    QD_TRY(launched(ctx));
+    QD_TRY(pre());
     const uint64_t est_tiles = (nc >> kGroupBits) / kLeaderTile + 1;
     const unsigned g = (unsigned)std::min<uint64_t>(
-        est_tiles, (uint64_t)ctx->num_sms * resident_per_sm(k_symbolic_grouped<RS, child_records>, prim::kThreads));
+        est_tiles,
+        (uint64_t)ctx->num_sms * resident_per_sm(k_symbolic_grouped<RS, child_records, Claim>, prim::kThreads));
     const child_records rec{bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG), bufp<uint32_t>(ctx, B_CSIZE),
                             bufp<uint32_t>(ctx, B_CPAR)};
-    k_symbolic_grouped<RS, child_records><<<g, prim::kThreads, 0, ctx->stream>>>(
+    k_symbolic_grouped<RS, child_records, Claim><<<g, prim::kThreads, 0, ctx->stream>>>(
         rs, pv, bufp<uint64_t>(ctx, B_LBEG), bufp<uint64_t>(ctx, B_TILEPAR), ctx->d_words + W_TMP, rec,
-        (unsigned long long *)(ctx->d_words + W_MAXABS), (int *)(ctx->d_words + W_STATUS));
-    return launched(ctx, 2);
+        (unsigned long long *)(ctx->d_words + W_MAXABS), (int *)(ctx->d_words + W_STATUS), claim);
+    return launched(ctx);
 }
 
 
@@ -1855,11 +1963,33 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, qu
     QD_TRY(ensure(ctx->buf[B_TILEPAR], (sym_tiles + 1) * sizeof(uint64_t)));
     QD_TRY(ensure(ctx->buf[B_CPAR], NC * sizeof(uint32_t)));
 
-    // ---- stage 1: symbolic iteration (src/quids.hpp:647-721)
+    // the collision table and its fill (slots free, the extra slot's sum, the
+    // group marks, the look-back chains of stages 3-4)
+    prim::table tb{bufp<prim::table_slot>(ctx, B_KEYS), bufp<unsigned long long>(ctx, B_ACC), M, probe_limit(prm)};
+    fill_set ftab{};
+    if (!pcs) {
+        ftab.p[0] = (unsigned char *)tb.slots, ftab.n[0] = (M + 1) * sizeof(prim::table_slot), ftab.v[0] = 0xff;
+        ftab.p[1] = (unsigned char *)(tb.acc + 4 * M), ftab.n[1] = 4 * sizeof(uint64_t), ftab.v[1] = 0;
+        ftab.p[2] = bufp<unsigned char>(ctx, B_NOTREP), ftab.n[2] = NC, ftab.v[2] = 0;
+        ftab.p[3] = bufp<unsigned char>(ctx, B_HASJOIN), ftab.n[3] = NC, ftab.v[3] = 0;
+        ftab.p[4] = bufp<unsigned char>(ctx, B_LOOKBACK), ftab.n[4] = 4 * (tiles_nc + 2) * sizeof(uint64_t),
+        ftab.v[4] = 0;
+        ftab.count = 5;
+    }
+
+    // ---- stage 1: symbolic iteration (src/quids.hpp:647-721); the grouped
+    // pass claims the table slots as well
     begin_stage(1);
     bool grouped = false;
     if constexpr (has_grouped<Rule>::value) grouped = fast;
-    if constexpr (has_grouped<Rule>::value) if (grouped) QD_TRY(launch_symbolic_grouped(ctx, rule, pv, NC));
+    const bool fused = grouped && !pcs;
+    if constexpr (has_grouped<Rule>::value) {
+        if (fused)
+            QD_TRY(launch_symbolic_grouped(ctx, rule, pv, NC, table_claim{tb, bufp<uint32_t>(ctx, B_SLOT), err},
+                                           [&] { return fill(ctx, ftab); }));
+        else if (grouped)
+            QD_TRY(launch_symbolic_grouped(ctx, rule, pv, NC));
+    }
     if (!grouped) {
         if (sym_tiles + 1 > tile_map_cap || bufp<uint64_t>(ctx, B_TILEPAR) != tile_map) {
             k_tile_parents<<<grid_for(ctx, NP), prim::kThreads, 0, ctx->stream>>>(
@@ -1885,26 +2015,19 @@ int simulate_rule(quids_gpu_ctx *ctx, quids_gpu_state *in, const Rule &rule_, qu
     } else {
         // ---- stage 2: collision table (src/quids.hpp:726-809)
         begin_stage(2);
-        prim::table tb{bufp<prim::table_slot>(ctx, B_KEYS), bufp<unsigned long long>(ctx, B_ACC), M, probe_limit(prm)};
-        {  // table slots free, the extra slot's sum, the group marks, the look-back chains of stages 3-4
-            fill_set f{};
-            f.p[0] = (unsigned char *)tb.slots, f.n[0] = (M + 1) * sizeof(prim::table_slot), f.v[0] = 0xff;
-            f.p[1] = (unsigned char *)(tb.acc + 4 * M), f.n[1] = 4 * sizeof(uint64_t), f.v[1] = 0;
-            f.p[2] = bufp<unsigned char>(ctx, B_NOTREP), f.n[2] = NC, f.v[2] = 0;
-            f.p[3] = bufp<unsigned char>(ctx, B_HASJOIN), f.n[3] = NC, f.v[3] = 0;
-            f.p[4] = bufp<unsigned char>(ctx, B_LOOKBACK), f.n[4] = 4 * (tiles_nc + 2) * sizeof(uint64_t), f.v[4] = 0;
-            f.count = 5;
-            QD_TRY(fill(ctx, f));
-        }
+        if (!fused) QD_TRY(fill(ctx, ftab));
         uint8_t *not_rep = bufp<uint8_t>(ctx, B_NOTREP), *has_join = bufp<uint8_t>(ctx, B_HASJOIN);
         const unsigned long long *d_maxabs = (const unsigned long long *)(ctx->d_words + W_MAXABS);
         {
             direct_src src{bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG)};
-            prim::k_table_claim<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
-                tb, src, ctx->d_words + W_NC, bufp<uint32_t>(ctx, B_SLOT), err);
+            if (!fused) {
+                prim::k_table_claim<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
+                    tb, src, ctx->d_words + W_NC, bufp<uint32_t>(ctx, B_SLOT), err);
+                QD_TRY(launched(ctx));
+            }
             prim::k_table_accumulate<<<grid_for(ctx, NC), prim::kThreads, 0, ctx->stream>>>(
                 tb, src, bufp<uint32_t>(ctx, B_SLOT), ctx->d_words + W_NC, d_maxabs, not_rep, has_join);
-            QD_TRY(launched(ctx, 2));
+            QD_TRY(launched(ctx));
         }
         end_stage(2);
 

@@ -354,10 +354,34 @@ int simulate_planned(quids_gpu_ctx *ctx, quids_gpu_state *in, const uint64_t *in
     parents_view pv{(const char *)in->objects.p, (const uint64_t *)in->begin.p, (const uint32_t *)in->size.p,
                     (const double2 *)in->mag.p, bufp<uint64_t>(ctx, B_CBEGIN), nullptr, N, words + W_NP};
 
-    // ---- stage 1: symbolic iteration
+    // the collision table, sized on the device, and its fill
+    const uint64_t tiles_nc = (NC + prim::kTile - 1) / prim::kTile;
+    prim::table tb{bufp<prim::table_slot>(ctx, B_KEYS), bufp<unsigned long long>(ctx, B_ACC), Mb, probe_limit(prm),
+                   words + W_M};
+    fill_set ftab{};
+    if (!ap.partition) {
+        ftab.p[0] = (unsigned char *)tb.slots, ftab.n[0] = (Mb + 1) * sizeof(prim::table_slot), ftab.v[0] = 0xff;
+        ftab.dn[0] = words + W_M, ftab.mul[0] = sizeof(prim::table_slot), ftab.add[0] = sizeof(prim::table_slot);
+        ftab.p[1] = bufp<unsigned char>(ctx, B_NOTREP), ftab.n[1] = NC, ftab.v[1] = 0;
+        ftab.dn[1] = words + W_NC, ftab.mul[1] = 1, ftab.add[1] = 0;
+        ftab.p[2] = bufp<unsigned char>(ctx, B_HASJOIN), ftab.n[2] = NC, ftab.v[2] = 0;
+        ftab.dn[2] = words + W_NC, ftab.mul[2] = 1, ftab.add[2] = 0;
+        ftab.p[3] = bufp<unsigned char>(ctx, B_LOOKBACK), ftab.n[3] = 4 * (tiles_nc + 2) * sizeof(uint64_t);
+        ftab.v[3] = 0;
+        ftab.count = 4;
+    }
+
+    // ---- stage 1: symbolic iteration (the grouped pass claims the table slots as well)
     bool grouped = false;
     if constexpr (has_grouped<Rule>::value) grouped = fast;
-    if constexpr (has_grouped<Rule>::value) if (grouped) QD_TRY(launch_symbolic_grouped(ctx, rule, pv, NC));
+    const bool fused = grouped && !ap.partition;
+    if constexpr (has_grouped<Rule>::value) {
+        if (fused)
+            QD_TRY(launch_symbolic_grouped(ctx, rule, pv, NC, table_claim{tb, bufp<uint32_t>(ctx, B_SLOT), err},
+                                           [&] { return fill(ctx, ftab); }));
+        else if (grouped)
+            QD_TRY(launch_symbolic_grouped(ctx, rule, pv, NC));
+    }
     if (!grouped) {
         if (ap.maxsize_lim <= 256) {
             QD_TRY((launch_symbolic<single_rule<Rule>, 256>(ctx, rule, pv, NC, fast)));
@@ -375,30 +399,19 @@ int simulate_planned(quids_gpu_ctx *ctx, quids_gpu_state *in, const uint64_t *in
                          hook_counter(ctx, W_DONE_LAYOUT), end_hook));
     } else {
         // ---- stage 2: collision table, sized on the device
-        const uint64_t tiles_nc = (NC + prim::kTile - 1) / prim::kTile;
-        prim::table tb{bufp<prim::table_slot>(ctx, B_KEYS), bufp<unsigned long long>(ctx, B_ACC), Mb, probe_limit(prm),
-                       words + W_M};
-        {
-            fill_set f{};
-            f.p[0] = (unsigned char *)tb.slots, f.n[0] = (Mb + 1) * sizeof(prim::table_slot), f.v[0] = 0xff;
-            f.dn[0] = words + W_M, f.mul[0] = sizeof(prim::table_slot), f.add[0] = sizeof(prim::table_slot);
-            f.p[1] = bufp<unsigned char>(ctx, B_NOTREP), f.n[1] = NC, f.v[1] = 0;
-            f.dn[1] = words + W_NC, f.mul[1] = 1, f.add[1] = 0;
-            f.p[2] = bufp<unsigned char>(ctx, B_HASJOIN), f.n[2] = NC, f.v[2] = 0;
-            f.dn[2] = words + W_NC, f.mul[2] = 1, f.add[2] = 0;
-            f.p[3] = bufp<unsigned char>(ctx, B_LOOKBACK), f.n[3] = 4 * (tiles_nc + 2) * sizeof(uint64_t), f.v[3] = 0;
-            f.count = 4;
-            QD_TRY(fill(ctx, f));
-        }
+        if (!fused) QD_TRY(fill(ctx, ftab));
         uint8_t *not_rep = bufp<uint8_t>(ctx, B_NOTREP), *has_join = bufp<uint8_t>(ctx, B_HASJOIN);
         const unsigned long long *d_maxabs = (const unsigned long long *)(words + W_MAXABS);
         {
             direct_src src{bufp<uint64_t>(ctx, B_HASH), bufp<double2>(ctx, B_CMAG)};
-            prim::k_table_claim<<<grid_for(ctx, NC), ctx->tune.table_block, 0, ctx->stream>>>(tb, src, words + W_NC,
-                                                                                       bufp<uint32_t>(ctx, B_SLOT), err);
+            if (!fused) {
+                prim::k_table_claim<<<grid_for(ctx, NC), ctx->tune.table_block, 0, ctx->stream>>>(
+                    tb, src, words + W_NC, bufp<uint32_t>(ctx, B_SLOT), err);
+                QD_TRY(launched(ctx));
+            }
             prim::k_table_accumulate<<<grid_for(ctx, NC), ctx->tune.table_block, 0, ctx->stream>>>(
                 tb, src, bufp<uint32_t>(ctx, B_SLOT), words + W_NC, d_maxabs, not_rep, has_join);
-            QD_TRY(launched(ctx, 2));
+            QD_TRY(launched(ctx));
         }
 
         // ---- stages 3-4: groups above tolerance, truncation, output layout
