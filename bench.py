@@ -75,19 +75,18 @@ L2_BYTES = 129 * 1024 * 1024
 # profile it comes from.  dram__bytes_read.sum + dram__bytes_write.sum over
 # the stage's kernels, per rule application of the timed step.
 #
-# qcgd12's collision table is too large to capture under ncu's replay (the
-# step holds about 60 GB on the device), so its figure is the capture of the
-# qcgd10 erase_create table (6.06e7 children, about 3.1e6 joiners: the
-# k_table_claim launch moved 8.745 GB = 144.3 B per child, the
-# k_table_accumulate launch 0.961 GB = 310 B per joiner, k_fill 16 B per
-# slot; that table, like qcgd12's, is far larger than L2) scaled kernel by
-# kernel to the units of the three qcgd12 applications (7.26e8 children,
-# 1.63e8 joiners, 1.45e9 slots): 178.5 GB per step, 59.5 GB per application.
+# qcgd12 holds about 60 GB on the device, too much for ncu's replay, so its
+# figure comes from a capture of qcgd10's erase_create application (whose
+# table, like qcgd12's, is far larger than L2), scaled by qcgd12's units:
+# the grouped symbolic pass with its fused table claim moved 10.98 GB for
+# 6.06e7 children (181 B per child) and the table clear before it 16 B per
+# slot; qcgd12's three applications have 7.26e8 children and 1.45e9 slots:
+# 154.6 GB per step, 51.5 GB per application.
 RECORDED_TRAFFIC = {
-    ("qcgd12", "collisions", "table"): {
-        "bytes_per_launch": 59.5e9,
-        "source": "profiles/collision_table_qcgd10.md (ncu capture of the qcgd10 erase_create table kernels, "
-                  "scaled per kernel to qcgd12's children, joiners and slots)"},
+    ("qcgd12", "symbolic+table_claim", "table"): {
+        "bytes_per_launch": 51.5e9,
+        "source": "profiles/symbolic_table_claim_qcgd10.md (ncu capture of qcgd10's erase_create grouped pass "
+                  "with its fused table claim and the table clear, scaled to qcgd12's children and slots)"},
 }
 
 
@@ -271,7 +270,7 @@ def run_step_gpu(ctx, quids, wl, init_state, stats_acc=None, flags=0, spare=None
 
 
 # per-stage algorithmic bytes (compulsory HBM traffic of each stage's kernels)
-def stage_bytes(st):
+def stage_bytes(st, fused=False):
     NP, NC, NU, NS = st["num_parents_kept"], st["num_object"], st["num_object_after_interferences"], st["num_object_out"]
     sp = st.get("_in_bytes", 0)
     sbar_p = sp / NP if NP else 0
@@ -291,6 +290,17 @@ def stage_bytes(st):
         # magnitude read once, each group's record (key, representative,
         # magnitude) written and read once, the survivors laid out
         base.update({2: 24.0 * NC + 56.0 * NU + out_layout, 3: 0.0, 4: 0.0})
+        return base
+    if fused:
+        # the grouped symbolic pass clears the table and claims the slots
+        # (slot out per child; the hash stays in registers); stage 2 is the
+        # accumulate: each child's slot, the joiners' magnitudes
+        base[1] += 8.0 * M + 4.0 * NC
+        base.update({
+            2: 20.0 * NC,
+            3: 8.0 * NC + 32.0 * NU + (40.0 * NU if trunc else out_layout),
+            4: (8.0 * NU + 40.0 * NU + out_layout) if trunc else 0.0,
+        })
         return base
     # collision table: insert (24 in, 4 out); per child slot + rep, per rep its sum
     base.update({
@@ -378,16 +388,19 @@ def ours(args, rank, world):
     ctx.synchronize()
     value, total_ms = job_value(children, sum(ms), world, dev)
 
-    # dominant stage and its roofline (stage times are CUDA events on the library's stream)
+    # dominant stage and its roofline (stage times are CUDA events on the library's stream);
+    # the QCGD rules' grouped symbolic pass claims the collision-table slots itself
+    fused = wl["name"].startswith("qcgd") and args.collisions == "table"
     stage_t = [0.0] * 8
     stage_b = [0.0] * 8
     for st in stats:
-        sb = stage_bytes(st)
+        sb = stage_bytes(st, fused)
         for k in range(8):
             stage_t[k] += st["stage_ms"][k]
             stage_b[k] += sb[k]
     dom = max(range(8), key=lambda k: stage_t[k])
-    names = ["num_child+offsets", "symbolic", "collisions", "group_compaction+layout",
+    names = ["num_child+offsets", "symbolic+table_claim" if fused else "symbolic",
+             "collision_accumulate" if fused else "collisions", "group_compaction+layout",
              "truncation+layout", "total_proba", "finalize_populate+normalize", "unused"]
     peak, peak_kind = peaks()
     achieved = stage_b[dom] / (stage_t[dom] / 1e3) / 1e9 if stage_t[dom] > 0 else 0.0
