@@ -200,6 +200,18 @@ int quids_gpu_state_total_proba(const quids_gpu_state *st, double *total_proba);
  * (begin has num_object + 1 entries).  Any pointer may be NULL to skip it. */
 int quids_gpu_state_download(quids_gpu_state *st, uint8_t *objects, uint64_t *begin,
                              uint32_t *size, double *magnitude);
+/* No counterpart in the reference (its states live in host memory).  The
+ * copies of quids_gpu_state_download, issued on the context's copy stream
+ * after the work already issued on the context: the call returns at once,
+ * so a loop can download one step's result while the next step runs.  The
+ * host buffers must stay valid, and should be pinned (page-locked) for the
+ * copies to overlap anything.  Until quids_gpu_state_download_wait(st)
+ * returns, the buffers are not complete.  Work that writes the state
+ * (upload, simulate, run, modifiers, a tape's final state) waits for the
+ * copies on the device, so it cannot overwrite what is still being read. */
+int quids_gpu_state_download_async(quids_gpu_state *st, uint8_t *objects, uint64_t *begin,
+                                   uint32_t *size, double *magnitude);
+int quids_gpu_state_download_wait(quids_gpu_state *st);
 /* Device pointers of the state's arrays (valid until the next call that
  * writes the state). */
 int quids_gpu_state_device_arrays(quids_gpu_state *st, void **objects, void **begin, void **size,

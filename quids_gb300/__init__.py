@@ -231,6 +231,24 @@ class it_t:
                                                      size.ctypes.data, mag.ctypes.data), "state_download")
         return objects[:nb], begin, size[:n], mag[:n]
 
+    def download_async(self, objects, begin, size, mag):
+        """Starts the device -> host copies of the state into the given arrays
+        (objects >= num_bytes bytes, begin >= num_object + 1 u64, size >=
+        num_object u32, mag >= num_object complex128; pinned memory lets the
+        copies overlap later steps) and returns; download_wait() completes
+        them.  Later writes to the state wait for the copies on the device."""
+        self._flush()
+        n, nb = self.num_object, self.num_bytes
+        arrays = ((objects, nb, 1), (begin, n + 1, 8), (size, n, 4), (mag, n, 16))
+        for a, count, item in arrays:
+            if _nbytes(a) < count * item:
+                raise ValueError("download_async: a host buffer is too small for the state")
+        capi.check(self.lib.quids_gpu_state_download_async(self.h, *(_address(a) for a, _, _ in arrays)),
+                   "state_download_async")
+
+    def download_wait(self):
+        capi.check(self.lib.quids_gpu_state_download_wait(self.h), "state_download_wait")
+
     def _flush(self):
         if not self._pending:
             return
@@ -347,6 +365,15 @@ class it_t:
             b = int(begin[i])
             tot += observable(objects[b: b + int(size[i])].tobytes()) * abs(mag[i]) ** 2
         return tot
+
+
+def _nbytes(a) -> int:
+    """Bytes of a host buffer: a numpy array or a (pinned) torch tensor."""
+    return int(a.nbytes) if isinstance(a, np.ndarray) else int(a.numel() * a.element_size())
+
+
+def _address(a) -> int:
+    return int(a.ctypes.data) if isinstance(a, np.ndarray) else int(a.data_ptr())
 
 
 def _params(max_num_object, flags=0):

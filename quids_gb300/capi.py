@@ -86,6 +86,7 @@ EXPORTS = [
     "quids_gpu_ctx_run_counts", "quids_gpu_ctx_last_tuning",
     "quids_gpu_state_create", "quids_gpu_state_destroy", "quids_gpu_state_upload", "quids_gpu_state_num_object",
     "quids_gpu_state_num_bytes", "quids_gpu_state_total_proba", "quids_gpu_state_download",
+    "quids_gpu_state_download_async", "quids_gpu_state_download_wait",
     "quids_gpu_state_device_arrays", "quids_gpu_simulate", "quids_gpu_apply_modifier",
     "quids_gpu_rule_children", "quids_gpu_state_hash", "quids_gpu_rule_children_noalloc", "quids_gpu_run",
     "quids_gpu_average_value", "quids_gpu_qcgd_statistics", "quids_gpu_state_upload_batched",
@@ -135,6 +136,8 @@ def load(build_if_missing: bool = True):
     L.quids_gpu_state_num_bytes.argtypes = [vp, u64p]
     L.quids_gpu_state_total_proba.argtypes = [vp, C.POINTER(C.c_double)]
     L.quids_gpu_state_download.argtypes = [vp, vp, vp, vp, vp]
+    L.quids_gpu_state_download_async.argtypes = [vp, vp, vp, vp, vp]
+    L.quids_gpu_state_download_wait.argtypes = [vp]
     L.quids_gpu_state_device_arrays.argtypes = [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)]
     L.quids_gpu_simulate.argtypes = [vp, vp, C.c_int, C.POINTER(RuleParams), vp, C.POINTER(Params),
                                      C.POINTER(StepStats)]

@@ -226,6 +226,8 @@ int quids_gpu_forward(quids_gpu_ctx *ctx, quids_gpu_tape *t, quids_gpu_state *in
 
 int quids_gpu_tape_final_state(quids_gpu_tape *t, quids_gpu_state *out) {
     if (!t || !t->ready || !out || out->ctx != t->ctx) return QUIDS_ERR_BAD_ARG;
+    QD_CUDA(cudaSetDevice(t->ctx->device));
+    QD_TRY(after_download(out));
     QD_TRY(copy_state(t->ctx, t->final, out));
     return cuda_status(cudaStreamSynchronize(t->ctx->stream));
 }

@@ -290,6 +290,9 @@ int quids_gpu_simulate_batched(quids_gpu_ctx *ctx, quids_gpu_state *iteration, i
     if (iteration->n_inst == 0) return QUIDS_ERR_BAD_ARG;
     const quids_gpu_params prm = *params;
     const alloc_limit_scope alloc_limit(prm.max_alloc_bytes);
+    QD_CUDA(cudaSetDevice(ctx->device));
+    QD_TRY(after_download(iteration));
+    QD_TRY(after_download(next_iteration));
     switch (rule_kind) {
     case QUIDS_RULE_HADAMARD:
         return simulate_batched_with(ctx, iteration, rules, next_iteration, prm, inst_stats, stats,
@@ -317,6 +320,8 @@ int quids_gpu_run_batched(quids_gpu_ctx *ctx, quids_gpu_state *a, quids_gpu_stat
     if (!ctx || !a || !b || a == b || (!ops && n_ops) || !params || !final_index) return QUIDS_ERR_BAD_ARG;
     if (a->n_inst == 0 || a->ctx != ctx || b->ctx != ctx) return QUIDS_ERR_BAD_ARG;
     QD_CUDA(cudaSetDevice(ctx->device));
+    QD_TRY(after_download(a));
+    QD_TRY(after_download(b));
     const uint32_t G = a->n_inst;
     const quids_gpu_params prm = *params;
     const alloc_limit_scope alloc_limit(prm.max_alloc_bytes);

@@ -260,6 +260,55 @@ __global__ void k_set_words_zero(uint64_t *w, int n) {
     for (int i = threadIdx.x; i < n; i += blockDim.x) w[i] = 0;
 }
 
+// Device -> host copies of a state.  Into page-locked host memory the SMs
+// store the bytes themselves, through the buffer's device-mapped address: on
+// GB300 the copy engine's device-to-host rate varied between about 25 and
+// 190 GB/s from one copy of a 5.7 GB state to the next, while SM stores over
+// the CPU link ran at 193 GB/s every time.  Pageable memory (or a buffer
+// whose address is not 16-byte aligned) goes through cudaMemcpyAsync.
+__global__ void k_to_host(const uint4 *__restrict__ src, uint4 *__restrict__ dst, uint64_t n16,
+                          const unsigned char *__restrict__ tail_src, unsigned char *__restrict__ tail_dst,
+                          uint32_t tail) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n16; i += stride) dst[i] = src[i];
+    if (blockIdx.x == 0 && threadIdx.x < tail) tail_dst[threadIdx.x] = tail_src[threadIdx.x];
+}
+
+int copy_to_host(quids_gpu_ctx *ctx, cudaStream_t s, void *dst, const void *src, uint64_t bytes) {
+    if (!bytes) return QUIDS_OK;
+    cudaPointerAttributes a{};
+    void *mapped = nullptr;
+    if (cudaPointerGetAttributes(&a, dst) == cudaSuccess && a.type == cudaMemoryTypeHost && a.devicePointer)
+        mapped = a.devicePointer;
+    else
+        cudaGetLastError();
+    if (!mapped || ((uintptr_t)mapped & 15) || ((uintptr_t)src & 15))
+        return cuda_status(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s));
+    const uint64_t n16 = bytes / 16;
+    const uint32_t tail = (uint32_t)(bytes - n16 * 16);
+    const uint64_t want = (n16 + 255) / 256;
+    const uint64_t cap = (uint64_t)ctx->num_sms * 8;
+    const unsigned grid = (unsigned)(want < cap ? (want ? want : 1) : cap);
+    k_to_host<<<grid, 256, 0, s>>>((const uint4 *)src, (uint4 *)mapped, n16, (const unsigned char *)src + n16 * 16,
+                                   (unsigned char *)mapped + n16 * 16, tail);
+    return launched(ctx);
+}
+
+// the copies of a download, on stream s
+int download_on(quids_gpu_ctx *ctx, quids_gpu_state *st, cudaStream_t s, uint8_t *objects, uint64_t *begin,
+                uint32_t *size, double *magnitude) {
+    if (objects) QD_TRY(copy_to_host(ctx, s, objects, st->objects.p, st->nbytes));
+    if (begin) {
+        if (st->n)
+            QD_TRY(copy_to_host(ctx, s, begin, st->begin.p, (st->n + 1) * sizeof(uint64_t)));
+        else
+            begin[0] = 0;
+    }
+    if (size) QD_TRY(copy_to_host(ctx, s, size, st->size.p, st->n * sizeof(uint32_t)));
+    if (magnitude) QD_TRY(copy_to_host(ctx, s, magnitude, st->mag.p, st->n * 2 * sizeof(double)));
+    return QUIDS_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -327,6 +376,7 @@ int quids_gpu_ctx_destroy(quids_gpu_ctx *ctx) {
     if (!ctx) return QUIDS_ERR_BAD_ARG;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
     for (quids_gpu_state *st : ctx->states) {
         release_state(st);
         st->ctx = nullptr;
@@ -344,6 +394,8 @@ int quids_gpu_ctx_destroy(quids_gpu_ctx *ctx) {
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     for (auto &e : ctx->ev_stage)
         if (e) cudaEventDestroy(e);
+    if (ctx->ev_copy) cudaEventDestroy(ctx->ev_copy);
+    if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return QUIDS_OK;
@@ -401,6 +453,12 @@ int quids_gpu_state_create(quids_gpu_ctx *ctx, quids_gpu_state **out) {
 
 int quids_gpu_state_destroy(quids_gpu_state *st) {
     if (!st) return QUIDS_ERR_BAD_ARG;
+    if (st->dl_done) {  // (a pending download ends before the buffers go)
+        cudaEventSynchronize(st->dl_done);
+        cudaEventDestroy(st->dl_done);
+        st->dl_done = nullptr;
+        st->dl_pending = false;
+    }
     if (!st->ctx) {  // its context is gone and has already released the memory
         delete st;
         return QUIDS_OK;
@@ -423,6 +481,7 @@ int quids_gpu_state_upload(quids_gpu_state *st, uint64_t n, const uint8_t *objec
         if (begin[i] + size[i] > num_bytes) return QUIDS_ERR_BAD_ARG;
     quids_gpu_ctx *ctx = st->ctx;
     QD_CUDA(cudaSetDevice(ctx->device));
+    QD_TRY(after_download(st));
     QD_TRY(ensure_state(st, n, num_bytes));
     cudaStream_t s = ctx->stream;
     if (num_bytes) QD_CUDA(cudaMemcpyAsync(st->objects.p, objects, num_bytes, cudaMemcpyHostToDevice, s));
@@ -475,18 +534,38 @@ int quids_gpu_state_download(quids_gpu_state *st, uint8_t *objects, uint64_t *be
     quids_gpu_ctx *ctx = st->ctx;
     QD_CUDA(cudaSetDevice(ctx->device));
     cudaStream_t s = ctx->stream;
-    if (objects && st->nbytes)
-        QD_CUDA(cudaMemcpyAsync(objects, st->objects.p, st->nbytes, cudaMemcpyDeviceToHost, s));
-    if (begin) {
-        if (st->n)
-            QD_CUDA(cudaMemcpyAsync(begin, st->begin.p, (st->n + 1) * sizeof(uint64_t), cudaMemcpyDeviceToHost, s));
-        else
-            begin[0] = 0;
-    }
-    if (size && st->n) QD_CUDA(cudaMemcpyAsync(size, st->size.p, st->n * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-    if (magnitude && st->n)
-        QD_CUDA(cudaMemcpyAsync(magnitude, st->mag.p, st->n * 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    QD_TRY(download_on(ctx, st, s, objects, begin, size, magnitude));
     QD_CUDA(cudaStreamSynchronize(s));
+    return QUIDS_OK;
+}
+
+// The copies of quids_gpu_state_download on the context's copy stream,
+// ordered after the work already issued on its stream; st->dl_done marks
+// their end.  Later work that writes the state waits for it on the device
+// (after_download); the host waits in quids_gpu_state_download_wait.
+int quids_gpu_state_download_async(quids_gpu_state *st, uint8_t *objects, uint64_t *begin, uint32_t *size,
+                                   double *magnitude) {
+    if (!st || !st->ctx) return QUIDS_ERR_BAD_ARG;
+    quids_gpu_ctx *ctx = st->ctx;
+    QD_CUDA(cudaSetDevice(ctx->device));
+    if (!ctx->copy_stream) QD_CUDA(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+    if (!ctx->ev_copy) QD_CUDA(cudaEventCreateWithFlags(&ctx->ev_copy, cudaEventDisableTiming));
+    if (!st->dl_done) QD_CUDA(cudaEventCreateWithFlags(&st->dl_done, cudaEventDisableTiming));
+    cudaStream_t s = ctx->copy_stream;
+    QD_CUDA(cudaEventRecord(ctx->ev_copy, ctx->stream));
+    QD_CUDA(cudaStreamWaitEvent(s, ctx->ev_copy, 0));
+    QD_TRY(download_on(ctx, st, s, objects, begin, size, magnitude));
+    QD_CUDA(cudaEventRecord(st->dl_done, s));
+    st->dl_pending = true;
+    return QUIDS_OK;
+}
+
+int quids_gpu_state_download_wait(quids_gpu_state *st) {
+    if (!st) return QUIDS_ERR_BAD_ARG;
+    if (!st->dl_pending) return QUIDS_OK;
+    if (st->ctx) QD_CUDA(cudaSetDevice(st->ctx->device));
+    QD_CUDA(cudaEventSynchronize(st->dl_done));
+    st->dl_pending = false;
     return QUIDS_OK;
 }
 
@@ -505,6 +584,11 @@ int quids_gpu_simulate(quids_gpu_ctx *ctx, quids_gpu_state *iteration, int rule_
     if (!params) return QUIDS_ERR_BAD_ARG;
     quids_gpu_params prm = *params;
     const alloc_limit_scope alloc_limit(prm.max_alloc_bytes);
+    if (ctx) {
+        QD_CUDA(cudaSetDevice(ctx->device));
+        QD_TRY(after_download(iteration));
+        QD_TRY(after_download(next_iteration));
+    }
     return dispatch_rule(rule_kind, rule, [&](auto r) {
         return ranges::simulate_step(ctx, iteration, r, next_iteration, prm, stats);
     });
@@ -512,6 +596,10 @@ int quids_gpu_simulate(quids_gpu_ctx *ctx, quids_gpu_state *iteration, int rule_
 
 int quids_gpu_apply_modifier(quids_gpu_ctx *ctx, quids_gpu_state *st, int kind, const quids_gpu_rule_params *p) {
     if (!p) return QUIDS_ERR_BAD_ARG;
+    if (ctx && st && st->ctx == ctx) {
+        QD_CUDA(cudaSetDevice(ctx->device));
+        QD_TRY(after_download(st));
+    }
     switch (kind) {
     case QUIDS_MOD_CNOT: return apply_modifier(ctx, st, rules::cnot{p->control, p->bit});
     case QUIDS_MOD_X: return apply_modifier(ctx, st, rules::xgate{p->bit});
@@ -528,6 +616,9 @@ int quids_gpu_run(quids_gpu_ctx *ctx, quids_gpu_state *a, quids_gpu_state *b, co
                   int *final_index) {
     if (!ctx || !a || !b || a == b || (!ops && n_ops) || !params || !final_index) return QUIDS_ERR_BAD_ARG;
     if (a->ctx != ctx || b->ctx != ctx) return QUIDS_ERR_BAD_ARG;
+    QD_CUDA(cudaSetDevice(ctx->device));
+    QD_TRY(after_download(a));
+    QD_TRY(after_download(b));
     QD_CUDA(cudaSetDevice(ctx->device));
     const quids_gpu_params prm = *params;
     const alloc_limit_scope alloc_limit(prm.max_alloc_bytes);

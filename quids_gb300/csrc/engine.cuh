@@ -134,6 +134,9 @@ struct quids_gpu_ctx {
     unsigned long long *d_hist = nullptr;    // 256
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     cudaEvent_t ev_stage[16] = {};  // start/end of the 8 stages of a step
+    // asynchronous downloads: a copy stream, ordered after `stream` by ev_copy
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_copy = nullptr;
     uint64_t launches = 0;          // kernels launched by this context
     // live states: destroying the context releases their device memory and
     // orphans them, so states may be destroyed after their context
@@ -168,6 +171,11 @@ struct quids_gpu_state {
     uint32_t n_inst = 0;
     qd_dbuf inst, inst_begin, inst_total;
     std::vector<uint64_t> h_inst_begin;
+    // an asynchronous download still reading the buffers: work that writes
+    // them waits on dl_done first (on the device), the host in
+    // quids_gpu_state_download_wait
+    cudaEvent_t dl_done = nullptr;
+    bool dl_pending = false;
 };
 
 namespace qd::engine {
@@ -260,6 +268,13 @@ inline void release(qd_dbuf &b) {
     b.p = nullptr;
     b.cap = 0;
 }
+// the context's stream waits for a pending asynchronous download of st (a
+// device-side wait: the host does not block)
+inline int after_download(const quids_gpu_state *st) {
+    if (!st || !st->ctx || !st->dl_pending) return QUIDS_OK;
+    return cuda_status(cudaStreamWaitEvent(st->ctx->stream, st->dl_done, 0));
+}
+
 inline void release_state(quids_gpu_state *st) {
     for (qd_dbuf *b : {&st->objects, &st->begin, &st->size, &st->mag, &st->d_total, &st->meta, &st->inst,
                        &st->inst_begin, &st->inst_total})
