@@ -274,7 +274,7 @@ __global__ void k_to_host(const uint4 *__restrict__ src, uint4 *__restrict__ dst
     if (blockIdx.x == 0 && threadIdx.x < tail) tail_dst[threadIdx.x] = tail_src[threadIdx.x];
 }
 
-int copy_to_host(quids_gpu_ctx *ctx, cudaStream_t s, void *dst, const void *src, uint64_t bytes) {
+int copy_to_host(quids_gpu_ctx *ctx, cudaStream_t s, void *dst, const void *src, uint64_t bytes, uint64_t max_blocks) {
     if (!bytes) return QUIDS_OK;
     cudaPointerAttributes a{};
     void *mapped = nullptr;
@@ -287,25 +287,26 @@ int copy_to_host(quids_gpu_ctx *ctx, cudaStream_t s, void *dst, const void *src,
     const uint64_t n16 = bytes / 16;
     const uint32_t tail = (uint32_t)(bytes - n16 * 16);
     const uint64_t want = (n16 + 255) / 256;
-    const uint64_t cap = (uint64_t)ctx->num_sms * 8;
+    const uint64_t cap = max_blocks;
     const unsigned grid = (unsigned)(want < cap ? (want ? want : 1) : cap);
     k_to_host<<<grid, 256, 0, s>>>((const uint4 *)src, (uint4 *)mapped, n16, (const unsigned char *)src + n16 * 16,
                                    (unsigned char *)mapped + n16 * 16, tail);
     return launched(ctx);
 }
 
-// the copies of a download, on stream s
+// the copies of a download, on stream s, by at most `blocks` blocks of SM
+// stores (a download that overlaps a step leaves it most of the SMs)
 int download_on(quids_gpu_ctx *ctx, quids_gpu_state *st, cudaStream_t s, uint8_t *objects, uint64_t *begin,
-                uint32_t *size, double *magnitude) {
-    if (objects) QD_TRY(copy_to_host(ctx, s, objects, st->objects.p, st->nbytes));
+                uint32_t *size, double *magnitude, uint64_t blocks) {
+    if (objects) QD_TRY(copy_to_host(ctx, s, objects, st->objects.p, st->nbytes, blocks));
     if (begin) {
         if (st->n)
-            QD_TRY(copy_to_host(ctx, s, begin, st->begin.p, (st->n + 1) * sizeof(uint64_t)));
+            QD_TRY(copy_to_host(ctx, s, begin, st->begin.p, (st->n + 1) * sizeof(uint64_t), blocks));
         else
             begin[0] = 0;
     }
-    if (size) QD_TRY(copy_to_host(ctx, s, size, st->size.p, st->n * sizeof(uint32_t)));
-    if (magnitude) QD_TRY(copy_to_host(ctx, s, magnitude, st->mag.p, st->n * 2 * sizeof(double)));
+    if (size) QD_TRY(copy_to_host(ctx, s, size, st->size.p, st->n * sizeof(uint32_t), blocks));
+    if (magnitude) QD_TRY(copy_to_host(ctx, s, magnitude, st->mag.p, st->n * 2 * sizeof(double), blocks));
     return QUIDS_OK;
 }
 
@@ -534,7 +535,7 @@ int quids_gpu_state_download(quids_gpu_state *st, uint8_t *objects, uint64_t *be
     quids_gpu_ctx *ctx = st->ctx;
     QD_CUDA(cudaSetDevice(ctx->device));
     cudaStream_t s = ctx->stream;
-    QD_TRY(download_on(ctx, st, s, objects, begin, size, magnitude));
+    QD_TRY(download_on(ctx, st, s, objects, begin, size, magnitude, (uint64_t)ctx->num_sms * 8));
     QD_CUDA(cudaStreamSynchronize(s));
     return QUIDS_OK;
 }
@@ -554,7 +555,7 @@ int quids_gpu_state_download_async(quids_gpu_state *st, uint8_t *objects, uint64
     cudaStream_t s = ctx->copy_stream;
     QD_CUDA(cudaEventRecord(ctx->ev_copy, ctx->stream));
     QD_CUDA(cudaStreamWaitEvent(s, ctx->ev_copy, 0));
-    QD_TRY(download_on(ctx, st, s, objects, begin, size, magnitude));
+    QD_TRY(download_on(ctx, st, s, objects, begin, size, magnitude, (uint64_t)(ctx->num_sms + 1) / 2));
     QD_CUDA(cudaEventRecord(st->dl_done, s));
     st->dl_pending = true;
     return QUIDS_OK;
