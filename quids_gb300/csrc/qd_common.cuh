@@ -9,9 +9,11 @@
 
 #if defined(__CUDACC__)
 #define QD_HD __host__ __device__ __forceinline__
+#define QD_HD_CALL __host__ __device__ inline __noinline__  // a real call: one copy of the code
 #define QD_D __device__ __forceinline__
 #else
 #define QD_HD inline
+#define QD_HD_CALL inline
 #define QD_D inline
 #endif
 

@@ -123,40 +123,46 @@ QD_HD void get_operations(const char *p, int n, int i, bool &split, bool &merge)
 enum name_op { OP_COPY = 0, OP_LEFT = 1, OP_RIGHT = 2, OP_MERGE = 3 };
 
 // writes the name into dst[d..) and returns the end index
+// The name writer's copies go through one out-of-line function: inlined at
+// its eight call sites, the copy loops made split_merge's populate kernel large
+// enough to stall on instruction fetch (qcgd12: 22.4 ms, against 9.5 ms with
+// the call).
+QD_HD_CALL void copy_name_bytes(char *dst, const char *src, uint32_t n) { copy_bytes(dst, src, n); }
+
 QD_HD int write_name(const char *src, char *dst, int d, int op, int b1, int e1, int b2, int e2) {
     switch (op) {
     case OP_COPY:
-        copy_bytes(dst + 16 * d, src + 16 * b1, 16u * (uint32_t)(e1 - b1));
+        copy_name_bytes(dst + 16 * d, src + 16 * b1, 16u * (uint32_t)(e1 - b1));
         return d + (e1 - b1);
     case OP_LEFT: {  // operations::left, :194-200
         int16_t rot = node_rot(src, b1);
         if (rot >= 0) {
-            copy_bytes(dst + 16 * d, src + 16 * (b1 + 1), 16u * (uint32_t)(rot - 1));
+            copy_name_bytes(dst + 16 * d, src + 16 * (b1 + 1), 16u * (uint32_t)(rot - 1));
             return d + rot - 1;
         }
         put_node(dst, d, make_dot(get_node(src, b1), dot_l_t));
-        copy_bytes(dst + 16 * (d + 1), src + 16 * b1, 16u * (uint32_t)(e1 - b1));
+        copy_name_bytes(dst + 16 * (d + 1), src + 16 * b1, 16u * (uint32_t)(e1 - b1));
         return d + 1 + (e1 - b1);
     }
     case OP_RIGHT: {  // operations::right, :202-208
         int16_t rot = node_rot(src, b1);
         if (rot >= 0) {
-            copy_bytes(dst + 16 * d, src + 16 * (b1 + rot), 16u * (uint32_t)(e1 - b1 - rot));
+            copy_name_bytes(dst + 16 * d, src + 16 * (b1 + rot), 16u * (uint32_t)(e1 - b1 - rot));
             return d + (e1 - b1 - rot);
         }
         put_node(dst, d, make_dot(get_node(src, b1), dot_r_t));
-        copy_bytes(dst + 16 * (d + 1), src + 16 * b1, 16u * (uint32_t)(e1 - b1));
+        copy_name_bytes(dst + 16 * (d + 1), src + 16 * b1, 16u * (uint32_t)(e1 - b1));
         return d + 1 + (e1 - b1);
     }
     default: {  // operations::merge, :181-192
         if (node_rot(src, b1) == dot_l_t && node_rot(src, b2) == dot_r_t &&
             node_hash(src, b1 + 1) == node_hash(src, b2 + 1)) {
-            copy_bytes(dst + 16 * d, src + 16 * (b1 + 1), 16u * (uint32_t)(e1 - b1 - 1));
+            copy_name_bytes(dst + 16 * d, src + 16 * (b1 + 1), 16u * (uint32_t)(e1 - b1 - 1));
             return d + (e1 - b1 - 1);
         }
         put_node(dst, d, make_pair(get_node(src, b1), get_node(src, b2), (int16_t)(e1 - b1 + 1)));
-        copy_bytes(dst + 16 * (d + 1), src + 16 * b1, 16u * (uint32_t)(e1 - b1));
-        copy_bytes(dst + 16 * (d + 1 + e1 - b1), src + 16 * b2, 16u * (uint32_t)(e2 - b2));
+        copy_name_bytes(dst + 16 * (d + 1), src + 16 * b1, 16u * (uint32_t)(e1 - b1));
+        copy_name_bytes(dst + 16 * (d + 1 + e1 - b1), src + 16 * b2, 16u * (uint32_t)(e2 - b2));
         return d + 1 + (e1 - b1) + (e2 - b2);
     }
     }
