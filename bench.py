@@ -505,8 +505,8 @@ def ours(args, rank, world):
 
 
 def extra_ratios(args, rank, world):
-    """The benchmark spec's two ratios on the same GPU, beside the default line:
-    the batched form against the plain path instance by instance (batch256),
+    """Two ratios on the same GPU, beside the default line: the batched form
+    against the plain path instance by instance (batch256),
     and the adjoint's forward + backward against the plain forward
     (adjoint10).  Fewer steps than the main line (each is a full workload)."""
     import torch
