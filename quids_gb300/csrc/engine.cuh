@@ -469,7 +469,8 @@ struct has_grouped<R, std::void_t<decltype(R::grouped_children)>> : std::bool_co
 // blocks per SM the grouped pass with a fused table claim is compiled for
 // (the register cap of __launch_bounds__): claimed_pass_blocks in the rule,
 // else 1 (no cap).  The flip rules' walk keeps its FP64 pipe busy only with
-// three resident blocks; split_merge's larger walk is slower when capped.
+// several resident blocks (four, some spilling, ran fastest); split_merge's
+// larger walk is slower when capped.
 // The batched pass (per-instance rules, more live state) is not capped.
 template <class R, class = void>
 struct claimed_pass_blocks : std::integral_constant<int, 1> {};

@@ -249,7 +249,7 @@ template <bool ON_XOR>
 struct flip_rule {
     factors f;
     static constexpr bool grouped_children = true;  // 2^sites children, one factor per site
-    static constexpr int claimed_pass_blocks = 3;    // resident blocks of the grouped pass with a table claim
+    static constexpr int claimed_pass_blocks = 4;    // resident blocks of the grouped pass with a table claim
 
     QD_HD static bool site(bool l, bool r) { return ON_XOR ? (l != r) : (l == r); }
     QD_HD static bool conj_of(bool l, bool r) { return ON_XOR ? l : (l && r); }
